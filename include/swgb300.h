@@ -1,0 +1,159 @@
+/*
+ * swgb300 -- GB300-native backend for the finite-difference time-stepping hot
+ * path of SeismicWaves.jl (acoustic constant-density C-PML, 2D and 3D).
+ *
+ * Plain C ABI: no C++ types, no exceptions, no torch types.  Every entry point
+ * returns an int status (SW_OK on success); the text of the last error of a
+ * context is available from sw_ctx_last_error().
+ *
+ * Array conventions follow the reference's Julia structures: all grids are
+ * column-major with axis 0 fastest (x), the last axis is depth, indices are
+ * 1-based; traces are (nt, nrec) column-major with time fastest; positions are
+ * (npos, ndim) column-major.  Unless a call takes an `on_device` flag set to
+ * 1, every pointer is a host pointer and the call copies in and out.  With
+ * on_device = 1 the bulk arrays (vp, srctf, traces, observed, invcov_diag,
+ * grad, misfit) are device pointers; the small tables (grid indices, C-PML
+ * coefficients, windows, positions) are always host memory.
+ *
+ * Where each entry point sits in the reference (SeismicWaves.jl v0.9.0, paths
+ * relative to its source tree):
+ *
+ *   sw_ctx_create / sw_ctx_destroy
+ *       the backend module a package extension returns from select_backend
+ *       (ext/SeismicWaves_CUDABackendExt.jl:13-25, src/models/backend_selection.jl:2-40)
+ *   sw_cpml_coefficients
+ *       compute_CPML_coefficientsAxis! + the free-top override
+ *       (src/models/cpmlcoeffs.jl:18-100, src/models/acoustic/acou_init_bc.jl:7-40)
+ *   sw_wavesim_create / sw_wavesim_destroy
+ *       build_wavesim -> AcousticCDCPMLWaveSimulation (src/apis/build.jl:18-40,
+ *       src/models/acoustic/acou_models.jl:90-202): preallocated device fields
+ *   sw_wavesim_set_vp
+ *       set_wavesim_matprop! -> update_matprop! -> precompute_fact!
+ *       (src/apis/utils.jl:3-8, src/models/acoustic/acou_models.jl:53-60)
+ *   sw_acoustic_forward
+ *       run_swforward! shot loop + swforward_1shot! time loop + forward_onestep_CPML!
+ *       (src/apis/forward.jl:71-114, src/models/acoustic/acou_forward.jl:22-62,
+ *       src/models/acoustic/backends/shared/acoustic2D_xPU.jl:78-126, acoustic3D_xPU.jl:96-160);
+ *       all shots of the call advance together in one launch per time step
+ *   sw_acoustic_gradient
+ *       run_swgradient! + swgradient_1shot! (CD) with LinearCheckpointer, L2 misfit,
+ *       prescale_residuals!, adjoint_onestep_CPML!, correlate_gradient!, muting and
+ *       the 2/vp^3 rescaling (src/apis/gradient.jl:93-136,
+ *       src/models/acoustic/acou_gradient.jl:4-95, src/utils/checkpointers.jl:1-107,
+ *       src/inversion/misfits/L2Misfit.jl:24-77, acoustic2D_xPU.jl:64-76 and :128-169,
+ *       correlate_gradient_xPU.jl:1-10, src/utils/mute_grad.jl:13-80)
+ */
+#ifndef SWGB300_H
+#define SWGB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+  SW_OK = 0,
+  SW_ERR_ARG = 1,         /* invalid argument (the reference's @assert / error) */
+  SW_ERR_OOM = 2,         /* device allocation failed */
+  SW_ERR_CUDA = 3,        /* CUDA runtime error */
+  SW_ERR_TIMEOUT = 4,     /* a bounded device-side wait gave up */
+  SW_ERR_STATE = 5,       /* call made in the wrong state (e.g. gradient on a forward-only wavesim) */
+  SW_ERR_UNSUPPORTED = 6  /* input the backend deliberately rejects (see sw_ctx_last_error) */
+};
+
+typedef struct sw_ctx sw_ctx;
+typedef struct sw_wavesim sw_wavesim;
+
+/* Library version (major*10000 + minor*100 + patch). */
+int sw_version(void);
+
+/* One context per device; `stream` is a cudaStream_t to launch on, or NULL
+ * for a stream owned by the context.  A context is used by one host thread. */
+int sw_ctx_create(int device, void* stream, sw_ctx** out);
+int sw_ctx_destroy(sw_ctx* ctx);
+const char* sw_ctx_last_error(const sw_ctx* ctx);
+/* The stream the context launches on (cudaStream_t). */
+void* sw_ctx_stream(const sw_ctx* ctx);
+
+/* InputParametersAcoustic{T,N} + CPMLBoundaryConditionParameters{T}. */
+typedef struct {
+  int32_t ndim;      /* 2 or 3 */
+  int32_t n[3];      /* grid points per axis (axis 0 fastest; last axis = depth) */
+  double h[3];       /* grid spacing per axis [m] */
+  double dt;         /* time step [s] */
+  int32_t halo;      /* C-PML thickness in grid points (>= 0) */
+  double rcoef;      /* target reflection coefficient */
+  int32_t freetop;   /* 1: free surface at index 1 of the last axis */
+} sw_acoustic_params;
+
+/* C-PML coefficients of one axis, as compute_CPML_coefficientsAxis! returns
+ * them: a and b have 2*(halo+1) entries, a_h and b_h 2*halo entries.
+ * freetop_axis = 1 applies the free-surface override of the first half. */
+int sw_cpml_coefficients(double vel_max, double dt, int32_t halo, double rcoef, double h, double f0,
+                         int32_t freetop_axis, float* a, float* a_h, float* b, float* b_h);
+
+/* One shot (ScalarShot) as possrcrec_scaletf hands it to the backend:
+ * nearest-grid-point indices and the scaled source time functions. */
+typedef struct {
+  int32_t nt;               /* time steps of this shot (may differ between shots) */
+  int32_t nsrc;
+  const int32_t* src_idx;   /* (nsrc, ndim), 1-based grid indices */
+  const float* srctf;       /* (nt, nsrc), already scaled by dt^2 vp(src)^2 / prod(h) */
+  int32_t nrec;
+  const int32_t* rec_idx;   /* (nrec, ndim), 1-based grid indices */
+  float* traces;            /* (nt, nrec) output: pressure after injection, every step */
+  const float* cpml;        /* ndim blocks [a, a_h, b, b_h] of this shot's C-PML coefficients */
+  /* used by sw_acoustic_gradient only */
+  const float* observed;    /* (nt, nrec) observed data of the L2 misfit */
+  const float* invcov_diag; /* NULL: identity inverse covariance; else its diagonal (nt) */
+  int32_t nwin;             /* number of time windows (0 = whole trace) */
+  const int32_t* windows;   /* (2, nwin): 1-based inclusive [first, last] pairs (host memory) */
+  const double* src_pos;    /* (nsrc, ndim) metres, muting only (host memory) */
+  const double* rec_pos;    /* (nrec, ndim) metres, muting only (host memory) */
+} sw_acoustic_shot;
+
+/* GradParameters. */
+typedef struct {
+  int32_t check_freq;       /* checkpoint period K (>= 1, < nt of every shot) */
+  int32_t mute_radius_src;  /* grid points; 0 = off */
+  int32_t mute_radius_rec;
+  int32_t compute_misfit;
+  int32_t snapshot_bf16;    /* 1: checkpoints held as per-snapshot-scaled BF16 */
+} sw_grad_params;
+
+/* build_wavesim.  `gradient` = 1 allows sw_acoustic_gradient.  Device memory
+ * for the shots is allocated at the first call that needs it and reused. */
+int sw_wavesim_create(sw_ctx* ctx, const sw_acoustic_params* params, int32_t gradient,
+                      const sw_grad_params* gparams, sw_wavesim** out);
+int sw_wavesim_destroy(sw_wavesim* ws);
+
+/* set_wavesim_matprop!: vp has prod(n) entries (column-major). */
+int sw_wavesim_set_vp(sw_wavesim* ws, const float* vp, int32_t on_device);
+
+/* run_swforward!: all shots advance together (shots that do not fit in device
+ * memory at once run in consecutive groups). */
+int sw_acoustic_forward(sw_wavesim* ws, int32_t nshots, const sw_acoustic_shot* shots, int32_t on_device);
+
+/* run_swgradient! with the L2 misfit: grad (prod(n) entries, float64) is the
+ * sum over shots of each shot's muted, 2/vp^3-rescaled gradient; misfit
+ * (may be NULL) receives the sum of the shots' misfits.  Traces are written
+ * to each shot's `traces`. */
+int sw_acoustic_gradient(sw_wavesim* ws, int32_t nshots, const sw_acoustic_shot* shots, int32_t on_device,
+                         double* grad, double* misfit);
+
+/* Height (in planes of the marching axis) of the stencil tiles; 0 restores
+ * the built-in heuristic.  Used by the tile autotuner. */
+int sw_wavesim_set_tile(sw_wavesim* ws, int32_t tz);
+
+/* Per-kernel timing collected with CUDA events on the context's stream while
+ * enabled (0 = off).  kind: 0 = forward/recompute stencil, 1 = adjoint
+ * stencil with correlation, 2 = source/receiver kernel, 3 = other. */
+int sw_profile_enable(sw_ctx* ctx, int32_t on);
+int sw_profile_read(sw_ctx* ctx, int32_t kind, double* total_ms, int64_t* launches, double* bytes);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SWGB300_H */

@@ -1,0 +1,1080 @@
+// Acoustic constant-density C-PML path: shot tables, the batched forward and
+// the batched gradient (forward with checkpoints, misfit and adjoint source,
+// adjoint with recompute and fused correlation, reduction over shots).
+//
+// Reference behaviour restated here (SeismicWaves.jl v0.9.0):
+//   run_swforward! / swforward_1shot!     src/apis/forward.jl:71-114, src/models/acoustic/acou_forward.jl:22-62
+//   run_swgradient! / swgradient_1shot!   src/apis/gradient.jl:93-136, src/models/acoustic/acou_gradient.jl:4-95
+//   inject_sources! / record_receivers!   src/models/acoustic/backends/shared/acoustic2D_xPU.jl:48-62
+//   prescale_residuals!                   acoustic2D_xPU.jl:64-76
+//   L2 misfit and dchi/du                 src/inversion/misfits/L2Misfit.jl:24-77
+//   mutearoundpoint!                      src/utils/mute_grad.jl:13-80
+//   LinearCheckpointer schedule           src/utils/checkpointers.jl:1-107
+//
+// Gradient schedule.  The reference stores p at every K-th step (width 2),
+// psi and xi at every K-th step, and a buffer of K+1 fields that recover!
+// refills by re-running K-1 forward steps whenever the adjoint loop reaches a
+// checkpoint it = mK.  The correlation at adjoint step it needs the second
+// time difference D(it-1) = p[it-2] - 2 p[it-1] + p[it], which the forward
+// step that produces p[it] already knows exactly: D(it-1) = fact * lap(p[it-1])
+// (+ the injected source).  So the forward (for the top segment) and the
+// recompute write D directly (one field per step instead of three re-reads),
+// the recompute runs K steps (m-1)K+1 .. mK from the checkpoint at (m-1)K,
+// and checkpoints are written by the forward stencil itself in the step after
+// they are reached (no copy kernels).  Recovery events fall on it = mK for
+// every shot regardless of its nt, so shots with different record lengths
+// share one schedule; a shot takes part in step it only while it <= nt.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <numeric>
+#include <sstream>
+
+#include "acoustic_kernels.cuh"
+#include "internal.h"
+
+namespace swgb {
+
+// ---------------------------------------------------------------------------
+// Per-shot descriptor (device) and the small kernels around the stencil
+// ---------------------------------------------------------------------------
+struct ShotDesc {
+  int nt, nsrc, nrec;
+  int nsp, nrp;             // unique source / receiver points
+  int last;                 // floor(nt/K)*K (gradient)
+  long long sp_off, sp_ptr;  // unique source points: pts[sp_off + u], csr ptr[sp_ptr + u .. +1]
+  long long rp_off, rp_ptr;  // unique receiver points
+  long long rec_off;         // rec_lin[rec_off + r]
+  const float* tf;           // (nt, nsrc)
+  float* tr;                 // (nt, nrec)
+  const float* obs;          // (nt, nrec)
+  const float* ic;           // (nt) or nullptr
+  const float* mask;         // (nt) or nullptr
+  float* adj;                // (nt, nrec) adjoint source (prescaled)
+};
+
+// inject_sources! + record_receivers! for every active shot: one block per
+// shot.  Duplicated points are summed in source order by one thread, like the
+// reference's serial loop.  Optionally adds the injected amount to D.
+__global__ void k_inject_record(const ShotDesc* __restrict__ desc, const long long* __restrict__ pts,
+                                const int* __restrict__ ptr, const int* __restrict__ ids,
+                                const long long* __restrict__ rec_lin, FieldArg pnew, FieldArg dfield,
+                                int d_first, int it, int record) {
+  const int shot = blockIdx.x;
+  const ShotDesc D = desc[shot];
+  if (it > D.nt) return;
+  float* pn = pnew.p + (long long)shot * pnew.s;
+  float* dd = (dfield.p && shot >= d_first) ? dfield.p + (long long)shot * dfield.s : nullptr;
+  for (int u = threadIdx.x; u < D.nsp; u += blockDim.x) {
+    const long long lin = pts[D.sp_off + u];
+    float acc = pn[lin];
+    float add = 0.f;
+    for (int k = ptr[D.sp_ptr + u]; k < ptr[D.sp_ptr + u + 1]; ++k) {
+      const float v = D.tf[(long long)(it - 1) + (long long)ids[k] * D.nt];
+      acc += v;
+      add += v;
+    }
+    pn[lin] = acc;
+    if (dd) dd[lin] += add;
+  }
+  if (!record) return;
+  __syncthreads();
+  for (int r = threadIdx.x; r < D.nrec; r += blockDim.x)
+    D.tr[(long long)(it - 1) + (long long)r * D.nt] = pn[rec_lin[D.rec_off + r]];
+}
+
+// Adjoint injection at the receivers (adjoint_onestep_CPML! -> inject_sources!
+// with the prescaled residuals) and the matching correlation term: the fused
+// stencil correlated lambda before injection, so g += a * D is added here.
+__global__ void k_adj_inject(const ShotDesc* __restrict__ desc, const long long* __restrict__ pts,
+                             const int* __restrict__ ptr, const int* __restrict__ ids, FieldArg lam,
+                             FieldArg dcorr, FieldArg g, FieldArg gc, int it) {
+  const int shot = blockIdx.x;
+  const ShotDesc D = desc[shot];
+  if (it > D.nt) return;
+  float* lp = lam.p + (long long)shot * lam.s;
+  const float* dp = dcorr.p + (long long)shot * dcorr.s;
+  float* gp = g.p + (long long)shot * g.s;
+  float* cp = gc.p + (long long)shot * gc.s;
+  for (int u = threadIdx.x; u < D.nrp; u += blockDim.x) {
+    const long long lin = pts[D.rp_off + u];
+    float acc = lp[lin];
+    float add = 0.f;
+    for (int k = ptr[D.rp_ptr + u]; k < ptr[D.rp_ptr + u + 1]; ++k) {
+      const float v = D.adj[(long long)(it - 1) + (long long)ids[k] * D.nt];
+      acc += v;
+      add += v;
+    }
+    lp[lin] = acc;
+    float gv = gp[lin], cv = cp[lin];
+    kahan_add(gv, cv, add * dp[lin]);
+    gp[lin] = gv;
+    cp[lin] = cv;
+  }
+}
+
+// Residuals, window mask, C^-1 r, misfit (FP64) and the prescaled adjoint
+// source -C^-1 r * fact(rec).  gridDim = (blocks per shot, shots).
+__global__ void k_misfit_adjsrc(const ShotDesc* __restrict__ desc, const long long* __restrict__ rec_lin,
+                                const float* __restrict__ fact, double* __restrict__ partial) {
+  const int shot = blockIdx.y;
+  const ShotDesc D = desc[shot];
+  const long long total = (long long)D.nt * D.nrec;
+  double acc = 0.0;
+  for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < total;
+       q += (long long)gridDim.x * blockDim.x) {
+    const int t = (int)(q % D.nt);
+    const int r = (int)(q / D.nt);
+    float res = D.tr[q] - D.obs[q];
+    if (D.mask) res *= D.mask[t];
+    const float cres = D.ic ? D.ic[t] * res : res;
+    acc += (double)res * (double)cres;
+    D.adj[q] = (-cres) * fact[rec_lin[D.rec_off + r]];
+  }
+  __shared__ double red[256];
+  red[threadIdx.x] = acc;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) partial[(long long)shot * gridDim.x + blockIdx.x] = red[0];
+}
+
+__global__ void k_misfit_sum(const double* __restrict__ partial, int nblk, int nshots, double* out,
+                             int accumulate) {
+  double acc = 0.0;
+  for (int i = threadIdx.x; i < nblk * nshots; i += blockDim.x) acc += partial[i];
+  __shared__ double red[256];
+  red[threadIdx.x] = acc;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *out = (accumulate ? *out : 0.0) + 0.5 * red[0];
+}
+
+// mutearoundpoint!: multiplies g (and its Kahan compensation) by r/rmax inside
+// the ball around each listed point, sequentially over the points of a shot.
+struct MutePoint {
+  int shot;
+  int lo[3], hi[3];
+  double pos[3];
+};
+__global__ void k_mute(const MutePoint* __restrict__ mp, const int* __restrict__ shot_ptr, int N, int n0, int n1,
+                       int n2, int P, double h0, double h1, double h2, double rmax, FieldArg g, FieldArg gc) {
+  const int shot = blockIdx.x;
+  float* gp = g.p + (long long)shot * g.s;
+  float* cp = gc.p + (long long)shot * gc.s;
+  const double h[3] = {h0, h1, h2};
+  const int n[3] = {n0, n1, n2};
+  for (int k = shot_ptr[shot]; k < shot_ptr[shot + 1]; ++k) {
+    const MutePoint m = mp[k];
+    const int e0 = m.hi[0] - m.lo[0] + 1, e1 = m.hi[1] - m.lo[1] + 1, e2 = N == 3 ? m.hi[2] - m.lo[2] + 1 : 1;
+    const int cnt = e0 * e1 * e2;
+    for (int t = threadIdx.x; t < cnt; t += blockDim.x) {
+      int I[3];
+      I[0] = m.lo[0] + t % e0;
+      I[1] = m.lo[1] + (t / e0) % e1;
+      I[2] = N == 3 ? m.lo[2] + t / (e0 * e1) : 1;
+      bool inb = true;
+      double r2 = 0.0;
+      for (int d = 0; d < N; ++d) {
+        if (I[d] < 1 || I[d] > n[d]) inb = false;
+        const double xc = (I[d] - 1) * h[d];
+        r2 += (m.pos[d] - xc) * (m.pos[d] - xc);
+      }
+      if (!inb) continue;
+      const double r = sqrt(r2);
+      if (r <= rmax) {
+        const float att = (float)(r / rmax);
+        const long long lin = N == 3 ? ((long long)(I[2] - 1) * n1 + (I[1] - 1)) * P + (I[0] - 1)
+                                     : (long long)(I[1] - 1) * P + (I[0] - 1);
+        gp[lin] *= att;
+        cp[lin] *= att;
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// grad[c] (+)= 2/vp^3 * sum_s (g_s - c_s)  in FP64, unpadded column-major output.
+__global__ void k_reduce_grad(const float* __restrict__ g, const float* __restrict__ gc, long long fstride,
+                              int nshots, const float* __restrict__ vp, int n0, long long npts, int P,
+                              double* __restrict__ out, int accumulate) {
+  for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < npts;
+       c += (long long)gridDim.x * blockDim.x) {
+    const long long rowi = c / n0;
+    const long long lin = rowi * P + (c - rowi * n0);
+    double s = 0.0;
+    for (int k = 0; k < nshots; ++k) {
+      const long long q = (long long)k * fstride + lin;
+      s += (double)g[q] - (double)gc[q];
+    }
+    const double v = (double)vp[c];
+    const double val = (2.0 / (v * v * v)) * s;
+    out[c] = accumulate ? out[c] + val : val;
+  }
+}
+
+// fact = dt^2 vp^2 into the padded layout; vp kept unpadded (float).
+__global__ void k_set_fact(const float* __restrict__ vp, int n0, long long npts, int P, double dt2,
+                           float* __restrict__ fact) {
+  for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < npts;
+       c += (long long)gridDim.x * blockDim.x) {
+    const long long rowi = c / n0;
+    const double v = (double)vp[c];
+    fact[rowi * P + (c - rowi * n0)] = (float)(dt2 * v * v);
+  }
+}
+
+}  // namespace swgb
+
+// ---------------------------------------------------------------------------
+// Host side
+// ---------------------------------------------------------------------------
+using namespace swgb;
+
+struct sw_wavesim {
+  sw_ctx* ctx = nullptr;
+  sw_acoustic_params prm{};
+  bool gradient = false;
+  sw_grad_params gp{};
+  int N = 2;
+  int n[3] = {1, 1, 1};
+  int P = 0;
+  long long F = 0;           // floats per field (padded)
+  long long npts = 0;        // unpadded points
+  long long psz[3] = {0, 0, 0}, xsz[3] = {0, 0, 0};
+  long long strip_total = 0;  // sum psi + sum xi (floats)
+  bool has_vp = false;
+  DevMem vp, fact;
+  // capacity (shots) of the state buffers
+  int cap = 0;
+  DevMem pb[3], psi[2][3], xi[3];     // forward state
+  DevMem ab[3], apsi[2][3], axi[3];   // adjoint state
+  DevMem g, gc;
+  DevMem dbuf;                         // D slots
+  long long d_slots = 0;
+  DevMem ck;                           // checkpoint slots
+  long long ck_slots = 0;
+  DevMem zero;                         // zero state (one shot, stride 0)
+  // tables
+  DevMem d_desc, d_pts, d_ptr, d_ids, d_rec, d_tf, d_tr, d_obs, d_ic, d_mask, d_adj, d_cpml, d_partial, d_mis;
+  DevMem d_mute, d_mute_ptr;
+  int tile_tz = 0;  // 0 = heuristic
+};
+
+namespace {
+
+struct HostShot {
+  int orig;  // index in the caller's array
+  int nt;
+};
+
+inline long long round_up(long long v, long long m) { return (v + m - 1) / m * m; }
+
+void ensure(DevMem& m, size_t bytes, const char* what) {
+  if (m.bytes >= bytes && m.p) return;
+  m.release();
+  dev_alloc(m, bytes, what);
+}
+
+template <typename T>
+void upload(sw_wavesim* ws, DevMem& m, const std::vector<T>& v, const char* what) {
+  const size_t bytes = std::max<size_t>(v.size() * sizeof(T), 16);
+  ensure(m, bytes, what);
+  if (!v.empty())
+    check_cuda(cudaMemcpyAsync(m.p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, ws->ctx->stream), what);
+}
+
+struct Tables {
+  std::vector<ShotDesc> desc;
+  std::vector<long long> pts, rec;
+  std::vector<int> ptr, ids;
+  std::vector<HostShot> order;  // sorted by nt descending
+  int max_nt = 0;
+};
+
+long long lin_of(const sw_wavesim* ws, const int* I) {  // 1-based -> padded linear
+  if (ws->N == 2) return (long long)(I[1] - 1) * ws->P + (I[0] - 1);
+  return ((long long)(I[2] - 1) * ws->n[1] + (I[1] - 1)) * ws->P + (I[0] - 1);
+}
+
+void unique_points(const sw_wavesim* ws, const int32_t* idx, int npos, Tables& T, long long& off,
+                   long long& ptr_off, int& nunique, std::vector<long long>* per_pos) {
+  std::vector<long long> lin(npos);
+  for (int p = 0; p < npos; ++p) {
+    int I[3] = {1, 1, 1};
+    for (int d = 0; d < ws->N; ++d) I[d] = idx[p + (long long)d * npos];
+    lin[p] = lin_of(ws, I);
+    if (per_pos) per_pos->push_back(lin[p]);
+  }
+  // unique points in order of first appearance; ids listed in position order
+  std::vector<long long> uniq;
+  std::vector<std::vector<int>> members;
+  for (int p = 0; p < npos; ++p) {
+    auto it = std::find(uniq.begin(), uniq.end(), lin[p]);
+    if (it == uniq.end()) {
+      uniq.push_back(lin[p]);
+      members.push_back({p});
+    } else {
+      members[it - uniq.begin()].push_back(p);
+    }
+  }
+  off = (long long)T.pts.size();
+  ptr_off = (long long)T.ptr.size();
+  nunique = (int)uniq.size();
+  for (size_t u = 0; u < uniq.size(); ++u) {
+    T.pts.push_back(uniq[u]);
+    T.ptr.push_back((int)T.ids.size());
+    for (int m : members[u]) T.ids.push_back(m);
+  }
+  T.ptr.push_back((int)T.ids.size());
+}
+
+void validate_shot(const sw_wavesim* ws, const sw_acoustic_shot& s, int k, bool grad) {
+  std::ostringstream os;
+  if (s.nt < 1) { os << "shot " << k << ": nt must be positive"; fail(SW_ERR_ARG, os.str()); }
+  if (s.nsrc < 1) { os << "shot " << k << ": there must be at least one source"; fail(SW_ERR_ARG, os.str()); }
+  if (s.nrec < 1) { os << "shot " << k << ": there must be at least one receiver"; fail(SW_ERR_ARG, os.str()); }
+  if (!s.src_idx || !s.rec_idx || !s.srctf || !s.traces || !s.cpml) {
+    os << "shot " << k << ": missing array";
+    fail(SW_ERR_ARG, os.str());
+  }
+  auto chk = [&](const int32_t* idx, int np, const char* what) {
+    for (int p = 0; p < np; ++p)
+      for (int d = 0; d < ws->N; ++d) {
+        const int v = idx[p + (long long)d * np];
+        if (v < 1 || v > ws->n[d]) {
+          std::ostringstream e;
+          e << "shot " << k << ": " << what << " " << p + 1 << " index " << v << " outside 1.." << ws->n[d]
+            << " on axis " << d + 1;
+          fail(SW_ERR_ARG, e.str());
+        }
+      }
+  };
+  chk(s.src_idx, s.nsrc, "source");
+  chk(s.rec_idx, s.nrec, "receiver");
+  if (grad) {
+    if (!s.observed) { os << "shot " << k << ": gradient needs observed data"; fail(SW_ERR_ARG, os.str()); }
+    const int K = ws->gp.check_freq;
+    if (K >= s.nt) {
+      os << "shot " << k << ": checkpointing frequency must be smaller than the number of timesteps";
+      fail(SW_ERR_ARG, os.str());
+    }
+    if (K > 1) {
+      for (int p = 0; p < s.nsrc; ++p)
+        for (int d = 0; d < ws->N; ++d) {
+          const int v = s.src_idx[p + (long long)d * s.nsrc];
+          if (v == 1 || v == ws->n[d]) {
+            std::ostringstream e;
+            e << "shot " << k << ": source " << p + 1
+              << " lies on the outermost grid line; with check_freq > 1 the reference's recompute reads a "
+                 "stale buffer there, so no well-defined gradient exists (use check_freq = 1 or move the source)";
+            fail(SW_ERR_UNSUPPORTED, e.str());
+          }
+        }
+    }
+    for (int w = 0; w < s.nwin; ++w) {
+      const int a = s.windows[2 * w], b = s.windows[2 * w + 1];
+      if (!(1 <= a && a <= b && b <= s.nt)) {
+        os << "shot " << k << ": windows indices must be between 1 and maximum number of timesteps";
+        fail(SW_ERR_ARG, os.str());
+      }
+    }
+  }
+}
+
+// Builds and uploads the shot tables for shots[first .. first+count) in the
+// sorted order; bulk arrays are uploaded (host) or referenced (device).
+void build_tables(sw_wavesim* ws, const sw_acoustic_shot* shots, const std::vector<HostShot>& group,
+                  bool on_device, bool grad, Tables& T) {
+  cudaStream_t st = ws->ctx->stream;
+  const int S = (int)group.size();
+  T.desc.assign(S, ShotDesc{});
+  T.pts.clear(); T.rec.clear(); T.ptr.clear(); T.ids.clear();
+  long long tf_total = 0, tr_total = 0, ic_total = 0, mask_total = 0;
+  for (int k = 0; k < S; ++k) {
+    const sw_acoustic_shot& s = shots[group[k].orig];
+    tf_total += (long long)s.nt * s.nsrc;
+    tr_total += (long long)s.nt * s.nrec;
+    if (s.invcov_diag) ic_total += s.nt;
+    if (s.nwin > 0) mask_total += s.nt;
+  }
+  // device staging
+  if (!on_device) ensure(ws->d_tf, std::max<long long>(tf_total, 4) * sizeof(float), "srctf");
+  ensure(ws->d_tr, std::max<long long>(tr_total, 4) * sizeof(float), "traces");
+  if (grad) {
+    if (!on_device) {
+      ensure(ws->d_obs, std::max<long long>(tr_total, 4) * sizeof(float), "observed");
+      ensure(ws->d_ic, std::max<long long>(ic_total, 4) * sizeof(float), "invcov");
+    }
+    ensure(ws->d_mask, std::max<long long>(mask_total, 4) * sizeof(float), "window mask");
+    ensure(ws->d_adj, std::max<long long>(tr_total, 4) * sizeof(float), "adjoint source");
+  }
+  const int na = 2 * ws->prm.halo + 2, nh = 2 * ws->prm.halo;
+  const int cstride = ws->N * (2 * na + 2 * nh);
+  std::vector<float> cpml((size_t)S * cstride);
+  std::vector<float> masks;
+  long long tf_o = 0, tr_o = 0, ic_o = 0;
+  for (int k = 0; k < S; ++k) {
+    const sw_acoustic_shot& s = shots[group[k].orig];
+    ShotDesc& D = T.desc[k];
+    D.nt = s.nt; D.nsrc = s.nsrc; D.nrec = s.nrec;
+    D.last = grad ? (s.nt / ws->gp.check_freq) * ws->gp.check_freq : 0;
+    unique_points(ws, s.src_idx, s.nsrc, T, D.sp_off, D.sp_ptr, D.nsp, nullptr);
+    unique_points(ws, s.rec_idx, s.nrec, T, D.rp_off, D.rp_ptr, D.nrp, nullptr);
+    D.rec_off = (long long)T.rec.size();
+    for (int r = 0; r < s.nrec; ++r) {
+      int I[3] = {1, 1, 1};
+      for (int d = 0; d < ws->N; ++d) I[d] = s.rec_idx[r + (long long)d * s.nrec];
+      T.rec.push_back(lin_of(ws, I));
+    }
+    std::memcpy(&cpml[(size_t)k * cstride], s.cpml, sizeof(float) * cstride);
+    const long long ntf = (long long)s.nt * s.nsrc, ntr = (long long)s.nt * s.nrec;
+    if (on_device) {
+      D.tf = s.srctf;
+      D.obs = s.observed;
+      D.ic = s.invcov_diag;
+    } else {
+      float* tfp = ws->d_tf.as<float>() + tf_o;
+      check_cuda(cudaMemcpyAsync(tfp, s.srctf, ntf * sizeof(float), cudaMemcpyHostToDevice, st), "srctf upload");
+      D.tf = tfp;
+      if (grad) {
+        float* op = ws->d_obs.as<float>() + tr_o;
+        check_cuda(cudaMemcpyAsync(op, s.observed, ntr * sizeof(float), cudaMemcpyHostToDevice, st), "observed upload");
+        D.obs = op;
+        if (s.invcov_diag) {
+          float* ip = ws->d_ic.as<float>() + ic_o;
+          check_cuda(cudaMemcpyAsync(ip, s.invcov_diag, s.nt * sizeof(float), cudaMemcpyHostToDevice, st), "invcov upload");
+          D.ic = ip;
+          ic_o += s.nt;
+        }
+      }
+    }
+    D.tr = ws->d_tr.as<float>() + tr_o;
+    if (grad) {
+      D.adj = ws->d_adj.as<float>() + tr_o;
+      if (s.nwin > 0) {
+        const size_t mo = masks.size();
+        masks.resize(mo + s.nt, 0.f);
+        for (int w = 0; w < s.nwin; ++w)
+          for (int t = s.windows[2 * w] - 1; t <= s.windows[2 * w + 1] - 1; ++t) masks[mo + t] = 1.f;
+        D.mask = ws->d_mask.as<float>() + mo;
+      }
+    }
+    tf_o += ntf;
+    tr_o += ntr;
+  }
+  upload(ws, ws->d_desc, T.desc, "shot descriptors");
+  upload(ws, ws->d_pts, T.pts, "point table");
+  upload(ws, ws->d_ptr, T.ptr, "point csr");
+  upload(ws, ws->d_ids, T.ids, "point ids");
+  upload(ws, ws->d_rec, T.rec, "receiver table");
+  upload(ws, ws->d_cpml, cpml, "cpml coefficients");
+  if (!masks.empty())
+    check_cuda(cudaMemcpyAsync(ws->d_mask.p, masks.data(), masks.size() * sizeof(float), cudaMemcpyHostToDevice, st),
+               "mask upload");
+}
+
+void ensure_state(sw_wavesim* ws, int S, bool grad, int max_nt) {
+  const long long F = ws->F;
+  if (S > ws->cap) {
+    for (int b = 0; b < 3; ++b) dev_alloc(ws->pb[b], (size_t)S * F * sizeof(float), "pressure field");
+    for (int k = 0; k < 2; ++k)
+      for (int d = 0; d < ws->N; ++d) dev_alloc(ws->psi[k][d], (size_t)S * ws->psz[d] * sizeof(float), "psi");
+    for (int d = 0; d < ws->N; ++d) dev_alloc(ws->xi[d], (size_t)S * ws->xsz[d] * sizeof(float), "xi");
+    if (ws->gradient) {
+      for (int b = 0; b < 3; ++b) dev_alloc(ws->ab[b], (size_t)S * F * sizeof(float), "adjoint field");
+      for (int k = 0; k < 2; ++k)
+        for (int d = 0; d < ws->N; ++d) dev_alloc(ws->apsi[k][d], (size_t)S * ws->psz[d] * sizeof(float), "adjoint psi");
+      for (int d = 0; d < ws->N; ++d) dev_alloc(ws->axi[d], (size_t)S * ws->xsz[d] * sizeof(float), "adjoint xi");
+      dev_alloc(ws->g, (size_t)S * F * sizeof(float), "gradient");
+      dev_alloc(ws->gc, (size_t)S * F * sizeof(float), "gradient compensation");
+    }
+    ws->cap = S;
+    ws->d_slots = 0;
+    ws->ck_slots = 0;
+  }
+  if (grad) {
+    const int K = ws->gp.check_freq;
+    const long long dslots = K == 1 ? max_nt : K;
+    if (dslots > ws->d_slots) {
+      ws->dbuf.release();
+      dev_alloc(ws->dbuf, (size_t)ws->cap * dslots * F * sizeof(float), "D buffer");
+      ws->d_slots = dslots;
+    }
+    const long long cks = K == 1 ? 0 : max_nt / K;
+    if (cks > ws->ck_slots) {
+      ws->ck.release();
+      const long long slot = 2 * F + ws->strip_total;
+      dev_alloc(ws->ck, (size_t)ws->cap * cks * slot * sizeof(float), "checkpoints");
+      ws->ck_slots = cks;
+    }
+    if (!ws->zero.p) dev_alloc(ws->zero, (size_t)(2 * F + ws->strip_total) * sizeof(float), "zero state");
+  }
+}
+
+// Memory (bytes) one shot needs in a batch.
+size_t per_shot_bytes(const sw_wavesim* ws, bool grad, int max_nt) {
+  // three pressure buffers, two psi buffers, xi; the same again for the adjoint, plus g and its compensation
+  long long floats = 3 * ws->F + ws->strip_total;
+  for (int d = 0; d < ws->N; ++d) floats += ws->psz[d];
+  if (ws->gradient) floats = 2 * floats + 2 * ws->F;
+  if (grad) {
+    const int K = ws->gp.check_freq;
+    floats += (K == 1 ? (long long)max_nt : K) * ws->F;
+    if (K > 1) floats += (long long)(max_nt / K) * (2 * ws->F + ws->strip_total);
+  }
+  return (size_t)floats * sizeof(float);
+}
+
+struct StepCtx {
+  sw_wavesim* ws;
+  int TZ;
+  int tiles_x, tiles_y, tiles_z;
+};
+
+StepCtx make_step_ctx(sw_wavesim* ws, int S) {
+  StepCtx c{ws, 0, 0, 1, 0};
+  const int sms = ws->ctx->num_sms > 0 ? ws->ctx->num_sms : 148;
+  const int nint = ws->n[ws->N - 1] - 2;  // interior extent of the marching axis
+  if (ws->N == 2) {
+    c.tiles_x = (int)((ws->P + 511) / 512);
+  } else {
+    c.tiles_x = (int)((ws->P + 127) / 128);
+    c.tiles_y = (ws->n[1] - 2 + 3) / 4;
+  }
+  int TZ = ws->tile_tz;
+  if (TZ <= 0) {
+    // aim for >= ~8 blocks per SM in total, with TZ in [8, 64]
+    TZ = 64;
+    while (TZ > 8) {
+      const long long blocks = (long long)S * c.tiles_x * c.tiles_y * ((nint + TZ - 1) / TZ);
+      if (blocks >= 8LL * sms) break;
+      TZ /= 2;
+    }
+  }
+  c.TZ = TZ;
+  c.tiles_z = (nint + TZ - 1) / TZ;
+  return c;
+}
+
+// Algorithmic bytes of one stencil launch (FP32 words), see the design doc.
+double stencil_bytes(const sw_wavesim* ws, int S, int mode, int n_dwrite, bool ckpt) {
+  double pts = 1.0;
+  for (int d = 0; d < ws->N; ++d) pts *= (double)(ws->n[d] - 2);
+  double strip = 0.0;  // interior points inside the damping strips, summed over axes
+  const int H = ws->prm.halo;
+  for (int d = 0; d < ws->N; ++d) {
+    double w = 0.0;
+    for (int x = 1; x <= ws->n[d] - 2; ++x) w += (x < H || x >= ws->n[d] - H) ? 1.0 : 0.0;
+    double other = 1.0;
+    for (int e = 0; e < ws->N; ++e)
+      if (e != d) other *= (double)(ws->n[e] - 2);
+    strip += w * other;
+  }
+  double per = 12.0 * S + 4.0;  // R pcur, R pold, W pnew per shot; R fact once
+  double b = per * pts + 16.0 * strip * S;
+  if (mode == MODE_FWD_D) b += 4.0 * pts * n_dwrite;
+  if (mode == MODE_ADJ) b += 20.0 * pts * S;  // R D, RMW g and c
+  if (ckpt) b += 8.0 * pts * S + 8.0 * strip * S;
+  return b;
+}
+
+struct Launcher {
+  sw_wavesim* ws;
+  cudaStream_t st;
+  template <int MODE>
+  void step(const StepArgs& a, const StepCtx& c, double bytes) {
+    const long long blocks = (long long)a.nshots * c.tiles_x * c.tiles_y * c.tiles_z;
+    cudaEvent_t ev = nullptr;
+    const int kind = MODE == MODE_ADJ ? KK_ADJOINT : KK_STENCIL;
+    ws->ctx->prof.begin(st, kind, bytes, &ev);
+    if (ws->N == 2)
+      k_ac2d_step<MODE><<<(unsigned)blocks, 128, 0, st>>>(a);
+    else
+      k_ac3d_step<MODE><<<(unsigned)blocks, 128, 0, st>>>(a);
+    check_cuda(cudaGetLastError(), "stencil launch");
+    ws->ctx->prof.end(st, kind, ev);
+  }
+};
+
+StepArgs base_args(sw_wavesim* ws, const StepCtx& c, int S) {
+  StepArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.n0 = ws->n[0];
+  a.n1 = ws->n[1];
+  a.n2 = ws->N == 3 ? ws->n[2] : 1;
+  a.P = ws->P;
+  a.halo = ws->prm.halo;
+  for (int d = 0; d < ws->N; ++d) {
+    const double ih = 1.0 / ws->prm.h[d];
+    a.ih[d] = (float)ih;
+    a.ih2[d] = (float)(ih * ih);
+  }
+  a.fact = ws->fact.as<float>();
+  a.cpml = ws->d_cpml.as<float>();
+  a.cpml_stride = ws->N * (2 * (2 * ws->prm.halo + 2) + 2 * (2 * ws->prm.halo));
+  a.nshots = S;
+  a.tiles_x = c.tiles_x;
+  a.tiles_y = c.tiles_y;
+  a.tiles_z = c.tiles_z;
+  a.TZ = c.TZ;
+  return a;
+}
+
+FieldArg fa(const DevMem& m, long long stride) { return FieldArg{m.as<float>(), stride}; }
+
+int active_count(const std::vector<HostShot>& g, int it) {
+  int k = 0;
+  while (k < (int)g.size() && g[k].nt >= it) ++k;
+  return k;
+}
+
+void zero_state(sw_wavesim* ws, int S, bool adjoint) {
+  cudaStream_t st = ws->ctx->stream;
+  DevMem* b = adjoint ? ws->ab : ws->pb;
+  for (int k = 0; k < 3; ++k) check_cuda(cudaMemsetAsync(b[k].p, 0, (size_t)S * ws->F * sizeof(float), st), "reset");
+  for (int k = 0; k < 2; ++k)
+    for (int d = 0; d < ws->N; ++d)
+      check_cuda(cudaMemsetAsync((adjoint ? ws->apsi : ws->psi)[k][d].p, 0, (size_t)S * ws->psz[d] * sizeof(float), st),
+                 "reset psi");
+  for (int d = 0; d < ws->N; ++d)
+    check_cuda(cudaMemsetAsync((adjoint ? ws->axi : ws->xi)[d].p, 0, (size_t)S * ws->xsz[d] * sizeof(float), st),
+               "reset xi");
+}
+
+// Download traces of a group back to the caller (host or device pointers).
+void download_traces(sw_wavesim* ws, const sw_acoustic_shot* shots, const std::vector<HostShot>& group,
+                     bool on_device) {
+  cudaStream_t st = ws->ctx->stream;
+  long long o = 0;
+  for (const HostShot& h : group) {
+    const sw_acoustic_shot& s = shots[h.orig];
+    const long long n = (long long)s.nt * s.nrec;
+    check_cuda(cudaMemcpyAsync(s.traces, ws->d_tr.as<float>() + o, n * sizeof(float),
+                               on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, st),
+               "traces download");
+    o += n;
+  }
+}
+
+// Forward of one group: all shots step together.  Gradient mode (grad = true)
+// also writes checkpoints and the top-segment D.
+void forward_group(sw_wavesim* ws, const std::vector<HostShot>& group, bool grad) {
+  const int S = (int)group.size();
+  cudaStream_t st = ws->ctx->stream;
+  zero_state(ws, S, false);
+  const int max_nt = group.front().nt;
+  const int K = grad ? ws->gp.check_freq : 0;
+  const long long F = ws->F;
+  const long long slot = 2 * F + ws->strip_total;
+  int io = 0, ic = 1, inew = 2, pk = 0;
+  Launcher L{ws, st};
+  for (int it = 1; it <= max_nt; ++it) {
+    const int Sa = active_count(group, it);
+    const StepCtx c = make_step_ctx(ws, Sa);
+    StepArgs a = base_args(ws, c, Sa);
+    a.pold = fa(ws->pb[io], F);
+    a.pcur = fa(ws->pb[ic], F);
+    a.pnew = fa(ws->pb[inew], F);
+    for (int d = 0; d < ws->N; ++d) {
+      a.psi_in[d] = fa(ws->psi[pk][d], ws->psz[d]);
+      a.psi_out[d] = fa(ws->psi[1 - pk][d], ws->psz[d]);
+      a.xi_in[d] = fa(ws->xi[d], ws->xsz[d]);
+      a.xi_out[d] = a.xi_in[d];
+    }
+    bool ckpt = false;
+    int d_first = Sa;
+    long long dslot = -1;
+    if (grad) {
+      // checkpoint m = (it-1)/K holds the state after step mK
+      if (K > 1 && (it - 1) % K == 0 && (it - 1) / K >= 1) {
+        const int m = (it - 1) / K;
+        float* base = ws->ck.as<float>() + (long long)(m - 1) * slot;
+        const long long sstride = ws->ck_slots * slot;
+        a.ck_pold = FieldArg{base, sstride};
+        a.ck_pcur = FieldArg{base + F, sstride};
+        long long off = 2 * F;
+        for (int d = 0; d < ws->N; ++d) { a.ck_psi[d] = FieldArg{base + off, sstride}; off += ws->psz[d]; }
+        for (int d = 0; d < ws->N; ++d) { a.ck_xi[d] = FieldArg{base + off, sstride}; off += ws->xsz[d]; }
+        ckpt = true;
+      }
+      // D(it-1) is kept for shots whose top segment contains it-1 (all steps when K == 1)
+      if (K == 1) {
+        d_first = 0;
+        dslot = it - 1;
+      } else {
+        d_first = Sa;
+        for (int k = 0; k < Sa; ++k)
+          if (it - 1 >= group[k].nt / K * K) { d_first = k; break; }
+        dslot = (it - 1) % K;
+      }
+      a.dout = FieldArg{ws->dbuf.as<float>() + dslot * F, ws->d_slots * F};
+      a.d_first = d_first;
+    }
+    const int n_dwrite = grad ? Sa - d_first : 0;
+    const double bytes = stencil_bytes(ws, Sa, grad ? MODE_FWD_D : MODE_FWD, n_dwrite, ckpt);
+    if (grad)
+      L.step<MODE_FWD_D>(a, c, bytes);
+    else
+      L.step<MODE_FWD>(a, c, bytes);
+    cudaEvent_t ev = nullptr;
+    ws->ctx->prof.begin(st, KK_SRCREC, 0.0, &ev);
+    k_inject_record<<<Sa, 128, 0, st>>>(ws->d_desc.as<ShotDesc>(), ws->d_pts.as<long long>(), ws->d_ptr.as<int>(),
+                                        ws->d_ids.as<int>(), ws->d_rec.as<long long>(), a.pnew,
+                                        grad ? a.dout : FieldArg{nullptr, 0}, d_first, it, 1);
+    check_cuda(cudaGetLastError(), "inject/record launch");
+    ws->ctx->prof.end(st, KK_SRCREC, ev);
+    const int o = io;
+    io = ic; ic = inew; inew = o;
+    pk = 1 - pk;
+  }
+}
+
+void adjoint_group(sw_wavesim* ws, const std::vector<HostShot>& group) {
+  const int S = (int)group.size();
+  cudaStream_t st = ws->ctx->stream;
+  const int max_nt = group.front().nt;
+  const int K = ws->gp.check_freq;
+  const long long F = ws->F;
+  const long long slot = 2 * F + ws->strip_total;
+  Launcher L{ws, st};
+  zero_state(ws, S, true);
+  check_cuda(cudaMemsetAsync(ws->g.p, 0, (size_t)S * F * sizeof(float), st), "reset g");
+  check_cuda(cudaMemsetAsync(ws->gc.p, 0, (size_t)S * F * sizeof(float), st), "reset gc");
+  int ao = 0, ac = 1, an = 2, apk = 0;
+  for (int it = max_nt; it >= 1; --it) {
+    const int Sa = active_count(group, it);
+    if (K > 1 && it % K == 0) {
+      // recover segment m: forward steps (m-1)K+1 .. mK from the checkpoint at (m-1)K
+      const int m = it / K;
+      const StepCtx c = make_step_ctx(ws, Sa);
+      float* cbase;
+      long long cstride;
+      if (m - 1 >= 1) {
+        cbase = ws->ck.as<float>() + (long long)(m - 2) * slot;
+        cstride = ws->ck_slots * slot;
+      } else {
+        cbase = ws->zero.as<float>();
+        cstride = 0;
+      }
+      FieldArg ck_po{cbase, cstride}, ck_pc{cbase + F, cstride}, ck_psi[3], ck_xi[3];
+      long long off = 2 * F;
+      for (int d = 0; d < ws->N; ++d) { ck_psi[d] = FieldArg{cbase + off, cstride}; off += ws->psz[d]; }
+      for (int d = 0; d < ws->N; ++d) { ck_xi[d] = FieldArg{cbase + off, cstride}; off += ws->xsz[d]; }
+      // working buffers W0..W2 = pb[0..2]; psi ping-pong in psi[0/1]
+      int w_old = -1, w_cur = -1, w_new = 0, pk = 0;
+      for (int t = (m - 1) * K + 1; t <= m * K; ++t) {
+        StepArgs a = base_args(ws, c, Sa);
+        const int step = t - (m - 1) * K;  // 1-based within the segment
+        a.pold = step == 1 ? ck_po : (step == 2 ? ck_pc : fa(ws->pb[w_old], F));
+        a.pcur = step == 1 ? ck_pc : fa(ws->pb[w_cur], F);
+        a.pnew = fa(ws->pb[w_new], F);
+        for (int d = 0; d < ws->N; ++d) {
+          a.psi_in[d] = step == 1 ? ck_psi[d] : fa(ws->psi[pk][d], ws->psz[d]);
+          a.psi_out[d] = fa(ws->psi[step == 1 ? 0 : 1 - pk][d], ws->psz[d]);
+          a.xi_in[d] = step == 1 ? ck_xi[d] : fa(ws->xi[d], ws->xsz[d]);
+          a.xi_out[d] = fa(ws->xi[d], ws->xsz[d]);
+        }
+        const long long dslot = (t - 1) % K;
+        a.dout = FieldArg{ws->dbuf.as<float>() + dslot * F, ws->d_slots * F};
+        a.d_first = 0;
+        L.step<MODE_FWD_D>(a, c, stencil_bytes(ws, Sa, MODE_FWD_D, Sa, false));
+        cudaEvent_t ev = nullptr;
+        ws->ctx->prof.begin(st, KK_SRCREC, 0.0, &ev);
+        k_inject_record<<<Sa, 128, 0, st>>>(ws->d_desc.as<ShotDesc>(), ws->d_pts.as<long long>(),
+                                            ws->d_ptr.as<int>(), ws->d_ids.as<int>(), ws->d_rec.as<long long>(),
+                                            a.pnew, a.dout, 0, t, 0);
+        check_cuda(cudaGetLastError(), "recompute inject launch");
+        ws->ctx->prof.end(st, KK_SRCREC, ev);
+        // rotate roles: (old, cur, new) <- (cur, new, next free)
+        if (step == 1) {
+          w_cur = w_new; w_new = 1; pk = 0;
+        } else if (step == 2) {
+          w_old = w_cur; w_cur = w_new; w_new = 2; pk = 1 - pk;
+        } else {
+          const int fr = w_old;
+          w_old = w_cur; w_cur = w_new; w_new = fr; pk = 1 - pk;
+        }
+      }
+    }
+    // adjoint step it with the fused correlation against D(it-1)
+    {
+      const StepCtx c = make_step_ctx(ws, Sa);
+      StepArgs a = base_args(ws, c, Sa);
+      a.pold = fa(ws->ab[ao], F);
+      a.pcur = fa(ws->ab[ac], F);
+      a.pnew = fa(ws->ab[an], F);
+      for (int d = 0; d < ws->N; ++d) {
+        a.psi_in[d] = fa(ws->apsi[apk][d], ws->psz[d]);
+        a.psi_out[d] = fa(ws->apsi[1 - apk][d], ws->psz[d]);
+        a.xi_in[d] = fa(ws->axi[d], ws->xsz[d]);
+        a.xi_out[d] = a.xi_in[d];
+      }
+      const long long dslot = K == 1 ? it - 1 : (it - 1) % K;
+      a.dcorr = FieldArg{ws->dbuf.as<float>() + dslot * F, ws->d_slots * F};
+      a.g = fa(ws->g, F);
+      a.gc = fa(ws->gc, F);
+      L.step<MODE_ADJ>(a, c, stencil_bytes(ws, Sa, MODE_ADJ, 0, false));
+      cudaEvent_t ev = nullptr;
+      ws->ctx->prof.begin(st, KK_SRCREC, 0.0, &ev);
+      k_adj_inject<<<Sa, 128, 0, st>>>(ws->d_desc.as<ShotDesc>(), ws->d_pts.as<long long>(), ws->d_ptr.as<int>(),
+                                       ws->d_ids.as<int>(), a.pnew, a.dcorr, a.g, a.gc, it);
+      check_cuda(cudaGetLastError(), "adjoint inject launch");
+      ws->ctx->prof.end(st, KK_SRCREC, ev);
+      const int o = ao;
+      ao = ac; ac = an; an = o;
+      apk = 1 - apk;
+    }
+  }
+}
+
+std::vector<std::vector<HostShot>> plan_groups(sw_wavesim* ws, const std::vector<HostShot>& order, bool grad) {
+  size_t free_b = 0, total_b = 0;
+  check_cuda(cudaMemGetInfo(&free_b, &total_b), "cudaMemGetInfo");
+  // keep the buffers already allocated in the budget
+  size_t owned = 0;
+  for (int b = 0; b < 3; ++b) owned += ws->pb[b].bytes + ws->ab[b].bytes;
+  owned += ws->g.bytes + ws->gc.bytes + ws->dbuf.bytes + ws->ck.bytes;
+  for (int k = 0; k < 2; ++k)
+    for (int d = 0; d < 3; ++d) owned += ws->psi[k][d].bytes + ws->apsi[k][d].bytes;
+  const double budget = 0.85 * (double)(free_b + owned);
+  std::vector<std::vector<HostShot>> groups;
+  size_t i = 0;
+  while (i < order.size()) {
+    const int max_nt = order[i].nt;  // sorted descending: the first of a group is the longest
+    const size_t per = per_shot_bytes(ws, grad, max_nt);
+    size_t cnt = (size_t)std::max(1.0, std::floor(budget / (double)per));
+    cnt = std::min(cnt, order.size() - i);
+    groups.emplace_back(order.begin() + i, order.begin() + i + cnt);
+    i += cnt;
+  }
+  return groups;
+}
+
+std::vector<HostShot> sorted_order(int nshots, const sw_acoustic_shot* shots) {
+  std::vector<HostShot> order(nshots);
+  for (int k = 0; k < nshots; ++k) order[k] = HostShot{k, shots[k].nt};
+  std::stable_sort(order.begin(), order.end(), [](const HostShot& a, const HostShot& b) { return a.nt > b.nt; });
+  return order;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// Entry points used by api.cu
+// ---------------------------------------------------------------------------
+namespace swgb {
+
+void wavesim_init(sw_wavesim* ws, sw_ctx* ctx, const sw_acoustic_params* p, int gradient, const sw_grad_params* gp) {
+  if (!p) fail(SW_ERR_ARG, "params is NULL");
+  if (p->ndim != 2 && p->ndim != 3) fail(SW_ERR_ARG, "Only 2D and 3D acoustic simulations are supported");
+  if (p->halo < 0) fail(SW_ERR_ARG, "CPML halo size must be non-negative!");
+  if (!(p->dt > 0)) fail(SW_ERR_ARG, "Timestep size must be positive!");
+  for (int d = 0; d < p->ndim; ++d) {
+    if (p->n[d] <= 0) fail(SW_ERR_ARG, "All numbers of grid points must be positive!");
+    if (!(p->h[d] > 0)) fail(SW_ERR_ARG, "All grid spacings must be positive!");
+    const bool cpml_axis = !(p->freetop && d == p->ndim - 1);
+    if (cpml_axis && p->n[d] < 2 * p->halo + 3) {
+      std::ostringstream os;
+      os << "Number grid points in the dimensions with C-PML boundaries must be at least 2*halo+3 = "
+         << 2 * p->halo + 3 << "!";
+      fail(SW_ERR_ARG, os.str());
+    }
+    if (!cpml_axis && p->n[d] < 2 * p->halo + 3) {
+      std::ostringstream os;
+      os << "the free-surface axis needs at least 2*halo+3 = " << 2 * p->halo + 3
+         << " grid points in this backend (its two damping strips must not overlap)";
+      fail(SW_ERR_UNSUPPORTED, os.str());
+    }
+  }
+  ws->ctx = ctx;
+  ws->prm = *p;
+  ws->gradient = gradient != 0;
+  if (ws->gradient) {
+    ws->gp = gp ? *gp : sw_grad_params{1, 0, 0, 0, 0};
+    if (ws->gp.check_freq < 1) fail(SW_ERR_ARG, "check_freq must be positive");
+    if (ws->gp.mute_radius_src < 0 || ws->gp.mute_radius_rec < 0)
+      fail(SW_ERR_ARG, "mutearoundpoint!(): The smoothing radius must be positive.");
+    if (ws->gp.snapshot_bf16) fail(SW_ERR_UNSUPPORTED, "BF16 checkpoint snapshots are not available in this build");
+  }
+  ws->N = p->ndim;
+  for (int d = 0; d < 3; ++d) ws->n[d] = d < p->ndim ? p->n[d] : 1;
+  ws->P = (int)round_up(ws->n[0], 32);
+  ws->F = (long long)ws->P * ws->n[1] * (ws->N == 3 ? ws->n[2] : 1);
+  ws->npts = (long long)ws->n[0] * ws->n[1] * (ws->N == 3 ? ws->n[2] : 1);
+  const int H = p->halo;
+  ws->strip_total = 0;
+  for (int d = 0; d < ws->N; ++d) {
+    long long ps = 1, xs = 1;
+    for (int e = 0; e < ws->N; ++e) {
+      const long long ext = e == 0 ? ws->P : ws->n[e];
+      ps *= e == d ? 2 * H : ext;
+      xs *= e == d ? 2 * H + 2 : ext;
+    }
+    ws->psz[d] = std::max<long long>(ps, 4);
+    ws->xsz[d] = std::max<long long>(xs, 4);
+    ws->strip_total += ws->psz[d] + ws->xsz[d];
+  }
+  dev_alloc(ws->vp, (size_t)ws->npts * sizeof(float), "vp");
+  dev_alloc(ws->fact, (size_t)ws->F * sizeof(float), "fact");
+}
+
+void wavesim_set_vp(sw_wavesim* ws, const float* vp, bool on_device) {
+  if (!vp) fail(SW_ERR_ARG, "vp is NULL");
+  cudaStream_t st = ws->ctx->stream;
+  if (!on_device) {
+    for (long long c = 0; c < ws->npts; ++c)
+      if (!(vp[c] > 0)) fail(SW_ERR_ARG, "Pressure velocity material property must be positive!");
+  }
+  check_cuda(cudaMemcpyAsync(ws->vp.p, vp, ws->npts * sizeof(float),
+                             on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, st),
+             "vp upload");
+  const double dt = ws->prm.dt;
+  k_set_fact<<<std::min<long long>((ws->npts + 255) / 256, 4096), 256, 0, st>>>(
+      ws->vp.as<float>(), ws->n[0], ws->npts, ws->P, dt * dt, ws->fact.as<float>());
+  check_cuda(cudaGetLastError(), "fact launch");
+  ws->has_vp = true;
+}
+
+void acoustic_forward(sw_wavesim* ws, int nshots, const sw_acoustic_shot* shots, bool on_device) {
+  if (!ws->has_vp) fail(SW_ERR_STATE, "material properties not set (sw_wavesim_set_vp)");
+  if (nshots < 1 || !shots) fail(SW_ERR_ARG, "no shots");
+  for (int k = 0; k < nshots; ++k) validate_shot(ws, shots[k], k, false);
+  const std::vector<HostShot> order = sorted_order(nshots, shots);
+  for (const auto& group : plan_groups(ws, order, false)) {
+    ensure_state(ws, (int)group.size(), false, group.front().nt);
+    Tables T;
+    build_tables(ws, shots, group, on_device, false, T);
+    forward_group(ws, group, false);
+    download_traces(ws, shots, group, on_device);
+  }
+  check_cuda(cudaStreamSynchronize(ws->ctx->stream), "forward");
+  ws->ctx->prof.resolve();
+}
+
+void acoustic_gradient(sw_wavesim* ws, int nshots, const sw_acoustic_shot* shots, bool on_device, double* grad,
+                       double* misfit) {
+  if (!ws->gradient) fail(SW_ERR_STATE, "The wavesim object was not built for gradient computations.");
+  if (!ws->has_vp) fail(SW_ERR_STATE, "material properties not set (sw_wavesim_set_vp)");
+  if (nshots < 1 || !shots) fail(SW_ERR_ARG, "no shots");
+  if (!grad) fail(SW_ERR_ARG, "grad output is NULL");
+  for (int k = 0; k < nshots; ++k) validate_shot(ws, shots[k], k, true);
+  const bool mute = ws->gp.mute_radius_src > 0 || ws->gp.mute_radius_rec > 0;
+  if (mute)
+    for (int k = 0; k < nshots; ++k) {
+      const sw_acoustic_shot& s = shots[k];
+      if ((ws->gp.mute_radius_src > 0 && !s.src_pos) || (ws->gp.mute_radius_rec > 0 && !s.rec_pos))
+        fail(SW_ERR_ARG, "muting needs src_pos / rec_pos");
+      auto chk = [&](const double* pos, int np) {
+        for (int p = 0; p < np; ++p)
+          for (int d = 0; d < ws->N; ++d) {
+            const double x = pos[p + (long long)d * np], ext = ws->prm.h[d] * (ws->n[d] - 1);
+            if (!(0.0 <= x && x <= ext)) fail(SW_ERR_ARG, "mutearoundpoint!(): The point lies outside the grid");
+          }
+      };
+      if (ws->gp.mute_radius_src > 0) chk(s.src_pos, s.nsrc);
+      if (ws->gp.mute_radius_rec > 0) chk(s.rec_pos, s.nrec);
+    }
+  cudaStream_t st = ws->ctx->stream;
+  const std::vector<HostShot> order = sorted_order(nshots, shots);
+  DevMem dgrad, dmis;
+  double* gout = grad;
+  double* mout = misfit;
+  if (!on_device) {
+    dev_alloc(dgrad, (size_t)ws->npts * sizeof(double), "gradient output");
+    gout = dgrad.as<double>();
+    dev_alloc(dmis, sizeof(double), "misfit output");
+    mout = dmis.as<double>();
+  } else if (!mout) {
+    dev_alloc(dmis, sizeof(double), "misfit output");
+    mout = dmis.as<double>();
+  }
+  bool first_group = true;
+  for (const auto& group : plan_groups(ws, order, true)) {
+    const int S = (int)group.size();
+    const int max_nt = group.front().nt;
+    ensure_state(ws, S, true, max_nt);
+    Tables T;
+    build_tables(ws, shots, group, on_device, true, T);
+    forward_group(ws, group, true);
+    download_traces(ws, shots, group, on_device);
+    // misfit and adjoint source
+    const int nblk = 64;
+    ensure(ws->d_partial, (size_t)nblk * S * sizeof(double), "misfit partials");
+    {
+      cudaEvent_t ev = nullptr;
+      ws->ctx->prof.begin(st, KK_OTHER, 0.0, &ev);
+      k_misfit_adjsrc<<<dim3(nblk, S), 256, 0, st>>>(ws->d_desc.as<ShotDesc>(), ws->d_rec.as<long long>(),
+                                                     ws->fact.as<float>(), ws->d_partial.as<double>());
+      k_misfit_sum<<<1, 256, 0, st>>>(ws->d_partial.as<double>(), nblk, S, mout, first_group ? 0 : 1);
+      check_cuda(cudaGetLastError(), "misfit launch");
+      ws->ctx->prof.end(st, KK_OTHER, ev);
+    }
+    adjoint_group(ws, group);
+    if (mute) {
+      // sources first, then receivers, like the reference; rmax depends on the radius
+      double hmax = 0;
+      for (int d = 0; d < ws->N; ++d) hmax = std::max(hmax, ws->prm.h[d]);
+      for (int fam = 0; fam < 2; ++fam) {
+        const int radius = fam == 0 ? ws->gp.mute_radius_src : ws->gp.mute_radius_rec;
+        if (radius <= 0) continue;
+        std::vector<MutePoint> pts;
+        std::vector<int> ptr(S + 1, 0);
+        for (int k = 0; k < S; ++k) {
+          const sw_acoustic_shot& s = shots[group[k].orig];
+          const double* pos = fam == 0 ? s.src_pos : s.rec_pos;
+          const int np = fam == 0 ? s.nsrc : s.nrec;
+          for (int p = 0; p < np; ++p) {
+            MutePoint m{};
+            m.shot = k;
+            for (int d = 0; d < ws->N; ++d) {
+              const double x = pos[p + (long long)d * np], h = ws->prm.h[d];
+              const int ijk = (int)std::round((x - std::fmod(x, h)) / h) + 1;  // floor(Int, div(x, h)) + 1
+              m.lo[d] = ijk - radius;
+              m.hi[d] = ijk + radius;
+              m.pos[d] = x;
+            }
+            pts.push_back(m);
+          }
+          ptr[k + 1] = (int)pts.size();
+        }
+        upload(ws, ws->d_mute, pts, "mute points");
+        upload(ws, ws->d_mute_ptr, ptr, "mute csr");
+        k_mute<<<S, 256, 0, st>>>(ws->d_mute.as<MutePoint>(), ws->d_mute_ptr.as<int>(), ws->N, ws->n[0], ws->n[1],
+                                  ws->n[2], ws->P, ws->prm.h[0], ws->prm.h[1], ws->prm.h[2], radius * hmax,
+                                  fa(ws->g, ws->F), fa(ws->gc, ws->F));
+        check_cuda(cudaGetLastError(), "mute launch");
+        check_cuda(cudaStreamSynchronize(st), "mute");
+      }
+    }
+    {
+      cudaEvent_t ev = nullptr;
+      ws->ctx->prof.begin(st, KK_OTHER, 0.0, &ev);
+      const long long blocks = std::min<long long>((ws->npts + 255) / 256, 8192);
+      k_reduce_grad<<<(unsigned)blocks, 256, 0, st>>>(ws->g.as<float>(), ws->gc.as<float>(), ws->F, S,
+                                                      ws->vp.as<float>(), ws->n[0], ws->npts, ws->P, gout,
+                                                      first_group ? 0 : 1);
+      check_cuda(cudaGetLastError(), "gradient reduction launch");
+      ws->ctx->prof.end(st, KK_OTHER, ev);
+    }
+    first_group = false;
+  }
+  if (!on_device) {
+    check_cuda(cudaMemcpyAsync(grad, gout, ws->npts * sizeof(double), cudaMemcpyDeviceToHost, st), "grad download");
+    if (misfit) check_cuda(cudaMemcpyAsync(misfit, mout, sizeof(double), cudaMemcpyDeviceToHost, st), "misfit download");
+  }
+  check_cuda(cudaStreamSynchronize(st), "gradient");
+  ws->ctx->prof.resolve();
+}
+
+void wavesim_set_tile(sw_wavesim* ws, int tz) { ws->tile_tz = tz; }
+sw_ctx* wavesim_ctx(sw_wavesim* ws) { return ws->ctx; }
+sw_wavesim* wavesim_new() { return new sw_wavesim(); }
+void wavesim_delete(sw_wavesim* ws) { delete ws; }
+
+}  // namespace swgb

@@ -1,0 +1,217 @@
+"""GPU parity of the acoustic constant-density path against the FP64 CPU oracle.
+
+Every test calls libswgb300 through its C ABI (tests/cases.py:GpuRun) with
+the same inputs the oracle gets.  Tolerances are the ones the FP32 backend is
+held to against the FP64 restatement of the reference: traces within 1e-5
+relative L2, misfit within 1e-6, gradient within 1e-5.
+"""
+import numpy as np
+import pytest
+
+from cases import Case, GpuRun, make_shot, oracle_forward, oracle_gradient, rel_l2, smooth_model, stable_dt
+
+pytestmark = pytest.mark.gpu
+
+TRACE_TOL = 1e-5
+MISFIT_TOL = 1e-6
+GRAD_TOL = 1e-5
+
+
+def _case2d(nx, nz, h, halo, freetop, seed=1, frac=0.6, vmin=1500.0, vmax=3000.0):
+    vp = smooth_model((nx, nz), vmin, vmax, seed)
+    return Case(vp=vp, h=(h, h), dt=stable_dt(vp, (h, h), frac), halo=halo, freetop=freetop)
+
+
+def _extent(case):
+    return [h * (n - 1) for n, h in zip(case.vp.shape, case.h)]
+
+
+@pytest.mark.parametrize("halo,freetop", [(20, False), (20, True), (8, True), (3, False), (2, False), (1, False),
+                                          (0, False)])
+def test_forward_2d_matches_oracle(sw, oracle, halo, freetop):
+    case = _case2d(120 + 3, 97, 8.0, halo, freetop, seed=halo)
+    ex = _extent(case)
+    nt = 500
+    recx = np.linspace(0.1 * ex[0], 0.9 * ex[0], 13)
+    shot = make_shot(case.h, ex, nt, case.dt, 14.0, [[0.43 * ex[0], 0.37 * ex[1]]],
+                     np.stack([recx, np.full_like(recx, 0.6 * ex[1])], 1))
+    run = GpuRun(sw, case)
+    tr = run.forward([shot])[0]
+    run.close()
+    ref = oracle_forward(oracle, sw, case, shot)
+    assert np.all(np.isfinite(tr))
+    assert rel_l2(tr, ref) < TRACE_TOL
+
+
+def test_forward_2d_odd_grid_duplicates_and_boundary(sw, oracle):
+    """Ragged 23x29 grid, halo 3: sources and receivers sharing grid points,
+    receivers on the outermost lines and a source on the free surface."""
+    case = _case2d(23, 29, 5.0, 3, True, seed=7)
+    ex = _extent(case)
+    nt = 240
+    src = [[0.5 * ex[0], 0.0], [0.5 * ex[0], 0.0], [0.3 * ex[0], 0.5 * ex[1]]]
+    rec = [[0.0, 0.2 * ex[1]], [ex[0], ex[1]], [0.3 * ex[0], 0.5 * ex[1]], [0.3 * ex[0], 0.5 * ex[1]],
+           [0.7 * ex[0], 0.4 * ex[1]], [0.5 * ex[0], 0.0]]
+    shot = make_shot(case.h, ex, nt, case.dt, 20.0, src, rec)
+    run = GpuRun(sw, case)
+    tr = run.forward([shot])[0]
+    run.close()
+    ref = oracle_forward(oracle, sw, case, shot)
+    assert rel_l2(tr, ref) < TRACE_TOL
+    # the duplicated receivers see the same value
+    assert np.array_equal(tr[:, 2], tr[:, 3])
+
+
+def test_forward_batched_equals_single(sw, oracle):
+    """Shots with different nt and receiver counts in one call: each matches
+    the oracle and is bit-identical to running it alone."""
+    case = _case2d(150, 110, 10.0, 12, False, seed=3)
+    ex = _extent(case)
+    rng = np.random.default_rng(5)
+    shots = []
+    for k, nt in enumerate([420, 300, 511, 300]):
+        nrec = int(rng.integers(3, 17))
+        recx = np.linspace(0.15 * ex[0], 0.85 * ex[0], nrec)
+        shots.append(make_shot(case.h, ex, nt, case.dt, 12.0, [[(0.2 + 0.2 * k) * ex[0], 0.3 * ex[1]]],
+                               np.stack([recx, np.full_like(recx, 0.5 * ex[1])], 1)))
+    run = GpuRun(sw, case)
+    batched = run.forward(shots)
+    singles = [run.forward([s])[0] for s in shots]
+    run.close()
+    for s, b, one in zip(shots, batched, singles):
+        assert b.shape == (s.nt, s.rec_pos.shape[0])
+        assert np.array_equal(b, one)
+        assert rel_l2(b, oracle_forward(oracle, sw, case, s)) < TRACE_TOL
+
+
+def test_forward_2d_long_run(sw, oracle):
+    """3000 steps on a 301x201 smooth model: FP32 error growth stays inside the bound."""
+    case = _case2d(301, 201, 5.0, 20, False, seed=11, vmin=1500.0, vmax=3500.0)
+    ex = _extent(case)
+    recx = np.linspace(0.05 * ex[0], 0.95 * ex[0], 41)
+    shot = make_shot(case.h, ex, 3000, case.dt, 10.0, [[0.5 * ex[0], 0.12 * ex[1]]],
+                     np.stack([recx, np.full_like(recx, 0.1 * ex[1])], 1))
+    run = GpuRun(sw, case)
+    tr = run.forward([shot])[0]
+    run.close()
+    assert rel_l2(tr, oracle_forward(oracle, sw, case, shot)) < TRACE_TOL
+
+
+def _grad_case(sw, oracle, nt=400, freetop=False, halo=10, seed=2):
+    case = _case2d(110, 90, 10.0, halo, freetop, seed=seed)
+    ex = _extent(case)
+    recx = np.linspace(0.1 * ex[0], 0.9 * ex[0], 9)
+    shot = make_shot(case.h, ex, nt, case.dt, 12.0, [[0.35 * ex[0], 0.25 * ex[1]]],
+                     np.stack([recx, np.full_like(recx, 0.2 * ex[1])], 1))
+    pert = Case(vp=np.asfortranarray(case.vp * 1.05), h=case.h, dt=case.dt, halo=case.halo,
+                freetop=case.freetop)
+    shot.observed = oracle_forward(oracle, sw, pert, shot)
+    return case, shot
+
+
+@pytest.mark.parametrize("check_freq", [1, 7, 20])
+def test_gradient_2d_matches_oracle(sw, oracle, check_freq):
+    case, shot = _grad_case(sw, oracle)
+    run = GpuRun(sw, case, gradient=True, check_freq=check_freq)
+    g, msf, tr = run.gradient([shot])
+    run.close()
+    gref, mref, tref = oracle_gradient(oracle, sw, case, shot, check_freq=check_freq)
+    assert rel_l2(tr[0], tref) < TRACE_TOL
+    assert abs(msf - mref) / abs(mref) < MISFIT_TOL
+    assert rel_l2(g, gref) < GRAD_TOL
+
+
+def test_gradient_checkpointing_is_exact(sw, oracle):
+    """check_freq = floor(sqrt(nt)) gives the same gradient bits as storing every step."""
+    case, shot = _grad_case(sw, oracle, nt=500)
+    r1 = GpuRun(sw, case, gradient=True, check_freq=1)
+    g1, m1, _ = r1.gradient([shot])
+    r1.close()
+    r2 = GpuRun(sw, case, gradient=True, check_freq=int(np.sqrt(500)))
+    g2, m2, _ = r2.gradient([shot])
+    r2.close()
+    assert np.array_equal(g1, g2) and m1 == m2
+    assert np.any(g1 != 0)
+
+
+def test_gradient_windows_invcov_mute_freetop(sw, oracle):
+    case, shot = _grad_case(sw, oracle, nt=360, freetop=True, halo=8, seed=4)
+    rng = np.random.default_rng(3)
+    shot.invcov = rng.uniform(0.5, 2.0, shot.nt)
+    shot.windows = [(20, 150), (200, 330)]
+    run = GpuRun(sw, case, gradient=True, check_freq=9, mute_src=4, mute_rec=2)
+    g, msf, _ = run.gradient([shot])
+    run.close()
+    gref, mref, _ = oracle_gradient(oracle, sw, case, shot, check_freq=9, mute_src=4, mute_rec=2)
+    assert abs(msf - mref) / abs(mref) < MISFIT_TOL
+    assert rel_l2(g, gref) < GRAD_TOL
+
+
+def test_gradient_batched_shots_sum(sw, oracle):
+    """Several shots with different nt in one call: gradient = sum of the
+    oracle's per-shot gradients, misfit = sum of misfits."""
+    case = _case2d(120, 100, 10.0, 10, False, seed=9)
+    ex = _extent(case)
+    shots = []
+    pert = Case(vp=np.asfortranarray(case.vp * 0.97), h=case.h, dt=case.dt, halo=case.halo, freetop=False)
+    for k, nt in enumerate([350, 280, 401]):
+        nrec = 5 + 3 * k
+        recx = np.linspace(0.1 * ex[0], 0.9 * ex[0], nrec)
+        s = make_shot(case.h, ex, nt, case.dt, 12.0, [[(0.25 + 0.25 * k) * ex[0], 0.2 * ex[1]]],
+                      np.stack([recx, np.full_like(recx, 0.15 * ex[1])], 1))
+        s.observed = oracle_forward(oracle, sw, pert, s)
+        shots.append(s)
+    run = GpuRun(sw, case, gradient=True, check_freq=10)
+    g, msf, _ = run.gradient(shots)
+    run.close()
+    gref = np.zeros_like(g)
+    mref = 0.0
+    for s in shots:
+        gg, mm, _ = oracle_gradient(oracle, sw, case, s, check_freq=10)
+        gref += gg
+        mref += mm
+    assert abs(msf - mref) / abs(mref) < MISFIT_TOL
+    assert rel_l2(g, gref) < GRAD_TOL
+
+
+def test_gradient_rejects_boundary_source_with_checkpoints(sw, oracle):
+    case, shot = _grad_case(sw, oracle, nt=200, freetop=True)
+    shot.src_pos = np.array([[0.5 * _extent(case)[0], 0.0]])
+    run = GpuRun(sw, case, gradient=True, check_freq=10)
+    with pytest.raises(sw._lib.SwError) as e:
+        run.gradient([shot])
+    assert e.value.code == sw._lib.SW_ERR_UNSUPPORTED
+    run.close()
+
+
+def _case3d(n, h, halo, freetop, seed=1):
+    vp = smooth_model(n, 1800.0, 3200.0, seed, blobs=3)
+    return Case(vp=vp, h=(h, h, h), dt=stable_dt(vp, (h, h, h), 0.6), halo=halo, freetop=freetop)
+
+
+@pytest.mark.parametrize("halo,freetop", [(5, False), (6, True), (0, False)])
+def test_forward_3d_matches_oracle(sw, oracle, halo, freetop):
+    case = _case3d((37, 29, 33), 10.0, halo, freetop, seed=halo + 1)
+    ex = _extent(case)
+    rec = [[0.2 * ex[0], 0.3 * ex[1], 0.5 * ex[2]], [0.8 * ex[0], 0.6 * ex[1], 0.4 * ex[2]],
+           [0.5 * ex[0], 0.5 * ex[1], 0.9 * ex[2]]]
+    shot = make_shot(case.h, ex, 260, case.dt, 15.0, [[0.45 * ex[0], 0.55 * ex[1], 0.35 * ex[2]]], rec)
+    run = GpuRun(sw, case)
+    tr = run.forward([shot])[0]
+    run.close()
+    assert rel_l2(tr, oracle_forward(oracle, sw, case, shot)) < TRACE_TOL
+
+
+def test_gradient_3d_matches_oracle(sw, oracle):
+    case = _case3d((34, 30, 32), 10.0, 5, False, seed=4)
+    ex = _extent(case)
+    rec = [[x, 0.5 * ex[1], 0.3 * ex[2]] for x in np.linspace(0.2 * ex[0], 0.8 * ex[0], 5)]
+    shot = make_shot(case.h, ex, 200, case.dt, 15.0, [[0.5 * ex[0], 0.5 * ex[1], 0.6 * ex[2]]], rec)
+    pert = Case(vp=np.asfortranarray(case.vp * 1.04), h=case.h, dt=case.dt, halo=case.halo, freetop=False)
+    shot.observed = oracle_forward(oracle, sw, pert, shot)
+    run = GpuRun(sw, case, gradient=True, check_freq=13)
+    g, msf, _ = run.gradient([shot])
+    run.close()
+    gref, mref, _ = oracle_gradient(oracle, sw, case, shot, check_freq=13)
+    assert abs(msf - mref) / abs(mref) < MISFIT_TOL
+    assert rel_l2(g, gref) < GRAD_TOL

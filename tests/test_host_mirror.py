@@ -1,0 +1,54 @@
+"""Host logic of the reference-API mirror (no GPU): rounding, source scaling,
+the L2 misfit and the checks the reference asserts."""
+import numpy as np
+import pytest
+
+
+def test_nearest_grid_points_ties_up(sw):
+    # RoundNearestTiesUp of pos/h + 1
+    idx = sw.nearest_grid_points(np.array([[2.5, 7.5], [0.0, 12.49], [4.999, 5.0]]), (5.0, 5.0))
+    assert idx.tolist() == [[2, 3], [1, 3], [2, 2]]
+    assert idx.dtype == np.int32 and idx.flags.f_contiguous
+
+
+def test_scale_srctf(sw):
+    vp = np.asfortranarray(np.arange(1, 13, dtype=float).reshape(3, 4, order="F") * 100)
+    tf = np.ones((5, 2))
+    si = np.array([[2, 3], [1, 1]], dtype=np.int32)
+    out = sw.scale_srctf(tf, si, vp, (2.0, 4.0), 1e-3)
+    assert out.dtype == np.float32
+    np.testing.assert_allclose(out[:, 0], 1e-6 / 8.0 * vp[1, 2] ** 2, rtol=1e-6)
+    np.testing.assert_allclose(out[:, 1], 1e-6 / 8.0 * vp[0, 0] ** 2, rtol=1e-6)
+
+
+def test_l2_misfit(sw):
+    rng = np.random.default_rng(0)
+    obs = rng.standard_normal((50, 3))
+    syn = rng.standard_normal((50, 3))
+    recs = sw.ScalarReceivers(np.zeros((3, 2)), 50)
+    recs.seismograms[...] = syn
+    ic = rng.uniform(0.5, 2, 50)
+    m = sw.L2Misfit(observed=obs, invcov=np.diag(ic), windows=[(5, 20), (30, 40)])
+    mask = np.zeros(50)
+    mask[4:20] = 1
+    mask[29:40] = 1
+    r = mask[:, None] * (syn - obs)
+    assert np.isclose(m.calcmisfit(recs), 0.5 * np.sum(r * ic[:, None] * r))
+    np.testing.assert_allclose(m.dchi_du(recs), ic[:, None] * r)
+    np.testing.assert_allclose(m.invcov_diagonal(), ic)
+    dense = sw.L2Misfit(observed=obs, invcov=np.ones((50, 50)))
+    with pytest.raises(NotImplementedError):
+        dense.invcov_diagonal()
+    with pytest.raises(AssertionError):
+        sw.L2Misfit(observed=obs, windows=[(0, 3)])
+
+
+def test_parameter_checks(sw):
+    with pytest.raises(AssertionError, match="positive"):
+        sw.InputParametersAcoustic(0, 1e-3, (10, 10), (1.0, 1.0), sw.CPMLBoundaryConditionParameters())
+    with pytest.raises(AssertionError):
+        sw.GradParameters(check_freq=0)
+    with pytest.raises(AssertionError, match="at least one source"):
+        sw.ScalarSources(np.zeros((0, 2)), np.zeros((10, 0)), 5.0)
+    assert sw.courant_number(np.full((3, 3), 2000.0), 1e-3, (5.0, 5.0)) == pytest.approx(2000 * 1e-3 * np.sqrt(0.08))
+    assert sw.points_per_wavelength(np.full((3, 3), 1500.0), (10.0, 8.0), 8.0) == pytest.approx(1500 / 160)
