@@ -51,31 +51,57 @@ struct ShotDesc {
   const float* ic;           // (nt) or nullptr
   const float* mask;         // (nt) or nullptr
   float* adj;                // (nt, nrec) adjoint source (prescaled)
+  float* ring;               // 3 values per boundary injection point (see k_inject_record)
 };
+
+// Boundary injection points.  The reference never updates the outermost grid
+// nodes and rotates three pressure buffers, so a node on the boundary that
+// receives an injection evolves as p[t] = p[t-3] + s[t].  The increment-form
+// stencil keeps two pressure buffers, so such nodes carry their own 3-value
+// ring (slot t mod 3 holds p[t-3] before the update) and are written here.
+__device__ __forceinline__ float ring_update(float* ring, int slot, int it, float add, float* second_diff) {
+  float* r = ring + 3 * slot;
+  const float v = r[it % 3] + add;
+  r[it % 3] = v;
+  if (second_diff) *second_diff = v - 2.f * r[(it + 2) % 3] + r[(it + 1) % 3];
+  return v;
+}
 
 // inject_sources! + record_receivers! for every active shot: one block per
 // shot.  Duplicated points are summed in source order by one thread, like the
-// reference's serial loop.  Optionally adds the injected amount to D.
+// reference's serial loop.  Interior points add the source to p[n+1] and to
+// the increment d[n+1] (and to D when the gradient keeps it).
 __global__ void k_inject_record(const ShotDesc* __restrict__ desc, const long long* __restrict__ pts,
                                 const int* __restrict__ ptr, const int* __restrict__ ids,
-                                const long long* __restrict__ rec_lin, FieldArg pnew, FieldArg dfield,
-                                int d_first, int it, int record) {
+                                const int* __restrict__ bslot, const long long* __restrict__ rec_lin,
+                                FieldArg pnew, FieldArg dnew, FieldArg dfield, int d_first, int it, int record) {
   const int shot = blockIdx.x;
   const ShotDesc D = desc[shot];
   if (it > D.nt) return;
   float* pn = pnew.p + (long long)shot * pnew.s;
+  float* dn = dnew.p + (long long)shot * dnew.s;
   float* dd = (dfield.p && shot >= d_first) ? dfield.p + (long long)shot * dfield.s : nullptr;
   for (int u = threadIdx.x; u < D.nsp; u += blockDim.x) {
     const long long lin = pts[D.sp_off + u];
-    float acc = pn[lin];
     float add = 0.f;
-    for (int k = ptr[D.sp_ptr + u]; k < ptr[D.sp_ptr + u + 1]; ++k) {
-      const float v = D.tf[(long long)(it - 1) + (long long)ids[k] * D.nt];
-      acc += v;
-      add += v;
+    const int k0 = ptr[D.sp_ptr + u], k1 = ptr[D.sp_ptr + u + 1];
+    const int slot = bslot[D.sp_off + u];
+    if (slot >= 0) {
+      for (int k = k0; k < k1; ++k) add += D.tf[(long long)(it - 1) + (long long)ids[k] * D.nt];
+      float sd;
+      pn[lin] = ring_update(D.ring, slot, it, add, &sd);
+      if (dd) dd[lin] = sd;
+    } else {
+      float acc = pn[lin];
+      for (int k = k0; k < k1; ++k) {
+        const float v = D.tf[(long long)(it - 1) + (long long)ids[k] * D.nt];
+        acc += v;
+        add += v;
+      }
+      pn[lin] = acc;
+      dn[lin] += add;
+      if (dd) dd[lin] += add;
     }
-    pn[lin] = acc;
-    if (dd) dd[lin] += add;
   }
   if (!record) return;
   __syncthreads();
@@ -85,29 +111,44 @@ __global__ void k_inject_record(const ShotDesc* __restrict__ desc, const long lo
 
 // Adjoint injection at the receivers (adjoint_onestep_CPML! -> inject_sources!
 // with the prescaled residuals) and the matching correlation term: the fused
-// stencil correlated lambda before injection, so g += a * D is added here.
+// stencil correlated interior lambda before injection, so g += a * D is added
+// here (boundary nodes, which the stencil skips, add their full lambda * D).
 __global__ void k_adj_inject(const ShotDesc* __restrict__ desc, const long long* __restrict__ pts,
-                             const int* __restrict__ ptr, const int* __restrict__ ids, FieldArg lam,
-                             FieldArg dcorr, FieldArg g, FieldArg gc, int it) {
+                             const int* __restrict__ ptr, const int* __restrict__ ids,
+                             const int* __restrict__ bslot, FieldArg lam, FieldArg lamd, FieldArg dcorr, FieldArg g,
+                             FieldArg gc, int it) {
   const int shot = blockIdx.x;
   const ShotDesc D = desc[shot];
   if (it > D.nt) return;
   float* lp = lam.p + (long long)shot * lam.s;
+  float* ld = lamd.p + (long long)shot * lamd.s;
   const float* dp = dcorr.p + (long long)shot * dcorr.s;
   float* gp = g.p + (long long)shot * g.s;
   float* cp = gc.p + (long long)shot * gc.s;
   for (int u = threadIdx.x; u < D.nrp; u += blockDim.x) {
     const long long lin = pts[D.rp_off + u];
-    float acc = lp[lin];
-    float add = 0.f;
-    for (int k = ptr[D.rp_ptr + u]; k < ptr[D.rp_ptr + u + 1]; ++k) {
-      const float v = D.adj[(long long)(it - 1) + (long long)ids[k] * D.nt];
-      acc += v;
-      add += v;
+    const int k0 = ptr[D.rp_ptr + u], k1 = ptr[D.rp_ptr + u + 1];
+    const int slot = bslot[D.rp_off + u];
+    float add = 0.f, corr;
+    if (slot >= 0) {
+      // the adjoint iterates it = nt..1; its ring is indexed by the adjoint step count
+      for (int k = k0; k < k1; ++k) add += D.adj[(long long)(it - 1) + (long long)ids[k] * D.nt];
+      const float v = ring_update(D.ring, slot, D.nt - it + 1, add, nullptr);
+      lp[lin] = v;
+      corr = v;
+    } else {
+      float acc = lp[lin];
+      for (int k = k0; k < k1; ++k) {
+        const float v = D.adj[(long long)(it - 1) + (long long)ids[k] * D.nt];
+        acc += v;
+        add += v;
+      }
+      lp[lin] = acc;
+      ld[lin] += add;
+      corr = add;
     }
-    lp[lin] = acc;
     float gv = gp[lin], cv = cp[lin];
-    kahan_add(gv, cv, add * dp[lin]);
+    kahan_add(gv, cv, corr * dp[lin]);
     gp[lin] = gv;
     cp[lin] = cv;
   }
@@ -252,8 +293,8 @@ struct sw_wavesim {
   DevMem vp, fact;
   // capacity (shots) of the state buffers
   int cap = 0;
-  DevMem pb[3], psi[2][3], xi[3];     // forward state
-  DevMem ab[3], apsi[2][3], axi[3];   // adjoint state
+  DevMem pb[2], db, psi[2][3], xi[3];     // forward state: p ping-pong, increment d, psi ping-pong, xi
+  DevMem ab[2], adb, apsi[2][3], axi[3];  // adjoint state
   DevMem g, gc;
   DevMem dbuf;                         // D slots
   long long d_slots = 0;
@@ -261,7 +302,8 @@ struct sw_wavesim {
   long long ck_slots = 0;
   DevMem zero;                         // zero state (one shot, stride 0)
   // tables
-  DevMem d_desc, d_pts, d_ptr, d_ids, d_rec, d_tf, d_tr, d_obs, d_ic, d_mask, d_adj, d_cpml, d_partial, d_mis;
+  DevMem d_desc, d_pts, d_ptr, d_ids, d_bslot, d_rec, d_tf, d_tr, d_obs, d_ic, d_mask, d_adj, d_cpml, d_partial, d_mis;
+  DevMem d_ring;  // boundary-injection rings (3 floats per point)
   DevMem d_mute, d_mute_ptr;
   int tile_tz = 0;  // 0 = heuristic
 };
@@ -275,16 +317,16 @@ struct HostShot {
 
 inline long long round_up(long long v, long long m) { return (v + m - 1) / m * m; }
 
-void ensure(DevMem& m, size_t bytes, const char* what) {
+void ensure(sw_wavesim* ws, DevMem& m, size_t bytes, const char* what) {
   if (m.bytes >= bytes && m.p) return;
   m.release();
-  dev_alloc(m, bytes, what);
+  dev_alloc(m, bytes, what, ws->ctx->stream);
 }
 
 template <typename T>
 void upload(sw_wavesim* ws, DevMem& m, const std::vector<T>& v, const char* what) {
   const size_t bytes = std::max<size_t>(v.size() * sizeof(T), 16);
-  ensure(m, bytes, what);
+  ensure(ws, m, bytes, what);
   if (!v.empty())
     check_cuda(cudaMemcpyAsync(m.p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, ws->ctx->stream), what);
 }
@@ -293,6 +335,8 @@ struct Tables {
   std::vector<ShotDesc> desc;
   std::vector<long long> pts, rec;
   std::vector<int> ptr, ids;
+  std::vector<int> bslot;  // per unique point: ring slot (boundary node) or -1
+  int nring = 0;
   std::vector<HostShot> order;  // sorted by nt descending
   int max_nt = 0;
 };
@@ -302,14 +346,20 @@ long long lin_of(const sw_wavesim* ws, const int* I) {  // 1-based -> padded lin
   return ((long long)(I[2] - 1) * ws->n[1] + (I[1] - 1)) * ws->P + (I[0] - 1);
 }
 
-void unique_points(const sw_wavesim* ws, const int32_t* idx, int npos, Tables& T, long long& off,
-                   long long& ptr_off, int& nunique, std::vector<long long>* per_pos) {
+// Unique grid points of a list of positions (CSR of the position ids, in
+// order).  Points on the outermost grid lines get consecutive ring slots
+// starting at slot_base; returns the number of slots used.
+int unique_points(const sw_wavesim* ws, const int32_t* idx, int npos, Tables& T, long long& off,
+                  long long& ptr_off, int& nunique, int slot_base) {
   std::vector<long long> lin(npos);
+  std::vector<char> bnd(npos, 0);
   for (int p = 0; p < npos; ++p) {
     int I[3] = {1, 1, 1};
-    for (int d = 0; d < ws->N; ++d) I[d] = idx[p + (long long)d * npos];
+    for (int d = 0; d < ws->N; ++d) {
+      I[d] = idx[p + (long long)d * npos];
+      if (I[d] == 1 || I[d] == ws->n[d]) bnd[p] = 1;
+    }
     lin[p] = lin_of(ws, I);
-    if (per_pos) per_pos->push_back(lin[p]);
   }
   // unique points in order of first appearance; ids listed in position order
   std::vector<long long> uniq;
@@ -326,12 +376,15 @@ void unique_points(const sw_wavesim* ws, const int32_t* idx, int npos, Tables& T
   off = (long long)T.pts.size();
   ptr_off = (long long)T.ptr.size();
   nunique = (int)uniq.size();
+  int nr = 0;
   for (size_t u = 0; u < uniq.size(); ++u) {
     T.pts.push_back(uniq[u]);
+    T.bslot.push_back(bnd[members[u][0]] ? slot_base + nr++ : -1);
     T.ptr.push_back((int)T.ids.size());
     for (int m : members[u]) T.ids.push_back(m);
   }
   T.ptr.push_back((int)T.ids.size());
+  return nr;
 }
 
 void validate_shot(const sw_wavesim* ws, const sw_acoustic_shot& s, int k, bool grad) {
@@ -394,7 +447,9 @@ void build_tables(sw_wavesim* ws, const sw_acoustic_shot* shots, const std::vect
   cudaStream_t st = ws->ctx->stream;
   const int S = (int)group.size();
   T.desc.assign(S, ShotDesc{});
-  T.pts.clear(); T.rec.clear(); T.ptr.clear(); T.ids.clear();
+  T.pts.clear(); T.rec.clear(); T.ptr.clear(); T.ids.clear(); T.bslot.clear();
+  T.nring = 0;
+  std::vector<int> ring_off(S);
   long long tf_total = 0, tr_total = 0, ic_total = 0, mask_total = 0;
   for (int k = 0; k < S; ++k) {
     const sw_acoustic_shot& s = shots[group[k].orig];
@@ -404,15 +459,15 @@ void build_tables(sw_wavesim* ws, const sw_acoustic_shot* shots, const std::vect
     if (s.nwin > 0) mask_total += s.nt;
   }
   // device staging
-  if (!on_device) ensure(ws->d_tf, std::max<long long>(tf_total, 4) * sizeof(float), "srctf");
-  ensure(ws->d_tr, std::max<long long>(tr_total, 4) * sizeof(float), "traces");
+  if (!on_device) ensure(ws, ws->d_tf, std::max<long long>(tf_total, 4) * sizeof(float), "srctf");
+  ensure(ws, ws->d_tr, std::max<long long>(tr_total, 4) * sizeof(float), "traces");
   if (grad) {
     if (!on_device) {
-      ensure(ws->d_obs, std::max<long long>(tr_total, 4) * sizeof(float), "observed");
-      ensure(ws->d_ic, std::max<long long>(ic_total, 4) * sizeof(float), "invcov");
+      ensure(ws, ws->d_obs, std::max<long long>(tr_total, 4) * sizeof(float), "observed");
+      ensure(ws, ws->d_ic, std::max<long long>(ic_total, 4) * sizeof(float), "invcov");
     }
-    ensure(ws->d_mask, std::max<long long>(mask_total, 4) * sizeof(float), "window mask");
-    ensure(ws->d_adj, std::max<long long>(tr_total, 4) * sizeof(float), "adjoint source");
+    ensure(ws, ws->d_mask, std::max<long long>(mask_total, 4) * sizeof(float), "window mask");
+    ensure(ws, ws->d_adj, std::max<long long>(tr_total, 4) * sizeof(float), "adjoint source");
   }
   const int na = 2 * ws->prm.halo + 2, nh = 2 * ws->prm.halo;
   const int cstride = ws->N * (2 * na + 2 * nh);
@@ -424,8 +479,12 @@ void build_tables(sw_wavesim* ws, const sw_acoustic_shot* shots, const std::vect
     ShotDesc& D = T.desc[k];
     D.nt = s.nt; D.nsrc = s.nsrc; D.nrec = s.nrec;
     D.last = grad ? (s.nt / ws->gp.check_freq) * ws->gp.check_freq : 0;
-    unique_points(ws, s.src_idx, s.nsrc, T, D.sp_off, D.sp_ptr, D.nsp, nullptr);
-    unique_points(ws, s.rec_idx, s.nrec, T, D.rp_off, D.rp_ptr, D.nrp, nullptr);
+    // ring slots are relative to this shot's part of the ring array:
+    // boundary source points first, then boundary receiver points
+    const int nsb = unique_points(ws, s.src_idx, s.nsrc, T, D.sp_off, D.sp_ptr, D.nsp, 0);
+    const int nrb = unique_points(ws, s.rec_idx, s.nrec, T, D.rp_off, D.rp_ptr, D.nrp, nsb);
+    ring_off[k] = T.nring;
+    T.nring += nsb + nrb;
     D.rec_off = (long long)T.rec.size();
     for (int r = 0; r < s.nrec; ++r) {
       int I[3] = {1, 1, 1};
@@ -468,7 +527,10 @@ void build_tables(sw_wavesim* ws, const sw_acoustic_shot* shots, const std::vect
     tf_o += ntf;
     tr_o += ntr;
   }
+  ensure(ws, ws->d_ring, (size_t)std::max(3 * T.nring, 4) * sizeof(float), "boundary rings");
+  for (int k = 0; k < S; ++k) T.desc[k].ring = ws->d_ring.as<float>() + 3LL * ring_off[k];
   upload(ws, ws->d_desc, T.desc, "shot descriptors");
+  upload(ws, ws->d_bslot, T.bslot, "boundary slots");
   upload(ws, ws->d_pts, T.pts, "point table");
   upload(ws, ws->d_ptr, T.ptr, "point csr");
   upload(ws, ws->d_ids, T.ids, "point ids");
@@ -481,18 +543,21 @@ void build_tables(sw_wavesim* ws, const sw_acoustic_shot* shots, const std::vect
 
 void ensure_state(sw_wavesim* ws, int S, bool grad, int max_nt) {
   const long long F = ws->F;
+  cudaStream_t st = ws->ctx->stream;
   if (S > ws->cap) {
-    for (int b = 0; b < 3; ++b) dev_alloc(ws->pb[b], (size_t)S * F * sizeof(float), "pressure field");
+    for (int b = 0; b < 2; ++b) dev_alloc(ws->pb[b], (size_t)S * F * sizeof(float), "pressure field", st);
+    dev_alloc(ws->db, (size_t)S * F * sizeof(float), "pressure increment", st);
     for (int k = 0; k < 2; ++k)
-      for (int d = 0; d < ws->N; ++d) dev_alloc(ws->psi[k][d], (size_t)S * ws->psz[d] * sizeof(float), "psi");
-    for (int d = 0; d < ws->N; ++d) dev_alloc(ws->xi[d], (size_t)S * ws->xsz[d] * sizeof(float), "xi");
+      for (int d = 0; d < ws->N; ++d) dev_alloc(ws->psi[k][d], (size_t)S * ws->psz[d] * sizeof(float), "psi", st);
+    for (int d = 0; d < ws->N; ++d) dev_alloc(ws->xi[d], (size_t)S * ws->xsz[d] * sizeof(float), "xi", st);
     if (ws->gradient) {
-      for (int b = 0; b < 3; ++b) dev_alloc(ws->ab[b], (size_t)S * F * sizeof(float), "adjoint field");
+      for (int b = 0; b < 2; ++b) dev_alloc(ws->ab[b], (size_t)S * F * sizeof(float), "adjoint field", st);
+      dev_alloc(ws->adb, (size_t)S * F * sizeof(float), "adjoint increment", st);
       for (int k = 0; k < 2; ++k)
-        for (int d = 0; d < ws->N; ++d) dev_alloc(ws->apsi[k][d], (size_t)S * ws->psz[d] * sizeof(float), "adjoint psi");
-      for (int d = 0; d < ws->N; ++d) dev_alloc(ws->axi[d], (size_t)S * ws->xsz[d] * sizeof(float), "adjoint xi");
-      dev_alloc(ws->g, (size_t)S * F * sizeof(float), "gradient");
-      dev_alloc(ws->gc, (size_t)S * F * sizeof(float), "gradient compensation");
+        for (int d = 0; d < ws->N; ++d) dev_alloc(ws->apsi[k][d], (size_t)S * ws->psz[d] * sizeof(float), "adjoint psi", st);
+      for (int d = 0; d < ws->N; ++d) dev_alloc(ws->axi[d], (size_t)S * ws->xsz[d] * sizeof(float), "adjoint xi", st);
+      dev_alloc(ws->g, (size_t)S * F * sizeof(float), "gradient", st);
+      dev_alloc(ws->gc, (size_t)S * F * sizeof(float), "gradient compensation", st);
     }
     ws->cap = S;
     ws->d_slots = 0;
@@ -503,23 +568,23 @@ void ensure_state(sw_wavesim* ws, int S, bool grad, int max_nt) {
     const long long dslots = K == 1 ? max_nt : K;
     if (dslots > ws->d_slots) {
       ws->dbuf.release();
-      dev_alloc(ws->dbuf, (size_t)ws->cap * dslots * F * sizeof(float), "D buffer");
+      dev_alloc(ws->dbuf, (size_t)ws->cap * dslots * F * sizeof(float), "D buffer", st);
       ws->d_slots = dslots;
     }
     const long long cks = K == 1 ? 0 : max_nt / K;
     if (cks > ws->ck_slots) {
       ws->ck.release();
       const long long slot = 2 * F + ws->strip_total;
-      dev_alloc(ws->ck, (size_t)ws->cap * cks * slot * sizeof(float), "checkpoints");
+      dev_alloc(ws->ck, (size_t)ws->cap * cks * slot * sizeof(float), "checkpoints", st);
       ws->ck_slots = cks;
     }
-    if (!ws->zero.p) dev_alloc(ws->zero, (size_t)(2 * F + ws->strip_total) * sizeof(float), "zero state");
+    if (!ws->zero.p) dev_alloc(ws->zero, (size_t)(2 * F + ws->strip_total) * sizeof(float), "zero state", st);
   }
 }
 
-// Memory (bytes) one shot needs in a batch.
+// Device memory (bytes) one shot needs in a batch.
 size_t per_shot_bytes(const sw_wavesim* ws, bool grad, int max_nt) {
-  // three pressure buffers, two psi buffers, xi; the same again for the adjoint, plus g and its compensation
+  // p ping-pong + increment, two psi buffers and xi; the same for the adjoint, plus g and its compensation
   long long floats = 3 * ws->F + ws->strip_total;
   for (int d = 0; d < ws->N; ++d) floats += ws->psz[d];
   if (ws->gradient) floats = 2 * floats + 2 * ws->F;
@@ -562,7 +627,11 @@ StepCtx make_step_ctx(sw_wavesim* ws, int S) {
   return c;
 }
 
-// Algorithmic bytes of one stencil launch (FP32 words), see the design doc.
+// Algorithmic bytes of one stencil launch (FP32 words): per interior point and
+// shot R p[n], R d[n], W p[n+1], W d[n+1]; fact is read once for all shots of
+// the launch; per damping-strip cell and axis R/W psi and R/W xi; D write
+// (forward of the gradient), R D + RMW g and its compensation (adjoint);
+// checkpoint copies of p, d, psi, xi.
 double stencil_bytes(const sw_wavesim* ws, int S, int mode, int n_dwrite, bool ckpt) {
   double pts = 1.0;
   for (int d = 0; d < ws->N; ++d) pts *= (double)(ws->n[d] - 2);
@@ -576,10 +645,9 @@ double stencil_bytes(const sw_wavesim* ws, int S, int mode, int n_dwrite, bool c
       if (e != d) other *= (double)(ws->n[e] - 2);
     strip += w * other;
   }
-  double per = 12.0 * S + 4.0;  // R pcur, R pold, W pnew per shot; R fact once
-  double b = per * pts + 16.0 * strip * S;
+  double b = (16.0 * S + 4.0) * pts + 16.0 * strip * S;
   if (mode == MODE_FWD_D) b += 4.0 * pts * n_dwrite;
-  if (mode == MODE_ADJ) b += 20.0 * pts * S;  // R D, RMW g and c
+  if (mode == MODE_ADJ) b += 20.0 * pts * S;
   if (ckpt) b += 8.0 * pts * S + 8.0 * strip * S;
   return b;
 }
@@ -637,7 +705,8 @@ int active_count(const std::vector<HostShot>& g, int it) {
 void zero_state(sw_wavesim* ws, int S, bool adjoint) {
   cudaStream_t st = ws->ctx->stream;
   DevMem* b = adjoint ? ws->ab : ws->pb;
-  for (int k = 0; k < 3; ++k) check_cuda(cudaMemsetAsync(b[k].p, 0, (size_t)S * ws->F * sizeof(float), st), "reset");
+  for (int k = 0; k < 2; ++k) check_cuda(cudaMemsetAsync(b[k].p, 0, (size_t)S * ws->F * sizeof(float), st), "reset");
+  check_cuda(cudaMemsetAsync((adjoint ? ws->adb : ws->db).p, 0, (size_t)S * ws->F * sizeof(float), st), "reset d");
   for (int k = 0; k < 2; ++k)
     for (int d = 0; d < ws->N; ++d)
       check_cuda(cudaMemsetAsync((adjoint ? ws->apsi : ws->psi)[k][d].p, 0, (size_t)S * ws->psz[d] * sizeof(float), st),
@@ -645,6 +714,7 @@ void zero_state(sw_wavesim* ws, int S, bool adjoint) {
   for (int d = 0; d < ws->N; ++d)
     check_cuda(cudaMemsetAsync((adjoint ? ws->axi : ws->xi)[d].p, 0, (size_t)S * ws->xsz[d] * sizeof(float), st),
                "reset xi");
+  check_cuda(cudaMemsetAsync(ws->d_ring.p, 0, ws->d_ring.bytes, st), "reset rings");
 }
 
 // Download traces of a group back to the caller (host or device pointers).
@@ -662,6 +732,18 @@ void download_traces(sw_wavesim* ws, const sw_acoustic_shot* shots, const std::v
   }
 }
 
+void launch_inject(sw_wavesim* ws, int Sa, const FieldArg& pnew, const FieldArg& dnew, const FieldArg& Dw,
+                   int d_first, int it, int record) {
+  cudaStream_t st = ws->ctx->stream;
+  cudaEvent_t ev = nullptr;
+  ws->ctx->prof.begin(st, KK_SRCREC, 0.0, &ev);
+  k_inject_record<<<Sa, 128, 0, st>>>(ws->d_desc.as<ShotDesc>(), ws->d_pts.as<long long>(), ws->d_ptr.as<int>(),
+                                      ws->d_ids.as<int>(), ws->d_bslot.as<int>(), ws->d_rec.as<long long>(), pnew,
+                                      dnew, Dw, d_first, it, record);
+  check_cuda(cudaGetLastError(), "inject/record launch");
+  ws->ctx->prof.end(st, KK_SRCREC, ev);
+}
+
 // Forward of one group: all shots step together.  Gradient mode (grad = true)
 // also writes checkpoints and the top-segment D.
 void forward_group(sw_wavesim* ws, const std::vector<HostShot>& group, bool grad) {
@@ -672,15 +754,16 @@ void forward_group(sw_wavesim* ws, const std::vector<HostShot>& group, bool grad
   const int K = grad ? ws->gp.check_freq : 0;
   const long long F = ws->F;
   const long long slot = 2 * F + ws->strip_total;
-  int io = 0, ic = 1, inew = 2, pk = 0;
+  int pc = 0, pk = 0;
   Launcher L{ws, st};
   for (int it = 1; it <= max_nt; ++it) {
     const int Sa = active_count(group, it);
     const StepCtx c = make_step_ctx(ws, Sa);
     StepArgs a = base_args(ws, c, Sa);
-    a.pold = fa(ws->pb[io], F);
-    a.pcur = fa(ws->pb[ic], F);
-    a.pnew = fa(ws->pb[inew], F);
+    a.pcur = fa(ws->pb[pc], F);
+    a.pnew = fa(ws->pb[1 - pc], F);
+    a.din = fa(ws->db, F);
+    a.dout = a.din;
     for (int d = 0; d < ws->N; ++d) {
       a.psi_in[d] = fa(ws->psi[pk][d], ws->psz[d]);
       a.psi_out[d] = fa(ws->psi[1 - pk][d], ws->psz[d]);
@@ -689,31 +772,30 @@ void forward_group(sw_wavesim* ws, const std::vector<HostShot>& group, bool grad
     }
     bool ckpt = false;
     int d_first = Sa;
-    long long dslot = -1;
     if (grad) {
-      // checkpoint m = (it-1)/K holds the state after step mK
+      // checkpoint m = (it-1)/K holds the state (p, d, psi, xi) after step mK
       if (K > 1 && (it - 1) % K == 0 && (it - 1) / K >= 1) {
         const int m = (it - 1) / K;
         float* base = ws->ck.as<float>() + (long long)(m - 1) * slot;
         const long long sstride = ws->ck_slots * slot;
-        a.ck_pold = FieldArg{base, sstride};
-        a.ck_pcur = FieldArg{base + F, sstride};
+        a.ck_p = FieldArg{base, sstride};
+        a.ck_d = FieldArg{base + F, sstride};
         long long off = 2 * F;
         for (int d = 0; d < ws->N; ++d) { a.ck_psi[d] = FieldArg{base + off, sstride}; off += ws->psz[d]; }
         for (int d = 0; d < ws->N; ++d) { a.ck_xi[d] = FieldArg{base + off, sstride}; off += ws->xsz[d]; }
         ckpt = true;
       }
-      // D(it-1) is kept for shots whose top segment contains it-1 (all steps when K == 1)
+      // D(it-1) is kept for shots whose top segment contains it-1 (every step when K == 1)
+      long long dslot;
       if (K == 1) {
         d_first = 0;
         dslot = it - 1;
       } else {
-        d_first = Sa;
         for (int k = 0; k < Sa; ++k)
           if (it - 1 >= group[k].nt / K * K) { d_first = k; break; }
         dslot = (it - 1) % K;
       }
-      a.dout = FieldArg{ws->dbuf.as<float>() + dslot * F, ws->d_slots * F};
+      a.Dout = FieldArg{ws->dbuf.as<float>() + dslot * F, ws->d_slots * F};
       a.d_first = d_first;
     }
     const int n_dwrite = grad ? Sa - d_first : 0;
@@ -722,15 +804,8 @@ void forward_group(sw_wavesim* ws, const std::vector<HostShot>& group, bool grad
       L.step<MODE_FWD_D>(a, c, bytes);
     else
       L.step<MODE_FWD>(a, c, bytes);
-    cudaEvent_t ev = nullptr;
-    ws->ctx->prof.begin(st, KK_SRCREC, 0.0, &ev);
-    k_inject_record<<<Sa, 128, 0, st>>>(ws->d_desc.as<ShotDesc>(), ws->d_pts.as<long long>(), ws->d_ptr.as<int>(),
-                                        ws->d_ids.as<int>(), ws->d_rec.as<long long>(), a.pnew,
-                                        grad ? a.dout : FieldArg{nullptr, 0}, d_first, it, 1);
-    check_cuda(cudaGetLastError(), "inject/record launch");
-    ws->ctx->prof.end(st, KK_SRCREC, ev);
-    const int o = io;
-    io = ic; ic = inew; inew = o;
+    launch_inject(ws, Sa, a.pnew, a.dout, grad ? a.Dout : FieldArg{nullptr, 0}, d_first, it, 1);
+    pc = 1 - pc;
     pk = 1 - pk;
   }
 }
@@ -746,7 +821,7 @@ void adjoint_group(sw_wavesim* ws, const std::vector<HostShot>& group) {
   zero_state(ws, S, true);
   check_cuda(cudaMemsetAsync(ws->g.p, 0, (size_t)S * F * sizeof(float), st), "reset g");
   check_cuda(cudaMemsetAsync(ws->gc.p, 0, (size_t)S * F * sizeof(float), st), "reset gc");
-  int ao = 0, ac = 1, an = 2, apk = 0;
+  int apc = 0, apk = 0;
   for (int it = max_nt; it >= 1; --it) {
     const int Sa = active_count(group, it);
     if (K > 1 && it % K == 0) {
@@ -762,74 +837,65 @@ void adjoint_group(sw_wavesim* ws, const std::vector<HostShot>& group) {
         cbase = ws->zero.as<float>();
         cstride = 0;
       }
-      FieldArg ck_po{cbase, cstride}, ck_pc{cbase + F, cstride}, ck_psi[3], ck_xi[3];
+      FieldArg ck_p{cbase, cstride}, ck_d{cbase + F, cstride}, ck_psi[3], ck_xi[3];
       long long off = 2 * F;
       for (int d = 0; d < ws->N; ++d) { ck_psi[d] = FieldArg{cbase + off, cstride}; off += ws->psz[d]; }
       for (int d = 0; d < ws->N; ++d) { ck_xi[d] = FieldArg{cbase + off, cstride}; off += ws->xsz[d]; }
-      // working buffers W0..W2 = pb[0..2]; psi ping-pong in psi[0/1]
-      int w_old = -1, w_cur = -1, w_new = 0, pk = 0;
+      int pc = 0, pk = 0;
       for (int t = (m - 1) * K + 1; t <= m * K; ++t) {
+        const bool first = t == (m - 1) * K + 1;
         StepArgs a = base_args(ws, c, Sa);
-        const int step = t - (m - 1) * K;  // 1-based within the segment
-        a.pold = step == 1 ? ck_po : (step == 2 ? ck_pc : fa(ws->pb[w_old], F));
-        a.pcur = step == 1 ? ck_pc : fa(ws->pb[w_cur], F);
-        a.pnew = fa(ws->pb[w_new], F);
+        a.pcur = first ? ck_p : fa(ws->pb[pc], F);
+        a.pnew = fa(ws->pb[first ? 0 : 1 - pc], F);
+        a.din = first ? ck_d : fa(ws->db, F);
+        a.dout = fa(ws->db, F);
         for (int d = 0; d < ws->N; ++d) {
-          a.psi_in[d] = step == 1 ? ck_psi[d] : fa(ws->psi[pk][d], ws->psz[d]);
-          a.psi_out[d] = fa(ws->psi[step == 1 ? 0 : 1 - pk][d], ws->psz[d]);
-          a.xi_in[d] = step == 1 ? ck_xi[d] : fa(ws->xi[d], ws->xsz[d]);
+          a.psi_in[d] = first ? ck_psi[d] : fa(ws->psi[pk][d], ws->psz[d]);
+          a.psi_out[d] = fa(ws->psi[first ? 0 : 1 - pk][d], ws->psz[d]);
+          a.xi_in[d] = first ? ck_xi[d] : fa(ws->xi[d], ws->xsz[d]);
           a.xi_out[d] = fa(ws->xi[d], ws->xsz[d]);
         }
         const long long dslot = (t - 1) % K;
-        a.dout = FieldArg{ws->dbuf.as<float>() + dslot * F, ws->d_slots * F};
+        a.Dout = FieldArg{ws->dbuf.as<float>() + dslot * F, ws->d_slots * F};
         a.d_first = 0;
         L.step<MODE_FWD_D>(a, c, stencil_bytes(ws, Sa, MODE_FWD_D, Sa, false));
-        cudaEvent_t ev = nullptr;
-        ws->ctx->prof.begin(st, KK_SRCREC, 0.0, &ev);
-        k_inject_record<<<Sa, 128, 0, st>>>(ws->d_desc.as<ShotDesc>(), ws->d_pts.as<long long>(),
-                                            ws->d_ptr.as<int>(), ws->d_ids.as<int>(), ws->d_rec.as<long long>(),
-                                            a.pnew, a.dout, 0, t, 0);
-        check_cuda(cudaGetLastError(), "recompute inject launch");
-        ws->ctx->prof.end(st, KK_SRCREC, ev);
-        // rotate roles: (old, cur, new) <- (cur, new, next free)
-        if (step == 1) {
-          w_cur = w_new; w_new = 1; pk = 0;
-        } else if (step == 2) {
-          w_old = w_cur; w_cur = w_new; w_new = 2; pk = 1 - pk;
+        launch_inject(ws, Sa, a.pnew, a.dout, a.Dout, 0, t, 0);
+        if (first) {
+          pc = 0;
+          pk = 0;
         } else {
-          const int fr = w_old;
-          w_old = w_cur; w_cur = w_new; w_new = fr; pk = 1 - pk;
+          pc = 1 - pc;
+          pk = 1 - pk;
         }
       }
     }
     // adjoint step it with the fused correlation against D(it-1)
-    {
-      const StepCtx c = make_step_ctx(ws, Sa);
-      StepArgs a = base_args(ws, c, Sa);
-      a.pold = fa(ws->ab[ao], F);
-      a.pcur = fa(ws->ab[ac], F);
-      a.pnew = fa(ws->ab[an], F);
-      for (int d = 0; d < ws->N; ++d) {
-        a.psi_in[d] = fa(ws->apsi[apk][d], ws->psz[d]);
-        a.psi_out[d] = fa(ws->apsi[1 - apk][d], ws->psz[d]);
-        a.xi_in[d] = fa(ws->axi[d], ws->xsz[d]);
-        a.xi_out[d] = a.xi_in[d];
-      }
-      const long long dslot = K == 1 ? it - 1 : (it - 1) % K;
-      a.dcorr = FieldArg{ws->dbuf.as<float>() + dslot * F, ws->d_slots * F};
-      a.g = fa(ws->g, F);
-      a.gc = fa(ws->gc, F);
-      L.step<MODE_ADJ>(a, c, stencil_bytes(ws, Sa, MODE_ADJ, 0, false));
-      cudaEvent_t ev = nullptr;
-      ws->ctx->prof.begin(st, KK_SRCREC, 0.0, &ev);
-      k_adj_inject<<<Sa, 128, 0, st>>>(ws->d_desc.as<ShotDesc>(), ws->d_pts.as<long long>(), ws->d_ptr.as<int>(),
-                                       ws->d_ids.as<int>(), a.pnew, a.dcorr, a.g, a.gc, it);
-      check_cuda(cudaGetLastError(), "adjoint inject launch");
-      ws->ctx->prof.end(st, KK_SRCREC, ev);
-      const int o = ao;
-      ao = ac; ac = an; an = o;
-      apk = 1 - apk;
+    const StepCtx c = make_step_ctx(ws, Sa);
+    StepArgs a = base_args(ws, c, Sa);
+    a.pcur = fa(ws->ab[apc], F);
+    a.pnew = fa(ws->ab[1 - apc], F);
+    a.din = fa(ws->adb, F);
+    a.dout = a.din;
+    for (int d = 0; d < ws->N; ++d) {
+      a.psi_in[d] = fa(ws->apsi[apk][d], ws->psz[d]);
+      a.psi_out[d] = fa(ws->apsi[1 - apk][d], ws->psz[d]);
+      a.xi_in[d] = fa(ws->axi[d], ws->xsz[d]);
+      a.xi_out[d] = a.xi_in[d];
     }
+    const long long dslot = K == 1 ? it - 1 : (it - 1) % K;
+    a.dcorr = FieldArg{ws->dbuf.as<float>() + dslot * F, ws->d_slots * F};
+    a.g = fa(ws->g, F);
+    a.gc = fa(ws->gc, F);
+    L.step<MODE_ADJ>(a, c, stencil_bytes(ws, Sa, MODE_ADJ, 0, false));
+    cudaEvent_t ev = nullptr;
+    ws->ctx->prof.begin(st, KK_SRCREC, 0.0, &ev);
+    k_adj_inject<<<Sa, 128, 0, st>>>(ws->d_desc.as<ShotDesc>(), ws->d_pts.as<long long>(), ws->d_ptr.as<int>(),
+                                     ws->d_ids.as<int>(), ws->d_bslot.as<int>(), a.pnew, a.dout, a.dcorr, a.g, a.gc,
+                                     it);
+    check_cuda(cudaGetLastError(), "adjoint inject launch");
+    ws->ctx->prof.end(st, KK_SRCREC, ev);
+    apc = 1 - apc;
+    apk = 1 - apk;
   }
 }
 
@@ -838,8 +904,8 @@ std::vector<std::vector<HostShot>> plan_groups(sw_wavesim* ws, const std::vector
   check_cuda(cudaMemGetInfo(&free_b, &total_b), "cudaMemGetInfo");
   // keep the buffers already allocated in the budget
   size_t owned = 0;
-  for (int b = 0; b < 3; ++b) owned += ws->pb[b].bytes + ws->ab[b].bytes;
-  owned += ws->g.bytes + ws->gc.bytes + ws->dbuf.bytes + ws->ck.bytes;
+  for (int b = 0; b < 2; ++b) owned += ws->pb[b].bytes + ws->ab[b].bytes;
+  owned += ws->db.bytes + ws->adb.bytes + ws->g.bytes + ws->gc.bytes + ws->dbuf.bytes + ws->ck.bytes;
   for (int k = 0; k < 2; ++k)
     for (int d = 0; d < 3; ++d) owned += ws->psi[k][d].bytes + ws->apsi[k][d].bytes;
   const double budget = 0.85 * (double)(free_b + owned);
@@ -920,8 +986,8 @@ void wavesim_init(sw_wavesim* ws, sw_ctx* ctx, const sw_acoustic_params* p, int 
     ws->xsz[d] = std::max<long long>(xs, 4);
     ws->strip_total += ws->psz[d] + ws->xsz[d];
   }
-  dev_alloc(ws->vp, (size_t)ws->npts * sizeof(float), "vp");
-  dev_alloc(ws->fact, (size_t)ws->F * sizeof(float), "fact");
+  dev_alloc(ws->vp, (size_t)ws->npts * sizeof(float), "vp", ws->ctx->stream);
+  dev_alloc(ws->fact, (size_t)ws->F * sizeof(float), "fact", ws->ctx->stream);
 }
 
 void wavesim_set_vp(sw_wavesim* ws, const float* vp, bool on_device) {
@@ -986,12 +1052,12 @@ void acoustic_gradient(sw_wavesim* ws, int nshots, const sw_acoustic_shot* shots
   double* gout = grad;
   double* mout = misfit;
   if (!on_device) {
-    dev_alloc(dgrad, (size_t)ws->npts * sizeof(double), "gradient output");
+    dev_alloc(dgrad, (size_t)ws->npts * sizeof(double), "gradient output", ws->ctx->stream);
     gout = dgrad.as<double>();
-    dev_alloc(dmis, sizeof(double), "misfit output");
+    dev_alloc(dmis, sizeof(double), "misfit output", ws->ctx->stream);
     mout = dmis.as<double>();
   } else if (!mout) {
-    dev_alloc(dmis, sizeof(double), "misfit output");
+    dev_alloc(dmis, sizeof(double), "misfit output", ws->ctx->stream);
     mout = dmis.as<double>();
   }
   bool first_group = true;
@@ -1005,7 +1071,7 @@ void acoustic_gradient(sw_wavesim* ws, int nshots, const sw_acoustic_shot* shots
     download_traces(ws, shots, group, on_device);
     // misfit and adjoint source
     const int nblk = 64;
-    ensure(ws->d_partial, (size_t)nblk * S * sizeof(double), "misfit partials");
+    ensure(ws, ws->d_partial, (size_t)nblk * S * sizeof(double), "misfit partials");
     {
       cudaEvent_t ev = nullptr;
       ws->ctx->prof.begin(st, KK_OTHER, 0.0, &ev);

@@ -17,12 +17,21 @@
 //  * the adjoint variant also accumulates the gradient correlation
 //    g += lambda * D with Kahan compensation (correlate_gradient_xPU.jl:1-10).
 //
+// Time stepping in increment form.  The reference advances
+//     p[n+1] = 2 p[n] - p[n-1] + fact * lap(p[n]);
+// here the state is (p[n], d[n] = p[n] - p[n-1]) and a step is
+//     d[n+1] = d[n] + fact * lap(p[n]),   p[n+1] = p[n] + d[n+1],
+// the same recurrence in exact arithmetic.  In FP32 the three-level form
+// rounds p every step and feeds that rounding back as a velocity error that
+// grows linearly in time (1.4e-5 relative trace error after 3000 steps on an
+// 801 x 801 model, against 1e-7 once the increment is carried separately).
+// p is double-buffered (the stencil reads neighbours); d is updated in place.
+//
 // Layout: column-major with axis 0 (x) padded to a pitch P (multiple of 32
 // floats); every thread owns four consecutive x points (one float4) and
 // marches along the last axis keeping three planes of p in registers.
-// Boundary nodes (first and last index of every axis) are never written,
-// exactly like the reference, so the three-buffer rotation reproduces its
-// boundary behaviour.
+// Boundary nodes (first and last index of every axis) are never written by
+// the stencil, exactly like the reference.
 #pragma once
 
 #include "internal.h"
@@ -36,10 +45,10 @@ struct StepArgs {
   int P;           // pitch of axis 0 in floats
   int halo;
   float ih[3], ih2[3];
-  FieldArg pold, pcur, pnew;
+  FieldArg pcur, pnew, din, dout;                  // p[n] (read), p[n+1] (write), d[n] -> d[n+1]
   FieldArg psi_in[3], psi_out[3], xi_in[3], xi_out[3];
-  FieldArg ck_pold, ck_pcur, ck_psi[3], ck_xi[3];  // checkpoint outputs (p == nullptr: none)
-  FieldArg dout;                                   // MODE_FWD_D: D output
+  FieldArg ck_p, ck_d, ck_psi[3], ck_xi[3];        // checkpoint outputs (p == nullptr: none)
+  FieldArg Dout;                                   // MODE_FWD_D: D = fact*lap output
   int d_first;                                     // MODE_FWD_D: shots >= d_first write D
   FieldArg dcorr, g, gc;                           // MODE_ADJ
   const float* fact;                               // shared by all shots
@@ -152,8 +161,9 @@ __global__ void __launch_bounds__(128) k_ac2d_step(const StepArgs A) {
   const int xa = inb ? x0 : P - 4;
 
   const float* __restrict__ pc = fptr(A.pcur, shot);
-  const float* __restrict__ po = fptr(A.pold, shot);
   float* __restrict__ pn = fptr(A.pnew, shot);
+  const float* di = fptr(A.din, shot);
+  float* dn = fptr(A.dout, shot);
   const float* __restrict__ fa = A.fact;
   const float* cp = A.cpml + (long long)shot * A.cpml_stride;
   const int na = 2 * H + 2, nh = 2 * H, L = 2 * na + 2 * nh;
@@ -172,10 +182,10 @@ __global__ void __launch_bounds__(128) k_ac2d_step(const StepArgs A) {
 
   const bool xstrip = inb && (x0 < H || x0 + 3 >= nx - H);
   const bool vec_interior = (x0 >= 1) && (x0 + 3 <= nx - 2);
-  float* ckpo = fptr(A.ck_pold, shot);
-  float* ckpc = fptr(A.ck_pcur, shot);
-  float* dout = nullptr;
-  if (MODE == MODE_FWD_D && shot >= A.d_first) dout = fptr(A.dout, shot);
+  float* ckp = fptr(A.ck_p, shot);
+  float* ckd = fptr(A.ck_d, shot);
+  float* Dw = nullptr;
+  if (MODE == MODE_FWD_D && shot >= A.d_first) Dw = fptr(A.Dout, shot);
   const float* dcr = MODE == MODE_ADJ ? fptr(A.dcorr, shot) : nullptr;
   float* gg = MODE == MODE_ADJ ? fptr(A.g, shot) : nullptr;
   float* gcp = MODE == MODE_ADJ ? fptr(A.gc, shot) : nullptr;
@@ -191,12 +201,12 @@ __global__ void __launch_bounds__(128) k_ac2d_step(const StepArgs A) {
     if (lane == 0) left = xa > 0 ? pc[row + xa - 1] : 0.f;
     if (lane == 31) right = xa + 4 < P ? pc[row + xa + 4] : 0.f;
     float o[4], f[4];
-    ld4(o, po + row + xa);
+    ld4rw(o, di + row + xa);
     ld4(f, fa + row + xa);
     const bool zstrip = (z < H) || (z >= nz - H);
     sx.psi_base = (long long)z * nh;
     sx.xi_base = (long long)z * na;
-    float outp[4], outd[4];
+    float outp[4], outd[4], outD[4];
 #pragma unroll
     for (int e = 0; e < 4; ++e) {
       const float xm = e == 0 ? left : r0[e - 1];
@@ -213,13 +223,14 @@ __global__ void __launch_bounds__(128) k_ac2d_step(const StepArgs A) {
         tz = cpml_axis_term(tz, rm[e], c, rp[e], z, nz, H, A.ih[1], sz);
       }
       const float lap = tx + tz;
-      outd[e] = f[e] * lap;
-      outp[e] = fmaf(f[e], lap, 2.f * c - o[e]);
+      outD[e] = f[e] * lap;
+      outd[e] = o[e] + outD[e];
+      outp[e] = c + outd[e];
     }
     if (inb) {
-      if (ckpo) {
-        st4(ckpo + row + x0, o);
-        st4(ckpc + row + x0, r0);
+      if (ckp) {
+        st4(ckp + row + x0, r0);
+        st4(ckd + row + x0, o);
       }
       if (MODE == MODE_ADJ) {
         float dv[4], g4[4], c4[4];
@@ -240,14 +251,16 @@ __global__ void __launch_bounds__(128) k_ac2d_step(const StepArgs A) {
       }
       if (vec_interior) {
         st4(pn + row + x0, outp);
-        if (MODE == MODE_FWD_D && dout) st4(dout + row + x0, outd);
+        st4(dn + row + x0, outd);
+        if (MODE == MODE_FWD_D && Dw) st4(Dw + row + x0, outD);
       } else {
 #pragma unroll
         for (int e = 0; e < 4; ++e) {
           const int x = x0 + e;
           if (x >= 1 && x <= nx - 2) {
             pn[row + x] = outp[e];
-            if (MODE == MODE_FWD_D && dout) dout[row + x] = outd[e];
+            dn[row + x] = outd[e];
+            if (MODE == MODE_FWD_D && Dw) Dw[row + x] = outD[e];
           }
         }
       }
@@ -284,8 +297,9 @@ __global__ void __launch_bounds__(128) k_ac3d_step(const StepArgs A) {
   const long long plane = (long long)P * ny;
 
   const float* __restrict__ pc = fptr(A.pcur, shot);
-  const float* __restrict__ po = fptr(A.pold, shot);
   float* __restrict__ pn = fptr(A.pnew, shot);
+  const float* di = fptr(A.din, shot);
+  float* dn = fptr(A.dout, shot);
   const float* __restrict__ fa = A.fact;
   const float* cp = A.cpml + (long long)shot * A.cpml_stride;
   const int na = 2 * H + 2, nh = 2 * H, L = 2 * na + 2 * nh;
@@ -307,10 +321,10 @@ __global__ void __launch_bounds__(128) k_ac3d_step(const StepArgs A) {
   const bool xstrip = inb && (x0 < H || x0 + 3 >= nx - H);
   const bool ystrip = (y < H) || (y >= ny - H);
   const bool vec_interior = (x0 >= 1) && (x0 + 3 <= nx - 2);
-  float* ckpo = fptr(A.ck_pold, shot);
-  float* ckpc = fptr(A.ck_pcur, shot);
-  float* dout = nullptr;
-  if (MODE == MODE_FWD_D && shot >= A.d_first) dout = fptr(A.dout, shot);
+  float* ckp = fptr(A.ck_p, shot);
+  float* ckd = fptr(A.ck_d, shot);
+  float* Dw = nullptr;
+  if (MODE == MODE_FWD_D && shot >= A.d_first) Dw = fptr(A.Dout, shot);
   const float* dcr = MODE == MODE_ADJ ? fptr(A.dcorr, shot) : nullptr;
   float* gg = MODE == MODE_ADJ ? fptr(A.g, shot) : nullptr;
   float* gcp = MODE == MODE_ADJ ? fptr(A.gc, shot) : nullptr;
@@ -331,12 +345,12 @@ __global__ void __launch_bounds__(128) k_ac3d_step(const StepArgs A) {
     if (lane == 0) left = xa > 0 ? pc[idx - 1] : 0.f;
     if (lane == 31) right = xa + 4 < P ? pc[idx + 4] : 0.f;
     float o[4], f[4];
-    ld4(o, po + idx);
+    ld4rw(o, di + idx);
     ld4(f, fa + idx);
     const bool zstrip = (z < H) || (z >= nz - H);
     s0.psi_base = ((long long)z * ny + y) * nh;
     s0.xi_base = ((long long)z * ny + y) * na;
-    float outp[4], outd[4];
+    float outp[4], outd[4], outD[4];
 #pragma unroll
     for (int e = 0; e < 4; ++e) {
       const float xm = e == 0 ? left : r0[e - 1];
@@ -359,13 +373,14 @@ __global__ void __launch_bounds__(128) k_ac3d_step(const StepArgs A) {
         tz = cpml_axis_term(tz, rm[e], c, rp[e], z, nz, H, A.ih[2], s2);
       }
       const float lap = (tx + ty) + tz;
-      outd[e] = f[e] * lap;
-      outp[e] = fmaf(f[e], lap, 2.f * c - o[e]);
+      outD[e] = f[e] * lap;
+      outd[e] = o[e] + outD[e];
+      outp[e] = c + outd[e];
     }
     if (inb) {
-      if (ckpo) {
-        st4(ckpo + idx, o);
-        st4(ckpc + idx, r0);
+      if (ckp) {
+        st4(ckp + idx, r0);
+        st4(ckd + idx, o);
       }
       if (MODE == MODE_ADJ) {
         float dv[4], g4[4], c4[4];
@@ -386,14 +401,16 @@ __global__ void __launch_bounds__(128) k_ac3d_step(const StepArgs A) {
       }
       if (vec_interior) {
         st4(pn + idx, outp);
-        if (MODE == MODE_FWD_D && dout) st4(dout + idx, outd);
+        st4(dn + idx, outd);
+        if (MODE == MODE_FWD_D && Dw) st4(Dw + idx, outD);
       } else {
 #pragma unroll
         for (int e = 0; e < 4; ++e) {
           const int x = x0 + e;
           if (x >= 1 && x <= nx - 2) {
             pn[idx + e] = outp[e];
-            if (MODE == MODE_FWD_D && dout) dout[idx + e] = outd[e];
+            dn[idx + e] = outd[e];
+            if (MODE == MODE_FWD_D && Dw) Dw[idx + e] = outD[e];
           }
         }
       }

@@ -29,7 +29,7 @@ void check_cuda(cudaError_t e, const char* what) {
   fail(code, std::string(what) + ": " + cudaGetErrorString(e));
 }
 
-void dev_alloc(DevMem& m, size_t bytes, const char* what) {
+void dev_alloc(DevMem& m, size_t bytes, const char* what, cudaStream_t st) {
   m.release();
   if (bytes == 0) bytes = 16;
   void* p = nullptr;
@@ -42,7 +42,7 @@ void dev_alloc(DevMem& m, size_t bytes, const char* what) {
   }
   m.p = p;
   m.bytes = bytes;
-  check_cuda(cudaMemset(p, 0, bytes), what);
+  check_cuda(cudaMemsetAsync(p, 0, bytes, st), what);
 }
 
 cudaEvent_t Profiler::get() {

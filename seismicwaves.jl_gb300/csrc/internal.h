@@ -42,7 +42,8 @@ struct SwError {
 
 [[noreturn]] void fail(int code, const std::string& msg);
 void check_cuda(cudaError_t e, const char* what);
-void dev_alloc(DevMem& m, size_t bytes, const char* what);  // zero-filled
+// Allocates and zero-fills on `st` (so later work on that stream sees the zeros).
+void dev_alloc(DevMem& m, size_t bytes, const char* what, cudaStream_t st);
 
 // Per-kernel-kind event timing (sw_profile_*).
 enum KernelKind { KK_STENCIL = 0, KK_ADJOINT = 1, KK_SRCREC = 2, KK_OTHER = 3, KK_COUNT = 4 };
