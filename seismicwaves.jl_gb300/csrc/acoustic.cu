@@ -240,10 +240,13 @@ __global__ void k_mute(const MutePoint* __restrict__ mp, const int* __restrict__
   }
 }
 
-// grad[c] (+)= 2/vp^3 * sum_s (g_s - c_s)  in FP64, unpadded column-major output.
+// grad[c] (+)= 2/vp^3 * (1/dt^2) * sum_s (g_s - c_s)  in FP64, unpadded
+// column-major output.  g accumulates lambda * D with D = p[t-2] - 2 p[t-1] + p[t];
+// the 1/dt^2 of correlate_gradient! (correlate_gradient_xPU.jl:1-10) and the
+// 2/vp^3 rescaling of swgradient_1shot! (acou_gradient.jl:93) are applied here once.
 __global__ void k_reduce_grad(const float* __restrict__ g, const float* __restrict__ gc, long long fstride,
                               int nshots, const float* __restrict__ vp, int n0, long long npts, int P,
-                              double* __restrict__ out, int accumulate) {
+                              double inv_dt2, double* __restrict__ out, int accumulate) {
   for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < npts;
        c += (long long)gridDim.x * blockDim.x) {
     const long long rowi = c / n0;
@@ -254,7 +257,7 @@ __global__ void k_reduce_grad(const float* __restrict__ g, const float* __restri
       s += (double)g[q] - (double)gc[q];
     }
     const double v = (double)vp[c];
-    const double val = (2.0 / (v * v * v)) * s;
+    const double val = (2.0 / (v * v * v)) * inv_dt2 * s;
     out[c] = accumulate ? out[c] + val : val;
   }
 }
@@ -652,11 +655,25 @@ double stencil_bytes(const sw_wavesim* ws, int S, int mode, int n_dwrite, bool c
   return b;
 }
 
+// The stencil moves p, d, D, g and the checkpoint copies of p and d with
+// 16-byte vector accesses: refuse to launch on a misaligned base or stride.
+void check_vector_alignment(const StepArgs& a) {
+  auto ok = [](const FieldArg& f) {
+    return f.p == nullptr || ((reinterpret_cast<uintptr_t>(f.p) % 16) == 0 && f.s % 4 == 0);
+  };
+  const FieldArg* vec[] = {&a.pcur, &a.pnew, &a.din, &a.dout, &a.ck_p, &a.ck_d, &a.Dout, &a.dcorr, &a.g, &a.gc};
+  for (const FieldArg* f : vec)
+    if (!ok(*f)) fail(SW_ERR_CUDA, "internal error: misaligned field handed to the stencil");
+  if (a.P % 4 != 0 || reinterpret_cast<uintptr_t>(a.fact) % 16 != 0)
+    fail(SW_ERR_CUDA, "internal error: misaligned pitch or fact");
+}
+
 struct Launcher {
   sw_wavesim* ws;
   cudaStream_t st;
   template <int MODE>
   void step(const StepArgs& a, const StepCtx& c, double bytes) {
+    check_vector_alignment(a);
     const long long blocks = (long long)a.nshots * c.tiles_x * c.tiles_y * c.tiles_z;
     cudaEvent_t ev = nullptr;
     const int kind = MODE == MODE_ADJ ? KK_ADJOINT : KK_STENCIL;
@@ -982,8 +999,10 @@ void wavesim_init(sw_wavesim* ws, sw_ctx* ctx, const sw_acoustic_params* p, int 
       ps *= e == d ? 2 * H : ext;
       xs *= e == d ? 2 * H + 2 : ext;
     }
-    ws->psz[d] = std::max<long long>(ps, 4);
-    ws->xsz[d] = std::max<long long>(xs, 4);
+    // multiples of 32 floats keep every array that follows in a checkpoint slot
+    // 128-byte aligned (the stencil moves p and d with 16-byte vector accesses)
+    ws->psz[d] = round_up(std::max<long long>(ps, 1), 32);
+    ws->xsz[d] = round_up(std::max<long long>(xs, 1), 32);
     ws->strip_total += ws->psz[d] + ws->xsz[d];
   }
   dev_alloc(ws->vp, (size_t)ws->npts * sizeof(float), "vp", ws->ctx->stream);
@@ -1123,7 +1142,8 @@ void acoustic_gradient(sw_wavesim* ws, int nshots, const sw_acoustic_shot* shots
       ws->ctx->prof.begin(st, KK_OTHER, 0.0, &ev);
       const long long blocks = std::min<long long>((ws->npts + 255) / 256, 8192);
       k_reduce_grad<<<(unsigned)blocks, 256, 0, st>>>(ws->g.as<float>(), ws->gc.as<float>(), ws->F, S,
-                                                      ws->vp.as<float>(), ws->n[0], ws->npts, ws->P, gout,
+                                                      ws->vp.as<float>(), ws->n[0], ws->npts, ws->P,
+                                                      1.0 / (ws->prm.dt * ws->prm.dt), gout,
                                                       first_group ? 0 : 1);
       check_cuda(cudaGetLastError(), "gradient reduction launch");
       ws->ctx->prof.end(st, KK_OTHER, ev);
