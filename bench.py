@@ -1,0 +1,417 @@
+#!/usr/bin/env python
+"""Benchmark of the batched acoustic FWI gradient (forward + checkpoints,
+L2 misfit, adjoint with recompute and fused correlation, shot sum) on GB300.
+
+Default workload: 64 shots on a 2001 x 801 layered model (h = 10 m), 50-300
+receivers and 2000-4000 time steps per shot, 8 Hz Ricker, checkpoint period
+50 (the batched configuration of the benchmark set).  One "step" is one full
+gradient of all shots.  Prints one JSON line.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl {gb300,reference}]
+
+--impl reference times the reference's CPU algorithm (the C++ restatement in
+oracle/, OpenMP on all host cores; Julia is not available to run
+SeismicWaves.jl itself) on a bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "Gpts/s & shots/s fwd+adjoint gradient, batched vs plain, % of HBM roofline"
+UNIT = "Gpts/s"
+
+
+def _args():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=3)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    p.add_argument("--workload", default="acoustic2d_2001x801")
+    p.add_argument("--shots", type=int, default=0, help="override the number of shots (0 = workload's)")
+    p.add_argument("--no-plain", action="store_true")
+    p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--cpu-sample-nt", type=int, default=400)
+    return p.parse_args()
+
+
+def _dist():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def _workload(name, shots):
+    import __graft_entry__
+
+    sw = __graft_entry__.load_package()
+    from seismicwaves_gb300 import configs
+
+    w = configs.WORKLOADS[name]()
+    if shots:
+        w.shots = w.shots[:shots]
+    return sw, w
+
+
+# ----------------------------------------------------------------------------- clocks
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() in ("active", "yes", "1"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ----------------------------------------------------------------------------- GPU driver
+class GradientRun:
+    """The workload's shots as C-ABI structs over device (or pinned host) buffers."""
+
+    def __init__(self, sw, w, device, on_device=True):
+        import torch
+
+        L = sw._lib
+        self.sw, self.w, self.L, self.torch = sw, w, L, torch
+        self.dev = torch.device("cuda", device)
+        self.ctx = L.Context(device)
+        self.lib = self.ctx.lib
+        nd = w.vp.ndim
+        prm = L.SwAcousticParams()
+        prm.ndim = nd
+        for d in range(nd):
+            prm.n[d], prm.h[d] = w.vp.shape[d], w.h[d]
+        prm.dt, prm.halo, prm.rcoef, prm.freetop = w.dt, w.halo, 1e-4, int(w.freetop)
+        gp = L.SwGradParams()
+        gp.check_freq = w.check_freq
+        self.h = ctypes.c_void_p()
+        self.ctx.check(self.lib.sw_wavesim_create(self.ctx.h, ctypes.byref(prm), 1, ctypes.byref(gp),
+                                                  ctypes.byref(self.h)), "sw_wavesim_create")
+        self.hf = ctypes.c_void_p()
+        self.ctx.check(self.lib.sw_wavesim_create(self.ctx.h, ctypes.byref(prm), 0, None, ctypes.byref(self.hf)),
+                       "sw_wavesim_create")
+        self.stream = torch.cuda.ExternalStream(self.ctx.stream, device=self.dev)
+        vmax = float(np.max(w.vp))  # init_bdc!: max of the simulated model
+        self.host = []
+        for s in w.shots:
+            si = sw.nearest_grid_points(s.src_pos, w.h)
+            ri = sw.nearest_grid_points(s.rec_pos, w.h)
+            tf = sw.scale_srctf(s.stf(w.dt), si, w.vp, w.h, w.dt)
+            parts = []
+            for d in range(nd):
+                parts += L.cpml_coefficients(vmax, w.dt, w.halo, 1e-4, w.h[d], s.f0, w.freetop and d == nd - 1)
+            cp = np.concatenate(parts).astype(np.float32)
+            self.host.append((si, ri, tf, cp))
+        # device-resident inputs and outputs
+        t = torch
+        self.vp_d = t.from_numpy(np.ascontiguousarray(w.vp.ravel(order="F"), dtype=np.float32)).to(self.dev)
+        self.vpo_d = t.from_numpy(np.ascontiguousarray(w.vp_observed.ravel(order="F"), dtype=np.float32)).to(self.dev)
+        self.tf_d = [t.from_numpy(np.ascontiguousarray(h[2].ravel(order="F"))).to(self.dev) for h in self.host]
+        self.tr_d = [t.zeros(s.nt * h[1].shape[0], dtype=t.float32, device=self.dev) for s, h in zip(w.shots, self.host)]
+        self.obs_d = [t.zeros_like(x) for x in self.tr_d]
+        self.grad_d = t.zeros(int(np.prod(w.vp.shape)), dtype=t.float64, device=self.dev)
+        self.mis_d = t.zeros(1, dtype=t.float64, device=self.dev)
+
+    def structs(self, idx, tf, tr, obs):
+        arr = (self.L.SwAcousticShot * len(idx))()
+        for k, i in enumerate(idx):
+            si, ri, _, cp = self.host[i]
+            st = arr[k]
+            st.nt, st.nsrc, st.nrec = self.w.shots[i].nt, si.shape[0], ri.shape[0]
+            st.src_idx, st.rec_idx, st.cpml = si.ctypes.data, ri.ctypes.data, cp.ctypes.data
+            st.srctf, st.traces = tf[i], tr[i]
+            if obs is not None:
+                st.observed = obs[i]
+        return arr
+
+    def make_observed(self):
+        """Observed data: a forward run on the perturbed model."""
+        self.ctx.check(self.lib.sw_wavesim_set_vp(self.hf, self.vpo_d.data_ptr(), 1), "set_vp")
+        idx = list(range(len(self.w.shots)))
+        arr = self.structs(idx, [x.data_ptr() for x in self.tf_d], [x.data_ptr() for x in self.obs_d], None)
+        self.ctx.check(self.lib.sw_acoustic_forward(self.hf, len(idx), arr, 1), "observed forward")
+        self.lib.sw_wavesim_destroy(self.hf)
+        self.ctx.check(self.lib.sw_wavesim_set_vp(self.h, self.vp_d.data_ptr(), 1), "set_vp")
+
+    def gradient_device(self, idx):
+        arr = self.structs(idx, [x.data_ptr() for x in self.tf_d], [x.data_ptr() for x in self.tr_d],
+                           [x.data_ptr() for x in self.obs_d])
+        self.ctx.check(self.lib.sw_acoustic_gradient(self.h, len(idx), arr, 1, self.grad_d.data_ptr(),
+                                                      self.mis_d.data_ptr()), "sw_acoustic_gradient")
+
+    def setup_host(self):
+        """Pinned host copies of the per-step inputs and outputs (end-to-end leg)."""
+        t = self.torch
+        self.vp_h = self.vp_d.cpu().pin_memory()
+        self.tf_h = [x.cpu().pin_memory() for x in self.tf_d]
+        self.obs_h = [x.cpu().pin_memory() for x in self.obs_d]
+        self.tr_h = [t.zeros(x.numel(), dtype=t.float32).pin_memory() for x in self.tr_d]
+        self.grad_h = t.zeros(self.grad_d.numel(), dtype=t.float64).pin_memory()
+        self.mis_h = t.zeros(1, dtype=t.float64).pin_memory()
+        h2d = self.vp_h.numel() * 4 + sum(x.numel() * 4 for x in self.tf_h) + sum(x.numel() * 4 for x in self.obs_h)
+        d2h = sum(x.numel() * 4 for x in self.tr_h) + self.grad_h.numel() * 8 + 8
+        return h2d, d2h
+
+    def gradient_host(self):
+        idx = list(range(len(self.w.shots)))
+        self.ctx.check(self.lib.sw_wavesim_set_vp(self.h, self.vp_h.data_ptr(), 0), "set_vp")
+        arr = self.structs(idx, [x.data_ptr() for x in self.tf_h], [x.data_ptr() for x in self.tr_h],
+                           [x.data_ptr() for x in self.obs_h])
+        self.ctx.check(self.lib.sw_acoustic_gradient(self.h, len(idx), arr, 0, self.grad_h.data_ptr(),
+                                                      self.mis_h.data_ptr()), "sw_acoustic_gradient")
+
+    def timed(self, fn, n):
+        t = self.torch
+        a, b = t.cuda.Event(enable_timing=True), t.cuda.Event(enable_timing=True)
+        t.cuda.synchronize(self.dev)
+        a.record(self.stream)
+        for _ in range(n):
+            fn()
+        b.record(self.stream)
+        b.synchronize()
+        return a.elapsed_time(b) / 1e3
+
+
+def _peak():
+    f = ROOT / "MEASURED_PEAKS.json"
+    if f.exists():
+        try:
+            return float(json.loads(f.read_text())["hbm_gbs"]), "measured"
+        except (KeyError, ValueError):
+            pass
+    return 6800.0, "fallback"
+
+
+def _traffic_from_profiles(kernel, workload):
+    """dram bytes per launch of `kernel` recorded from an ncu capture (profiles/*.md)."""
+    for f in sorted((ROOT / "profiles").glob("*.md")):
+        txt = f.read_text()
+        if f"kernel: {kernel}" in txt and f"workload: {workload}" in txt:
+            for line in txt.splitlines():
+                if line.startswith("dram_bytes_per_launch:"):
+                    try:
+                        return float(line.split(":", 1)[1].split()[0])
+                    except ValueError:
+                        return None
+    return None
+
+
+def _cpu_baseline(sw, w, nt_sample):
+    import oracle
+
+    s = w.shots[0]
+    si = sw.nearest_grid_points(s.src_pos, w.h)
+    ri = sw.nearest_grid_points(s.rec_pos, w.h)
+    stf = s.stf(w.dt)[:nt_sample]
+    tf = sw.scale_srctf(stf, si, w.vp, w.h, w.dt).astype(np.float64)
+    cp = oracle.cpml_blocks(w.vp, w.h, w.dt, w.halo, 1e-4, s.f0, w.freetop)
+    obs = np.zeros((nt_sample, ri.shape[0]))
+    threads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    oracle.acoustic_gradient(w.vp, w.h, w.dt, w.halo, cp, tf, si, ri, obs,
+                             check_freq=min(w.check_freq, nt_sample - 1), nthreads=threads)
+    dt = time.perf_counter() - t0
+    pts = float(np.prod(w.vp.shape)) * nt_sample
+    sample = (f"one shot of {w.name}, {nt_sample} time steps, checkpoint period "
+              f"{min(w.check_freq, nt_sample - 1)}, FP64 gradient (forward + recompute + adjoint)")
+    return pts / dt / 1e9, threads, sample, dt
+
+
+def run_reference(a):
+    rank, world, _ = _dist()
+    if rank != 0:
+        return
+    sw, w = _workload(a.workload, a.shots)
+    import oracle
+
+    oracle.load()
+    vals = []
+    for i in range(a.warmup + a.steps):
+        v, threads, sample, dt = _cpu_baseline(sw, w, a.cpu_sample_nt)
+        if i >= a.warmup:
+            vals.append((v, dt))
+    value = statistics.mean(v for v, _ in vals)
+    ms = statistics.mean(d for _, d in vals) * 1e3
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": a.gpus,
+            "steps": a.steps, "warmup": a.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": w.name, "sample": sample},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_gb300(a):
+    import torch
+
+    rank, world, local = _dist()
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    sw, w = _workload(a.workload, a.shots)
+    R = GradientRun(sw, w, local)
+    R.make_observed()
+    nshots = len(w.shots)
+    allidx = list(range(nshots))
+    pts = float(w.point_steps())
+
+    def barrier():
+        torch.cuda.synchronize(R.dev)
+        if dist:
+            dist.barrier()
+
+    # warm-up (also allocates all device memory once)
+    for _ in range(a.warmup):
+        R.gradient_device(allidx)
+    barrier()
+    clocks = ClockSampler(local)
+    clocks.start()
+    R.ctx.profile(True)
+    t_dev = R.timed(lambda: R.gradient_device(allidx), a.steps)
+    R.ctx.profile(False)
+    clk = clocks.stop()
+    prof = {k: R.ctx.profile_read(k) for k in range(4)}
+    if dist:
+        tt = torch.tensor([t_dev], device=R.dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_dev = float(tt.item())
+    barrier()
+    value = pts * a.steps * world / t_dev / 1e9
+    shots_per_s = nshots * a.steps * world / t_dev
+
+    # end to end through the C ABI with pinned host buffers (inputs up, gradient/traces down, every step)
+    h2d, d2h = R.setup_host()
+    R.gradient_host()
+    t_e2e = R.timed(R.gradient_host, a.steps)
+    e2e = pts * a.steps * world / t_e2e / 1e9
+
+    # plain per-shot path: the same library, one shot per call
+    plain = None
+    if not a.no_plain:
+        R.gradient_device([0])
+        t_plain = R.timed(lambda: [R.gradient_device([i]) for i in allidx], 1)
+        plain = {"value": pts / t_plain / 1e9, "unit": UNIT, "shots_per_s": nshots / t_plain,
+                 "ms_per_step": t_plain * 1e3, "what": "same kernels, one shot per call"}
+
+    if rank != 0:
+        return
+    # roofline of the dominant kernel
+    kinds = {0: "k_ac2d_step (forward/recompute)", 1: "k_ac2d_step<MODE_ADJ> (adjoint + correlation)"}
+    if w.vp.ndim == 3:
+        kinds = {0: "k_ac3d_step (forward/recompute)", 1: "k_ac3d_step<MODE_ADJ> (adjoint + correlation)"}
+    dom = max((0, 1), key=lambda k: prof[k][0])
+    ms_tot, launches, bytes_tot = prof[dom]
+    achieved = bytes_tot / (ms_tot / 1e3) / 1e9 if ms_tot > 0 else None
+    peak, peak_kind = _peak()
+    kname = ("k_ac2d_step" if w.vp.ndim == 2 else "k_ac3d_step") + ("<2>" if dom == 1 else "<1>")
+    traffic = _traffic_from_profiles(kname, w.name)
+    roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak if achieved else None,
+            "traffic": traffic,
+            "kernel": kinds[dom], "peak_kind": peak_kind,
+            "algorithmic_bytes_per_launch": bytes_tot / max(launches, 1),
+            "avg_launch_us": ms_tot * 1e3 / max(launches, 1),
+            "launches": launches}
+    total_launches = sum(prof[k][1] for k in range(4))
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
+            "ms_per_step": t_dev * 1e3 / a.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic",
+            "config": {"workload": w.name, "grid": list(w.vp.shape), "h_m": w.h[0], "shots": nshots,
+                       "nt_range": [min(s.nt for s in w.shots), max(s.nt for s in w.shots)],
+                       "receivers_range": [min(s.rec_pos.shape[0] for s in w.shots),
+                                           max(s.rec_pos.shape[0] for s in w.shots)],
+                       "check_freq": w.check_freq, "halo": w.halo,
+                       "cache": "inputs larger than L2 (each step streams tens of GB of wavefield state)",
+                       "precision": "fp32 wavefields and stencil, Kahan fp32 correlation, fp64 misfit and shot sum",
+                       "parallelism": f"replicas x{world}" if world > 1 else "1 GPU, all shots batched"},
+            "shots_per_s": shots_per_s,
+            "plain": plain,
+            "batched_vs_plain": (shots_per_s / plain["shots_per_s"]) if plain else None,
+            "clocks": clk,
+            "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+            "gpu_launches": total_launches,
+            "roofline": roof}
+    if not a.no_cpu:
+        import oracle
+
+        oracle.load()
+        v, threads, sample, _ = _cpu_baseline(sw, w, a.cpu_sample_nt)
+        line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    a = _args()
+    if a.impl == "reference":
+        run_reference(a)
+        return
+    try:
+        run_gb300(a)
+    finally:
+        if int(os.environ.get("WORLD_SIZE", "1")) > 1:
+            import torch.distributed as dist
+
+            if dist.is_initialized():
+                dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

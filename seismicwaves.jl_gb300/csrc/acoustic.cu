@@ -1020,9 +1020,12 @@ void wavesim_set_vp(sw_wavesim* ws, const float* vp, bool on_device) {
                              on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, st),
              "vp upload");
   const double dt = ws->prm.dt;
+  cudaEvent_t ev = nullptr;
+  ws->ctx->prof.begin(st, KK_OTHER, 0.0, &ev);
   k_set_fact<<<std::min<long long>((ws->npts + 255) / 256, 4096), 256, 0, st>>>(
       ws->vp.as<float>(), ws->n[0], ws->npts, ws->P, dt * dt, ws->fact.as<float>());
   check_cuda(cudaGetLastError(), "fact launch");
+  ws->ctx->prof.end(st, KK_OTHER, ev);
   ws->has_vp = true;
 }
 
@@ -1096,8 +1099,11 @@ void acoustic_gradient(sw_wavesim* ws, int nshots, const sw_acoustic_shot* shots
       ws->ctx->prof.begin(st, KK_OTHER, 0.0, &ev);
       k_misfit_adjsrc<<<dim3(nblk, S), 256, 0, st>>>(ws->d_desc.as<ShotDesc>(), ws->d_rec.as<long long>(),
                                                      ws->fact.as<float>(), ws->d_partial.as<double>());
-      k_misfit_sum<<<1, 256, 0, st>>>(ws->d_partial.as<double>(), nblk, S, mout, first_group ? 0 : 1);
       check_cuda(cudaGetLastError(), "misfit launch");
+      ws->ctx->prof.end(st, KK_OTHER, ev);
+      ws->ctx->prof.begin(st, KK_OTHER, 0.0, &ev);
+      k_misfit_sum<<<1, 256, 0, st>>>(ws->d_partial.as<double>(), nblk, S, mout, first_group ? 0 : 1);
+      check_cuda(cudaGetLastError(), "misfit sum launch");
       ws->ctx->prof.end(st, KK_OTHER, ev);
     }
     adjoint_group(ws, group);
@@ -1130,10 +1136,13 @@ void acoustic_gradient(sw_wavesim* ws, int nshots, const sw_acoustic_shot* shots
         }
         upload(ws, ws->d_mute, pts, "mute points");
         upload(ws, ws->d_mute_ptr, ptr, "mute csr");
+        cudaEvent_t ev = nullptr;
+        ws->ctx->prof.begin(st, KK_OTHER, 0.0, &ev);
         k_mute<<<S, 256, 0, st>>>(ws->d_mute.as<MutePoint>(), ws->d_mute_ptr.as<int>(), ws->N, ws->n[0], ws->n[1],
                                   ws->n[2], ws->P, ws->prm.h[0], ws->prm.h[1], ws->prm.h[2], radius * hmax,
                                   fa(ws->g, ws->F), fa(ws->gc, ws->F));
         check_cuda(cudaGetLastError(), "mute launch");
+        ws->ctx->prof.end(st, KK_OTHER, ev);
         check_cuda(cudaStreamSynchronize(st), "mute");
       }
     }
