@@ -46,6 +46,7 @@ def _args():
     p.add_argument("--no-plain", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--cpu-sample-nt", type=int, default=400)
+    p.add_argument("--nt", type=int, default=0, help="cap every shot's time steps (small profiling cases)")
     return p.parse_args()
 
 
@@ -56,7 +57,7 @@ def _dist():
     return rank, world, local
 
 
-def _workload(name, shots):
+def _workload(name, shots, nt_cap=0):
     import __graft_entry__
 
     sw = __graft_entry__.load_package()
@@ -65,6 +66,9 @@ def _workload(name, shots):
     w = configs.WORKLOADS[name]()
     if shots:
         w.shots = w.shots[:shots]
+    if nt_cap:
+        for s in w.shots:
+            s.nt = min(s.nt, nt_cap)
     return sw, w
 
 
@@ -276,7 +280,7 @@ def run_reference(a):
     rank, world, _ = _dist()
     if rank != 0:
         return
-    sw, w = _workload(a.workload, a.shots)
+    sw, w = _workload(a.workload, a.shots, a.nt)
     import oracle
 
     oracle.load()
@@ -306,7 +310,7 @@ def run_gb300(a):
 
         torch.cuda.set_device(local)
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
-    sw, w = _workload(a.workload, a.shots)
+    sw, w = _workload(a.workload, a.shots, a.nt)
     R = GradientRun(sw, w, local)
     R.make_observed()
     nshots = len(w.shots)
@@ -369,7 +373,10 @@ def run_gb300(a):
             "kernel": kinds[dom], "peak_kind": peak_kind,
             "algorithmic_bytes_per_launch": bytes_tot / max(launches, 1),
             "avg_launch_us": ms_tot * 1e3 / max(launches, 1),
-            "launches": launches}
+            "launches": launches,
+            "kernels": {kinds[k]: {"ms": prof[k][0], "launches": prof[k][1],
+                                   "GB_per_s": (prof[k][2] / (prof[k][0] / 1e3) / 1e9) if prof[k][0] else None}
+                        for k in (0, 1)}}
     total_launches = sum(prof[k][1] for k in range(4))
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
             "ms_per_step": t_dev * 1e3 / a.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
