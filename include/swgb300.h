@@ -59,7 +59,8 @@ enum {
   SW_ERR_CUDA = 3,        /* CUDA runtime error */
   SW_ERR_TIMEOUT = 4,     /* a bounded device-side wait gave up */
   SW_ERR_STATE = 5,       /* call made in the wrong state (e.g. gradient on a forward-only wavesim) */
-  SW_ERR_UNSUPPORTED = 6  /* input the backend deliberately rejects (see sw_ctx_last_error) */
+  SW_ERR_UNSUPPORTED = 6, /* input the backend deliberately rejects (see sw_ctx_last_error) */
+  SW_ERR_CAPACITY = 7     /* problem larger than the fixed scratch of sw_acoustic2d_forward_noalloc */
 };
 
 typedef struct sw_ctx sw_ctx;
@@ -151,6 +152,26 @@ int sw_wavesim_set_tile(sw_wavesim* ws, int32_t tz);
  * stencil with correlation, 2 = source/receiver kernel, 3 = other. */
 int sw_profile_enable(sw_ctx* ctx, int32_t on);
 int sw_profile_read(sw_ctx* ctx, int32_t kind, double* total_ms, int64_t* launches, double* bytes);
+
+/* 2D forward of one shot that allocates no device memory.  Has no
+ * counterpart in the reference: it exists for callers that cannot let a
+ * library call cudaMalloc -- code running inside another runtime's device
+ * memory pool (CUDA.jl, PyTorch) that must account for every byte, fixed
+ * device-memory budgets, and pipelines that cannot take the device-wide
+ * synchronisation cudaMalloc/cudaFree may impose.  Its wavefields, memory
+ * variables and shot tables live in a fixed 64 MiB device array inside the
+ * library (every GPU that loads the library holds it until exit), enough for
+ * grids up to about 3.5 million points; larger problems return
+ * SW_ERR_CAPACITY.  vp (prod(n) floats), shot->srctf and shot->traces are
+ * device pointers; the index tables and shot->cpml are host memory.  Work is
+ * issued on `stream` (cudaStream_t, NULL = legacy default stream) and the call
+ * returns after it finished.  Every call reuses the same array and clears
+ * what must start at zero itself; calls whose GPU work overlaps race on it.
+ * The first call on a device looks the array up (cudaGetSymbolAddress, with
+ * that device current), so make it before any stream capture.  Status codes
+ * only (no context, no message). */
+int sw_acoustic2d_forward_noalloc(const sw_acoustic_params* params, const float* vp, const sw_acoustic_shot* shot,
+                                  void* stream);
 
 #ifdef __cplusplus
 }

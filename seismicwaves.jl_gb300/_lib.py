@@ -11,10 +11,12 @@ from pathlib import Path
 HERE = Path(__file__).resolve().parent
 LIB_PATH = HERE / "libswgb300.so"
 
-SW_OK, SW_ERR_ARG, SW_ERR_OOM, SW_ERR_CUDA, SW_ERR_TIMEOUT, SW_ERR_STATE, SW_ERR_UNSUPPORTED = range(7)
+(SW_OK, SW_ERR_ARG, SW_ERR_OOM, SW_ERR_CUDA, SW_ERR_TIMEOUT, SW_ERR_STATE, SW_ERR_UNSUPPORTED,
+ SW_ERR_CAPACITY) = range(8)
 STATUS_NAMES = {
     SW_ERR_ARG: "SW_ERR_ARG", SW_ERR_OOM: "SW_ERR_OOM", SW_ERR_CUDA: "SW_ERR_CUDA",
     SW_ERR_TIMEOUT: "SW_ERR_TIMEOUT", SW_ERR_STATE: "SW_ERR_STATE", SW_ERR_UNSUPPORTED: "SW_ERR_UNSUPPORTED",
+    SW_ERR_CAPACITY: "SW_ERR_CAPACITY",
 }
 
 # Every function declared in include/swgb300.h (checked by the test-suite).
@@ -22,7 +24,7 @@ EXPORTS = [
     "sw_version", "sw_ctx_create", "sw_ctx_destroy", "sw_ctx_last_error", "sw_ctx_stream",
     "sw_cpml_coefficients", "sw_wavesim_create", "sw_wavesim_destroy", "sw_wavesim_set_vp",
     "sw_acoustic_forward", "sw_acoustic_gradient", "sw_wavesim_set_tile", "sw_profile_enable",
-    "sw_profile_read",
+    "sw_profile_read", "sw_acoustic2d_forward_noalloc",
 ]
 
 i32, f64, vp_ = ctypes.c_int32, ctypes.c_double, ctypes.c_void_p
@@ -80,6 +82,7 @@ def load() -> ctypes.CDLL:
     lib.sw_wavesim_set_tile.argtypes = [vp_, i32]
     lib.sw_profile_enable.argtypes = [vp_, i32]
     lib.sw_profile_read.argtypes = [vp_, i32, P(f64), P(ctypes.c_int64), P(f64)]
+    lib.sw_acoustic2d_forward_noalloc.argtypes = [P(SwAcousticParams), vp_, P(SwAcousticShot), vp_]
     _lib = lib
     return lib
 
