@@ -47,6 +47,8 @@ def _args():
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--cpu-sample-nt", type=int, default=400)
     p.add_argument("--nt", type=int, default=0, help="cap every shot's time steps (small profiling cases)")
+    p.add_argument("--tz", type=int, default=0, help="stencil tile height (0 = library heuristic)")
+    p.add_argument("--variant", type=int, default=-1, help="2D stencil variant (-1 = library default)")
     return p.parse_args()
 
 
@@ -312,6 +314,8 @@ def run_gb300(a):
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     sw, w = _workload(a.workload, a.shots, a.nt)
     R = GradientRun(sw, w, local)
+    if a.tz or a.variant >= 0:
+        R.ctx.check(R.lib.sw_wavesim_set_tuning(R.h, a.tz, max(a.variant, 0)), "sw_wavesim_set_tuning")
     R.make_observed()
     nshots = len(w.shots)
     allidx = list(range(nshots))
@@ -395,7 +399,8 @@ def run_gb300(a):
             "clocks": clk,
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "gpu_launches": total_launches,
-            "roofline": roof}
+            "roofline": roof,
+            "tuning": {"tz": a.tz, "variant": a.variant}}
     if not a.no_cpu:
         import oracle
 

@@ -143,9 +143,11 @@ int sw_acoustic_forward(sw_wavesim* ws, int32_t nshots, const sw_acoustic_shot* 
 int sw_acoustic_gradient(sw_wavesim* ws, int32_t nshots, const sw_acoustic_shot* shots, int32_t on_device,
                          double* grad, double* misfit);
 
-/* Height (in planes of the marching axis) of the stencil tiles; 0 restores
- * the built-in heuristic.  Used by the tile autotuner. */
-int sw_wavesim_set_tile(sw_wavesim* ws, int32_t tz);
+/* Stencil tuning knobs used by the autotuner: tz = height (in planes of the
+ * marching axis) of a block's tile, 0 = built-in heuristic; variant selects
+ * the 2D stencil implementation (0 = register-pipelined loads, 1 = TMA bulk
+ * copies through shared memory).  Results do not depend on either. */
+int sw_wavesim_set_tuning(sw_wavesim* ws, int32_t tz, int32_t variant);
 
 /* Per-kernel timing collected with CUDA events on the context's stream while
  * enabled (0 = off).  kind: 0 = forward/recompute stencil, 1 = adjoint

@@ -453,8 +453,8 @@ class AcousticCDCPMLWaveSimulation:
             shot.recs.seismograms[...] = traces
         return grad, float(misfit[0])
 
-    def set_tile(self, tz: int):
-        self.ctx.check(self.ctx.lib.sw_wavesim_set_tile(self._h, int(tz)), "sw_wavesim_set_tile")
+    def set_tuning(self, tz: int = 0, variant: int = 0):
+        self.ctx.check(self.ctx.lib.sw_wavesim_set_tuning(self._h, int(tz), int(variant)), "sw_wavesim_set_tuning")
 
 
 def _check_sim_consistency(matprop, shots):

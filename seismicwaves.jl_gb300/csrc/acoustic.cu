@@ -309,6 +309,7 @@ struct sw_wavesim {
   DevMem d_ring;  // boundary-injection rings (3 floats per point)
   DevMem d_mute, d_mute_ptr;
   int tile_tz = 0;  // 0 = heuristic
+  int variant = 0;  // 2D stencil: 0 = register-pipelined, 1 = TMA
 };
 
 namespace {
@@ -617,9 +618,11 @@ StepCtx make_step_ctx(sw_wavesim* ws, int S) {
   }
   int TZ = ws->tile_tz;
   if (TZ <= 0) {
-    // aim for >= ~8 blocks per SM in total, with TZ in [8, 64]
+    // aim for >= ~8 blocks per SM in total, with TZ in [16, 64] (the 2D kernel's
+    // row pipeline needs a few rows per block to fill)
     TZ = 64;
-    while (TZ > 8) {
+    const int tz_min = (ws->N == 2 && ws->variant == 1) ? 16 : 8;
+    while (TZ > tz_min) {
       const long long blocks = (long long)S * c.tiles_x * c.tiles_y * ((nint + TZ - 1) / TZ);
       if (blocks >= 8LL * sms) break;
       TZ /= 2;
@@ -668,6 +671,18 @@ void check_vector_alignment(const StepArgs& a) {
     fail(SW_ERR_CUDA, "internal error: misaligned pitch or fact");
 }
 
+template <int MODE>
+void enable_tma_smem() {
+  static int done_for_device = -1;
+  int dev = 0;
+  check_cuda(cudaGetDevice(&dev), "cudaGetDevice");
+  if (done_for_device == dev) return;
+  check_cuda(cudaFuncSetAttribute(k_ac2d_tma<MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)TmaLayout<MODE>::BYTES),
+             "shared memory attribute");
+  done_for_device = dev;
+}
+
 struct Launcher {
   sw_wavesim* ws;
   cudaStream_t st;
@@ -678,10 +693,14 @@ struct Launcher {
     cudaEvent_t ev = nullptr;
     const int kind = MODE == MODE_ADJ ? KK_ADJOINT : KK_STENCIL;
     ws->ctx->prof.begin(st, kind, bytes, &ev);
-    if (ws->N == 2)
+    if (ws->N == 2 && ws->variant == 1) {
+      enable_tma_smem<MODE>();
+      k_ac2d_tma<MODE><<<(unsigned)blocks, 128, TmaLayout<MODE>::BYTES, st>>>(a);
+    } else if (ws->N == 2) {
       k_ac2d_step<MODE><<<(unsigned)blocks, 128, 0, st>>>(a);
-    else
+    } else {
       k_ac3d_step<MODE><<<(unsigned)blocks, 128, 0, st>>>(a);
+    }
     check_cuda(cudaGetLastError(), "stencil launch");
     ws->ctx->prof.end(st, kind, ev);
   }
@@ -708,6 +727,7 @@ StepArgs base_args(sw_wavesim* ws, const StepCtx& c, int S) {
   a.tiles_y = c.tiles_y;
   a.tiles_z = c.tiles_z;
   a.TZ = c.TZ;
+  a.err = ws->ctx->err.as<int>();
   return a;
 }
 
@@ -953,6 +973,16 @@ std::vector<HostShot> sorted_order(int nshots, const sw_acoustic_shot* shots) {
 // ---------------------------------------------------------------------------
 namespace swgb {
 
+// Raised by kernels whose bounded waits gave up: report it and re-arm the flag.
+void check_timeout(sw_wavesim* ws) {
+  int flag = 0;
+  check_cuda(cudaMemcpy(&flag, ws->ctx->err.p, sizeof(int), cudaMemcpyDeviceToHost), "error flag");
+  if (flag) {
+    check_cuda(cudaMemset(ws->ctx->err.p, 0, sizeof(int)), "error flag");
+    fail(SW_ERR_TIMEOUT, "a device-side wait on a data pipeline stage timed out");
+  }
+}
+
 void wavesim_init(sw_wavesim* ws, sw_ctx* ctx, const sw_acoustic_params* p, int gradient, const sw_grad_params* gp) {
   if (!p) fail(SW_ERR_ARG, "params is NULL");
   if (p->ndim != 2 && p->ndim != 3) fail(SW_ERR_ARG, "Only 2D and 3D acoustic simulations are supported");
@@ -976,6 +1006,7 @@ void wavesim_init(sw_wavesim* ws, sw_ctx* ctx, const sw_acoustic_params* p, int 
     }
   }
   ws->ctx = ctx;
+  if (!ctx->err.p) dev_alloc(ctx->err, sizeof(int), "error flag", ctx->stream);
   ws->prm = *p;
   ws->gradient = gradient != 0;
   if (ws->gradient) {
@@ -1042,6 +1073,7 @@ void acoustic_forward(sw_wavesim* ws, int nshots, const sw_acoustic_shot* shots,
     download_traces(ws, shots, group, on_device);
   }
   check_cuda(cudaStreamSynchronize(ws->ctx->stream), "forward");
+  check_timeout(ws);
   ws->ctx->prof.resolve();
 }
 
@@ -1164,10 +1196,14 @@ void acoustic_gradient(sw_wavesim* ws, int nshots, const sw_acoustic_shot* shots
     if (misfit) check_cuda(cudaMemcpyAsync(misfit, mout, sizeof(double), cudaMemcpyDeviceToHost, st), "misfit download");
   }
   check_cuda(cudaStreamSynchronize(st), "gradient");
+  check_timeout(ws);
   ws->ctx->prof.resolve();
 }
 
-void wavesim_set_tile(sw_wavesim* ws, int tz) { ws->tile_tz = tz; }
+void wavesim_set_tuning(sw_wavesim* ws, int tz, int variant) {
+  ws->tile_tz = tz;
+  ws->variant = variant;
+}
 sw_ctx* wavesim_ctx(sw_wavesim* ws) { return ws->ctx; }
 sw_wavesim* wavesim_new() { return new sw_wavesim(); }
 void wavesim_delete(sw_wavesim* ws) { delete ws; }

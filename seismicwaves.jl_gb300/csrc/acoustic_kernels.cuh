@@ -56,6 +56,7 @@ struct StepArgs {
   int cpml_stride;
   int nshots;
   int tiles_x, tiles_y, tiles_z, TZ;
+  int* err;                                        // set to 1 when a bounded wait gives up
 };
 
 struct StripIO {
@@ -190,19 +191,42 @@ __global__ void __launch_bounds__(128) k_ac2d_step(const StepArgs A) {
   float* gg = MODE == MODE_ADJ ? fptr(A.g, shot) : nullptr;
   float* gcp = MODE == MODE_ADJ ? fptr(A.gc, shot) : nullptr;
 
-  float rm[4], r0[4], rp[4];
+  // The loads of row z+1 (p of row z+2, d, fact and for the adjoint D, g, gc)
+  // are issued before the stores of row z, so each warp keeps two rows of
+  // loads in flight instead of waiting on every row.
+  float rm[4], r0[4], rp[4], o[4], f[4], dv[4], g4[4], c4[4];
   ld4(rm, pc + (long long)(z_begin - 1) * P + xa);
   ld4(r0, pc + (long long)z_begin * P + xa);
+  {
+    const long long row = (long long)z_begin * P;
+    ld4(rp, pc + row + P + xa);
+    ld4rw(o, di + row + xa);
+    ld4(f, fa + row + xa);
+    if (MODE == MODE_ADJ) {
+      ld4(dv, dcr + row + xa);
+      ld4rw(g4, gg + row + xa);
+      ld4rw(c4, gcp + row + xa);
+    }
+  }
   for (int z = z_begin; z < z_end; ++z) {
     const long long row = (long long)z * P;
-    ld4(rp, pc + row + P + xa);
+    float rpn[4], on[4], fn[4], dvn[4], g4n[4], c4n[4];
+    const bool more = z + 1 < z_end;
+    if (more) {
+      const long long nrow = row + P;
+      ld4(rpn, pc + nrow + P + xa);
+      ld4rw(on, di + nrow + xa);
+      ld4(fn, fa + nrow + xa);
+      if (MODE == MODE_ADJ) {
+        ld4(dvn, dcr + nrow + xa);
+        ld4rw(g4n, gg + nrow + xa);
+        ld4rw(c4n, gcp + nrow + xa);
+      }
+    }
     float left = __shfl_up_sync(FULL, r0[3], 1);
     float right = __shfl_down_sync(FULL, r0[0], 1);
     if (lane == 0) left = xa > 0 ? pc[row + xa - 1] : 0.f;
     if (lane == 31) right = xa + 4 < P ? pc[row + xa + 4] : 0.f;
-    float o[4], f[4];
-    ld4rw(o, di + row + xa);
-    ld4(f, fa + row + xa);
     const bool zstrip = (z < H) || (z >= nz - H);
     sx.psi_base = (long long)z * nh;
     sx.xi_base = (long long)z * na;
@@ -233,10 +257,6 @@ __global__ void __launch_bounds__(128) k_ac2d_step(const StepArgs A) {
         st4(ckd + row + x0, o);
       }
       if (MODE == MODE_ADJ) {
-        float dv[4], g4[4], c4[4];
-        ld4(dv, dcr + row + x0);
-        ld4rw(g4, gg + row + x0);
-        ld4rw(c4, gcp + row + x0);
 #pragma unroll
         for (int e = 0; e < 4; ++e)
           if (x0 + e >= 1 && x0 + e <= nx - 2) kahan_add(g4[e], c4[e], outp[e] * dv[e]);
@@ -266,7 +286,16 @@ __global__ void __launch_bounds__(128) k_ac2d_step(const StepArgs A) {
       }
     }
 #pragma unroll
-    for (int e = 0; e < 4; ++e) { rm[e] = r0[e]; r0[e] = rp[e]; }
+    for (int e = 0; e < 4; ++e) {
+      rm[e] = r0[e];
+      r0[e] = rp[e];
+      if (more) {
+        rp[e] = rpn[e];
+        o[e] = on[e];
+        f[e] = fn[e];
+        if (MODE == MODE_ADJ) { dv[e] = dvn[e]; g4[e] = g4n[e]; c4[e] = c4n[e]; }
+      }
+    }
   }
 }
 
@@ -417,6 +446,252 @@ __global__ void __launch_bounds__(128) k_ac3d_step(const StepArgs A) {
     }
 #pragma unroll
     for (int e = 0; e < 4; ++e) { rm[e] = r0[e]; r0[e] = rp[e]; }
+  }
+}
+
+
+// ---------------------------------------------------------------------------
+// 2D, TMA-pipelined.  Same arithmetic as k_ac2d_step, but a CTA (4 warps,
+// 512 x points) streams its rows through shared memory: one thread issues
+// cp.async.bulk copies of the next rows (p with a 4-float halo on each side,
+// d, fact and, for the adjoint, D, g and its compensation) TMA_D rows ahead
+// of the row being computed, each stage signalled by its own mbarrier.  The
+// row loads no longer sit on every warp's critical path, so the kernel keeps
+// ~25-50 KB per CTA in flight independently of register occupancy.
+// Every wait on an mbarrier is bounded (clock64); on expiry the CTA sets
+// A.err and leaves after the next block-wide barrier, with no copy left in
+// flight (a stage is only issued after all earlier stages were consumed).
+// ---------------------------------------------------------------------------
+constexpr int TMA_W = 512;            // x points per CTA tile
+constexpr int TMA_D = 4;              // rows prefetched ahead
+constexpr int TMA_NS = TMA_D + 3;     // stage slots (3 p rows are live per iteration)
+constexpr int TMA_PROW = TMA_W + 8;   // p row in shared memory: 4 halo floats each side
+constexpr long long TMA_TIMEOUT_CYCLES = 4000000000LL;  // ~2 s at 2 GHz
+
+template <int MODE>
+struct TmaLayout {
+  static constexpr int NAUX = MODE == MODE_ADJ ? 5 : 2;  // d, fact (+ D, g, gc)
+  static constexpr int STAGE = TMA_PROW + NAUX * TMA_W;  // floats per stage (multiple of 4)
+  static constexpr size_t BYTES = (size_t)TMA_NS * STAGE * sizeof(float) + TMA_NS * sizeof(unsigned long long);
+};
+
+__device__ __forceinline__ unsigned smem_u32(const void* p) {
+  return static_cast<unsigned>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void mbar_init(unsigned long long* b, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(b)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive_expect_tx(unsigned long long* b, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(b)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long* b, unsigned parity) {
+  unsigned ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(b)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// returns false when the wait gave up
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* b, unsigned parity) {
+  if (mbar_try_wait(b, parity)) return true;
+  const long long t0 = clock64();
+  while (!mbar_try_wait(b, parity))
+    if (clock64() - t0 > TMA_TIMEOUT_CYCLES) return false;
+  return true;
+}
+__device__ __forceinline__ void tma_load_1d(void* dst, const void* src, unsigned bytes, unsigned long long* b) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   smem_u32(dst)),
+               "l"(src), "r"(bytes), "r"(smem_u32(b))
+               : "memory");
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(128) k_ac2d_tma(const StepArgs A) {
+  using Lay = TmaLayout<MODE>;
+  extern __shared__ __align__(128) float smem[];
+  unsigned long long* bars = reinterpret_cast<unsigned long long*>(smem + (size_t)TMA_NS * Lay::STAGE);
+  constexpr unsigned FULL = 0xffffffffu;
+  const int tid = threadIdx.x, lane = tid & 31;
+  const int S = A.nshots;
+  const int shot = blockIdx.x % S;
+  const int tile = blockIdx.x / S;
+  const int txi = tile % A.tiles_x, tzi = tile / A.tiles_x;
+  const int nx = A.n0, nz = A.n1, P = A.P, H = A.halo;
+  const int z_begin = 1 + tzi * A.TZ;
+  const int z_end = min(z_begin + A.TZ, nz - 1);
+  const int X0 = txi * TMA_W;
+  if (z_begin >= z_end || X0 >= P) return;  // block-uniform
+  const int rows = z_end - z_begin, nst = rows + 2;
+  const int x0 = X0 + 4 * tid;
+  const bool inb = x0 < P;
+
+  const float* pc = fptr(A.pcur, shot);
+  float* __restrict__ pn = fptr(A.pnew, shot);
+  const float* di = fptr(A.din, shot);
+  float* dn = fptr(A.dout, shot);
+  const float* cp = A.cpml + (long long)shot * A.cpml_stride;
+  const int na = 2 * H + 2, nh = 2 * H, L = 2 * na + 2 * nh;
+  float* ckp = fptr(A.ck_p, shot);
+  float* ckd = fptr(A.ck_d, shot);
+  float* Dw = nullptr;
+  if (MODE == MODE_FWD_D && shot >= A.d_first) Dw = fptr(A.Dout, shot);
+  const float* dcr = MODE == MODE_ADJ ? fptr(A.dcorr, shot) : nullptr;
+  float* gg = MODE == MODE_ADJ ? fptr(A.g, shot) : nullptr;
+  float* gcp = MODE == MODE_ADJ ? fptr(A.gc, shot) : nullptr;
+
+  // producer: copies of stage j (p row z_begin-1+j; aux rows of z_begin+j-2)
+  const int gx0 = max(X0 - 4, 0), gx1 = min(X0 + TMA_W + 4, P);
+  const int aw = min(TMA_W, P - X0);
+  auto issue = [&](int j) {
+    const int slot = j % TMA_NS;
+    float* st = smem + (size_t)slot * Lay::STAGE;
+    const int r = z_begin - 1 + j;
+    unsigned bytes = (unsigned)(gx1 - gx0) * 4u;
+    const bool aux = j >= 2;
+    if (aux) bytes += (unsigned)aw * 4u * Lay::NAUX;
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    mbar_arrive_expect_tx(&bars[slot], bytes);
+    tma_load_1d(st + (gx0 - (X0 - 4)), pc + (long long)r * P + gx0, (unsigned)(gx1 - gx0) * 4u, &bars[slot]);
+    if (aux) {
+      const long long row = (long long)(r - 1) * P + X0;  // aux row z = r - 1
+      float* a = st + TMA_PROW;
+      tma_load_1d(a, di + row, aw * 4u, &bars[slot]);
+      tma_load_1d(a + TMA_W, A.fact + row, aw * 4u, &bars[slot]);
+      if (MODE == MODE_ADJ) {
+        tma_load_1d(a + 2 * TMA_W, dcr + row, aw * 4u, &bars[slot]);
+        tma_load_1d(a + 3 * TMA_W, gg + row, aw * 4u, &bars[slot]);
+        tma_load_1d(a + 4 * TMA_W, gcp + row, aw * 4u, &bars[slot]);
+      }
+    }
+  };
+
+  if (tid == 0) {
+    for (int k = 0; k < TMA_NS; ++k) mbar_init(&bars[k], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  if (tid == 0)
+    for (int j = 0; j < min(TMA_NS, nst); ++j) issue(j);
+
+  StripIO sx, sz;
+  sx.psi_in = fptr(A.psi_in[0], shot);  sx.psi_out = fptr(A.psi_out[0], shot);
+  sx.xi_in = fptr(A.xi_in[0], shot);    sx.xi_out = fptr(A.xi_out[0], shot);
+  sx.ck_psi = fptr(A.ck_psi[0], shot);  sx.ck_xi = fptr(A.ck_xi[0], shot);
+  sx.a = cp; sx.ah = cp + na; sx.b = cp + na + nh; sx.bh = cp + 2 * na + nh;
+  sx.psi_step = 1; sx.xi_step = 1;
+  sz.psi_in = fptr(A.psi_in[1], shot);  sz.psi_out = fptr(A.psi_out[1], shot);
+  sz.xi_in = fptr(A.xi_in[1], shot);    sz.xi_out = fptr(A.xi_out[1], shot);
+  sz.ck_psi = fptr(A.ck_psi[1], shot);  sz.ck_xi = fptr(A.ck_xi[1], shot);
+  sz.a = cp + L; sz.ah = cp + L + na; sz.b = cp + L + na + nh; sz.bh = cp + L + 2 * na + nh;
+  sz.psi_step = P; sz.xi_step = P;
+  const bool xstrip = inb && (x0 < H || x0 + 3 >= nx - H);
+  const bool vec_interior = (x0 >= 1) && (x0 + 3 <= nx - 2);
+
+  bool tout = false;
+  for (int k = 0; k < rows; ++k) {
+    // stage k + TMA_D + 2 reuses the slot of stage k - 1, released by the barrier ending iteration k - 1
+    if (k > 0 && tid == 0 && k + TMA_D + 2 < nst) issue(k + TMA_D + 2);
+    if (k == 0) {
+      tout |= !mbar_wait_bounded(&bars[0], 0);
+      tout |= !mbar_wait_bounded(&bars[1 % TMA_NS], 0);
+    }
+    const int j2 = k + 2;
+    tout |= !mbar_wait_bounded(&bars[j2 % TMA_NS], (j2 / TMA_NS) & 1);
+    if (__syncthreads_or(tout)) {
+      if (tid == 0 && A.err) atomicExch(A.err, 1);
+      return;
+    }
+    const float* sm_ = smem + (size_t)(k % TMA_NS) * Lay::STAGE;        // p row z-1
+    const float* s0_ = smem + (size_t)((k + 1) % TMA_NS) * Lay::STAGE;  // p row z
+    const float* sp_ = smem + (size_t)(j2 % TMA_NS) * Lay::STAGE;       // p row z+1, aux rows of z
+    const int z = z_begin + k;
+    const long long row = (long long)z * P;
+    const int so = 4 + 4 * tid;
+    float rm[4], r0[4], rp[4], o[4], f[4];
+    {
+      const float4 a = *reinterpret_cast<const float4*>(sm_ + so);
+      const float4 b = *reinterpret_cast<const float4*>(s0_ + so);
+      const float4 c = *reinterpret_cast<const float4*>(sp_ + so);
+      const float4 d = *reinterpret_cast<const float4*>(sp_ + TMA_PROW + 4 * tid);
+      const float4 e = *reinterpret_cast<const float4*>(sp_ + TMA_PROW + TMA_W + 4 * tid);
+      rm[0] = a.x; rm[1] = a.y; rm[2] = a.z; rm[3] = a.w;
+      r0[0] = b.x; r0[1] = b.y; r0[2] = b.z; r0[3] = b.w;
+      rp[0] = c.x; rp[1] = c.y; rp[2] = c.z; rp[3] = c.w;
+      o[0] = d.x; o[1] = d.y; o[2] = d.z; o[3] = d.w;
+      f[0] = e.x; f[1] = e.y; f[2] = e.z; f[3] = e.w;
+    }
+    float left = __shfl_up_sync(FULL, r0[3], 1);
+    float right = __shfl_down_sync(FULL, r0[0], 1);
+    if (lane == 0) left = s0_[so - 1];
+    if (lane == 31) right = s0_[so + 4];
+    const bool zstrip = (z < H) || (z >= nz - H);
+    sx.psi_base = (long long)z * nh;
+    sx.xi_base = (long long)z * na;
+    float outp[4], outd[4], outD[4];
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+      const float xm = e == 0 ? left : r0[e - 1];
+      const float xp = e == 3 ? right : r0[e + 1];
+      const float c = r0[e];
+      float tx = (xm - 2.f * c + xp) * A.ih2[0];
+      float tz = (rm[e] - 2.f * c + rp[e]) * A.ih2[1];
+      const int x = x0 + e;
+      const bool pin = inb && x >= 1 && x <= nx - 2;
+      if (xstrip && pin) tx = cpml_axis_term(tx, xm, c, xp, x, nx, H, A.ih[0], sx);
+      if (zstrip && pin) {
+        sz.psi_base = x;
+        sz.xi_base = x;
+        tz = cpml_axis_term(tz, rm[e], c, rp[e], z, nz, H, A.ih[1], sz);
+      }
+      const float lap = tx + tz;
+      outD[e] = f[e] * lap;
+      outd[e] = o[e] + outD[e];
+      outp[e] = c + outd[e];
+    }
+    if (inb) {
+      if (ckp) {
+        st4(ckp + row + x0, r0);
+        st4(ckd + row + x0, o);
+      }
+      if (MODE == MODE_ADJ) {
+        const float4 dv4 = *reinterpret_cast<const float4*>(sp_ + TMA_PROW + 2 * TMA_W + 4 * tid);
+        const float4 g4v = *reinterpret_cast<const float4*>(sp_ + TMA_PROW + 3 * TMA_W + 4 * tid);
+        const float4 c4v = *reinterpret_cast<const float4*>(sp_ + TMA_PROW + 4 * TMA_W + 4 * tid);
+        float dv[4] = {dv4.x, dv4.y, dv4.z, dv4.w};
+        float g4[4] = {g4v.x, g4v.y, g4v.z, g4v.w};
+        float c4[4] = {c4v.x, c4v.y, c4v.z, c4v.w};
+#pragma unroll
+        for (int e = 0; e < 4; ++e)
+          if (x0 + e >= 1 && x0 + e <= nx - 2) kahan_add(g4[e], c4[e], outp[e] * dv[e]);
+        if (vec_interior) {
+          st4(gg + row + x0, g4);
+          st4(gcp + row + x0, c4);
+        } else {
+#pragma unroll
+          for (int e = 0; e < 4; ++e)
+            if (x0 + e >= 1 && x0 + e <= nx - 2) { gg[row + x0 + e] = g4[e]; gcp[row + x0 + e] = c4[e]; }
+        }
+      }
+      if (vec_interior) {
+        st4(pn + row + x0, outp);
+        st4(dn + row + x0, outd);
+        if (MODE == MODE_FWD_D && Dw) st4(Dw + row + x0, outD);
+      } else {
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+          const int x = x0 + e;
+          if (x >= 1 && x <= nx - 2) {
+            pn[row + x] = outp[e];
+            dn[row + x] = outd[e];
+            if (MODE == MODE_FWD_D && Dw) Dw[row + x] = outD[e];
+          }
+        }
+      }
+    }
+    __syncthreads();  // the slot of p row z-1 is free again
   }
 }
 

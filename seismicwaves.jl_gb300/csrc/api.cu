@@ -16,7 +16,7 @@ void wavesim_set_vp(sw_wavesim* ws, const float* vp, bool on_device);
 void acoustic_forward(sw_wavesim* ws, int nshots, const sw_acoustic_shot* shots, bool on_device);
 void acoustic_gradient(sw_wavesim* ws, int nshots, const sw_acoustic_shot* shots, bool on_device, double* grad,
                        double* misfit);
-void wavesim_set_tile(sw_wavesim* ws, int tz);
+void wavesim_set_tuning(sw_wavesim* ws, int tz, int variant);
 sw_ctx* wavesim_ctx(sw_wavesim* ws);
 sw_wavesim* wavesim_new();
 void wavesim_delete(sw_wavesim* ws);
@@ -270,10 +270,9 @@ int sw_profile_read(sw_ctx* ctx, int32_t kind, double* total_ms, int64_t* launch
   });
 }
 
-/* Not part of the public header: tile-height override for the autotuner. */
-int sw_wavesim_set_tile(sw_wavesim* ws, int32_t tz) {
-  if (!ws || tz < 0) return SW_ERR_ARG;
-  swgb::wavesim_set_tile(ws, tz);
+int sw_wavesim_set_tuning(sw_wavesim* ws, int32_t tz, int32_t variant) {
+  if (!ws || tz < 0 || variant < 0 || variant > 1) return SW_ERR_ARG;
+  swgb::wavesim_set_tuning(ws, tz, variant);
   return SW_OK;
 }
 

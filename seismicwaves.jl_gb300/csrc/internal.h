@@ -75,6 +75,7 @@ struct sw_ctx {
   int num_sms = 0;
   std::string last_error;
   swgb::Profiler prof;
+  swgb::DevMem err;  // int flag raised by kernels whose bounded waits gave up
 };
 
 namespace swgb {
