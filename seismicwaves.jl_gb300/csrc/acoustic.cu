@@ -695,7 +695,7 @@ struct Launcher {
     ws->ctx->prof.begin(st, kind, bytes, &ev);
     if (ws->N == 2 && ws->variant == 1) {
       enable_tma_smem<MODE>();
-      k_ac2d_tma<MODE><<<(unsigned)blocks, 128, TmaLayout<MODE>::BYTES, st>>>(a);
+      k_ac2d_tma<MODE><<<(unsigned)blocks, 160, TmaLayout<MODE>::BYTES, st>>>(a);
     } else if (ws->N == 2) {
       k_ac2d_step<MODE><<<(unsigned)blocks, 128, 0, st>>>(a);
     } else {

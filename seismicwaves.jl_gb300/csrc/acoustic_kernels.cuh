@@ -451,28 +451,31 @@ __global__ void __launch_bounds__(128) k_ac3d_step(const StepArgs A) {
 
 
 // ---------------------------------------------------------------------------
-// 2D, TMA-pipelined.  Same arithmetic as k_ac2d_step, but a CTA (4 warps,
-// 512 x points) streams its rows through shared memory: one thread issues
-// cp.async.bulk copies of the next rows (p with a 4-float halo on each side,
-// d, fact and, for the adjoint, D, g and its compensation) TMA_D rows ahead
-// of the row being computed, each stage signalled by its own mbarrier.  The
-// row loads no longer sit on every warp's critical path, so the kernel keeps
-// ~25-50 KB per CTA in flight independently of register occupancy.
-// Every wait on an mbarrier is bounded (clock64); on expiry the CTA sets
-// A.err and leaves after the next block-wide barrier, with no copy left in
-// flight (a stage is only issued after all earlier stages were consumed).
+// 2D, TMA pipeline with a dedicated producer warp.  Same arithmetic as
+// k_ac2d_step.  A CTA has 4 consumer warps (512 x points, one float4 per
+// thread) and 1 producer warp.  The producer streams the CTA's rows through a
+// ring of TMA_NS shared-memory stages with cp.async.bulk copies (p row with a
+// 4-float halo on each side, d, fact and, for the adjoint, D, g and its
+// compensation); each stage has a "full" mbarrier (completed by the copies'
+// transaction count) and an "empty" mbarrier (one arrival per consumer warp
+// once it no longer reads the stage).  No block-wide barrier sits in the
+// loop: warps only wait for data or for free slots.  Every wait is bounded
+// (clock64); on expiry the warp raises A.err and leaves.
 // ---------------------------------------------------------------------------
 constexpr int TMA_W = 512;            // x points per CTA tile
-constexpr int TMA_D = 4;              // rows prefetched ahead
-constexpr int TMA_NS = TMA_D + 3;     // stage slots (3 p rows are live per iteration)
 constexpr int TMA_PROW = TMA_W + 8;   // p row in shared memory: 4 halo floats each side
 constexpr long long TMA_TIMEOUT_CYCLES = 4000000000LL;  // ~2 s at 2 GHz
 
+// Stage ring per mode: consumers hold 3 stages (p rows z-1, z, z+1), the rest
+// are in flight.  7 stages of 6.2 KB (forward) and 4 CTAs per SM, 6 stages
+// of 12.3 KB (adjoint) 3 CTAs.
 template <int MODE>
 struct TmaLayout {
   static constexpr int NAUX = MODE == MODE_ADJ ? 5 : 2;  // d, fact (+ D, g, gc)
+  static constexpr int NS = MODE == MODE_ADJ ? 6 : 7;    // stage slots
+  static constexpr int MIN_BLOCKS = MODE == MODE_ADJ ? 3 : 4;
   static constexpr int STAGE = TMA_PROW + NAUX * TMA_W;  // floats per stage (multiple of 4)
-  static constexpr size_t BYTES = (size_t)TMA_NS * STAGE * sizeof(float) + TMA_NS * sizeof(unsigned long long);
+  static constexpr size_t BYTES = (size_t)NS * STAGE * sizeof(float) + 2 * NS * sizeof(unsigned long long);
 };
 
 __device__ __forceinline__ unsigned smem_u32(const void* p) {
@@ -480,6 +483,9 @@ __device__ __forceinline__ unsigned smem_u32(const void* p) {
 }
 __device__ __forceinline__ void mbar_init(unsigned long long* b, unsigned count) {
   asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(b)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(unsigned long long* b) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(b)) : "memory");
 }
 __device__ __forceinline__ void mbar_arrive_expect_tx(unsigned long long* b, unsigned bytes) {
   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(b)), "r"(bytes) : "memory");
@@ -509,12 +515,14 @@ __device__ __forceinline__ void tma_load_1d(void* dst, const void* src, unsigned
 }
 
 template <int MODE>
-__global__ void __launch_bounds__(128) k_ac2d_tma(const StepArgs A) {
+__global__ void __launch_bounds__(160, TmaLayout<MODE>::MIN_BLOCKS) k_ac2d_tma(const StepArgs A) {
   using Lay = TmaLayout<MODE>;
+  constexpr int TMA_NS = Lay::NS;
   extern __shared__ __align__(128) float smem[];
-  unsigned long long* bars = reinterpret_cast<unsigned long long*>(smem + (size_t)TMA_NS * Lay::STAGE);
+  unsigned long long* full = reinterpret_cast<unsigned long long*>(smem + (size_t)TMA_NS * Lay::STAGE);
+  unsigned long long* empty = full + TMA_NS;
   constexpr unsigned FULL = 0xffffffffu;
-  const int tid = threadIdx.x, lane = tid & 31;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int S = A.nshots;
   const int shot = blockIdx.x % S;
   const int tile = blockIdx.x / S;
@@ -525,12 +533,59 @@ __global__ void __launch_bounds__(128) k_ac2d_tma(const StepArgs A) {
   const int X0 = txi * TMA_W;
   if (z_begin >= z_end || X0 >= P) return;  // block-uniform
   const int rows = z_end - z_begin, nst = rows + 2;
-  const int x0 = X0 + 4 * tid;
-  const bool inb = x0 < P;
+
+  if (tid == 0) {
+    for (int k = 0; k < TMA_NS; ++k) {
+      mbar_init(&full[k], 1);
+      mbar_init(&empty[k], 4);
+    }
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
 
   const float* pc = fptr(A.pcur, shot);
-  float* __restrict__ pn = fptr(A.pnew, shot);
   const float* di = fptr(A.din, shot);
+  const float* dcr = MODE == MODE_ADJ ? fptr(A.dcorr, shot) : nullptr;
+  float* gg = MODE == MODE_ADJ ? fptr(A.g, shot) : nullptr;
+  float* gcp = MODE == MODE_ADJ ? fptr(A.gc, shot) : nullptr;
+
+  if (warp == 4) {
+    // producer: stage j carries p row z_begin-1+j and the aux rows of z_begin+j-2
+    if (lane != 0) return;
+    const int gx0 = max(X0 - 4, 0), gx1 = min(X0 + TMA_W + 4, P);
+    const int aw = min(TMA_W, P - X0);
+    for (int j = 0; j < nst; ++j) {
+      const int slot = j % TMA_NS;
+      if (j >= TMA_NS && !mbar_wait_bounded(&empty[slot], ((j / TMA_NS) - 1) & 1)) {
+        if (A.err) atomicExch(A.err, 1);
+        return;
+      }
+      float* st = smem + (size_t)slot * Lay::STAGE;
+      const int r = z_begin - 1 + j;
+      const bool aux = j >= 2;
+      unsigned bytes = (unsigned)(gx1 - gx0) * 4u;
+      if (aux) bytes += (unsigned)aw * 4u * Lay::NAUX;
+      mbar_arrive_expect_tx(&full[slot], bytes);
+      tma_load_1d(st + (gx0 - (X0 - 4)), pc + (long long)r * P + gx0, (unsigned)(gx1 - gx0) * 4u, &full[slot]);
+      if (aux) {
+        const long long row = (long long)(r - 1) * P + X0;  // aux row z = r - 1
+        float* a = st + TMA_PROW;
+        tma_load_1d(a, di + row, aw * 4u, &full[slot]);
+        tma_load_1d(a + TMA_W, A.fact + row, aw * 4u, &full[slot]);
+        if (MODE == MODE_ADJ) {
+          tma_load_1d(a + 2 * TMA_W, dcr + row, aw * 4u, &full[slot]);
+          tma_load_1d(a + 3 * TMA_W, gg + row, aw * 4u, &full[slot]);
+          tma_load_1d(a + 4 * TMA_W, gcp + row, aw * 4u, &full[slot]);
+        }
+      }
+    }
+    return;
+  }
+
+  // consumers
+  const int x0 = X0 + 4 * tid;
+  const bool inb = x0 < P;
+  float* __restrict__ pn = fptr(A.pnew, shot);
   float* dn = fptr(A.dout, shot);
   const float* cp = A.cpml + (long long)shot * A.cpml_stride;
   const int na = 2 * H + 2, nh = 2 * H, L = 2 * na + 2 * nh;
@@ -538,44 +593,6 @@ __global__ void __launch_bounds__(128) k_ac2d_tma(const StepArgs A) {
   float* ckd = fptr(A.ck_d, shot);
   float* Dw = nullptr;
   if (MODE == MODE_FWD_D && shot >= A.d_first) Dw = fptr(A.Dout, shot);
-  const float* dcr = MODE == MODE_ADJ ? fptr(A.dcorr, shot) : nullptr;
-  float* gg = MODE == MODE_ADJ ? fptr(A.g, shot) : nullptr;
-  float* gcp = MODE == MODE_ADJ ? fptr(A.gc, shot) : nullptr;
-
-  // producer: copies of stage j (p row z_begin-1+j; aux rows of z_begin+j-2)
-  const int gx0 = max(X0 - 4, 0), gx1 = min(X0 + TMA_W + 4, P);
-  const int aw = min(TMA_W, P - X0);
-  auto issue = [&](int j) {
-    const int slot = j % TMA_NS;
-    float* st = smem + (size_t)slot * Lay::STAGE;
-    const int r = z_begin - 1 + j;
-    unsigned bytes = (unsigned)(gx1 - gx0) * 4u;
-    const bool aux = j >= 2;
-    if (aux) bytes += (unsigned)aw * 4u * Lay::NAUX;
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    mbar_arrive_expect_tx(&bars[slot], bytes);
-    tma_load_1d(st + (gx0 - (X0 - 4)), pc + (long long)r * P + gx0, (unsigned)(gx1 - gx0) * 4u, &bars[slot]);
-    if (aux) {
-      const long long row = (long long)(r - 1) * P + X0;  // aux row z = r - 1
-      float* a = st + TMA_PROW;
-      tma_load_1d(a, di + row, aw * 4u, &bars[slot]);
-      tma_load_1d(a + TMA_W, A.fact + row, aw * 4u, &bars[slot]);
-      if (MODE == MODE_ADJ) {
-        tma_load_1d(a + 2 * TMA_W, dcr + row, aw * 4u, &bars[slot]);
-        tma_load_1d(a + 3 * TMA_W, gg + row, aw * 4u, &bars[slot]);
-        tma_load_1d(a + 4 * TMA_W, gcp + row, aw * 4u, &bars[slot]);
-      }
-    }
-  };
-
-  if (tid == 0) {
-    for (int k = 0; k < TMA_NS; ++k) mbar_init(&bars[k], 1);
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-  }
-  __syncthreads();
-  if (tid == 0)
-    for (int j = 0; j < min(TMA_NS, nst); ++j) issue(j);
-
   StripIO sx, sz;
   sx.psi_in = fptr(A.psi_in[0], shot);  sx.psi_out = fptr(A.psi_out[0], shot);
   sx.xi_in = fptr(A.xi_in[0], shot);    sx.xi_out = fptr(A.xi_out[0], shot);
@@ -589,19 +606,18 @@ __global__ void __launch_bounds__(128) k_ac2d_tma(const StepArgs A) {
   sz.psi_step = P; sz.xi_step = P;
   const bool xstrip = inb && (x0 < H || x0 + 3 >= nx - H);
   const bool vec_interior = (x0 >= 1) && (x0 + 3 <= nx - 2);
+  const int so = 4 + 4 * tid;
 
-  bool tout = false;
   for (int k = 0; k < rows; ++k) {
-    // stage k + TMA_D + 2 reuses the slot of stage k - 1, released by the barrier ending iteration k - 1
-    if (k > 0 && tid == 0 && k + TMA_D + 2 < nst) issue(k + TMA_D + 2);
+    bool ok = true;
     if (k == 0) {
-      tout |= !mbar_wait_bounded(&bars[0], 0);
-      tout |= !mbar_wait_bounded(&bars[1 % TMA_NS], 0);
+      ok = ok && mbar_wait_bounded(&full[0], 0);
+      ok = ok && mbar_wait_bounded(&full[1 % TMA_NS], 0);
     }
     const int j2 = k + 2;
-    tout |= !mbar_wait_bounded(&bars[j2 % TMA_NS], (j2 / TMA_NS) & 1);
-    if (__syncthreads_or(tout)) {
-      if (tid == 0 && A.err) atomicExch(A.err, 1);
+    ok = ok && mbar_wait_bounded(&full[j2 % TMA_NS], (j2 / TMA_NS) & 1);
+    if (!__all_sync(FULL, ok)) {
+      if (lane == 0 && A.err) atomicExch(A.err, 1);
       return;
     }
     const float* sm_ = smem + (size_t)(k % TMA_NS) * Lay::STAGE;        // p row z-1
@@ -609,7 +625,6 @@ __global__ void __launch_bounds__(128) k_ac2d_tma(const StepArgs A) {
     const float* sp_ = smem + (size_t)(j2 % TMA_NS) * Lay::STAGE;       // p row z+1, aux rows of z
     const int z = z_begin + k;
     const long long row = (long long)z * P;
-    const int so = 4 + 4 * tid;
     float rm[4], r0[4], rp[4], o[4], f[4];
     {
       const float4 a = *reinterpret_cast<const float4*>(sm_ + so);
@@ -627,6 +642,19 @@ __global__ void __launch_bounds__(128) k_ac2d_tma(const StepArgs A) {
     float right = __shfl_down_sync(FULL, r0[0], 1);
     if (lane == 0) left = s0_[so - 1];
     if (lane == 31) right = s0_[so + 4];
+    float dv[4], g4[4], c4[4];
+    if (MODE == MODE_ADJ) {
+      const float4 dv4 = *reinterpret_cast<const float4*>(sp_ + TMA_PROW + 2 * TMA_W + 4 * tid);
+      const float4 g4v = *reinterpret_cast<const float4*>(sp_ + TMA_PROW + 3 * TMA_W + 4 * tid);
+      const float4 c4v = *reinterpret_cast<const float4*>(sp_ + TMA_PROW + 4 * TMA_W + 4 * tid);
+      dv[0] = dv4.x; dv[1] = dv4.y; dv[2] = dv4.z; dv[3] = dv4.w;
+      g4[0] = g4v.x; g4[1] = g4v.y; g4[2] = g4v.z; g4[3] = g4v.w;
+      c4[0] = c4v.x; c4[1] = c4v.y; c4[2] = c4v.z; c4[3] = c4v.w;
+    }
+    // stage k (p row z-1) is no longer read by this warp
+    __syncwarp();
+    if (lane == 0) mbar_arrive(&empty[k % TMA_NS]);
+
     const bool zstrip = (z < H) || (z >= nz - H);
     sx.psi_base = (long long)z * nh;
     sx.xi_base = (long long)z * na;
@@ -657,12 +685,6 @@ __global__ void __launch_bounds__(128) k_ac2d_tma(const StepArgs A) {
         st4(ckd + row + x0, o);
       }
       if (MODE == MODE_ADJ) {
-        const float4 dv4 = *reinterpret_cast<const float4*>(sp_ + TMA_PROW + 2 * TMA_W + 4 * tid);
-        const float4 g4v = *reinterpret_cast<const float4*>(sp_ + TMA_PROW + 3 * TMA_W + 4 * tid);
-        const float4 c4v = *reinterpret_cast<const float4*>(sp_ + TMA_PROW + 4 * TMA_W + 4 * tid);
-        float dv[4] = {dv4.x, dv4.y, dv4.z, dv4.w};
-        float g4[4] = {g4v.x, g4v.y, g4v.z, g4v.w};
-        float c4[4] = {c4v.x, c4v.y, c4v.z, c4v.w};
 #pragma unroll
         for (int e = 0; e < 4; ++e)
           if (x0 + e >= 1 && x0 + e <= nx - 2) kahan_add(g4[e], c4[e], outp[e] * dv[e]);
@@ -691,7 +713,6 @@ __global__ void __launch_bounds__(128) k_ac2d_tma(const StepArgs A) {
         }
       }
     }
-    __syncthreads();  // the slot of p row z-1 is free again
   }
 }
 
