@@ -105,7 +105,7 @@ def oracle_gradient(oracle, sw, case: Case, shot: Shot, check_freq=1, mute_src=0
 class GpuRun:
     """Drives libswgb300 directly through its C ABI for one case."""
 
-    def __init__(self, sw, case: Case, gradient=False, check_freq=1, mute_src=0, mute_rec=0):
+    def __init__(self, sw, case: Case, gradient=False, check_freq=1, mute_src=0, mute_rec=0, variant=0, tz=0):
         L = sw._lib
         self.sw, self.case, self.L = sw, case, L
         self.ctx = L.Context(0)
@@ -122,6 +122,8 @@ class GpuRun:
                                                       ctypes.byref(gp), ctypes.byref(self.h)), "create")
         vp32 = np.asfortranarray(case.vp, dtype=np.float32)
         self.ctx.check(self.ctx.lib.sw_wavesim_set_vp(self.h, vp32.ctypes.data, 0), "set_vp")
+        if variant or tz:
+            self.ctx.check(self.ctx.lib.sw_wavesim_set_tuning(self.h, int(tz), int(variant)), "set_tuning")
 
     def _structs(self, shots, grad):
         L = self.L

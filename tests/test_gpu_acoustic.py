@@ -215,3 +215,20 @@ def test_gradient_3d_matches_oracle(sw, oracle):
     gref, mref, _ = oracle_gradient(oracle, sw, case, shot, check_freq=13)
     assert abs(msf - mref) / abs(mref) < MISFIT_TOL
     assert rel_l2(g, gref) < GRAD_TOL
+
+
+@pytest.mark.parametrize("tz", [0, 7, 64])
+def test_2d_stencil_variants_match_oracle(sw, oracle, tz):
+    """The TMA-pipelined 2D stencil (variant 1) and the register-pipelined one
+    (variant 0) give the oracle's traces and gradient for any tile height."""
+    case, shot = _grad_case(sw, oracle, nt=300, freetop=True, halo=12, seed=8)
+    gref, mref, tref = oracle_gradient(oracle, sw, case, shot, check_freq=11)
+    for variant in (0, 1):
+        run = GpuRun(sw, case, gradient=True, check_freq=11, variant=variant, tz=tz)
+        g, msf, tr = run.gradient([shot])
+        fw = run.forward([shot])[0]
+        run.close()
+        assert rel_l2(tr[0], tref) < TRACE_TOL
+        assert rel_l2(fw, tref) < TRACE_TOL
+        assert abs(msf - mref) / abs(mref) < MISFIT_TOL
+        assert rel_l2(g, gref) < GRAD_TOL
