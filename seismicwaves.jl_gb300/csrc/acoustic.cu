@@ -606,12 +606,16 @@ struct StepCtx {
   int tiles_x, tiles_y, tiles_z;
 };
 
+// Warps per block of the register-pipelined 2D stencil (variant 0: 4, 2: 8, 3: 16).
+int block_warps(const sw_wavesim* ws) { return ws->variant == 2 ? 8 : ws->variant == 3 ? 16 : 4; }
+
 StepCtx make_step_ctx(sw_wavesim* ws, int S) {
   StepCtx c{ws, 0, 0, 1, 0};
   const int sms = ws->ctx->num_sms > 0 ? ws->ctx->num_sms : 148;
   const int nint = ws->n[ws->N - 1] - 2;  // interior extent of the marching axis
   if (ws->N == 2) {
-    c.tiles_x = (int)((ws->P + 511) / 512);
+    const int w = 128 * block_warps(ws);
+    c.tiles_x = (int)((ws->P + w - 1) / w);
   } else {
     c.tiles_x = (int)((ws->P + 127) / 128);
     c.tiles_y = (ws->n[1] - 2 + 3) / 4;
@@ -697,7 +701,13 @@ struct Launcher {
       enable_tma_smem<MODE>();
       k_ac2d_tma<MODE><<<(unsigned)blocks, 160, TmaLayout<MODE>::BYTES, st>>>(a);
     } else if (ws->N == 2) {
-      k_ac2d_step<MODE><<<(unsigned)blocks, 128, 0, st>>>(a);
+      const int nw = block_warps(ws);
+      if (nw == 4)
+        k_ac2d_step<MODE, 4><<<(unsigned)blocks, 128, 0, st>>>(a);
+      else if (nw == 8)
+        k_ac2d_step<MODE, 8><<<(unsigned)blocks, 256, 0, st>>>(a);
+      else
+        k_ac2d_step<MODE, 16><<<(unsigned)blocks, 512, 0, st>>>(a);
     } else {
       k_ac3d_step<MODE><<<(unsigned)blocks, 128, 0, st>>>(a);
     }

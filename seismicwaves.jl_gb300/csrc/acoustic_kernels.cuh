@@ -144,18 +144,29 @@ __device__ __forceinline__ float* fptr(const FieldArg& f, int shot) {
 // side in x (512 x points); tile = 512 x points x TZ rows.
 // psi_0 / xi_0 layout: [z][q] (q fastest);  psi_1 / xi_1 layout: [q][P].
 // ---------------------------------------------------------------------------
-template <int MODE>
-__global__ void __launch_bounds__(128) k_ac2d_step(const StepArgs A) {
+// Minimum resident blocks per SM for a block of NW warps: keeps the forward
+// kernels at <= 72 registers (4 warps) or <= 64 (8 and 16 warps); the adjoint,
+// which holds a second row of six arrays in registers, at 128.
+template <int MODE, int NW>
+struct Ac2dBounds {
+  static constexpr int MINB = MODE == MODE_ADJ ? (NW == 4 ? 4 : NW == 8 ? 2 : 1) : (NW == 4 ? 7 : NW == 8 ? 4 : 2);
+};
+
+template <int MODE, int NW>
+__global__ void __launch_bounds__(32 * NW, (Ac2dBounds<MODE, NW>::MINB)) k_ac2d_step(const StepArgs A) {
   constexpr unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  constexpr int nwarps = NW;
   const int S = A.nshots;
-  const int shot = blockIdx.x % S;
-  const int tile = blockIdx.x / S;
-  const int txi = tile % A.tiles_x, tzi = tile / A.tiles_x;
+  // block order: x tiles fastest (neighbouring CTAs stream one contiguous row
+  // together), then shots (the shots of a row band share fact through L2)
+  const int txi = blockIdx.x % A.tiles_x;
+  const int rest = blockIdx.x / A.tiles_x;
+  const int shot = rest % S, tzi = rest / S;
   const int nx = A.n0, nz = A.n1, P = A.P, H = A.halo;
   const int z_begin = 1 + tzi * A.TZ;
   const int z_end = min(z_begin + A.TZ, nz - 1);
-  const int wx0 = (txi * 4 + warp) * 128;
+  const int wx0 = (txi * nwarps + warp) * 128;
   if (z_begin >= z_end || wx0 >= P) return;  // warp-uniform
   const int x0 = wx0 + lane * 4;
   const bool inb = x0 < P;

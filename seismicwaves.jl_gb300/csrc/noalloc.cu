@@ -269,7 +269,7 @@ int run(const sw_acoustic_params* p, const float* vp, const sw_acoustic_shot* s,
       a.xi_in[d] = FieldArg{xi[d], 0};
       a.xi_out[d] = a.xi_in[d];
     }
-    k_ac2d_step<MODE_FWD><<<(unsigned)(tiles_x * tiles_z), 128, 0, st>>>(a);
+    k_ac2d_step<MODE_FWD, 4><<<(unsigned)(tiles_x * tiles_z), 128, 0, st>>>(a);
     k_noalloc_inject_record<<<1, 128, 0, st>>>(T, pb[1 - pc], db, it);
     pc = 1 - pc;
     pk = 1 - pk;
