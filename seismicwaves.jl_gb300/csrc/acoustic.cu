@@ -310,6 +310,7 @@ struct sw_wavesim {
   DevMem d_mute, d_mute_ptr;
   int tile_tz = 0;  // 0 = heuristic
   int variant = 0;  // 2D stencil: 0 = register-pipelined, 1 = TMA
+  int pf = 0;       // 2D stencil: L2 prefetch distance in rows (0 = off)
 };
 
 namespace {
@@ -738,6 +739,7 @@ StepArgs base_args(sw_wavesim* ws, const StepCtx& c, int S) {
   a.tiles_z = c.tiles_z;
   a.TZ = c.TZ;
   a.err = ws->ctx->err.as<int>();
+  a.pf = ws->pf;
   return a;
 }
 
@@ -1212,7 +1214,8 @@ void acoustic_gradient(sw_wavesim* ws, int nshots, const sw_acoustic_shot* shots
 
 void wavesim_set_tuning(sw_wavesim* ws, int tz, int variant) {
   ws->tile_tz = tz;
-  ws->variant = variant;
+  ws->variant = variant % 16;
+  ws->pf = variant / 16;
 }
 sw_ctx* wavesim_ctx(sw_wavesim* ws) { return ws->ctx; }
 sw_wavesim* wavesim_new() { return new sw_wavesim(); }

@@ -57,6 +57,7 @@ struct StepArgs {
   int nshots;
   int tiles_x, tiles_y, tiles_z, TZ;
   int* err;                                        // set to 1 when a bounded wait gives up
+  int pf;                                          // 2D stencil: rows ahead prefetched into L2 (0 = off)
 };
 
 struct StripIO {
@@ -133,6 +134,12 @@ __device__ __forceinline__ float cpml_axis_term(float d2, float pl, float p0, fl
   const float xn = s.b[qr] * xo + s.a[qr] * t;
   s.xi_out[iq] = xn;
   return t + xn;
+}
+
+// TMA prefetch of a contiguous global range into L2 (no registers, no
+// completion to wait for).  Address 16-byte aligned, size a multiple of 16.
+__device__ __forceinline__ void l2_prefetch(const void* p, unsigned bytes) {
+  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
 }
 
 __device__ __forceinline__ float* fptr(const FieldArg& f, int shot) {
@@ -219,8 +226,21 @@ __global__ void __launch_bounds__(32 * NW, (Ac2dBounds<MODE, NW>::MINB)) k_ac2d_
       ld4rw(c4, gcp + row + xa);
     }
   }
+  // one lane per warp asks the TMA unit to pull the warp's segments of a row
+  // A.pf rows ahead into L2, so the register loads of that row later hit L2
+  const unsigned seg = (unsigned)min(128, P - wx0) * 4u;
   for (int z = z_begin; z < z_end; ++z) {
     const long long row = (long long)z * P;
+    if (A.pf > 0 && lane == 0 && z + A.pf < z_end) {
+      const long long prow = row + (long long)A.pf * P + wx0;
+      l2_prefetch(pc + prow + P, seg);
+      l2_prefetch(di + prow, seg);
+      if (MODE == MODE_ADJ) {
+        l2_prefetch(dcr + prow, seg);
+        l2_prefetch(gg + prow, seg);
+        l2_prefetch(gcp + prow, seg);
+      }
+    }
     float rpn[4], on[4], fn[4], dvn[4], g4n[4], c4n[4];
     const bool more = z + 1 < z_end;
     if (more) {
