@@ -688,26 +688,6 @@ void enable_tma_smem() {
   done_for_device = dev;
 }
 
-// Blocks of a persistent launch: what the GPU holds at once (occupancy x SMs),
-// capped by the number of work items.
-template <typename K>
-unsigned persistent_grid(K kernel, int threads, long long items) {
-  static int cached_dev = -1, cached_threads = 0, cached_blocks = 0;
-  static const void* cached_fn = nullptr;
-  int dev = 0;
-  check_cuda(cudaGetDevice(&dev), "cudaGetDevice");
-  if (cached_fn != (const void*)kernel || cached_dev != dev || cached_threads != threads) {
-    int per_sm = 0, sms = 0;
-    check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, 0), "occupancy");
-    check_cuda(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "SM count");
-    cached_blocks = std::max(1, per_sm) * sms;
-    cached_fn = (const void*)kernel;
-    cached_dev = dev;
-    cached_threads = threads;
-  }
-  return (unsigned)std::min<long long>(items, cached_blocks);
-}
-
 struct Launcher {
   sw_wavesim* ws;
   cudaStream_t st;
@@ -724,11 +704,11 @@ struct Launcher {
     } else if (ws->N == 2) {
       const int nw = block_warps(ws);
       if (nw == 4)
-        k_ac2d_step<MODE, 4><<<persistent_grid(k_ac2d_step<MODE, 4>, 128, blocks), 128, 0, st>>>(a);
+        k_ac2d_step<MODE, 4><<<(unsigned)blocks, 128, 0, st>>>(a);
       else if (nw == 8)
-        k_ac2d_step<MODE, 8><<<persistent_grid(k_ac2d_step<MODE, 8>, 256, blocks), 256, 0, st>>>(a);
+        k_ac2d_step<MODE, 8><<<(unsigned)blocks, 256, 0, st>>>(a);
       else
-        k_ac2d_step<MODE, 16><<<persistent_grid(k_ac2d_step<MODE, 16>, 512, blocks), 512, 0, st>>>(a);
+        k_ac2d_step<MODE, 16><<<(unsigned)blocks, 512, 0, st>>>(a);
     } else {
       k_ac3d_step<MODE><<<(unsigned)blocks, 128, 0, st>>>(a);
     }

@@ -156,26 +156,25 @@ __device__ __forceinline__ float* fptr(const FieldArg& f, int shot) {
 // which holds a second row of six arrays in registers, at 128.
 template <int MODE, int NW>
 struct Ac2dBounds {
-  static constexpr int MINB = MODE == MODE_ADJ ? (NW == 4 ? 3 : NW == 8 ? 2 : 1) : (NW == 4 ? 6 : NW == 8 ? 4 : 2);
+  static constexpr int MINB = MODE == MODE_ADJ ? (NW == 4 ? 4 : NW == 8 ? 2 : 1) : (NW == 4 ? 7 : NW == 8 ? 4 : 2);
 };
 
-// Work item `item` of the 2D stencil: x tiles fastest (neighbouring blocks
-// stream one contiguous row together), then shots (the shots of a row band
-// share fact through L2), then row bands.
 template <int MODE, int NW>
-__device__ __forceinline__ void ac2d_item(const StepArgs& A, int item) {
+__global__ void __launch_bounds__(32 * NW, (Ac2dBounds<MODE, NW>::MINB)) k_ac2d_step(const StepArgs A) {
   constexpr unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   constexpr int nwarps = NW;
   const int S = A.nshots;
-  const int txi = item % A.tiles_x;
-  const int rest = item / A.tiles_x;
+  // block order: x tiles fastest (neighbouring CTAs stream one contiguous row
+  // together), then shots (the shots of a row band share fact through L2)
+  const int txi = blockIdx.x % A.tiles_x;
+  const int rest = blockIdx.x / A.tiles_x;
   const int shot = rest % S, tzi = rest / S;
   const int nx = A.n0, nz = A.n1, P = A.P, H = A.halo;
   const int z_begin = 1 + tzi * A.TZ;
   const int z_end = min(z_begin + A.TZ, nz - 1);
   const int wx0 = (txi * nwarps + warp) * 128;
-  if (z_begin >= z_end || wx0 >= P) return;  // warp-uniform (ends this item only)
+  if (z_begin >= z_end || wx0 >= P) return;  // warp-uniform
   const int x0 = wx0 + lane * 4;
   const bool inb = x0 < P;
   const int xa = inb ? x0 : P - 4;
@@ -328,42 +327,6 @@ __device__ __forceinline__ void ac2d_item(const StepArgs& A, int item) {
         if (MODE == MODE_ADJ) { dv[e] = dvn[e]; g4[e] = g4n[e]; c4[e] = c4n[e]; }
       }
     }
-  }
-}
-
-
-// L2 prefetch of the first rows a warp reads in work item `item`.
-template <int MODE, int NW>
-__device__ __forceinline__ void ac2d_prefetch_item(const StepArgs& A, int item) {
-  const int txi = item % A.tiles_x;
-  const int rest = item / A.tiles_x;
-  const int shot = rest % A.nshots, tzi = rest / A.nshots;
-  const int wx0 = (txi * NW + (threadIdx.x >> 5)) * 128;
-  const int z0 = 1 + tzi * A.TZ;
-  if (wx0 >= A.P || z0 >= A.n1 - 1) return;
-  const unsigned seg = (unsigned)min(128, A.P - wx0) * 4u;
-  const int zl = min(z0 + 2, A.n1 - 1);
-  for (int r = z0 - 1; r <= zl; ++r) l2_prefetch(fptr(A.pcur, shot) + (long long)r * A.P + wx0, seg);
-  l2_prefetch(fptr(A.din, shot) + (long long)z0 * A.P + wx0, seg);
-  if (MODE == MODE_ADJ) {
-    l2_prefetch(fptr(A.dcorr, shot) + (long long)z0 * A.P + wx0, seg);
-    l2_prefetch(fptr(A.g, shot) + (long long)z0 * A.P + wx0, seg);
-    l2_prefetch(fptr(A.gc, shot) + (long long)z0 * A.P + wx0, seg);
-  }
-}
-
-// Persistent launch: gridDim.x blocks (what fits on the GPU at once) walk the
-// work items with a fixed stride.  After finishing an item a warp asks for
-// the first rows of the item after next in L2, one item of lead time, which
-// hides most of the per-item start-up of the row march.
-template <int MODE, int NW>
-__global__ void __launch_bounds__(32 * NW, (Ac2dBounds<MODE, NW>::MINB)) k_ac2d_step(const StepArgs A) {
-  const int items = A.nshots * A.tiles_x * A.tiles_z;
-#pragma unroll 1
-  for (int item = blockIdx.x; item < items; item += gridDim.x) {
-    ac2d_item<MODE, NW>(A, item);
-    const int ahead = item + 2 * gridDim.x;
-    if (ahead < items && (threadIdx.x & 31) == 0) ac2d_prefetch_item<MODE, NW>(A, ahead);
   }
 }
 
