@@ -623,14 +623,20 @@ StepCtx make_step_ctx(sw_wavesim* ws, int S) {
   }
   int TZ = ws->tile_tz;
   if (TZ <= 0) {
-    // aim for >= ~8 blocks per SM in total, with TZ in [16, 64] (the 2D kernel's
-    // row pipeline needs a few rows per block to fill)
-    TZ = 64;
-    const int tz_min = (ws->N == 2 && ws->variant == 1) ? 16 : 8;
-    while (TZ > tz_min) {
-      const long long blocks = (long long)S * c.tiles_x * c.tiles_y * ((nint + TZ - 1) / TZ);
-      if (blocks >= 8LL * sms) break;
-      TZ /= 2;
+    if (ws->N == 2 && ws->variant != 1) {
+      // register-pipelined 2D stencil: short bands keep every SM at full
+      // occupancy with a negligible tail (8 rows measured best on GB300 for
+      // 64 shots of 2001 x 801: 55.6 Gpts/s against 48.4 at 64 rows)
+      TZ = 8;
+    } else {
+      // aim for >= ~8 blocks per SM in total, with TZ in [tz_min, 64]
+      TZ = 64;
+      const int tz_min = (ws->N == 2 && ws->variant == 1) ? 16 : 8;
+      while (TZ > tz_min) {
+        const long long blocks = (long long)S * c.tiles_x * c.tiles_y * ((nint + TZ - 1) / TZ);
+        if (blocks >= 8LL * sms) break;
+        TZ /= 2;
+      }
     }
   }
   c.TZ = TZ;
