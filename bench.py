@@ -49,6 +49,7 @@ def _args():
     p.add_argument("--nt", type=int, default=0, help="cap every shot's time steps (small profiling cases)")
     p.add_argument("--tz", type=int, default=0, help="stencil tile height (0 = library heuristic)")
     p.add_argument("--variant", type=int, default=-1, help="2D stencil variant (-1 = library default)")
+    p.add_argument("--autotune", action="store_true", help="pick variant and band height with the autotuner")
     return p.parse_args()
 
 
@@ -317,6 +318,16 @@ def run_gb300(a):
     if a.tz or a.variant >= 0:
         R.ctx.check(R.lib.sw_wavesim_set_tuning(R.h, a.tz, max(a.variant, 0)), "sw_wavesim_set_tuning")
     R.make_observed()
+    tuned = None
+    if a.autotune:
+        from seismicwaves_gb300 import tune
+
+        allidx0 = list(range(len(w.shots)))
+        arr = R.structs(allidx0, [x.data_ptr() for x in R.tf_d], [x.data_ptr() for x in R.tr_d], None)
+        choice, timings = tune.autotune(R.ctx, R.h, (w.vp.shape, w.halo), arr, len(allidx0), w.vp.ndim,
+                                        on_device=1)
+        tuned = {"variant": choice[0], "tz": choice[1],
+                 "trial_ms": {f"{v}/{tz}": round(t * 1e3, 3) for (v, tz), t in timings.items()}}
     nshots = len(w.shots)
     allidx = list(range(nshots))
     pts = float(w.point_steps())
@@ -400,7 +411,7 @@ def run_gb300(a):
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "gpu_launches": total_launches,
             "roofline": roof,
-            "tuning": {"tz": a.tz, "variant": a.variant}}
+            "tuning": tuned or {"tz": a.tz, "variant": a.variant}}
     if not a.no_cpu:
         import oracle
 

@@ -626,8 +626,9 @@ StepCtx make_step_ctx(sw_wavesim* ws, int S) {
     if (ws->N == 2 && ws->variant != 1) {
       // register-pipelined 2D stencil: short bands keep every SM at full
       // occupancy with a negligible tail (8 rows measured best on GB300 for
-      // 64 shots of 2001 x 801: 55.6 Gpts/s against 48.4 at 64 rows)
-      TZ = 8;
+      // 64 shots of 2001 x 801: 55.6 Gpts/s against 48.4 at 64 rows); small
+      // batches take 4-row bands to fill the GPU
+      TZ = (long long)S * c.tiles_x * ((nint + 7) / 8) < 4LL * sms ? 4 : 8;
     } else {
       // aim for >= ~8 blocks per SM in total, with TZ in [tz_min, 64]
       TZ = 64;
