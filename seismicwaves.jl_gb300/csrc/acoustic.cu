@@ -113,18 +113,32 @@ __global__ void k_inject_record(const ShotDesc* __restrict__ desc, const long lo
 // with the prescaled residuals) and the matching correlation term: the fused
 // stencil correlated interior lambda before injection, so g += a * D is added
 // here (boundary nodes, which the stencil skips, add their full lambda * D).
+__device__ void adj_inject_shot(const ShotDesc& D, const long long* __restrict__ pts, const int* __restrict__ ptr,
+                                const int* __restrict__ ids, const int* __restrict__ bslot, float* lp, float* ld,
+                                const float* dp, float* gp, float* cp, int it);
+
+// One block per accumulator group (grp consecutive shots share one gradient
+// pair); the group's shots are handled one after the other, so receivers of
+// different shots on the same grid point never update the pair concurrently.
 __global__ void k_adj_inject(const ShotDesc* __restrict__ desc, const long long* __restrict__ pts,
                              const int* __restrict__ ptr, const int* __restrict__ ids,
                              const int* __restrict__ bslot, FieldArg lam, FieldArg lamd, FieldArg dcorr, FieldArg g,
-                             FieldArg gc, int it) {
-  const int shot = blockIdx.x;
-  const ShotDesc D = desc[shot];
+                             FieldArg gc, int it, int nshots, int grp) {
+  float* gp = g.p + (long long)blockIdx.x * g.s;
+  float* cp = gc.p + (long long)blockIdx.x * gc.s;
+  for (int j = 0; j < grp; ++j) {
+    const int shot = blockIdx.x * grp + j;
+    if (shot >= nshots) break;
+    if (j > 0) __syncthreads();
+    adj_inject_shot(desc[shot], pts, ptr, ids, bslot, lam.p + (long long)shot * lam.s,
+                    lamd.p + (long long)shot * lamd.s, dcorr.p + (long long)shot * dcorr.s, gp, cp, it);
+  }
+}
+
+__device__ void adj_inject_shot(const ShotDesc& D, const long long* __restrict__ pts, const int* __restrict__ ptr,
+                                const int* __restrict__ ids, const int* __restrict__ bslot, float* lp, float* ld,
+                                const float* dp, float* gp, float* cp, int it) {
   if (it > D.nt) return;
-  float* lp = lam.p + (long long)shot * lam.s;
-  float* ld = lamd.p + (long long)shot * lamd.s;
-  const float* dp = dcorr.p + (long long)shot * dcorr.s;
-  float* gp = g.p + (long long)shot * g.s;
-  float* cp = gc.p + (long long)shot * gc.s;
   for (int u = threadIdx.x; u < D.nrp; u += blockDim.x) {
     const long long lin = pts[D.rp_off + u];
     const int k0 = ptr[D.rp_ptr + u], k1 = ptr[D.rp_ptr + u + 1];
@@ -311,6 +325,7 @@ struct sw_wavesim {
   int tile_tz = 0;  // 0 = heuristic
   int variant = 0;  // 2D stencil: 0 = register-pipelined, 1 = TMA
   int pf = 0;       // 2D stencil: L2 prefetch distance in rows (0 = off)
+  int grp = 1;      // shots per gradient accumulator in the adjoint (4: shot sum fused, 1: per shot)
 };
 
 namespace {
@@ -650,7 +665,7 @@ StepCtx make_step_ctx(sw_wavesim* ws, int S) {
 // the launch; per damping-strip cell and axis R/W psi and R/W xi; D write
 // (forward of the gradient), R D + RMW g and its compensation (adjoint);
 // checkpoint copies of p, d, psi, xi.
-double stencil_bytes(const sw_wavesim* ws, int S, int mode, int n_dwrite, bool ckpt) {
+double stencil_bytes(const sw_wavesim* ws, int S, int mode, int n_dwrite, bool ckpt, int ngroups = -1) {
   double pts = 1.0;
   for (int d = 0; d < ws->N; ++d) pts *= (double)(ws->n[d] - 2);
   double strip = 0.0;  // interior points inside the damping strips, summed over axes
@@ -665,7 +680,7 @@ double stencil_bytes(const sw_wavesim* ws, int S, int mode, int n_dwrite, bool c
   }
   double b = (16.0 * S + 4.0) * pts + 16.0 * strip * S;
   if (mode == MODE_FWD_D) b += 4.0 * pts * n_dwrite;
-  if (mode == MODE_ADJ) b += 20.0 * pts * S;
+  if (mode == MODE_ADJ) b += ngroups < 0 ? 20.0 * pts * S : (4.0 * S + 16.0 * ngroups) * pts;
   if (ckpt) b += 8.0 * pts * S + 8.0 * strip * S;
   return b;
 }
@@ -942,12 +957,27 @@ void adjoint_group(sw_wavesim* ws, const std::vector<HostShot>& group) {
     a.dcorr = FieldArg{ws->dbuf.as<float>() + dslot * F, ws->d_slots * F};
     a.g = fa(ws->g, F);
     a.gc = fa(ws->gc, F);
-    L.step<MODE_ADJ>(a, c, stencil_bytes(ws, Sa, MODE_ADJ, 0, false));
+    if (ws->grp == 4) {
+      // 4 shots per block (one per warp) over 128-wide tiles; the correlation is
+      // summed over the group before its single Kahan update
+      StepArgs b = a;
+      b.tiles_x = (int)((ws->P + 127) / 128);
+      const int ngrp = (Sa + 3) / 4;
+      const long long blocks = (long long)ngrp * b.tiles_x * b.tiles_z;
+      check_vector_alignment(b);
+      cudaEvent_t ev0 = nullptr;
+      ws->ctx->prof.begin(st, KK_ADJOINT, stencil_bytes(ws, Sa, MODE_ADJ, 0, false, ngrp), &ev0);
+      k_ac2d_adj_grp<<<(unsigned)blocks, 128, 0, st>>>(b);
+      check_cuda(cudaGetLastError(), "adjoint stencil launch");
+      ws->ctx->prof.end(st, KK_ADJOINT, ev0);
+    } else {
+      L.step<MODE_ADJ>(a, c, stencil_bytes(ws, Sa, MODE_ADJ, 0, false));
+    }
     cudaEvent_t ev = nullptr;
     ws->ctx->prof.begin(st, KK_SRCREC, 0.0, &ev);
-    k_adj_inject<<<Sa, 128, 0, st>>>(ws->d_desc.as<ShotDesc>(), ws->d_pts.as<long long>(), ws->d_ptr.as<int>(),
-                                     ws->d_ids.as<int>(), ws->d_bslot.as<int>(), a.pnew, a.dout, a.dcorr, a.g, a.gc,
-                                     it);
+    k_adj_inject<<<(Sa + ws->grp - 1) / ws->grp, 128, 0, st>>>(
+        ws->d_desc.as<ShotDesc>(), ws->d_pts.as<long long>(), ws->d_ptr.as<int>(), ws->d_ids.as<int>(),
+        ws->d_bslot.as<int>(), a.pnew, a.dout, a.dcorr, a.g, a.gc, it, Sa, ws->grp);
     check_cuda(cudaGetLastError(), "adjoint inject launch");
     ws->ctx->prof.end(st, KK_SRCREC, ev);
     apc = 1 - apc;
@@ -1133,6 +1163,9 @@ void acoustic_gradient(sw_wavesim* ws, int nshots, const sw_acoustic_shot* shots
     dev_alloc(dmis, sizeof(double), "misfit output", ws->ctx->stream);
     mout = dmis.as<double>();
   }
+  // the shot sum is fused into the 2D adjoint for batches of 4 or more shots,
+  // unless per-shot muting needs each shot's gradient
+  ws->grp = (!mute && ws->N == 2 && ws->variant != 1 && nshots >= 4) ? 4 : 1;
   bool first_group = true;
   for (const auto& group : plan_groups(ws, order, true)) {
     const int S = (int)group.size();
@@ -1201,7 +1234,8 @@ void acoustic_gradient(sw_wavesim* ws, int nshots, const sw_acoustic_shot* shots
       cudaEvent_t ev = nullptr;
       ws->ctx->prof.begin(st, KK_OTHER, 0.0, &ev);
       const long long blocks = std::min<long long>((ws->npts + 255) / 256, 8192);
-      k_reduce_grad<<<(unsigned)blocks, 256, 0, st>>>(ws->g.as<float>(), ws->gc.as<float>(), ws->F, S,
+      k_reduce_grad<<<(unsigned)blocks, 256, 0, st>>>(ws->g.as<float>(), ws->gc.as<float>(), ws->F,
+                                                      (S + ws->grp - 1) / ws->grp,
                                                       ws->vp.as<float>(), ws->n[0], ws->npts, ws->P,
                                                       1.0 / (ws->prm.dt * ws->prm.dt), gout,
                                                       first_group ? 0 : 1);

@@ -330,6 +330,174 @@ __global__ void __launch_bounds__(32 * NW, (Ac2dBounds<MODE, NW>::MINB)) k_ac2d_
   }
 }
 
+
+// ---------------------------------------------------------------------------
+// 2D adjoint step for a group of 4 shots with the correlation summed over the
+// group before it is accumulated.  Warp w of a block runs shot 4*group + w
+// over the same 128 x points and row band (the same per-shot arithmetic as
+// k_ac2d_step<MODE_ADJ>); per row the four products lambda * D of a point are
+// added in shot order and Kahan-accumulated once into the group's gradient
+// pair (g, gc).  The per-point read-modify-write of the accumulator is thus
+// shared by 4 shots (36 -> 24 bytes per shot and point); the fixed order
+// keeps the result deterministic.  Warps of inactive shots (it > nt) only
+// take part in the block barriers.
+// ---------------------------------------------------------------------------
+static __global__ void __launch_bounds__(128, 4) k_ac2d_adj_grp(const StepArgs A) {
+  constexpr unsigned FULL = 0xffffffffu;
+  __shared__ float4 prod[2][4][32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int S = A.nshots;
+  const int ngrp = (S + 3) / 4;
+  const int txi = blockIdx.x % A.tiles_x;
+  const int rest = blockIdx.x / A.tiles_x;
+  const int grp = rest % ngrp, tzi = rest / ngrp;
+  const int shot = grp * 4 + warp;
+  const bool active = shot < S;
+  const int nx = A.n0, nz = A.n1, P = A.P, H = A.halo;
+  const int z_begin = 1 + tzi * A.TZ;
+  const int z_end = min(z_begin + A.TZ, nz - 1);
+  const int wx0 = txi * 128;
+  if (z_begin >= z_end || wx0 >= P) return;  // block-uniform
+  const int x0 = wx0 + lane * 4;
+  const bool inb = x0 < P;
+  const int xa = inb ? x0 : P - 4;
+  const int sh = active ? shot : 0;
+
+  const float* __restrict__ pc = fptr(A.pcur, sh);
+  float* __restrict__ pn = fptr(A.pnew, sh);
+  const float* di = fptr(A.din, sh);
+  float* dn = fptr(A.dout, sh);
+  const float* __restrict__ fa = A.fact;
+  const float* dcr = fptr(A.dcorr, sh);
+  const float* cp = A.cpml + (long long)sh * A.cpml_stride;
+  const int na = 2 * H + 2, nh = 2 * H, L = 2 * na + 2 * nh;
+  StripIO sx, sz;
+  sx.psi_in = fptr(A.psi_in[0], sh);  sx.psi_out = fptr(A.psi_out[0], sh);
+  sx.xi_in = fptr(A.xi_in[0], sh);    sx.xi_out = fptr(A.xi_out[0], sh);
+  sx.ck_psi = nullptr;                sx.ck_xi = nullptr;
+  sx.a = cp; sx.ah = cp + na; sx.b = cp + na + nh; sx.bh = cp + 2 * na + nh;
+  sx.psi_step = 1; sx.xi_step = 1;
+  sz.psi_in = fptr(A.psi_in[1], sh);  sz.psi_out = fptr(A.psi_out[1], sh);
+  sz.xi_in = fptr(A.xi_in[1], sh);    sz.xi_out = fptr(A.xi_out[1], sh);
+  sz.ck_psi = nullptr;                sz.ck_xi = nullptr;
+  sz.a = cp + L; sz.ah = cp + L + na; sz.b = cp + L + na + nh; sz.bh = cp + L + 2 * na + nh;
+  sz.psi_step = P; sz.xi_step = P;
+  const bool xstrip = inb && (x0 < H || x0 + 3 >= nx - H);
+  const bool vec_interior = (x0 >= 1) && (x0 + 3 <= nx - 2);
+
+  // the block's reduction: thread t owns point wx0 + t of the group accumulator
+  const int xt = wx0 + threadIdx.x;
+  const bool tin = xt >= 1 && xt <= nx - 2;
+  float* gp = A.g.p + (long long)grp * A.g.s;
+  float* gcp = A.gc.p + (long long)grp * A.gc.s;
+
+  float rm[4], r0[4], rp[4], o[4], f[4], dv[4];
+  if (active) {
+    ld4(rm, pc + (long long)(z_begin - 1) * P + xa);
+    ld4(r0, pc + (long long)z_begin * P + xa);
+    const long long row = (long long)z_begin * P;
+    ld4(rp, pc + row + P + xa);
+    ld4rw(o, di + row + xa);
+    ld4(f, fa + row + xa);
+    ld4(dv, dcr + row + xa);
+  }
+  float gv = 0.f, cv = 0.f;
+  if (tin) {
+    gv = gp[(long long)z_begin * P + xt];
+    cv = gcp[(long long)z_begin * P + xt];
+  }
+  int par = 0;
+  for (int z = z_begin; z < z_end; ++z) {
+    const long long row = (long long)z * P;
+    const bool more = z + 1 < z_end;
+    float rpn[4], on[4], fn[4], dvn[4];
+    float gvn = 0.f, cvn = 0.f;
+    if (active && more) {
+      const long long nrow = row + P;
+      ld4(rpn, pc + nrow + P + xa);
+      ld4rw(on, di + nrow + xa);
+      ld4(fn, fa + nrow + xa);
+      ld4(dvn, dcr + nrow + xa);
+    }
+    if (tin && more) {
+      gvn = gp[row + P + xt];
+      cvn = gcp[row + P + xt];
+    }
+    float4 pr = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (active) {
+      float left = __shfl_up_sync(FULL, r0[3], 1);
+      float right = __shfl_down_sync(FULL, r0[0], 1);
+      if (lane == 0) left = xa > 0 ? pc[row + xa - 1] : 0.f;
+      if (lane == 31) right = xa + 4 < P ? pc[row + xa + 4] : 0.f;
+      const bool zstrip = (z < H) || (z >= nz - H);
+      sx.psi_base = (long long)z * nh;
+      sx.xi_base = (long long)z * na;
+      float outp[4], outd[4], prd[4];
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        const float xm = e == 0 ? left : r0[e - 1];
+        const float xp = e == 3 ? right : r0[e + 1];
+        const float c = r0[e];
+        float tx = (xm - 2.f * c + xp) * A.ih2[0];
+        float tz = (rm[e] - 2.f * c + rp[e]) * A.ih2[1];
+        const int x = x0 + e;
+        const bool pin = inb && x >= 1 && x <= nx - 2;
+        if (xstrip && pin) tx = cpml_axis_term(tx, xm, c, xp, x, nx, H, A.ih[0], sx);
+        if (zstrip && pin) {
+          sz.psi_base = x;
+          sz.xi_base = x;
+          tz = cpml_axis_term(tz, rm[e], c, rp[e], z, nz, H, A.ih[1], sz);
+        }
+        const float lap = tx + tz;
+        outd[e] = o[e] + f[e] * lap;
+        outp[e] = c + outd[e];
+        prd[e] = pin ? outp[e] * dv[e] : 0.f;
+      }
+      pr = make_float4(prd[0], prd[1], prd[2], prd[3]);
+      if (inb) {
+        if (vec_interior) {
+          st4(pn + row + x0, outp);
+          st4(dn + row + x0, outd);
+        } else {
+#pragma unroll
+          for (int e = 0; e < 4; ++e) {
+            const int x = x0 + e;
+            if (x >= 1 && x <= nx - 2) {
+              pn[row + x] = outp[e];
+              dn[row + x] = outd[e];
+            }
+          }
+        }
+      }
+    }
+    prod[par][warp][lane] = pr;
+    __syncthreads();
+    if (tin) {
+      const float* pf = reinterpret_cast<const float*>(&prod[par][0][0]);
+      const float sum = ((pf[threadIdx.x] + pf[128 + threadIdx.x]) + pf[256 + threadIdx.x]) + pf[384 + threadIdx.x];
+      kahan_add(gv, cv, sum);
+      gp[row + xt] = gv;
+      gcp[row + xt] = cv;
+    }
+    par ^= 1;
+    gv = gvn;
+    cv = cvn;
+    if (active) {
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        rm[e] = r0[e];
+        r0[e] = rp[e];
+        if (more) {
+          rp[e] = rpn[e];
+          o[e] = on[e];
+          f[e] = fn[e];
+          dv[e] = dvn[e];
+        }
+      }
+    }
+  }
+}
+
 // ---------------------------------------------------------------------------
 // 3D: axes 0 = x, 1 = y, 2 = z.  Block = 4 warps, one y row each (128 x
 // points per warp); tile = 128 x 4 y x TZ z.  y neighbours come through L1.
