@@ -147,8 +147,9 @@ int sw_acoustic_gradient(sw_wavesim* ws, int32_t nshots, const sw_acoustic_shot*
  * marching axis) of a block's tile, 0 = built-in heuristic; variant selects
  * the 2D stencil implementation: 0, 2, 3 = register-pipelined loads with 4,
  * 8 or 16 warps per block, 1 = TMA bulk copies through shared memory with a
- * producer warp; variant + 16*k additionally prefetches the rows k rows ahead
- * into L2 (k = 1..15).  Results do not depend on either. */
+ * producer warp; + 4 keeps a second row of loads in flight in the forward
+ * kernels of the 4-warp stencil; + 16*k additionally prefetches the rows k
+ * rows ahead into L2 (k = 1..15).  Results do not depend on either. */
 int sw_wavesim_set_tuning(sw_wavesim* ws, int32_t tz, int32_t variant);
 
 /* Per-kernel timing collected with CUDA events on the context's stream while

@@ -623,7 +623,7 @@ struct StepCtx {
 };
 
 // Warps per block of the register-pipelined 2D stencil (variant 0: 4, 2: 8, 3: 16).
-int block_warps(const sw_wavesim* ws) { return ws->variant == 2 ? 8 : ws->variant == 3 ? 16 : 4; }
+int block_warps(const sw_wavesim* ws) { return (ws->variant & 3) == 2 ? 8 : (ws->variant & 3) == 3 ? 16 : 4; }
 
 StepCtx make_step_ctx(sw_wavesim* ws, int S) {
   StepCtx c{ws, 0, 0, 1, 0};
@@ -638,7 +638,7 @@ StepCtx make_step_ctx(sw_wavesim* ws, int S) {
   }
   int TZ = ws->tile_tz;
   if (TZ <= 0) {
-    if (ws->N == 2 && ws->variant != 1) {
+    if (ws->N == 2 && (ws->variant & 3) != 1) {
       // register-pipelined 2D stencil: short bands keep every SM at full
       // occupancy with a negligible tail (8 rows measured best on GB300 for
       // 64 shots of 2001 x 801: 55.6 Gpts/s against 48.4 at 64 rows); small
@@ -647,7 +647,7 @@ StepCtx make_step_ctx(sw_wavesim* ws, int S) {
     } else {
       // aim for >= ~8 blocks per SM in total, with TZ in [tz_min, 64]
       TZ = 64;
-      const int tz_min = (ws->N == 2 && ws->variant == 1) ? 16 : 8;
+      const int tz_min = (ws->N == 2 && (ws->variant & 3) == 1) ? 16 : 8;
       while (TZ > tz_min) {
         const long long blocks = (long long)S * c.tiles_x * c.tiles_y * ((nint + TZ - 1) / TZ);
         if (blocks >= 8LL * sms) break;
@@ -720,12 +720,20 @@ struct Launcher {
     cudaEvent_t ev = nullptr;
     const int kind = MODE == MODE_ADJ ? KK_ADJOINT : KK_STENCIL;
     ws->ctx->prof.begin(st, kind, bytes, &ev);
-    if (ws->N == 2 && ws->variant == 1) {
+    if (ws->N == 2 && (ws->variant & 3) == 1) {
       enable_tma_smem<MODE>();
       k_ac2d_tma<MODE><<<(unsigned)blocks, 160, TmaLayout<MODE>::BYTES, st>>>(a);
     } else if (ws->N == 2) {
       const int nw = block_warps(ws);
-      if (nw == 4)
+      bool launched = false;
+      if constexpr (MODE != MODE_ADJ) {
+        if (nw == 4 && (ws->variant & 4)) {
+          k_ac2d_step<MODE, 4, 2><<<(unsigned)blocks, 128, 0, st>>>(a);
+          launched = true;
+        }
+      }
+      if (launched) {
+      } else if (nw == 4)
         k_ac2d_step<MODE, 4><<<(unsigned)blocks, 128, 0, st>>>(a);
       else if (nw == 8)
         k_ac2d_step<MODE, 8><<<(unsigned)blocks, 256, 0, st>>>(a);
@@ -1165,7 +1173,7 @@ void acoustic_gradient(sw_wavesim* ws, int nshots, const sw_acoustic_shot* shots
   }
   // the shot sum is fused into the 2D adjoint for batches of 4 or more shots,
   // unless per-shot muting needs each shot's gradient
-  ws->grp = (!mute && ws->N == 2 && ws->variant != 1 && nshots >= 4) ? 4 : 1;
+  ws->grp = (!mute && ws->N == 2 && (ws->variant & 3) != 1 && nshots >= 4) ? 4 : 1;
   bool first_group = true;
   for (const auto& group : plan_groups(ws, order, true)) {
     const int S = (int)group.size();

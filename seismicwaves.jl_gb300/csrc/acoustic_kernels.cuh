@@ -159,8 +159,8 @@ struct Ac2dBounds {
   static constexpr int MINB = MODE == MODE_ADJ ? (NW == 4 ? 4 : NW == 8 ? 2 : 1) : (NW == 4 ? 7 : NW == 8 ? 4 : 2);
 };
 
-template <int MODE, int NW>
-__global__ void __launch_bounds__(32 * NW, (Ac2dBounds<MODE, NW>::MINB)) k_ac2d_step(const StepArgs A) {
+template <int MODE, int NW, int DP = 1>
+__global__ void __launch_bounds__(32 * NW, (Ac2dBounds<MODE, NW>::MINB - (DP - 1))) k_ac2d_step(const StepArgs A) {
   constexpr unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   constexpr int nwarps = NW;
@@ -226,6 +226,17 @@ __global__ void __launch_bounds__(32 * NW, (Ac2dBounds<MODE, NW>::MINB)) k_ac2d_
       ld4rw(c4, gcp + row + xa);
     }
   }
+  // DP == 2 (forward kernels): a second row of loads in flight, issued one
+  // iteration earlier (q* hold p of row z+2 and d, fact of row z+1).
+  float qp[4], qo[4], qf[4];
+  if constexpr (DP == 2) {
+    if (z_begin + 1 < z_end) {
+      const long long nrow = (long long)(z_begin + 1) * P;
+      ld4(qp, pc + nrow + P + xa);
+      ld4rw(qo, di + nrow + xa);
+      ld4(qf, fa + nrow + xa);
+    }
+  }
   // one lane per warp asks the TMA unit to pull the warp's segments of a row
   // A.pf rows ahead into L2, so the register loads of that row later hit L2
   const unsigned seg = (unsigned)min(128, P - wx0) * 4u;
@@ -243,7 +254,14 @@ __global__ void __launch_bounds__(32 * NW, (Ac2dBounds<MODE, NW>::MINB)) k_ac2d_
     }
     float rpn[4], on[4], fn[4], dvn[4], g4n[4], c4n[4];
     const bool more = z + 1 < z_end;
-    if (more) {
+    if constexpr (DP == 2) {
+      if (z + 2 < z_end) {
+        const long long nrow = row + 2 * P;
+        ld4(rpn, pc + nrow + P + xa);
+        ld4rw(on, di + nrow + xa);
+        ld4(fn, fa + nrow + xa);
+      }
+    } else if (more) {
       const long long nrow = row + P;
       ld4(rpn, pc + nrow + P + xa);
       ld4rw(on, di + nrow + xa);
@@ -320,7 +338,14 @@ __global__ void __launch_bounds__(32 * NW, (Ac2dBounds<MODE, NW>::MINB)) k_ac2d_
     for (int e = 0; e < 4; ++e) {
       rm[e] = r0[e];
       r0[e] = rp[e];
-      if (more) {
+      if constexpr (DP == 2) {
+        rp[e] = qp[e];
+        o[e] = qo[e];
+        f[e] = qf[e];
+        qp[e] = rpn[e];
+        qo[e] = on[e];
+        qf[e] = fn[e];
+      } else if (more) {
         rp[e] = rpn[e];
         o[e] = on[e];
         f[e] = fn[e];
