@@ -153,8 +153,9 @@ int sw_acoustic_gradient(sw_wavesim* ws, int32_t nshots, const sw_acoustic_shot*
 int sw_wavesim_set_tuning(sw_wavesim* ws, int32_t tz, int32_t variant);
 
 /* Per-kernel timing collected with CUDA events on the context's stream while
- * enabled (0 = off).  kind: 0 = forward/recompute stencil, 1 = adjoint
- * stencil with correlation, 2 = source/receiver kernel, 3 = other. */
+ * enabled (0 = off).  kind: 0 = forward stencil, 1 = adjoint stencil with
+ * correlation, 2 = source/receiver kernels, 3 = other, 4 = recompute stencil
+ * of the gradient (forward stencil writing D); bytes = algorithmic bytes. */
 int sw_profile_enable(sw_ctx* ctx, int32_t on);
 int sw_profile_read(sw_ctx* ctx, int32_t kind, double* total_ms, int64_t* launches, double* bytes);
 

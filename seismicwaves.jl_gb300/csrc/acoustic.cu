@@ -714,11 +714,11 @@ struct Launcher {
   sw_wavesim* ws;
   cudaStream_t st;
   template <int MODE>
-  void step(const StepArgs& a, const StepCtx& c, double bytes) {
+  void step(const StepArgs& a, const StepCtx& c, double bytes, bool recompute = false) {
     check_vector_alignment(a);
     const long long blocks = (long long)a.nshots * c.tiles_x * c.tiles_y * c.tiles_z;
     cudaEvent_t ev = nullptr;
-    const int kind = MODE == MODE_ADJ ? KK_ADJOINT : KK_STENCIL;
+    const int kind = MODE == MODE_ADJ ? KK_ADJOINT : (recompute ? KK_RECOMPUTE : KK_STENCIL);
     ws->ctx->prof.begin(st, kind, bytes, &ev);
     if (ws->N == 2 && (ws->variant & 3) == 1) {
       enable_tma_smem<MODE>();
@@ -937,7 +937,7 @@ void adjoint_group(sw_wavesim* ws, const std::vector<HostShot>& group) {
         const long long dslot = (t - 1) % K;
         a.Dout = FieldArg{ws->dbuf.as<float>() + dslot * F, ws->d_slots * F};
         a.d_first = 0;
-        L.step<MODE_FWD_D>(a, c, stencil_bytes(ws, Sa, MODE_FWD_D, Sa, false));
+        L.step<MODE_FWD_D>(a, c, stencil_bytes(ws, Sa, MODE_FWD_D, Sa, false), true);
         launch_inject(ws, Sa, a.pnew, a.dout, a.Dout, 0, t, 0);
         if (first) {
           pc = 0;
