@@ -1,6 +1,7 @@
 /*
  * swgb300 -- GB300-native backend for the finite-difference time-stepping hot
- * path of SeismicWaves.jl (acoustic constant-density C-PML, 2D and 3D).
+ * path of SeismicWaves.jl (acoustic constant-density C-PML, 2D and 3D, and the
+ * isotropic elastic 2D (P-SV) C-PML path).
  *
  * Plain C ABI: no C++ types, no exceptions, no torch types.  Every entry point
  * returns an int status (SW_OK on success); the text of the last error of a
@@ -42,6 +43,21 @@
  *       src/models/acoustic/acou_gradient.jl:4-95, src/utils/checkpointers.jl:1-107,
  *       src/inversion/misfits/L2Misfit.jl:24-77, acoustic2D_xPU.jl:64-76 and :128-169,
  *       correlate_gradient_xPU.jl:1-10, src/utils/mute_grad.jl:13-80)
+ *   sw_elastic_create / sw_elastic_destroy
+ *       build_wavesim -> ElasticIsoCPMLWaveSimulation (src/models/elastic/ela_models.jl:177-420)
+ *   sw_elastic_set_material
+ *       update_matprop! -> precomp_elaprop! with the half-point interpolations
+ *       (ela_models.jl:143-173, src/utils/interpolations.jl:1-47)
+ *   sw_elastic_forward
+ *       run_swforward! shot loop + swforward_1shot! (moment-tensor and external-force shots)
+ *       + forward_onestep_CPML! (src/models/elastic/ela_forward.jl:4-159,
+ *       src/models/elastic/backends/shared/elastic2D_iso_xPU.jl:1-357)
+ *   sw_elastic_gradient
+ *       run_swgradient! + swgradient_1shot! (elastic) with LinearCheckpointer, L2 misfit,
+ *       adjoint_onestep_CPML!, correlate_gradients!, back-interpolation and muting
+ *       (src/models/elastic/ela_gradient.jl:4-362, elastic2D_iso_xPU.jl:359-448,
+ *       src/models/elastic/backends/shared/correlate_gradient_xPU.jl:1-83,
+ *       src/inversion/misfits/L2Misfit.jl:44-95)
  */
 #ifndef SWGB300_H
 #define SWGB300_H
@@ -65,6 +81,7 @@ enum {
 
 typedef struct sw_ctx sw_ctx;
 typedef struct sw_wavesim sw_wavesim;
+typedef struct sw_elastic sw_elastic;
 
 /* Library version (major*10000 + minor*100 + patch). */
 int sw_version(void);
@@ -153,11 +170,79 @@ int sw_acoustic_gradient(sw_wavesim* ws, int32_t nshots, const sw_acoustic_shot*
 int sw_wavesim_set_tuning(sw_wavesim* ws, int32_t tz, int32_t variant);
 
 /* Per-kernel timing collected with CUDA events on the context's stream while
- * enabled (0 = off).  kind: 0 = forward stencil, 1 = adjoint stencil with
- * correlation, 2 = source/receiver kernels, 3 = other, 4 = recompute stencil
- * of the gradient (forward stencil writing D); bytes = algorithmic bytes. */
+ * enabled (0 = off).  kind: 0 = forward stencil, 1 = adjoint stencil (with the
+ * correlation on the acoustic path), 2 = source/receiver kernels, 3 = other,
+ * 4 = recompute stencil of the gradient, 5 = elastic gradient correlation;
+ * bytes = algorithmic bytes. */
 int sw_profile_enable(sw_ctx* ctx, int32_t on);
 int sw_profile_read(sw_ctx* ctx, int32_t kind, double* total_ms, int64_t* launches, double* bytes);
+
+/* ---------------------------------------------------------------------------
+ * Isotropic elastic 2D (P-SV), 4th-order staggered displacement-stress scheme
+ * with C-PML.  Grids follow ElasticIsoCPMLWaveSimulation: sigma_xx, sigma_zz,
+ * lambda, mu, rho on (nx, nz) nodes; ux on (nx-1, nz); uz on (nx, nz-1);
+ * sigma_xz on (nx-1, nz-1).  Traces are (nt, 2, nrec) column-major (ux, uz).
+ * ------------------------------------------------------------------------- */
+typedef struct {
+  int32_t n[2];       /* nx, nz */
+  double h[2];        /* dx, dz */
+  double dt;
+  int32_t halo;
+  double rcoef;
+  int32_t freetop;    /* free surface at the top (mirror conditions, sigma_zz = 0 at j = 1) */
+  int32_t interp_rho; /* rho at half points: 0 = arithmetic average (reference default), 1 = harmonic */
+  int32_t interp_mu;  /* mu at (i+1/2, j+1/2): 0 = arithmetic (reference default), 1 = harmonic */
+} sw_elastic_params;
+
+/* Grid points of one table, grouped by item (a source or a receiver): item k
+ * owns entries offsets[k] .. offsets[k+1]-1; entry e is grid point
+ * (ij[2e], ij[2e+1]) (1-based, on the table's own grid) with weight coef[e].
+ * This is the output of spread_positions (src/utils/utils.jl:168-214) or, with
+ * sincinterp = false, one nearest point of weight 1 per item
+ * (ela_models.jl:6-90). */
+typedef struct {
+  const int32_t* offsets; /* count+1 entries */
+  const int32_t* ij;
+  const float* coef;
+} sw_point_table;
+
+typedef struct {
+  int32_t nt;
+  int32_t kind;            /* 0 = MomentTensorShot, 1 = ExternalForceShot */
+  int32_t nsrc;
+  const float* srctf;      /* kind 0: (nt, nsrc); kind 1: (nt, 2, nsrc); divided by dx*dz as possrcrec_scaletf does */
+  const float* momtens;    /* kind 0: (3, nsrc) = Mxx, Mzz, Mxz of each source; host memory */
+  sw_point_table src[2];   /* kind 0: [sigma_xx/sigma_zz nodes, sigma_xz nodes]; kind 1: [ux nodes, uz nodes] */
+  int32_t nrec;
+  sw_point_table rec[2];   /* [ux nodes, uz nodes] */
+  float* traces;           /* (nt, 2, nrec) output */
+  const float* cpml;       /* C-PML coefficients, axis x then z, each [a, a_h, b, b_h] (init_bdc!,
+                              src/models/elastic/ela_init_bc.jl:7-40) */
+  const float* observed;   /* gradient: observed traces (nt, 2, nrec) */
+  const float* invcov_diag;/* gradient: NULL (identity) or the diagonal of the inverse covariance (nt) */
+  int32_t nwin;
+  const int32_t* windows;  /* (2, nwin) 1-based inclusive time windows; host memory */
+  const double* src_pos;   /* (nsrc, 2) metres, for muting; host memory */
+  const double* rec_pos;   /* (nrec, 2) metres, for muting; host memory */
+} sw_elastic_shot;
+
+/* One elastic simulation (a set of preallocated device fields).  gradient = 1
+ * also prepares the adjoint fields and the checkpointing (gparams as for the
+ * acoustic path; snapshot_bf16 must be 0). */
+int sw_elastic_create(sw_ctx* ctx, const sw_elastic_params* params, int32_t gradient, const sw_grad_params* gparams,
+                      sw_elastic** out);
+int sw_elastic_destroy(sw_elastic* es);
+/* lambda, mu, rho: host arrays of (nx, nz) floats (check_matprop's conditions apply). */
+int sw_elastic_set_material(sw_elastic* es, const float* lambda, const float* mu, const float* rho);
+/* Forward modelling of nshots shots in one batch; traces written per shot.
+ * on_device = 1: srctf and traces are device pointers. */
+int sw_elastic_forward(sw_elastic* es, int32_t nshots, const sw_elastic_shot* shots, int32_t on_device);
+/* Gradient of the summed L2 misfit with respect to rho, lambda and mu, each
+ * (nx, nz) FP64, summed over the shots; misfit (may be NULL) = sum of the shots'
+ * misfits.  on_device = 1: srctf, traces, observed, invcov_diag and the
+ * outputs are device pointers. */
+int sw_elastic_gradient(sw_elastic* es, int32_t nshots, const sw_elastic_shot* shots, int32_t on_device,
+                        double* grad_rho, double* grad_lambda, double* grad_mu, double* misfit);
 
 /* 2D forward of one shot that allocates no device memory.  Has no
  * counterpart in the reference: it exists for callers that cannot let a

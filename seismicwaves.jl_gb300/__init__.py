@@ -12,11 +12,17 @@ from .api import (AcousticCDCPMLWaveSimulation, CPMLBoundaryConditionParameters,
                   UniformFiniteDifferenceGrid, VpAcousticCDMaterialProperties, build_wavesim, courant_number, gaussderivstf,
                   gaussstf, nearest_grid_points, points_per_wavelength, rickerstf, scale_srctf,
                   swforward, swgradient, swmisfit)
+from .elastic import (ArithmeticAverageInterpolation, ElasticIsoCPMLWaveSimulation, ElasticIsoMaterialProperties,
+                      ExternalForceShot, ExternalForceSources, HarmonicAverageInterpolation, InputParametersElastic,
+                      MomentTensor2D, MomentTensorShot, MomentTensorSources, VectorReceivers, spread_positions)
 
 __all__ = [
     "AcousticCDCPMLWaveSimulation", "CPMLBoundaryConditionParameters", "GradParameters", "InputParametersAcoustic",
     "L2Misfit", "RunParameters", "ScalarReceivers", "ScalarShot", "ScalarSources", "UniformFiniteDifferenceGrid",
     "VpAcousticCDMaterialProperties", "build_wavesim", "courant_number", "nearest_grid_points",
     "points_per_wavelength", "scale_srctf", "gaussderivstf", "gaussstf", "rickerstf", "swforward",
-    "swgradient", "swmisfit", "_lib",
+    "swgradient", "swmisfit", "_lib", "ArithmeticAverageInterpolation", "ElasticIsoCPMLWaveSimulation",
+    "ElasticIsoMaterialProperties", "ExternalForceShot", "ExternalForceSources", "HarmonicAverageInterpolation",
+    "InputParametersElastic", "MomentTensor2D", "MomentTensorShot", "MomentTensorSources", "VectorReceivers",
+    "spread_positions",
 ]

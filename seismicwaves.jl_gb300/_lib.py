@@ -24,7 +24,8 @@ EXPORTS = [
     "sw_version", "sw_ctx_create", "sw_ctx_destroy", "sw_ctx_last_error", "sw_ctx_stream",
     "sw_cpml_coefficients", "sw_wavesim_create", "sw_wavesim_destroy", "sw_wavesim_set_vp",
     "sw_acoustic_forward", "sw_acoustic_gradient", "sw_wavesim_set_tuning", "sw_profile_enable",
-    "sw_profile_read", "sw_acoustic2d_forward_noalloc",
+    "sw_profile_read", "sw_acoustic2d_forward_noalloc", "sw_elastic_create", "sw_elastic_destroy",
+    "sw_elastic_set_material", "sw_elastic_forward", "sw_elastic_gradient",
 ]
 
 i32, f64, vp_ = ctypes.c_int32, ctypes.c_double, ctypes.c_void_p
@@ -44,6 +45,22 @@ class SwAcousticShot(ctypes.Structure):
 class SwGradParams(ctypes.Structure):
     _fields_ = [("check_freq", i32), ("mute_radius_src", i32), ("mute_radius_rec", i32),
                 ("compute_misfit", i32), ("snapshot_bf16", i32)]
+
+
+class SwElasticParams(ctypes.Structure):
+    _fields_ = [("n", i32 * 2), ("h", f64 * 2), ("dt", f64), ("halo", i32), ("rcoef", f64), ("freetop", i32),
+                ("interp_rho", i32), ("interp_mu", i32)]
+
+
+class SwPointTable(ctypes.Structure):
+    _fields_ = [("offsets", vp_), ("ij", vp_), ("coef", vp_)]
+
+
+class SwElasticShot(ctypes.Structure):
+    _fields_ = [("nt", i32), ("kind", i32), ("nsrc", i32), ("srctf", vp_), ("momtens", vp_),
+                ("src", SwPointTable * 2), ("nrec", i32), ("rec", SwPointTable * 2), ("traces", vp_),
+                ("cpml", vp_), ("observed", vp_), ("invcov_diag", vp_), ("nwin", i32), ("windows", vp_),
+                ("src_pos", vp_), ("rec_pos", vp_)]
 
 
 class SwError(RuntimeError):
@@ -83,6 +100,11 @@ def load() -> ctypes.CDLL:
     lib.sw_profile_enable.argtypes = [vp_, i32]
     lib.sw_profile_read.argtypes = [vp_, i32, P(f64), P(ctypes.c_int64), P(f64)]
     lib.sw_acoustic2d_forward_noalloc.argtypes = [P(SwAcousticParams), vp_, P(SwAcousticShot), vp_]
+    lib.sw_elastic_create.argtypes = [vp_, P(SwElasticParams), i32, P(SwGradParams), P(vp_)]
+    lib.sw_elastic_destroy.argtypes = [vp_]
+    lib.sw_elastic_set_material.argtypes = [vp_, vp_, vp_, vp_]
+    lib.sw_elastic_forward.argtypes = [vp_, i32, P(SwElasticShot), i32]
+    lib.sw_elastic_gradient.argtypes = [vp_, i32, P(SwElasticShot), i32, vp_, vp_, vp_, vp_]
     _lib = lib
     return lib
 

@@ -172,23 +172,26 @@ class L2Misfit:
             mask = np.zeros(res.shape[0])
             for a, b in self.windows:
                 mask[a - 1:b] = 1.0
-            res = mask[:, None] * res
+            res = mask.reshape((-1,) + (1,) * (res.ndim - 1)) * res
         return res
 
     def _apply_invcov(self, res):
+        """C^-1 applied along time; for (nt, ncomp, nrec) traces per component (L2Misfit.jl:79-95)."""
         if self.invcov is None:
             return res
         if self.invcov.ndim == 1:
-            return self.invcov[:, None] * res
+            return self.invcov.reshape((-1,) + (1,) * (res.ndim - 1)) * res
+        if res.ndim == 3:
+            return np.einsum("tu,ucr->tcr", self.invcov, res)
         return self.invcov @ res
 
-    def calcmisfit(self, recs: ScalarReceivers) -> float:
-        """L2Misfit.jl:24-42: 1/2 r' C^-1 r."""
+    def calcmisfit(self, recs) -> float:
+        """L2Misfit.jl:24-62: 1/2 r' C^-1 r (summed over components for vector receivers)."""
         res = self._masked_residuals(recs.seismograms)
         return float(np.sum(res * self._apply_invcov(res)) / 2)
 
-    def dchi_du(self, recs: ScalarReceivers):
-        """L2Misfit.jl:64-77: C^-1 r."""
+    def dchi_du(self, recs):
+        """L2Misfit.jl:64-95: C^-1 r."""
         return self._apply_invcov(self._masked_residuals(recs.seismograms))
 
 
@@ -458,7 +461,18 @@ class AcousticCDCPMLWaveSimulation:
 
 
 def _check_sim_consistency(matprop, shots):
-    """src/utils/checks.jl:2-41 for the acoustic CD case."""
+    """src/utils/checks.jl:2-41 for the acoustic CD and the elastic isotropic 2D cases."""
+    from . import elastic as E
+    if isinstance(matprop, E.ElasticIsoMaterialProperties):
+        kinds = {type(s) for s in shots}
+        if len(kinds) != 1:
+            raise TypeError("Types of shots are inconsistent.")
+        for s in shots:
+            ok = (isinstance(s, E.MomentTensorShot) and isinstance(s.srcs, E.MomentTensorSources)) or \
+                 (isinstance(s, E.ExternalForceShot) and isinstance(s.srcs, E.ExternalForceSources))
+            if not (ok and isinstance(s.recs, E.VectorReceivers)):
+                raise TypeError("Types of WaveSimulation, MaterialProperties and Sources/Receivers are inconsistent")
+        return
     if not isinstance(matprop, VpAcousticCDMaterialProperties):
         raise TypeError("Types of WaveSimulation, MaterialProperties and Sources/Receivers are inconsistent")
     for s in shots:
@@ -466,10 +480,10 @@ def _check_sim_consistency(matprop, shots):
             raise TypeError("Types of shots are inconsistent.")
 
 
-def build_wavesim(params: InputParametersAcoustic, matprop: VpAcousticCDMaterialProperties, *,
-                  runparams: RunParameters, gradparams: GradParameters | None = None, gradient: bool | None = None,
-                  device: int = 0) -> AcousticCDCPMLWaveSimulation:
-    """src/apis/build.jl:18-40."""
+def build_wavesim(params, matprop, *, runparams: RunParameters, gradparams: GradParameters | None = None,
+                  gradient: bool | None = None, device: int = 0, sincinterp: bool = True):
+    """src/apis/build.jl:18-95: AcousticCDCPMLWaveSimulation or ElasticIsoCPMLWaveSimulation."""
+    from . import elastic as E
     if gradparams is None and gradient:
         gradparams = GradParameters()
     elif gradparams is not None:
@@ -477,6 +491,14 @@ def build_wavesim(params: InputParametersAcoustic, matprop: VpAcousticCDMaterial
             "build_wavesim(...) specifies GradParameters, however, gradient keyword argument is set to false."
     if not isinstance(params.boundcond, CPMLBoundaryConditionParameters):
         raise NotImplementedError("the GB300 backend implements C-PML boundaries")
+    if runparams.parall == "threadpersrc":
+        raise ValueError("`parall = :threadpersrc` is a CPU-threads mode; the GB300 backend batches shots itself")
+    if isinstance(params, E.InputParametersElastic):
+        if not isinstance(matprop, E.ElasticIsoMaterialProperties):
+            raise TypeError("elastic input parameters need ElasticIsoMaterialProperties")
+        return E.ElasticIsoCPMLWaveSimulation(params, matprop, params.boundcond, runparams=runparams,
+                                              gradparams=gradparams, gradient=bool(gradient), sincinterp=sincinterp,
+                                              device=device)
     if not isinstance(matprop, VpAcousticCDMaterialProperties):
         raise NotImplementedError("the GB300 backend implements the acoustic constant-density simulation")
     if runparams.parall == "threadpersrc":
@@ -486,7 +508,8 @@ def build_wavesim(params: InputParametersAcoustic, matprop: VpAcousticCDMaterial
 
 
 def _prepare(params_or_wavesim, matprop, runparams, gradient, gradparams=None):
-    if isinstance(params_or_wavesim, AcousticCDCPMLWaveSimulation):
+    from . import elastic as E
+    if isinstance(params_or_wavesim, (AcousticCDCPMLWaveSimulation, E.ElasticIsoCPMLWaveSimulation)):
         ws = params_or_wavesim
         if gradient and not ws.gradient:
             raise AssertionError("The wavesim object was not built for gradient computations. "
@@ -518,7 +541,8 @@ def swgradient(params_or_wavesim, matprop: VpAcousticCDMaterialProperties, shots
                gradparams: GradParameters | None = None):
     """swgradient! (src/apis/gradient.jl:31-136).
 
-    Returns {"vp": gradient} (float64), or ({"vp": gradient}, misfit) when
+    Acoustic: returns {"vp": gradient}; elastic: {"rho": , "lambda": , "mu": }
+    (float64), with the summed misfit as a second value when
     gradparams.compute_misfit is true.
     """
     gradparams = gradparams or GradParameters()
@@ -527,4 +551,5 @@ def swgradient(params_or_wavesim, matprop: VpAcousticCDMaterialProperties, shots
     ws.set_matprop(matprop)
     grad, msf = ws.run_gradient(list(shots), list(misfit))
     g = ws.gradparams or gradparams
-    return ({"vp": grad}, msf) if g.compute_misfit else {"vp": grad}
+    out = grad if isinstance(grad, dict) else {"vp": grad}
+    return (out, msf) if g.compute_misfit else out

@@ -20,6 +20,14 @@ void wavesim_set_tuning(sw_wavesim* ws, int tz, int variant);
 sw_ctx* wavesim_ctx(sw_wavesim* ws);
 sw_wavesim* wavesim_new();
 void wavesim_delete(sw_wavesim* ws);
+void elastic_init(sw_elastic* es, sw_ctx* ctx, const sw_elastic_params* p, int gradient, const sw_grad_params* gp);
+void elastic_set_material(sw_elastic* es, const float* lam, const float* mu, const float* rho);
+void elastic_forward(sw_elastic* es, int nshots, const sw_elastic_shot* shots, bool on_device);
+void elastic_gradient(sw_elastic* es, int nshots, const sw_elastic_shot* shots, bool on_device, double* g_rho,
+                      double* g_lam, double* g_mu, double* misfit);
+sw_ctx* elastic_ctx(sw_elastic* es);
+sw_elastic* elastic_new();
+void elastic_delete(sw_elastic* es);
 
 [[noreturn]] void fail(int code, const std::string& msg) { throw SwError{code, msg}; }
 
@@ -274,6 +282,63 @@ int sw_wavesim_set_tuning(sw_wavesim* ws, int32_t tz, int32_t variant) {
   if (!ws || tz < 0 || variant < 0 || variant / 16 > 15) return SW_ERR_ARG;
   swgb::wavesim_set_tuning(ws, tz, variant);
   return SW_OK;
+}
+
+int sw_elastic_create(sw_ctx* ctx, const sw_elastic_params* params, int32_t gradient, const sw_grad_params* gparams,
+                      sw_elastic** out) {
+  if (!ctx || !out) return SW_ERR_ARG;
+  *out = nullptr;
+  sw_elastic* es = nullptr;
+  const int rc = guarded(ctx, [&] {
+    swgb::check_cuda(cudaSetDevice(ctx->device), "cudaSetDevice");
+    es = swgb::elastic_new();
+    swgb::elastic_init(es, ctx, params, gradient, gparams);
+  });
+  if (rc != SW_OK) {
+    if (es) swgb::elastic_delete(es);
+    return rc;
+  }
+  *out = es;
+  return SW_OK;
+}
+
+int sw_elastic_destroy(sw_elastic* es) {
+  if (!es) return SW_ERR_ARG;
+  sw_ctx* ctx = swgb::elastic_ctx(es);
+  if (ctx) {
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+  }
+  swgb::elastic_delete(es);
+  return SW_OK;
+}
+
+int sw_elastic_set_material(sw_elastic* es, const float* lambda, const float* mu, const float* rho) {
+  if (!es) return SW_ERR_ARG;
+  sw_ctx* ctx = swgb::elastic_ctx(es);
+  return guarded(ctx, [&] {
+    swgb::check_cuda(cudaSetDevice(ctx->device), "cudaSetDevice");
+    swgb::elastic_set_material(es, lambda, mu, rho);
+  });
+}
+
+int sw_elastic_forward(sw_elastic* es, int32_t nshots, const sw_elastic_shot* shots, int32_t on_device) {
+  if (!es) return SW_ERR_ARG;
+  sw_ctx* ctx = swgb::elastic_ctx(es);
+  return guarded(ctx, [&] {
+    swgb::check_cuda(cudaSetDevice(ctx->device), "cudaSetDevice");
+    swgb::elastic_forward(es, nshots, shots, on_device != 0);
+  });
+}
+
+int sw_elastic_gradient(sw_elastic* es, int32_t nshots, const sw_elastic_shot* shots, int32_t on_device,
+                        double* grad_rho, double* grad_lambda, double* grad_mu, double* misfit) {
+  if (!es) return SW_ERR_ARG;
+  sw_ctx* ctx = swgb::elastic_ctx(es);
+  return guarded(ctx, [&] {
+    swgb::check_cuda(cudaSetDevice(ctx->device), "cudaSetDevice");
+    swgb::elastic_gradient(es, nshots, shots, on_device != 0, grad_rho, grad_lambda, grad_mu, misfit);
+  });
 }
 
 }  // extern "C"

@@ -46,13 +46,15 @@ void check_cuda(cudaError_t e, const char* what);
 void dev_alloc(DevMem& m, size_t bytes, const char* what, cudaStream_t st);
 
 // Per-kernel-kind event timing (sw_profile_*).
-enum KernelKind { KK_STENCIL = 0, KK_ADJOINT = 1, KK_SRCREC = 2, KK_OTHER = 3, KK_RECOMPUTE = 4, KK_COUNT = 5 };
+enum KernelKind {
+  KK_STENCIL = 0, KK_ADJOINT = 1, KK_SRCREC = 2, KK_OTHER = 3, KK_RECOMPUTE = 4, KK_CORR = 5, KK_COUNT = 6
+};
 
 struct Profiler {
   bool on = false;
-  double total_ms[KK_COUNT] = {0, 0, 0, 0, 0};
-  long long launches[KK_COUNT] = {0, 0, 0, 0, 0};
-  double bytes[KK_COUNT] = {0, 0, 0, 0, 0};
+  double total_ms[KK_COUNT] = {};
+  long long launches[KK_COUNT] = {};
+  double bytes[KK_COUNT] = {};
   struct Pending {
     cudaEvent_t a, b;
     int kind;
