@@ -39,10 +39,11 @@
 // window of K steps from its checkpoint, on one schedule for all shots of the
 // batch (a shot takes part in step it while it <= its nt).
 //
-// Scaling.  The forward sources and the adjoint sources are multiplied by
-// powers of two (chosen from their maxima) so that the FP32 fields and the
+// Scaling.  Each shot's forward sources and the adjoint sources are multiplied
+// by powers of two (chosen from their maxima) so that the FP32 fields and the
 // products of forward and adjoint strains stay far from the FP32 underflow
-// range; traces and gradients are scaled back exactly.
+// range; traces and gradients are scaled back exactly, and a shot's traces do
+// not depend on the other shots of its batch.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -293,6 +294,7 @@ struct ShotDesc {
   int nt, kind, nsrc, nrec;
   const float* tf;  // srctf, device: kind 0 (nt, nsrc), kind 1 (nt, 2, nsrc)
   const float* mtp; // (3, nsrc) moment tensors, device
+  float sf;         // this shot's source scale (a power of two)
   Inj src[2];       // sources: kind 0 -> sigma grids, kind 1 -> ux / uz grids
   Inj adj[2];       // receivers as adjoint forces on ux / uz
   const int* rptr[2];        // recording CSR by receiver (nrec+1)
@@ -306,11 +308,12 @@ struct ShotDesc {
 };
 
 // sigma_xx += Mxx w tf, sigma_zz += Mzz w tf (table 0), sigma_xz += Mxz w tf (table 1)
-__global__ void k_el_inject_sigma(const ShotDesc* __restrict__ desc, int it, float scale, long long F,
-                                  float* sxx, float* szz, float* sxz) {
+__global__ void k_el_inject_sigma(const ShotDesc* __restrict__ desc, int it, long long F, float* sxx, float* szz,
+                                  float* sxz) {
   const int s = blockIdx.y;
   const ShotDesc& D = desc[s];
   if (it > D.nt || D.kind != 0) return;
+  const float scale = D.sf;
   const long long so = (long long)s * F;
   for (int t = 0; t < 2; ++t) {
     const Inj J = D.src[t];
@@ -338,9 +341,10 @@ __global__ void k_el_inject_sigma(const ShotDesc* __restrict__ desc, int it, flo
 }
 
 // u += w tf / rho dt^2 on the ux (table 0) and uz (table 1) grids; adjoint = 1
-// uses the receivers' tables and the adjoint source.  With D slots, D(it) gets
-// the same increment (it is part of the second time difference).
-__global__ void k_el_inject_force(const ShotDesc* __restrict__ desc, int it, int adjoint, float scale, long long F,
+// uses the receivers' tables and the adjoint source scaled by adj_scale (the
+// forward sources use the shot's own scale).  With D slots, D(it) gets the
+// same increment (it is part of the second time difference).
+__global__ void k_el_inject_force(const ShotDesc* __restrict__ desc, int it, int adjoint, float adj_scale, long long F,
                                   float* ux, float* uz, float* dux, float* duz, float* Dx, float* Dz,
                                   const float* __restrict__ dtr_i, const float* __restrict__ dtr_j) {
   const int s = blockIdx.y;
@@ -349,6 +353,7 @@ __global__ void k_el_inject_force(const ShotDesc* __restrict__ desc, int it, int
   if (!adjoint && D.kind != 1) return;
   const long long so = (long long)s * F;
   const float* tf = adjoint ? D.adjsrc : D.tf;
+  const float scale = adjoint ? adj_scale : D.sf;
   for (int t = 0; t < 2; ++t) {
     const Inj J = adjoint ? D.adj[t] : D.src[t];
     float* u = t == 0 ? ux : uz;
@@ -370,12 +375,13 @@ __global__ void k_el_inject_force(const ShotDesc* __restrict__ desc, int it, int
   }
 }
 
-// trace(it, comp, r) = sum_e w_e u(p_e), scaled back by inv_scale
-__global__ void k_el_record(const ShotDesc* __restrict__ desc, int it, float inv_scale, long long F,
-                            const float* __restrict__ ux, const float* __restrict__ uz) {
+// trace(it, comp, r) = sum_e w_e u(p_e), scaled back by the shot's source scale
+__global__ void k_el_record(const ShotDesc* __restrict__ desc, int it, long long F, const float* __restrict__ ux,
+                            const float* __restrict__ uz) {
   const int s = blockIdx.y;
   const ShotDesc& D = desc[s];
   if (it > D.nt) return;
+  const float inv_scale = 1.0f / D.sf;
   const long long so = (long long)s * F;
   for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < 2 * D.nrec; q += gridDim.x * blockDim.x) {
     const int t = q & 1, r = q >> 1;
@@ -453,6 +459,7 @@ __global__ void k_el_misfit_sum(const double* __restrict__ partial, int n, doubl
 struct CorrArgs {
   Geo g;
   int nshots, gsize;
+  const float* cs;                     // per shot: common scale / own source scale (a power of two)
   const float* aux; const float* auz;  // adjoint displacement after step it
   const float* fux; const float* fuz;  // forward u[it-1] (slot)
   const float* Dx; const float* Dz;    // forward D(it) (slot)
@@ -490,12 +497,13 @@ __global__ void __launch_bounds__(BX) k_el_corr(const CorrArgs A) {
     }
     for (int s = s0; s < s1; ++s) {
       const long long so = (long long)s * g.F;
+      const float cs = __ldg(A.cs + s);
       const float* aux = A.aux + so;
       const float* auz = A.auz + so;
       const float* fux = A.fux + so;
       const float* fuz = A.fuz + so;
-      if (on_ux) vri += __ldg(aux + c) * __ldg(A.Dx + so + c);
-      if (on_uz) vrj += __ldg(auz + c) * __ldg(A.Dz + so + c);
+      if (on_ux) vri += cs * (__ldg(aux + c) * __ldg(A.Dx + so + c));
+      if (on_uz) vrj += cs * (__ldg(auz + c) * __ldg(A.Dz + so + c));
       if (on_xx) {
         const float exx = dux_dx(fux, c, g.idx);
         const float exa = dux_dx(aux, c, g.idx);
@@ -507,13 +515,13 @@ __global__ void __launch_bounds__(BX) k_el_corr(const CorrArgs A) {
           ezz = duz_dz_raw(fuz, c, g.P, j, g.ft, g.idz);
           eza = duz_dz_raw(auz, c, g.P, j, g.ft, g.idz);
         }
-        vl += (exx + ezz) * (exa + eza);
-        vm += exx * exa + ezz * eza;
+        vl += cs * ((exx + ezz) * (exa + eza));
+        vm += cs * (exx * exa + ezz * eza);
       }
       if (on_xz) {
         const float e = duz_dx(fuz, c, g.idx) + dux_dz(fux, c, g.P, j, g.ft, g.idz);
         const float ea = duz_dx(auz, c, g.idx) + dux_dz(aux, c, g.P, j, g.ft, g.idz);
-        vmij += e * ea;  // 2 (exz exz' + ezx ezx') with exz = e / 2
+        vmij += cs * (e * ea);  // 2 (exz exz' + ezx ezx') with exz = e / 2
       }
     }
     const bool half = g.ft && j == 1;
@@ -655,7 +663,7 @@ struct sw_elastic {
   DevMem acc;                      // [groups][10][F]
   // tables
   DevMem d_desc, d_ll, d_int, d_flt, d_tf, d_tr, d_obs, d_ic, d_mask, d_adj, d_mt, d_cp;
-  DevMem d_partial, d_amax, d_balls, d_ball_ptr;
+  DevMem d_partial, d_amax, d_balls, d_ball_ptr, d_cs;
 };
 
 namespace {
@@ -1019,7 +1027,7 @@ struct Run {
   sw_elastic* es;
   cudaStream_t st;
   const ShotDesc* ddesc;
-  float sf = 1.0f;  // forward source scale
+  float sf_ref = 1.0f;  // the largest source scale of the group (the gradient's common scale)
 
   Args args(bool adjoint) const {
     Args a{};
@@ -1049,7 +1057,7 @@ struct Run {
     DevMem* f = es->st;
     cudaEvent_t ev = nullptr;
     es->ctx->prof.begin(st, KK_SRCREC, 0.0, &ev);
-    k_el_inject_sigma<<<dim3(1, S), 128, 0, st>>>(ddesc, it, sf, es->g.F, f[4].as<float>(), f[5].as<float>(),
+    k_el_inject_sigma<<<dim3(1, S), 128, 0, st>>>(ddesc, it, es->g.F, f[4].as<float>(), f[5].as<float>(),
                                                   f[6].as<float>());
     check_cuda(cudaGetLastError(), "stress injection launch");
     es->ctx->prof.end(st, KK_SRCREC, ev);
@@ -1070,7 +1078,7 @@ struct Run {
     if (S <= 0) return;
     cudaEvent_t ev = nullptr;
     es->ctx->prof.begin(st, KK_SRCREC, 0.0, &ev);
-    k_el_record<<<dim3(2, S), 256, 0, st>>>(ddesc, it, 1.0f / sf, es->g.F, es->st[0].as<float>(), es->st[1].as<float>());
+    k_el_record<<<dim3(2, S), 256, 0, st>>>(ddesc, it, es->g.F, es->st[0].as<float>(), es->st[1].as<float>());
     check_cuda(cudaGetLastError(), "record launch");
     es->ctx->prof.end(st, KK_SRCREC, ev);
   }
@@ -1104,7 +1112,7 @@ void full_step(Run& R, int S, int it, bool record, int kind, float* sU[2], float
   k_el_disp<<<grid, BX, 0, R.st>>>(a);
   check_cuda(cudaGetLastError(), "displacement launch");
   es->ctx->prof.end(R.st, kind, ev);
-  R.inject_force(S, it, false, R.sf, sD);
+  R.inject_force(S, it, false, 1.0f, sD);
   if (record) R.record(S, it);
 }
 
@@ -1149,10 +1157,13 @@ std::vector<std::vector<HostShot>> plan_groups(sw_elastic* es, const std::vector
   return groups;
 }
 
-float forward_scale(sw_elastic* es, const sw_elastic_shot* shots, const std::vector<HostShot>& group,
-                    const std::vector<ShotDesc>& desc) {
-  // the largest |tf| (times |M| for moment tensors) over the group's sources
-  float mx = 0.0f;
+// Per-shot source scales from each shot's largest |tf| (times |M| for moment
+// tensors): a shot's fields do not depend on the other shots of the batch.
+// Returns the largest scale; the gradient correlation brings every shot to it
+// (cs = largest / own, a power of two).
+float set_forward_scales(sw_elastic* es, const sw_elastic_shot* shots, const std::vector<HostShot>& group,
+                         std::vector<ShotDesc>& desc) {
+  float ref = 0.0f;
   for (size_t k = 0; k < group.size(); ++k) {
     const sw_elastic_shot& s = shots[group[k].orig];
     const long long n = (long long)s.nt * s.nsrc * (s.kind == 1 ? 2 : 1);
@@ -1162,9 +1173,14 @@ float forward_scale(sw_elastic* es, const sw_elastic_shot* shots, const std::vec
       for (int q = 0; q < 3 * s.nsrc; ++q) mm = std::max(mm, std::fabs(s.momtens[q]));
       m *= mm;
     }
-    mx = std::max(mx, m);
+    desc[k].sf = pow2_scale(m);
+    ref = std::max(ref, desc[k].sf);
   }
-  return pow2_scale(mx);
+  std::vector<float> cs(group.size());
+  for (size_t k = 0; k < group.size(); ++k) cs[k] = ref / desc[k].sf;
+  upload(es, es->d_desc, desc, "shot descriptors");
+  upload(es, es->d_cs, cs, "shot scales");
+  return ref;
 }
 
 }  // namespace
@@ -1296,8 +1312,8 @@ void elastic_forward(sw_elastic* es, int nshots, const sw_elastic_shot* shots, b
     ensure_state(es, S, false, group.front().nt, 1);
     std::vector<ShotDesc> desc;
     build_tables(es, shots, group, on_device, false, desc);
-    Run R{es, es->ctx->stream, es->d_desc.as<ShotDesc>()};
-    R.sf = forward_scale(es, shots, group, desc);
+    const float sf_ref = set_forward_scales(es, shots, group, desc);
+    Run R{es, es->ctx->stream, es->d_desc.as<ShotDesc>(), sf_ref};
     zero_state(es, S, false);
     for (int it = 1; it <= group.front().nt; ++it) full_step(R, active_count(group, it), it, true, KK_STENCIL, nullptr, nullptr);
     download_traces(es, shots, group, desc, on_device);
@@ -1345,8 +1361,8 @@ void elastic_gradient(sw_elastic* es, int nshots, const sw_elastic_shot* shots, 
     ensure_state(es, S, true, ntmax, ngroups);
     std::vector<ShotDesc> desc;
     build_tables(es, shots, group, on_device, true, desc);
-    Run R{es, st, es->d_desc.as<ShotDesc>()};
-    R.sf = forward_scale(es, shots, group, desc);
+    const float sf_ref = set_forward_scales(es, shots, group, desc);
+    Run R{es, st, es->d_desc.as<ShotDesc>(), sf_ref};
     const long long F = g.F;
     const int cap = es->cap;
     float* slots = es->slots.as<float>();
@@ -1457,6 +1473,7 @@ void elastic_gradient(sw_elastic* es, int nshots, const sw_elastic_shot* shots, 
         c.g = g;
         c.nshots = A;
         c.gsize = gsize;
+        c.cs = es->d_cs.as<float>();
         c.aux = ca.ux; c.auz = ca.uz;
         c.fux = sU[0]; c.fuz = sU[1];
         c.Dx = sD[0]; c.Dz = sD[1];
@@ -1509,7 +1526,7 @@ void elastic_gradient(sw_elastic* es, int nshots, const sw_elastic_shot* shots, 
       cudaEvent_t ev = nullptr;
       es->ctx->prof.begin(st, KK_OTHER, 0.0, &ev);
       const int blocks = (int)std::min<long long>((np + 255) / 256, 8192);
-      const double inv_scale = 1.0 / ((double)R.sf * (double)sa);
+      const double inv_scale = 1.0 / ((double)R.sf_ref * (double)sa);
       k_el_reduce<<<blocks, 256, 0, st>>>(gh, ngroups, es->acc.as<float>(), es->rho_d.as<double>(), es->mu_d.as<double>(),
                                           es->prm.interp_rho, es->prm.interp_mu,
                                           1.0 / (es->prm.dt * es->prm.dt), inv_scale,

@@ -226,10 +226,11 @@ def small_case(kind="mt", freetop=False, sinc=True, nt=400, seed=0, interp=(0, 0
     h = 5.0
     lam, mu, rho = smooth(nx, nz, h, seed)
     dt = stable_dt(lam, mu, rho, h)
-    sz = 12 * h if freetop else 50 * h
+    ez = (nz - 1) * h
+    sz = 12 * h if freetop else 0.5 * ez
     src = np.array([[nx * h * 0.45 + 1.3, sz + 0.7]])
-    rz = 8 * h if freetop else 30 * h
-    rec = np.array([[x, rz] for x in np.linspace(25 * h, (nx - 25) * h, 9)])
+    rz = 8 * h if freetop else 0.3 * ez
+    rec = np.array([[x, rz] for x in np.linspace(0.2 * nx * h, 0.8 * nx * h, 9)])
     shot = ElShot(kind, src, rec, nt)
     return ElCase(nx, nz, h, dt, halo, lam, mu, rho, [shot], freetop=freetop, sinc=sinc, interp_rho=interp[0],
                   interp_mu=interp[1])
