@@ -234,6 +234,132 @@ class GradientRun:
         return a.elapsed_time(b) / 1e3
 
 
+class ElasticRun:
+    """The elastic workload's shots as C-ABI structs over device (or pinned host) buffers."""
+
+    def __init__(self, sw, w, device):
+        import torch
+
+        L = sw._lib
+        E = sys.modules[sw.__name__ + ".elastic"]
+        self.sw, self.w, self.L, self.torch, self.E = sw, w, L, torch, E
+        self.dev = torch.device("cuda", device)
+        self.ctx = L.Context(device)
+        self.lib = self.ctx.lib
+        nx, nz = w.lam.shape
+        prm = L.SwElasticParams()
+        prm.n[0], prm.n[1] = nx, nz
+        prm.h[0], prm.h[1] = w.h
+        prm.dt, prm.halo, prm.rcoef, prm.freetop = w.dt, w.halo, 1e-4, int(w.freetop)
+        gp = L.SwGradParams()
+        gp.check_freq = w.check_freq
+        self.h = ctypes.c_void_p()
+        self.ctx.check(self.lib.sw_elastic_create(self.ctx.h, ctypes.byref(prm), 1, ctypes.byref(gp),
+                                                  ctypes.byref(self.h)), "sw_elastic_create")
+        self.stream = torch.cuda.ExternalStream(self.ctx.stream, device=self.dev)
+        vmax = float(np.max(w.vp))
+        hx, hz = w.h
+        self.host = []
+        for s in w.shots:
+            sp = lambda pos, sh, mir: E.spread_positions((nx, nz), w.h, pos, shift=sh, mirror=mir)  # noqa: E731
+            src = [sp(s.src_pos, (0.0, 0.0), True), sp(s.src_pos, (hx / 2, hz / 2), True)]
+            rec = [sp(s.rec_pos, (hx / 2, 0.0), False), sp(s.rec_pos, (0.0, hz / 2), False)]
+            tabs = [[E._table(src[t]) for t in range(2)], [E._table(rec[t]) for t in range(2)]]
+            tf = (s.stf(w.dt) / (hx * hz)).astype(np.float32)
+            parts = []
+            for d in range(2):
+                parts += L.cpml_coefficients(vmax, w.dt, w.halo, 1e-4, w.h[d], s.f0, w.freetop and d == 1)
+            cp = np.concatenate(parts).astype(np.float32)
+            self.host.append((tabs, tf, cp))
+        self.mt = np.ascontiguousarray(np.array(w.momtens, dtype=np.float32).reshape(1, 3))
+        t = torch
+        self.tf_d = [t.from_numpy(np.ascontiguousarray(h[1].ravel(order="F"))).to(self.dev) for h in self.host]
+        self.tr_d = [t.zeros(s.nt * 2 * s.rec_pos.shape[0], dtype=t.float32, device=self.dev) for s in w.shots]
+        self.obs_d = [t.zeros_like(x) for x in self.tr_d]
+        self.grad_d = t.zeros(3 * nx * nz, dtype=t.float64, device=self.dev)
+        self.mis_d = t.zeros(1, dtype=t.float64, device=self.dev)
+
+    def set_material(self, lam, mu, rho):
+        arrs = [np.asfortranarray(a, dtype=np.float32) for a in (lam, mu, rho)]
+        self.ctx.check(self.lib.sw_elastic_set_material(self.h, *(a.ctypes.data for a in arrs)), "set_material")
+
+    def structs(self, idx, tf, tr, obs):
+        arr = (self.L.SwElasticShot * len(idx))()
+        for k, i in enumerate(idx):
+            tabs, _, cp = self.host[i]
+            s = self.w.shots[i]
+            st = arr[k]
+            st.nt, st.kind, st.nsrc, st.nrec = s.nt, 0, 1, s.rec_pos.shape[0]
+            st.srctf, st.traces, st.cpml, st.momtens = tf[i], tr[i], cp.ctypes.data, self.mt.ctypes.data
+            for t in range(2):
+                for (off, ij, coef), tgt in ((tabs[0][t], st.src[t]), (tabs[1][t], st.rec[t])):
+                    tgt.offsets, tgt.ij, tgt.coef = off.ctypes.data, ij.ctypes.data, coef.ctypes.data
+            if obs is not None:
+                st.observed = obs[i]
+        return arr
+
+    def make_observed(self):
+        self.set_material(*self.w.observed_model)
+        idx = list(range(len(self.w.shots)))
+        arr = self.structs(idx, [x.data_ptr() for x in self.tf_d], [x.data_ptr() for x in self.obs_d], None)
+        self.ctx.check(self.lib.sw_elastic_forward(self.h, len(idx), arr, 1), "observed forward")
+        self.set_material(self.w.lam, self.w.mu, self.w.rho)
+
+    def gradient_device(self, idx):
+        arr = self.structs(idx, [x.data_ptr() for x in self.tf_d], [x.data_ptr() for x in self.tr_d],
+                           [x.data_ptr() for x in self.obs_d])
+        n = self.grad_d.numel() // 3
+        p = self.grad_d.data_ptr()
+        self.ctx.check(self.lib.sw_elastic_gradient(self.h, len(idx), arr, 1, p, p + 8 * n, p + 16 * n,
+                                                     self.mis_d.data_ptr()), "sw_elastic_gradient")
+
+    def setup_host(self):
+        t = self.torch
+        self.tf_h = [x.cpu().pin_memory() for x in self.tf_d]
+        self.obs_h = [x.cpu().pin_memory() for x in self.obs_d]
+        self.tr_h = [t.zeros(x.numel(), dtype=t.float32).pin_memory() for x in self.tr_d]
+        self.grad_h = t.zeros(self.grad_d.numel(), dtype=t.float64).pin_memory()
+        self.mis_h = t.zeros(1, dtype=t.float64).pin_memory()
+        h2d = sum(x.numel() * 4 for x in self.tf_h) + sum(x.numel() * 4 for x in self.obs_h)
+        d2h = sum(x.numel() * 4 for x in self.tr_h) + self.grad_h.numel() * 8 + 8
+        return h2d, d2h
+
+    def gradient_host(self):
+        idx = list(range(len(self.w.shots)))
+        arr = self.structs(idx, [x.data_ptr() for x in self.tf_h], [x.data_ptr() for x in self.tr_h],
+                           [x.data_ptr() for x in self.obs_h])
+        n = self.grad_h.numel() // 3
+        p = self.grad_h.data_ptr()
+        self.ctx.check(self.lib.sw_elastic_gradient(self.h, len(idx), arr, 0, p, p + 8 * n, p + 16 * n,
+                                                     self.mis_h.data_ptr()), "sw_elastic_gradient")
+
+    timed = GradientRun.timed
+
+
+def _elastic_cpu_baseline(sw, w, nt_sample):
+    import oracle
+
+    E = sys.modules[sw.__name__ + ".elastic"]
+    s = w.shots[0]
+    nx, nz = w.lam.shape
+    hx, hz = w.h
+    sp = lambda pos, sh, mir: E.spread_positions((nx, nz), w.h, pos, shift=sh, mirror=mir)  # noqa: E731
+    shot = dict(kind="mt", srctf=s.stf(w.dt)[:nt_sample] / (hx * hz), momtens=np.array([w.momtens]),
+                src_tables=[sp(s.src_pos, (0.0, 0.0), True), sp(s.src_pos, (hx / 2, hz / 2), True)],
+                rec_tables=[sp(s.rec_pos, (hx / 2, 0.0), False), sp(s.rec_pos, (0.0, hz / 2), False)])
+    cp = oracle.cpml_blocks(w.vp, w.h, w.dt, w.halo, 1e-4, s.f0, w.freetop)
+    obs = np.zeros((nt_sample, 2, s.rec_pos.shape[0]))
+    threads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    oracle.elastic_gradient(w.lam, w.mu, w.rho, w.h, w.dt, w.halo, w.freetop, cp, shot, obs,
+                            check_freq=min(w.check_freq, nt_sample - 1), nthreads=threads)
+    dt = time.perf_counter() - t0
+    pts = float(nx * nz) * nt_sample
+    sample = (f"one shot of {w.name}, {nt_sample} time steps, checkpoint period "
+              f"{min(w.check_freq, nt_sample - 1)}, FP64 gradient (forward + recompute + adjoint)")
+    return pts / dt / 1e9, threads, sample, dt
+
+
 def _peak():
     f = ROOT / "MEASURED_PEAKS.json"
     if f.exists():
@@ -422,12 +548,90 @@ def run_gb300(a):
     print(json.dumps(line), flush=True)
 
 
+ELASTIC_KINDS = {0: "k_el_stress + k_el_disp forward", 4: "k_el_stress + k_el_disp recompute (writes slots)",
+                 1: "k_el_stress + k_el_disp adjoint", 5: "k_el_corr gradient correlation"}
+
+
+def measure_elastic(a, name="elastic2d_1200x600", shots=0, nt_cap=0, steps=None, warmup=None, plain=True,
+                    cpu=True, device=0):
+    """Batched elastic gradient: Gpts/s, shots/s, e2e, plain per-shot path, roofline of the dominant kind."""
+    import torch
+
+    steps = a.steps if steps is None else steps
+    warmup = a.warmup if warmup is None else warmup
+    sw, w = _workload(name, shots, nt_cap)
+    R = ElasticRun(sw, w, device)
+    if a.tz:
+        R.ctx.check(R.lib.sw_elastic_set_tuning(R.h, a.tz), "sw_elastic_set_tuning")
+    R.make_observed()
+    nshots = len(w.shots)
+    allidx = list(range(nshots))
+    pts = float(w.point_steps())
+    for _ in range(warmup):
+        R.gradient_device(allidx)
+    torch.cuda.synchronize(R.dev)
+    clocks = ClockSampler(device)
+    clocks.start()
+    R.ctx.profile(True)
+    t_dev = R.timed(lambda: R.gradient_device(allidx), steps)
+    R.ctx.profile(False)
+    clk = clocks.stop()
+    prof = {k: R.ctx.profile_read(k) for k in range(6)}
+    h2d, d2h = R.setup_host()
+    R.gradient_host()
+    t_e2e = R.timed(R.gradient_host, steps)
+    pl = None
+    if plain:
+        R.gradient_device([0])
+        t_plain = R.timed(lambda: [R.gradient_device([i]) for i in allidx], 1)
+        pl = {"value": pts / t_plain / 1e9, "unit": UNIT, "shots_per_s": nshots / t_plain,
+              "ms_per_step": t_plain * 1e3, "what": "same kernels, one shot per call"}
+    dom = max(ELASTIC_KINDS, key=lambda k: prof[k][0])
+    ms_tot, launches, bytes_tot = prof[dom]
+    achieved = bytes_tot / (ms_tot / 1e3) / 1e9 if ms_tot > 0 else None
+    peak, peak_kind = _peak()
+    roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak if achieved else None, "traffic": None, "kernel": ELASTIC_KINDS[dom],
+            "peak_kind": peak_kind,
+            "kernels": {ELASTIC_KINDS[k]: {"ms": prof[k][0], "launches": prof[k][1],
+                                           "GB_per_s": (prof[k][2] / (prof[k][0] / 1e3) / 1e9) if prof[k][0] else None}
+                        for k in ELASTIC_KINDS}}
+    out = {"metric": METRIC, "value": pts * steps / t_dev / 1e9, "unit": UNIT, "n_gpus": 1, "steps": steps,
+           "warmup": warmup, "ms_per_step": t_dev * 1e3 / steps, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+           "config": {"workload": w.name, "grid": list(w.lam.shape), "h_m": w.h[0], "shots": nshots,
+                      "nt": max(s.nt for s in w.shots), "receivers": w.shots[0].rec_pos.shape[0],
+                      "check_freq": w.check_freq, "halo": w.halo, "sources": "explosive moment tensor, sinc spread",
+                      "tz": a.tz or 8,
+                      "cache": "inputs larger than L2 (each step streams several GB of wavefield state)",
+                      "precision": "fp32 wavefields and stencil, Kahan fp32 correlation, fp64 misfit and shot sum"},
+           "shots_per_s": nshots * steps / t_dev, "plain": pl,
+           "batched_vs_plain": (nshots * steps / t_dev / pl["shots_per_s"]) if pl else None,
+           "clocks": clk,
+           "e2e": {"value": pts * steps / t_e2e / 1e9, "unit": UNIT, "h2d_bytes_per_step": h2d,
+                   "d2h_bytes_per_step": d2h},
+           "gpu_launches": sum(prof[k][1] for k in range(6)), "roofline": roof}
+    if cpu:
+        import oracle
+
+        oracle.load()
+        v, threads, sample, _ = _elastic_cpu_baseline(sw, w, a.cpu_sample_nt)
+        out["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample}
+    R.lib.sw_elastic_destroy(R.h)
+    return out
+
+
 def main():
     a = _args()
     if a.impl == "reference":
         run_reference(a)
         return
     try:
+        if a.workload.startswith("elastic"):
+            if int(os.environ.get("RANK", "0")) == 0:
+                print(json.dumps(measure_elastic(a, a.workload, a.shots, a.nt, plain=not a.no_plain,
+                                                 cpu=not a.no_cpu)), flush=True)
+            return
         run_gb300(a)
     finally:
         if int(os.environ.get("WORLD_SIZE", "1")) > 1:

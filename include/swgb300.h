@@ -243,6 +243,9 @@ int sw_elastic_forward(sw_elastic* es, int32_t nshots, const sw_elastic_shot* sh
  * outputs are device pointers. */
 int sw_elastic_gradient(sw_elastic* es, int32_t nshots, const sw_elastic_shot* shots, int32_t on_device,
                         double* grad_rho, double* grad_lambda, double* grad_mu, double* misfit);
+/* Rows per thread block of the elastic stencil kernels: 8, 16 or 32 (0 =
+ * default 8).  A tuning knob of this backend; no reference counterpart. */
+int sw_elastic_set_tuning(sw_elastic* es, int32_t tz);
 
 /* 2D forward of one shot that allocates no device memory.  Has no
  * counterpart in the reference: it exists for callers that cannot let a

@@ -10,6 +10,8 @@ exactly what a SeismicWaves.jl user passes to ScalarSources/ScalarReceivers.
   acoustic2d_801       801 x 801, h = 5 m, gradient + 8 blobs, 1 shot, 401 receivers, nt = 3000, K = 50
   acoustic2d_2001x801  2001 x 801, h = 10 m, 12 layers, 64 shots, 50-300 receivers, nt in [2000, 4000], K = 50
   acoustic3d_400       400^3, h = 10 m, smooth random 1800-4000 m/s, 16 shots, 40 x 40 receivers, nt = 2000, K = 100
+  elastic2d_1200x600   1200 x 600, h = 5 m, vp 2000-4500, vs = vp/sqrt(3) * U(0.9, 1.0), rho 1800-2700 (smooth
+                       seeded fields), 32 explosive moment-tensor shots, 300 receivers, nt = 4000, 15 Hz, K = 50
 """
 from __future__ import annotations
 
@@ -172,9 +174,68 @@ def acoustic3d_400(seed: int = 5, n: int = 400, nshots_side: int = 4, patch: int
                     vp_observed=np.asfortranarray(vp * 1.03))
 
 
+@dataclass
+class ElasticWorkload:
+    name: str
+    lam: np.ndarray       # Fortran order (nx, nz)
+    mu: np.ndarray
+    rho: np.ndarray
+    h: tuple
+    dt: float
+    halo: int
+    freetop: bool
+    check_freq: int
+    shots: list = field(default_factory=list)
+    observed_model: tuple | None = None  # (lam, mu, rho) that generates the observed data
+    momtens: tuple = (1.0, 1.0, 0.0)     # Mxx, Mzz, Mxz (explosive)
+
+    @property
+    def gridpoints(self):
+        return int(np.prod(self.lam.shape))
+
+    def point_steps(self):
+        return sum(self.gridpoints * s.nt for s in self.shots)
+
+    @property
+    def vp(self):
+        return np.sqrt((self.lam + 2 * self.mu) / self.rho)
+
+
+def _smooth_field(shape, sigma, seed):
+    f = _gauss_smooth(np.random.default_rng(seed).standard_normal(shape), sigma)
+    return (f - f.min()) / max(f.max() - f.min(), 1e-12)
+
+
+def _elastic_model(nx, nz, seed):
+    vp = 2000.0 + 2500.0 * _smooth_field((nx, nz), 20.0, seed)
+    vs = vp / np.sqrt(3.0) * (0.9 + 0.1 * _smooth_field((nx, nz), 20.0, seed + 1))
+    rho = 1800.0 + 900.0 * _smooth_field((nx, nz), 20.0, seed + 2)
+    lam = rho * (vp ** 2 - 2 * vs ** 2)
+    mu = rho * vs ** 2
+    return tuple(np.asfortranarray(a) for a in (lam, mu, rho))
+
+
+def elastic2d_1200x600(seed: int = 7, nshots: int = 32, nrec: int = 300, nt: int = 4000) -> ElasticWorkload:
+    nx, nz, h = 1200, 600, 5.0
+    lam, mu, rho = _elastic_model(nx, nz, seed)
+    # observed model: the simulated one with 3 % smooth perturbations (a second seed)
+    pert = 1.0 + 0.03 * (2.0 * _smooth_field((nx, nz), 20.0, seed + 200) - 1.0)
+    obs = (np.asfortranarray(lam * pert), np.asfortranarray(mu * pert), rho)
+    vmax = max(float(np.max(np.sqrt((lam + 2 * mu) / rho))), float(np.max(np.sqrt((obs[0] + 2 * obs[1]) / rho))))
+    dt = 0.6 / (vmax * np.sqrt(2.0 / h ** 2) * 7.0 / 6.0)  # CFL number 0.6 with the 7/6 factor
+    ext = (nx - 1) * h
+    shots = []
+    for x in np.linspace(0.1 * ext, 0.9 * ext, nshots):
+        rec = np.stack([np.linspace(0.05 * ext, 0.95 * ext, nrec), np.full(nrec, 120.0)], 1)
+        shots.append(WShot(np.array([[x, 150.0]]), rec, nt, 15.0, 1.2 / 15.0))
+    return ElasticWorkload("elastic2d_1200x600", lam, mu, rho, (h, h), float(dt), 20, False, 50, shots,
+                           observed_model=obs)
+
+
 WORKLOADS = {
     "acoustic2d_201": acoustic2d_201,
     "acoustic2d_801": acoustic2d_801,
     "acoustic2d_2001x801": acoustic2d_2001x801,
     "acoustic3d_400": acoustic3d_400,
+    "elastic2d_1200x600": elastic2d_1200x600,
 }

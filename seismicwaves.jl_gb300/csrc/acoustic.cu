@@ -30,6 +30,8 @@
 #include <numeric>
 #include <sstream>
 
+#include <cuda_bf16.h>
+
 #include "acoustic_kernels.cuh"
 #include "internal.h"
 
@@ -276,6 +278,50 @@ __global__ void k_reduce_grad(const float* __restrict__ g, const float* __restri
   }
 }
 
+// BF16 checkpoints.  The (p, d) pair of a checkpoint is staged in FP32 (the
+// stencil writes it there), then each field of each shot is stored as BF16
+// with its own power-of-two scale (2^-e with e the exponent of the field's
+// largest |value|, so the stored values lie in (-2, 2)); recovery expands it
+// back into the FP32 stage.  gridDim.y = 2 * shots (field-major per shot).
+__global__ void k_ck_absmax(const float* __restrict__ stage, long long F, unsigned int* __restrict__ maxbits) {
+  const int q = blockIdx.y;  // shot * 2 + field
+  const float* x = stage + (long long)q * F;
+  float mx = 0.0f;
+  for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < F; c += (long long)gridDim.x * blockDim.x)
+    mx = fmaxf(mx, fabsf(x[c]));
+  for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(maxbits + q, __float_as_uint(mx));
+}
+
+__device__ __forceinline__ int ck_exponent(unsigned int bits) {
+  const float mx = __uint_as_float(bits);
+  return (mx > 0.0f && mx < 3.0e38f) ? ilogbf(mx) : 0;
+}
+
+__global__ void k_ck_pack(const float* __restrict__ stage, long long F, const unsigned int* __restrict__ maxbits,
+                          __nv_bfloat16* __restrict__ dst, long long shot_stride, float* __restrict__ inv_scale) {
+  const int q = blockIdx.y;
+  const int shot = q >> 1, f = q & 1;
+  const int e = ck_exponent(maxbits[q]);
+  const float sc = ldexpf(1.0f, -e);
+  const float* x = stage + (long long)q * F;
+  __nv_bfloat16* y = dst + (long long)shot * shot_stride + (long long)f * F;
+  for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < F; c += (long long)gridDim.x * blockDim.x)
+    y[c] = __float2bfloat16_rn(x[c] * sc);
+  if (blockIdx.x == 0 && threadIdx.x == 0) inv_scale[q] = ldexpf(1.0f, e);
+}
+
+__global__ void k_ck_unpack(const __nv_bfloat16* __restrict__ src, long long shot_stride, long long F,
+                            const float* __restrict__ inv_scale, float* __restrict__ stage) {
+  const int q = blockIdx.y;
+  const int shot = q >> 1, f = q & 1;
+  const float is = inv_scale[q];
+  const __nv_bfloat16* x = src + (long long)shot * shot_stride + (long long)f * F;
+  float* y = stage + (long long)q * F;
+  for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < F; c += (long long)gridDim.x * blockDim.x)
+    y[c] = __bfloat162float(x[c]) * is;
+}
+
 // fact = dt^2 vp^2 into the padded layout; vp kept unpadded (float).
 __global__ void k_set_fact(const float* __restrict__ vp, int n0, long long npts, int P, double dt2,
                            float* __restrict__ fact) {
@@ -315,8 +361,9 @@ struct sw_wavesim {
   DevMem g, gc;
   DevMem dbuf;                         // D slots
   long long d_slots = 0;
-  DevMem ck;                           // checkpoint slots
+  DevMem ck;                           // checkpoint slots (with BF16 snapshots: the psi / xi strips only)
   long long ck_slots = 0;
+  DevMem ck16, ck_scale, ck_max, ck_stage;  // BF16 (p, d) per slot and shot, their scales, FP32 stage
   DevMem zero;                         // zero state (one shot, stride 0)
   // tables
   DevMem d_desc, d_pts, d_ptr, d_ids, d_bslot, d_rec, d_tf, d_tr, d_obs, d_ic, d_mask, d_adj, d_cpml, d_partial, d_mis;
@@ -594,8 +641,16 @@ void ensure_state(sw_wavesim* ws, int S, bool grad, int max_nt) {
     const long long cks = K == 1 ? 0 : max_nt / K;
     if (cks > ws->ck_slots) {
       ws->ck.release();
-      const long long slot = 2 * F + ws->strip_total;
+      const bool bf = ws->gp.snapshot_bf16 != 0;
+      const long long slot = bf ? ws->strip_total : 2 * F + ws->strip_total;
       dev_alloc(ws->ck, (size_t)ws->cap * cks * slot * sizeof(float), "checkpoints", st);
+      if (bf) {
+        ws->ck16.release();
+        dev_alloc(ws->ck16, (size_t)ws->cap * cks * 2 * F * sizeof(__nv_bfloat16), "BF16 checkpoints", st);
+        dev_alloc(ws->ck_scale, (size_t)ws->cap * cks * 2 * sizeof(float), "checkpoint scales", st);
+        dev_alloc(ws->ck_max, (size_t)ws->cap * 2 * sizeof(unsigned), "checkpoint maxima", st);
+        dev_alloc(ws->ck_stage, (size_t)ws->cap * 2 * F * sizeof(float), "checkpoint stage", st);
+      }
       ws->ck_slots = cks;
     }
     if (!ws->zero.p) dev_alloc(ws->zero, (size_t)(2 * F + ws->strip_total) * sizeof(float), "zero state", st);
@@ -611,7 +666,12 @@ size_t per_shot_bytes(const sw_wavesim* ws, bool grad, int max_nt) {
   if (grad) {
     const int K = ws->gp.check_freq;
     floats += (K == 1 ? (long long)max_nt : K) * ws->F;
-    if (K > 1) floats += (long long)(max_nt / K) * (2 * ws->F + ws->strip_total);
+    if (K > 1) {
+      if (ws->gp.snapshot_bf16)  // BF16 (p, d) = one float's worth per point, plus the FP32 stage
+        floats += (long long)(max_nt / K) * (ws->F + ws->strip_total) + 2 * ws->F;
+      else
+        floats += (long long)(max_nt / K) * (2 * ws->F + ws->strip_total);
+    }
   }
   return (size_t)floats * sizeof(float);
 }
@@ -823,6 +883,38 @@ void launch_inject(sw_wavesim* ws, int Sa, const FieldArg& pnew, const FieldArg&
   ws->ctx->prof.end(st, KK_SRCREC, ev);
 }
 
+// BF16 checkpoint slot `slot`: the staged (p, d) of the S first shots.
+void pack_checkpoint(sw_wavesim* ws, int S, int slot) {
+  cudaStream_t st = ws->ctx->stream;
+  const long long F = ws->F;
+  const long long sstride16 = ws->ck_slots * 2 * F;  // one shot's slots are contiguous
+  cudaEvent_t ev = nullptr;
+  ws->ctx->prof.begin(st, KK_OTHER, 0.0, &ev);
+  check_cuda(cudaMemsetAsync(ws->ck_max.p, 0, (size_t)S * 2 * sizeof(unsigned), st), "checkpoint max clear");
+  const dim3 grid((unsigned)std::min<long long>((F + 255) / 256, 256), 2 * S);
+  k_ck_absmax<<<grid, 256, 0, st>>>(ws->ck_stage.as<float>(), F, ws->ck_max.as<unsigned>());
+  check_cuda(cudaGetLastError(), "checkpoint max launch");
+  k_ck_pack<<<grid, 256, 0, st>>>(ws->ck_stage.as<float>(), F, ws->ck_max.as<unsigned>(),
+                                  ws->ck16.as<__nv_bfloat16>() + (long long)slot * 2 * F, sstride16,
+                                  ws->ck_scale.as<float>() + (long long)slot * 2 * ws->cap);
+  check_cuda(cudaGetLastError(), "checkpoint pack launch");
+  ws->ctx->prof.end(st, KK_OTHER, ev);
+}
+
+void unpack_checkpoint(sw_wavesim* ws, int S, int slot) {
+  cudaStream_t st = ws->ctx->stream;
+  const long long F = ws->F;
+  const long long sstride16 = ws->ck_slots * 2 * F;
+  cudaEvent_t ev = nullptr;
+  ws->ctx->prof.begin(st, KK_OTHER, 0.0, &ev);
+  const dim3 grid((unsigned)std::min<long long>((F + 255) / 256, 256), 2 * S);
+  k_ck_unpack<<<grid, 256, 0, st>>>(ws->ck16.as<__nv_bfloat16>() + (long long)slot * 2 * F, sstride16, F,
+                                    ws->ck_scale.as<float>() + (long long)slot * 2 * ws->cap,
+                                    ws->ck_stage.as<float>());
+  check_cuda(cudaGetLastError(), "checkpoint unpack launch");
+  ws->ctx->prof.end(st, KK_OTHER, ev);
+}
+
 // Forward of one group: all shots step together.  Gradient mode (grad = true)
 // also writes checkpoints and the top-segment D.
 void forward_group(sw_wavesim* ws, const std::vector<HostShot>& group, bool grad) {
@@ -832,10 +924,12 @@ void forward_group(sw_wavesim* ws, const std::vector<HostShot>& group, bool grad
   const int max_nt = group.front().nt;
   const int K = grad ? ws->gp.check_freq : 0;
   const long long F = ws->F;
-  const long long slot = 2 * F + ws->strip_total;
+  const bool bf16 = grad && ws->gp.snapshot_bf16;
+  const long long slot = bf16 ? ws->strip_total : 2 * F + ws->strip_total;
   int pc = 0, pk = 0;
   Launcher L{ws, st};
   for (int it = 1; it <= max_nt; ++it) {
+    int ck_slot = -1;
     const int Sa = active_count(group, it);
     const StepCtx c = make_step_ctx(ws, Sa);
     StepArgs a = base_args(ws, c, Sa);
@@ -857,9 +951,16 @@ void forward_group(sw_wavesim* ws, const std::vector<HostShot>& group, bool grad
         const int m = (it - 1) / K;
         float* base = ws->ck.as<float>() + (long long)(m - 1) * slot;
         const long long sstride = ws->ck_slots * slot;
-        a.ck_p = FieldArg{base, sstride};
-        a.ck_d = FieldArg{base + F, sstride};
-        long long off = 2 * F;
+        long long off = 0;
+        if (bf16) {  // p and d go to the FP32 stage, packed to BF16 after the step
+          a.ck_p = FieldArg{ws->ck_stage.as<float>(), 2 * F};
+          a.ck_d = FieldArg{ws->ck_stage.as<float>() + F, 2 * F};
+          ck_slot = m - 1;
+        } else {
+          a.ck_p = FieldArg{base, sstride};
+          a.ck_d = FieldArg{base + F, sstride};
+          off = 2 * F;
+        }
         for (int d = 0; d < ws->N; ++d) { a.ck_psi[d] = FieldArg{base + off, sstride}; off += ws->psz[d]; }
         for (int d = 0; d < ws->N; ++d) { a.ck_xi[d] = FieldArg{base + off, sstride}; off += ws->xsz[d]; }
         ckpt = true;
@@ -884,6 +985,7 @@ void forward_group(sw_wavesim* ws, const std::vector<HostShot>& group, bool grad
     else
       L.step<MODE_FWD>(a, c, bytes);
     launch_inject(ws, Sa, a.pnew, a.dout, grad ? a.Dout : FieldArg{nullptr, 0}, d_first, it, 1);
+    if (ck_slot >= 0) pack_checkpoint(ws, Sa, ck_slot);
     pc = 1 - pc;
     pk = 1 - pk;
   }
@@ -895,7 +997,8 @@ void adjoint_group(sw_wavesim* ws, const std::vector<HostShot>& group) {
   const int max_nt = group.front().nt;
   const int K = ws->gp.check_freq;
   const long long F = ws->F;
-  const long long slot = 2 * F + ws->strip_total;
+  const bool bf16 = ws->gp.snapshot_bf16 != 0;
+  const long long slot = bf16 ? ws->strip_total : 2 * F + ws->strip_total;
   Launcher L{ws, st};
   zero_state(ws, S, true);
   check_cuda(cudaMemsetAsync(ws->g.p, 0, (size_t)S * F * sizeof(float), st), "reset g");
@@ -918,6 +1021,12 @@ void adjoint_group(sw_wavesim* ws, const std::vector<HostShot>& group) {
       }
       FieldArg ck_p{cbase, cstride}, ck_d{cbase + F, cstride}, ck_psi[3], ck_xi[3];
       long long off = 2 * F;
+      if (bf16 && m - 1 >= 1) {  // expand the BF16 (p, d) into the FP32 stage; strips stay in the slot
+        unpack_checkpoint(ws, Sa, m - 2);
+        ck_p = FieldArg{ws->ck_stage.as<float>(), 2 * F};
+        ck_d = FieldArg{ws->ck_stage.as<float>() + F, 2 * F};
+        off = 0;
+      }
       for (int d = 0; d < ws->N; ++d) { ck_psi[d] = FieldArg{cbase + off, cstride}; off += ws->psz[d]; }
       for (int d = 0; d < ws->N; ++d) { ck_xi[d] = FieldArg{cbase + off, cstride}; off += ws->xsz[d]; }
       int pc = 0, pk = 0;
@@ -1071,7 +1180,6 @@ void wavesim_init(sw_wavesim* ws, sw_ctx* ctx, const sw_acoustic_params* p, int 
     if (ws->gp.check_freq < 1) fail(SW_ERR_ARG, "check_freq must be positive");
     if (ws->gp.mute_radius_src < 0 || ws->gp.mute_radius_rec < 0)
       fail(SW_ERR_ARG, "mutearoundpoint!(): The smoothing radius must be positive.");
-    if (ws->gp.snapshot_bf16) fail(SW_ERR_UNSUPPORTED, "BF16 checkpoint snapshots are not available in this build");
   }
   ws->N = p->ndim;
   for (int d = 0; d < 3; ++d) ws->n[d] = d < p->ndim ? p->n[d] : 1;

@@ -25,6 +25,7 @@ void elastic_set_material(sw_elastic* es, const float* lam, const float* mu, con
 void elastic_forward(sw_elastic* es, int nshots, const sw_elastic_shot* shots, bool on_device);
 void elastic_gradient(sw_elastic* es, int nshots, const sw_elastic_shot* shots, bool on_device, double* g_rho,
                       double* g_lam, double* g_mu, double* misfit);
+void elastic_set_tuning(sw_elastic* es, int tz);
 sw_ctx* elastic_ctx(sw_elastic* es);
 sw_elastic* elastic_new();
 void elastic_delete(sw_elastic* es);
@@ -339,6 +340,12 @@ int sw_elastic_gradient(sw_elastic* es, int32_t nshots, const sw_elastic_shot* s
     swgb::check_cuda(cudaSetDevice(ctx->device), "cudaSetDevice");
     swgb::elastic_gradient(es, nshots, shots, on_device != 0, grad_rho, grad_lambda, grad_mu, misfit);
   });
+}
+
+int sw_elastic_set_tuning(sw_elastic* es, int32_t tz) {
+  if (!es) return SW_ERR_ARG;
+  sw_ctx* ctx = swgb::elastic_ctx(es);
+  return guarded(ctx, [&] { swgb::elastic_set_tuning(es, tz); });
 }
 
 }  // extern "C"

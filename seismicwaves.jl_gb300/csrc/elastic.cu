@@ -18,7 +18,7 @@
 //
 // Layout.  Every field of a shot is a zero-padded (nz + 4) x P array (x
 // fastest, P a multiple of 32): node (i, j) (1-based) sits at row j + 1 and
-// column i + 3.  The reference's "missing point = 0" boundary rules of the
+// column i + 31.  The reference's "missing point = 0" boundary rules of the
 // 4th-order derivatives all read points outside their array, so the padding
 // (which no kernel writes) supplies them; only the free-surface mirror rules
 // are coded.  The C-PML memory variables live in compact strips: x strips
@@ -56,10 +56,10 @@
 namespace swgb {
 namespace el {
 
-constexpr int XPAD = 4;  // columns left of i = 1
+constexpr int XPAD = 32; // columns left of i = 1 (keeps each warp's 32 points on one 128-byte line)
 constexpr int ZPAD = 2;  // rows above j = 1
 constexpr int BX = 128;  // threads per block (x)
-constexpr int TZ = 8;    // rows per block
+constexpr int CTZ = 2;   // rows per block (correlation); the stencil kernels take theirs as a template parameter
 
 struct Geo {
   int nx, nz, P, halo, ft, W;
@@ -138,13 +138,27 @@ __device__ __forceinline__ float dux_dz(const float* __restrict__ u, long long c
   return d4(__ldg(u + c - P), __ldg(u + c), __ldg(u + c + P), __ldg(u + c + 2 * P), inv);
 }
 
-// Stress update (update_sigma_xx_sigma_zz! + update_sigma_xz!) for the shots
-// blockIdx.z; nodes i <= nx-1, j <= nz-1 of the band blockIdx.y.
+__device__ __forceinline__ float ldz(const float* __restrict__ p, long long c, bool ok) {
+  return ok ? __ldg(p + c) : 0.0f;
+}
+
+constexpr unsigned FULL = 0xffffffffu;
+
+// Stress update (update_sigma_xx_sigma_zz! + update_sigma_xz!) for the shot
+// blockIdx.z; nodes i <= nx-1, j <= nz-1 of the band blockIdx.y.  Each thread
+// walks its column down the band with the column's z neighbours in registers;
+// x neighbours come from the adjacent lanes (loaded at the warp edges).
+template <int TZ>
 __global__ void __launch_bounds__(BX) k_el_stress(const Args A) {
   const Geo g = A.g;
   const int s = blockIdx.z;
+  const int lane = threadIdx.x & 31;
   const int i = blockIdx.x * BX + threadIdx.x + 1;
-  if (i > g.nx - 1) return;
+  const int j0 = blockIdx.y * TZ + 1;
+  const int j1 = min(j0 + TZ - 1, g.nz - 1);
+  if (j0 > j1) return;
+  const bool act = i <= g.nx - 1;
+  const bool ldok = i <= g.nx + 2;  // columns inside the padded row
   const long long so = (long long)s * g.F;
   const float* __restrict__ ux = A.ux + so;
   const float* __restrict__ uz = A.uz + so;
@@ -162,44 +176,71 @@ __global__ void __launch_bounds__(BX) k_el_stress(const Args A) {
   const int kE = cpml_full(i, g.nx, g.halo, colE);  // dux/dx at sigma_xx nodes (ux has nx-1 points)
   const int kG = cpml_half(i, g.nx, g.halo, colG);  // duz/dx at sigma_xz nodes (uz has nx points)
   const int jlo = g.ft ? 1 : 2;
-  const int j0 = blockIdx.y * TZ + 1;
-  const int j1 = min(j0 + TZ - 1, g.nz - 1);
-  for (int j = j0; j <= j1; ++j) {
-    const long long c = g.lin(i, j);
-    if (i >= 2 && j >= jlo) {
-      const float l = __ldg(A.lam + c), m = __ldg(A.mu + c);
-      const float l2m = l + 2.0f * m;
-      const float dux = dux_dx(ux, c, g.idx);
-      const float duz = (g.ft && j == 1) ? (-l / l2m) * dux : duz_dz_raw(uz, c, g.P, j, g.ft, g.idz);
-      float duxc = dux, duzc = duz;
-      if (kE) duxc = cpml_upd(pxE + (long long)(j - 1) * g.W + colE, cx[kE - 1], cx[na + nh + kE - 1], dux);
-      int colF = 0;
-      const int kF = cpml_full(j, g.nz, g.halo, colF);  // duz/dz (uz has nz-1 points)
-      if (kF) duzc = cpml_upd(pzF + (long long)colF * g.P + (i - 1), cz[kF - 1], cz[na + nh + kF - 1], duz);
-      sxx[c] = l2m * duxc + l * duzc;
-      szz[c] = (j == 1) ? 0.0f : l * duxc + l2m * duzc;
+  const int P = g.P;
+  long long c = g.lin(i, j0);
+  // column windows: ux rows j-1 .. j+2, uz rows j-2 .. j+1
+  float xu0 = ldz(ux, c - P, ldok), xu1 = ldz(ux, c, ldok), xu2 = ldz(ux, c + P, ldok), xu3 = ldz(ux, c + 2 * P, ldok);
+  float zu0 = ldz(uz, c - 2 * P, ldok), zu1 = ldz(uz, c - P, ldok), zu2 = ldz(uz, c, ldok), zu3 = ldz(uz, c + P, ldok);
+  for (int j = j0; j <= j1; ++j, c += P) {
+    float uxm1 = __shfl_up_sync(FULL, xu1, 1), uxm2 = __shfl_up_sync(FULL, xu1, 2);
+    float uxp1 = __shfl_down_sync(FULL, xu1, 1);
+    float uzm1 = __shfl_up_sync(FULL, zu2, 1), uzp1 = __shfl_down_sync(FULL, zu2, 1);
+    float uzp2 = __shfl_down_sync(FULL, zu2, 2);
+    if (lane < 2) uxm2 = ldz(ux, c - 2, ldok);
+    if (lane == 0) {
+      uxm1 = ldz(ux, c - 1, ldok);
+      uzm1 = ldz(uz, c - 1, ldok);
     }
-    {
-      const float dzx = duz_dx(uz, c, g.idx);
-      const float dxz = dux_dz(ux, c, g.P, j, g.ft, g.idz);
+    if (lane == 31) {
+      uxp1 = ldz(ux, c + 1, ldok);
+      uzp1 = ldz(uz, c + 1, ldok);
+    }
+    if (lane >= 30) uzp2 = ldz(uz, c + 2, ldok);
+    if (act) {
+      if (i >= 2 && j >= jlo) {
+        const float l = __ldg(A.lam + c), m = __ldg(A.mu + c);
+        const float l2m = l + 2.0f * m;
+        const float dux = d4(uxm2, uxm1, xu1, uxp1, g.idx);
+        float duz;
+        if (g.ft && j == 1) duz = (-l / l2m) * dux;
+        else if (g.ft && j == 2) duz = d4(zu1, zu1, zu2, zu3, g.idz);
+        else duz = d4(zu0, zu1, zu2, zu3, g.idz);
+        float duxc = dux, duzc = duz;
+        if (kE) duxc = cpml_upd(pxE + (long long)(j - 1) * g.W + colE, cx[kE - 1], cx[na + nh + kE - 1], dux);
+        int colF = 0;
+        const int kF = cpml_full(j, g.nz, g.halo, colF);  // duz/dz (uz has nz-1 points)
+        if (kF) duzc = cpml_upd(pzF + (long long)colF * P + (i - 1), cz[kF - 1], cz[na + nh + kF - 1], duz);
+        sxx[c] = l2m * duxc + l * duzc;
+        szz[c] = (j == 1) ? 0.0f : l * duxc + l2m * duzc;
+      }
+      const float dzx = d4(uzm1, zu2, uzp1, uzp2, g.idx);
+      const float dxz = (g.ft && j == 1) ? d4(xu2, xu1, xu2, xu3, g.idz) : d4(xu0, xu1, xu2, xu3, g.idz);
       float dzxc = dzx, dxzc = dxz;
       if (kG) dzxc = cpml_upd(pxG + (long long)(j - 1) * g.W + colG, cx[na + kG - 1], cx[2 * na + nh + kG - 1], dzx);
       int colH = 0;
       const int kH = cpml_half(j, g.nz, g.halo, colH);  // dux/dz (ux has nz points)
-      if (kH) dxzc = cpml_upd(pzH + (long long)colH * g.P + (i - 1), cz[na + kH - 1], cz[2 * na + nh + kH - 1], dxz);
+      if (kH) dxzc = cpml_upd(pzH + (long long)colH * P + (i - 1), cz[na + kH - 1], cz[2 * na + nh + kH - 1], dxz);
       sxz[c] = __ldg(A.mu_ij + c) * (dzxc + dxzc);
     }
+    const bool more = j + 1 <= j1;
+    xu0 = xu1; xu1 = xu2; xu2 = xu3; xu3 = ldz(ux, c + 3 * P, ldok && more);
+    zu0 = zu1; zu1 = zu2; zu2 = zu3; zu3 = ldz(uz, c + 2 * P, ldok && more);
   }
 }
 
 // Displacement update (update_ux! + update_uz!) in increment form; nodes
 // i <= nx, j <= nz of the band blockIdx.y.  With slots, also stores u[it-1]
-// and D(it) for the gradient.
+// and D(it) for the gradient.  Same register walk as the stress update.
+template <int TZ>
 __global__ void __launch_bounds__(BX) k_el_disp(const Args A) {
   const Geo g = A.g;
   const int s = blockIdx.z;
+  const int lane = threadIdx.x & 31;
   const int i = blockIdx.x * BX + threadIdx.x + 1;
-  if (i > g.nx) return;
+  const int j0 = blockIdx.y * TZ + 1;
+  const int j1 = min(j0 + TZ - 1, g.nz);
+  if (j0 > j1) return;
+  const bool ldok = i <= g.nx + 2;
   const long long so = (long long)s * g.F;
   float* __restrict__ ux = A.ux + so;
   float* __restrict__ uz = A.uz + so;
@@ -220,22 +261,30 @@ __global__ void __launch_bounds__(BX) k_el_disp(const Args A) {
   const int kC = cpml_full(i, g.nx, g.halo, colC);  // dsxz/dx at uz nodes (sigma_xz has nx-1 points)
   const bool slots = A.sUx != nullptr;
   const int P = g.P;
-  const int j0 = blockIdx.y * TZ + 1;
-  const int j1 = min(j0 + TZ - 1, g.nz);
-  for (int j = j0; j <= j1; ++j) {
-    const long long c = g.lin(i, j);
+  long long c = g.lin(i, j0);
+  // column windows: sigma_xz rows j-2 .. j+1, sigma_zz rows j-1 .. j+2
+  float q0 = ldz(sxz, c - 2 * P, ldok), q1 = ldz(sxz, c - P, ldok), q2 = ldz(sxz, c, ldok), q3 = ldz(sxz, c + P, ldok);
+  float w0 = ldz(szz, c - P, ldok), w1 = ldz(szz, c, ldok), w2 = ldz(szz, c + P, ldok), w3 = ldz(szz, c + 2 * P, ldok);
+  for (int j = j0; j <= j1; ++j, c += P) {
+    const float xc = ldz(sxx, c, ldok);
+    float xm1 = __shfl_up_sync(FULL, xc, 1), xp1 = __shfl_down_sync(FULL, xc, 1), xp2 = __shfl_down_sync(FULL, xc, 2);
+    float qm1 = __shfl_up_sync(FULL, q2, 1), qm2 = __shfl_up_sync(FULL, q2, 2), qp1 = __shfl_down_sync(FULL, q2, 1);
+    if (lane == 0) {
+      xm1 = ldz(sxx, c - 1, ldok);
+      qm1 = ldz(sxz, c - 1, ldok);
+    }
+    if (lane < 2) qm2 = ldz(sxz, c - 2, ldok);
+    if (lane == 31) {
+      xp1 = ldz(sxx, c + 1, ldok);
+      qp1 = ldz(sxz, c + 1, ldok);
+    }
+    if (lane >= 30) xp2 = ldz(sxx, c + 2, ldok);
     if (i <= g.nx - 1) {
-      const float d1 = d4(__ldg(sxx + c - 1), __ldg(sxx + c), __ldg(sxx + c + 1), __ldg(sxx + c + 2), g.idx);
+      const float d1 = d4(xm1, xc, xp1, xp2, g.idx);
       float d2;
-      if (g.ft && j == 1) {
-        const float a0 = __ldg(sxz + c), a1 = __ldg(sxz + c + P);
-        d2 = d4(-a1, -a0, a0, a1, g.idz);
-      } else if (g.ft && j == 2) {
-        const float am = __ldg(sxz + c - P);
-        d2 = d4(-am, am, __ldg(sxz + c), __ldg(sxz + c + P), g.idz);
-      } else {
-        d2 = d4(__ldg(sxz + c - 2 * P), __ldg(sxz + c - P), __ldg(sxz + c), __ldg(sxz + c + P), g.idz);
-      }
+      if (g.ft && j == 1) d2 = d4(-q3, -q2, q2, q3, g.idz);
+      else if (g.ft && j == 2) d2 = d4(-q1, q1, q2, q3, g.idz);
+      else d2 = d4(q0, q1, q2, q3, g.idz);
       float d1c = d1, d2c = d2;
       if (kA) d1c = cpml_upd(pxA + (long long)(j - 1) * g.W + colA, cx[na + kA - 1], cx[2 * na + nh + kA - 1], d1);
       int colB = 0;
@@ -251,14 +300,9 @@ __global__ void __launch_bounds__(BX) k_el_disp(const Args A) {
       ux[c] = u + du;
       dux[c] = du;
     }
-    if (j <= g.nz - 1) {
-      const float d1 = d4(__ldg(sxz + c - 2), __ldg(sxz + c - 1), __ldg(sxz + c), __ldg(sxz + c + 1), g.idx);
-      float d2;
-      if (g.ft && j == 1) {
-        d2 = d4(-__ldg(szz + c + P), __ldg(szz + c), __ldg(szz + c + P), __ldg(szz + c + 2 * P), g.idz);
-      } else {
-        d2 = d4(__ldg(szz + c - P), __ldg(szz + c), __ldg(szz + c + P), __ldg(szz + c + 2 * P), g.idz);
-      }
+    if (i <= g.nx && j <= g.nz - 1) {
+      const float d1 = d4(qm2, qm1, q2, qp1, g.idx);
+      const float d2 = (g.ft && j == 1) ? d4(-w2, w1, w2, w3, g.idz) : d4(w0, w1, w2, w3, g.idz);
       float d1c = d1, d2c = d2;
       if (kC) d1c = cpml_upd(pxC + (long long)(j - 1) * g.W + colC, cx[kC - 1], cx[na + nh + kC - 1], d1);
       int colD = 0;
@@ -274,6 +318,9 @@ __global__ void __launch_bounds__(BX) k_el_disp(const Args A) {
       uz[c] = u + du;
       duz[c] = du;
     }
+    const bool more = j + 1 <= j1;
+    q0 = q1; q1 = q2; q2 = q3; q3 = ldz(sxz, c + 2 * P, ldok && more);
+    w0 = w1; w1 = w2; w2 = w3; w3 = ldz(szz, c + 3 * P, ldok && more);
   }
 }
 
@@ -474,6 +521,8 @@ __device__ __forceinline__ void kahan_add_el(float* g, float* c, float y) {
   *g = t;
 }
 
+// Shots outer, rows inner: each thread keeps the five sums of its CTZ rows in
+// registers while it walks the shots of its group (two shots in flight).
 __global__ void __launch_bounds__(BX) k_el_corr(const CorrArgs A) {
   const Geo g = A.g;
   const int grp = blockIdx.z;
@@ -482,56 +531,75 @@ __global__ void __launch_bounds__(BX) k_el_corr(const CorrArgs A) {
   const int s0 = grp * A.gsize, s1 = min(s0 + A.gsize, A.nshots);
   float* acc = A.acc + (long long)grp * 10 * g.F;
   const int jlo = g.ft ? 1 : 2;
-  const int j0 = blockIdx.y * TZ + 1;
-  const int j1 = min(j0 + TZ - 1, g.nz);
-  for (int j = j0; j <= j1; ++j) {
-    const long long c = g.lin(i, j);
-    const bool on_ux = i <= g.nx - 1, on_uz = j <= g.nz - 1;
-    const bool on_xx = i >= 2 && i <= g.nx - 1 && j >= jlo && j <= g.nz - 1;
-    const bool on_xz = on_ux && on_uz;
-    float vri = 0.0f, vrj = 0.0f, vl = 0.0f, vm = 0.0f, vmij = 0.0f;
-    float l = 0.0f, l2m = 1.0f;
-    if (on_xx && g.ft && j == 1) {
-      l = __ldg(A.lam + c);
-      l2m = l + 2.0f * __ldg(A.mu + c);
-    }
-    for (int s = s0; s < s1; ++s) {
-      const long long so = (long long)s * g.F;
-      const float cs = __ldg(A.cs + s);
-      const float* aux = A.aux + so;
-      const float* auz = A.auz + so;
-      const float* fux = A.fux + so;
-      const float* fuz = A.fuz + so;
-      if (on_ux) vri += cs * (__ldg(aux + c) * __ldg(A.Dx + so + c));
-      if (on_uz) vrj += cs * (__ldg(auz + c) * __ldg(A.Dz + so + c));
-      if (on_xx) {
-        const float exx = dux_dx(fux, c, g.idx);
-        const float exa = dux_dx(aux, c, g.idx);
-        float ezz, eza;
-        if (g.ft && j == 1) {
-          ezz = (-l / l2m) * exx;
-          eza = (-l / l2m) * exa;
-        } else {
-          ezz = duz_dz_raw(fuz, c, g.P, j, g.ft, g.idz);
-          eza = duz_dz_raw(auz, c, g.P, j, g.ft, g.idz);
+  const int j0 = blockIdx.y * CTZ + 1;
+  const bool on_ux = i <= g.nx - 1;
+  const bool xx_col = i >= 2 && i <= g.nx - 1;
+  float v[5][CTZ];
+#pragma unroll
+  for (int r = 0; r < CTZ; ++r) {
+#pragma unroll
+    for (int q = 0; q < 5; ++q) v[q][r] = 0.0f;
+  }
+  float fsr = 0.0f;  // -lambda / (lambda + 2 mu) on the free surface (row j = 1)
+  if (g.ft && j0 == 1 && xx_col) {
+    const long long c1 = g.lin(i, 1);
+    const float l = __ldg(A.lam + c1);
+    fsr = -l / (l + 2.0f * __ldg(A.mu + c1));
+  }
+#pragma unroll 2
+  for (int s = s0; s < s1; ++s) {
+    const long long so = (long long)s * g.F;
+    const float cs = __ldg(A.cs + s);
+    const float* aux = A.aux + so;
+    const float* auz = A.auz + so;
+    const float* fux = A.fux + so;
+    const float* fuz = A.fuz + so;
+    const float* Dx = A.Dx + so;
+    const float* Dz = A.Dz + so;
+#pragma unroll
+    for (int r = 0; r < CTZ; ++r) {
+      const int j = j0 + r;
+      if (j <= g.nz) {
+        const long long c = g.lin(i, j);
+        const bool on_uz = j <= g.nz - 1;
+        if (on_ux) v[0][r] += cs * (__ldg(aux + c) * __ldg(Dx + c));
+        if (on_uz) v[1][r] += cs * (__ldg(auz + c) * __ldg(Dz + c));
+        if (xx_col && j >= jlo && on_uz) {
+          const float exx = dux_dx(fux, c, g.idx);
+          const float exa = dux_dx(aux, c, g.idx);
+          float ezz, eza;
+          if (g.ft && j == 1) {
+            ezz = fsr * exx;
+            eza = fsr * exa;
+          } else {
+            ezz = duz_dz_raw(fuz, c, g.P, j, g.ft, g.idz);
+            eza = duz_dz_raw(auz, c, g.P, j, g.ft, g.idz);
+          }
+          v[2][r] += cs * ((exx + ezz) * (exa + eza));
+          v[3][r] += cs * (exx * exa + ezz * eza);
         }
-        vl += cs * ((exx + ezz) * (exa + eza));
-        vm += cs * (exx * exa + ezz * eza);
-      }
-      if (on_xz) {
-        const float e = duz_dx(fuz, c, g.idx) + dux_dz(fux, c, g.P, j, g.ft, g.idz);
-        const float ea = duz_dx(auz, c, g.idx) + dux_dz(aux, c, g.P, j, g.ft, g.idz);
-        vmij += cs * (e * ea);  // 2 (exz exz' + ezx ezx') with exz = e / 2
+        if (on_ux && on_uz) {
+          const float e = duz_dx(fuz, c, g.idx) + dux_dz(fux, c, g.P, j, g.ft, g.idz);
+          const float ea = duz_dx(auz, c, g.idx) + dux_dz(aux, c, g.P, j, g.ft, g.idz);
+          v[4][r] += cs * (e * ea);  // 2 (exz exz' + ezx ezx') with exz = e / 2
+        }
       }
     }
+  }
+#pragma unroll
+  for (int r = 0; r < CTZ; ++r) {
+    const int j = j0 + r;
+    if (j > g.nz) break;
+    const long long c = g.lin(i, j);
+    const bool on_uz = j <= g.nz - 1;
     const bool half = g.ft && j == 1;
-    if (on_ux) kahan_add_el(acc + c, acc + 5 * g.F + c, half ? 0.5f * vri : vri);
-    if (on_uz) kahan_add_el(acc + g.F + c, acc + 6 * g.F + c, vrj);
-    if (on_xx) {
-      kahan_add_el(acc + 2 * g.F + c, acc + 7 * g.F + c, half ? 0.5f * vl : vl);
-      kahan_add_el(acc + 3 * g.F + c, acc + 8 * g.F + c, half ? vm : 2.0f * vm);
+    if (on_ux) kahan_add_el(acc + c, acc + 5 * g.F + c, half ? 0.5f * v[0][r] : v[0][r]);
+    if (on_uz) kahan_add_el(acc + g.F + c, acc + 6 * g.F + c, v[1][r]);
+    if (xx_col && j >= jlo && on_uz) {
+      kahan_add_el(acc + 2 * g.F + c, acc + 7 * g.F + c, half ? 0.5f * v[2][r] : v[2][r]);
+      kahan_add_el(acc + 3 * g.F + c, acc + 8 * g.F + c, half ? v[3][r] : 2.0f * v[3][r]);
     }
-    if (on_xz) kahan_add_el(acc + 4 * g.F + c, acc + 9 * g.F + c, vmij);
+    if (on_ux && on_uz) kahan_add_el(acc + 4 * g.F + c, acc + 9 * g.F + c, v[4][r]);
   }
 }
 
@@ -664,6 +732,7 @@ struct sw_elastic {
   // tables
   DevMem d_desc, d_ll, d_int, d_flt, d_tf, d_tr, d_obs, d_ic, d_mask, d_adj, d_mt, d_cp;
   DevMem d_partial, d_amax, d_balls, d_ball_ptr, d_cs;
+  int tz = 8;  // rows per block of the stencil kernels (8, 16 or 32; 8 measured fastest)
 };
 
 namespace {
@@ -1047,10 +1116,13 @@ struct Run {
     a.cps = es->cps;
     return a;
   }
+  // algorithmic bytes of one step (stress + displacement kernels): per point and
+  // shot, stress R ux uz (8) W sigma x3 (12), displacement R sigma x3 (12),
+  // R/W u, du (32), slots W u[it-1], D (16); shared material 20 (lambda, mu,
+  // mu_ij, dt^2/rho on both half grids)
   double step_bytes(int S, bool slots) const {
     const double pts = (double)es->g.nx * es->g.nz;
-    // stress: R u (8) W sigma (12); displacement: R sigma (12), R/W u, du (32); material 20 B shared
-    return pts * (S * (52.0 + (slots ? 16.0 : 0.0)) + 20.0);
+    return pts * (S * (64.0 + (slots ? 16.0 : 0.0)) + 20.0);
   }
   void inject_sigma(int S, int it) {
     if (S <= 0) return;
@@ -1095,22 +1167,33 @@ void zero_state(sw_elastic* es, int S, bool adjoint) {
   }
 }
 
+template <int TZ>
+void launch_stencil_tz(const sw_elastic* es, cudaStream_t st, const Args& a, int S, bool stress) {
+  const dim3 grid((es->g.nx + BX - 1) / BX, (es->g.nz + TZ - 1) / TZ, S);
+  if (stress) k_el_stress<TZ><<<grid, BX, 0, st>>>(a);
+  else k_el_disp<TZ><<<grid, BX, 0, st>>>(a);
+  check_cuda(cudaGetLastError(), stress ? "stress launch" : "displacement launch");
+}
+
+void launch_stencil(const sw_elastic* es, cudaStream_t st, const Args& a, int S, bool stress) {
+  if (es->tz == 16) launch_stencil_tz<16>(es, st, a, S, stress);
+  else if (es->tz == 32) launch_stencil_tz<32>(es, st, a, S, stress);
+  else launch_stencil_tz<8>(es, st, a, S, stress);
+}
+
 // stress, [sigma sources], displacement, [force sources], [recording]
 void full_step(Run& R, int S, int it, bool record, int kind, float* sU[2], float* sD[2]) {
   if (S <= 0) return;
   sw_elastic* es = R.es;
   Args a = R.args(false);
   if (sU) { a.sUx = sU[0]; a.sUz = sU[1]; a.sDx = sD[0]; a.sDz = sD[1]; }
-  const dim3 grid((es->g.nx + BX - 1) / BX, (es->g.nz + TZ - 1) / TZ, S);
   cudaEvent_t ev = nullptr;
   es->ctx->prof.begin(R.st, kind, 0.0, &ev);
-  k_el_stress<<<grid, BX, 0, R.st>>>(a);
-  check_cuda(cudaGetLastError(), "stress launch");
+  launch_stencil(es, R.st, a, S, true);
   es->ctx->prof.end(R.st, kind, ev);
   R.inject_sigma(S, it);
   es->ctx->prof.begin(R.st, kind, R.step_bytes(S, sU != nullptr), &ev);
-  k_el_disp<<<grid, BX, 0, R.st>>>(a);
-  check_cuda(cudaGetLastError(), "displacement launch");
+  launch_stencil(es, R.st, a, S, false);
   es->ctx->prof.end(R.st, kind, ev);
   R.inject_force(S, it, false, 1.0f, sD);
   if (record) R.record(S, it);
@@ -1120,13 +1203,10 @@ void adjoint_step(Run& R, int S, int it, float sa) {
   if (S <= 0) return;
   sw_elastic* es = R.es;
   Args a = R.args(true);
-  const dim3 grid((es->g.nx + BX - 1) / BX, (es->g.nz + TZ - 1) / TZ, S);
   cudaEvent_t ev = nullptr;
   es->ctx->prof.begin(R.st, KK_ADJOINT, R.step_bytes(S, false), &ev);
-  k_el_stress<<<grid, BX, 0, R.st>>>(a);
-  check_cuda(cudaGetLastError(), "adjoint stress launch");
-  k_el_disp<<<grid, BX, 0, R.st>>>(a);
-  check_cuda(cudaGetLastError(), "adjoint displacement launch");
+  launch_stencil(es, R.st, a, S, true);
+  launch_stencil(es, R.st, a, S, false);
   es->ctx->prof.end(R.st, KK_ADJOINT, ev);
   R.inject_force(S, it, true, sa, nullptr);
 }
@@ -1480,7 +1560,7 @@ void elastic_gradient(sw_elastic* es, int nshots, const sw_elastic_shot* shots, 
         c.lam = es->lam.as<float>(); c.mu = es->mu.as<float>();
         c.acc = es->acc.as<float>();
         const int ng = (A + gsize - 1) / gsize;
-        const dim3 grid((g.nx + BX - 1) / BX, (g.nz + TZ - 1) / TZ, ng);
+        const dim3 grid((g.nx + BX - 1) / BX, (g.nz + CTZ - 1) / CTZ, ng);
         cudaEvent_t ev = nullptr;
         const double pts = (double)g.nx * g.nz;
         es->ctx->prof.begin(st, KK_CORR, pts * (A * 24.0 + ng * 80.0), &ev);
@@ -1551,6 +1631,10 @@ void elastic_gradient(sw_elastic* es, int nshots, const sw_elastic_shot* shots, 
   es->ctx->prof.resolve();
 }
 
+void elastic_set_tuning(sw_elastic* es, int tz) {
+  if (tz != 0 && tz != 8 && tz != 16 && tz != 32) fail(SW_ERR_ARG, "tz must be 0 (default), 8, 16 or 32");
+  es->tz = tz == 0 ? 8 : tz;
+}
 sw_ctx* elastic_ctx(sw_elastic* es) { return es->ctx; }
 sw_elastic* elastic_new() { return new sw_elastic(); }
 void elastic_delete(sw_elastic* es) { delete es; }

@@ -105,7 +105,8 @@ def oracle_gradient(oracle, sw, case: Case, shot: Shot, check_freq=1, mute_src=0
 class GpuRun:
     """Drives libswgb300 directly through its C ABI for one case."""
 
-    def __init__(self, sw, case: Case, gradient=False, check_freq=1, mute_src=0, mute_rec=0, variant=0, tz=0):
+    def __init__(self, sw, case: Case, gradient=False, check_freq=1, mute_src=0, mute_rec=0, variant=0, tz=0,
+                 bf16=False):
         L = sw._lib
         self.sw, self.case, self.L = sw, case, L
         self.ctx = L.Context(0)
@@ -117,6 +118,7 @@ class GpuRun:
         prm.dt, prm.halo, prm.rcoef, prm.freetop = case.dt, case.halo, case.rcoef, int(case.freetop)
         gp = L.SwGradParams()
         gp.check_freq, gp.mute_radius_src, gp.mute_radius_rec = check_freq, mute_src, mute_rec
+        gp.snapshot_bf16 = int(bf16)
         self.h = ctypes.c_void_p()
         self.ctx.check(self.ctx.lib.sw_wavesim_create(self.ctx.h, ctypes.byref(prm), int(gradient),
                                                       ctypes.byref(gp), ctypes.byref(self.h)), "create")
