@@ -137,7 +137,9 @@ typedef struct {
   int32_t mute_radius_src;  /* grid points; 0 = off */
   int32_t mute_radius_rec;
   int32_t compute_misfit;
-  int32_t snapshot_bf16;    /* 1: checkpoints held as per-snapshot-scaled BF16 */
+  int32_t snapshot_bf16;    /* 0: FP32 snapshots; 1: the recompute buffer (the second time differences
+                               kept between checkpoints) in BF16; 2: also the checkpoints' (p, d) in
+                               per-snapshot-scaled BF16.  Acoustic path only. */
 } sw_grad_params;
 
 /* build_wavesim.  `gradient` = 1 allows sw_acoustic_gradient.  Device memory

@@ -214,15 +214,17 @@ class RunParameters:
 class GradParameters:
     """src/models/genparameters.jl:63-79.
 
-    snapshot_bf16 (an addition of this backend, off by default): keep the
-    acoustic checkpoints as per-snapshot-scaled BF16 (half the checkpoint
-    memory; gradient within 1e-3 instead of 1e-5 of the FP64 result).
+    snapshot_bf16 (an addition of this backend, 0 by default): 1 keeps the
+    acoustic recompute buffer (the second time differences between
+    checkpoints) in BF16 -- half its memory and traffic, gradient within 1e-3
+    instead of 1e-5 of the FP64 result; 2 also keeps the checkpoints' (p, d)
+    as per-snapshot-scaled BF16 (a few 1e-3).
     """
     mute_radius_src: int = 0
     mute_radius_rec: int = 0
     compute_misfit: bool = False
     check_freq: int = 1
-    snapshot_bf16: bool = False
+    snapshot_bf16: int = 0
 
     def __post_init__(self):
         assert self.check_freq > 0

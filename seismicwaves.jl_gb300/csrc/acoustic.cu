@@ -76,13 +76,14 @@ __device__ __forceinline__ float ring_update(float* ring, int slot, int it, floa
 __global__ void k_inject_record(const ShotDesc* __restrict__ desc, const long long* __restrict__ pts,
                                 const int* __restrict__ ptr, const int* __restrict__ ids,
                                 const int* __restrict__ bslot, const long long* __restrict__ rec_lin,
-                                FieldArg pnew, FieldArg dnew, FieldArg dfield, int d_first, int it, int record) {
+                                FieldArg pnew, FieldArg dnew, FieldArg dfield, int d_first, int it, int record,
+                                int dbf16) {
   const int shot = blockIdx.x;
   const ShotDesc D = desc[shot];
   if (it > D.nt) return;
   float* pn = pnew.p + (long long)shot * pnew.s;
   float* dn = dnew.p + (long long)shot * dnew.s;
-  float* dd = (dfield.p && shot >= d_first) ? dfield.p + (long long)shot * dfield.s : nullptr;
+  float* dd = (dfield.p && shot >= d_first) ? dptr(dfield, shot, dbf16) : nullptr;
   for (int u = threadIdx.x; u < D.nsp; u += blockDim.x) {
     const long long lin = pts[D.sp_off + u];
     float add = 0.f;
@@ -92,7 +93,7 @@ __global__ void k_inject_record(const ShotDesc* __restrict__ desc, const long lo
       for (int k = k0; k < k1; ++k) add += D.tf[(long long)(it - 1) + (long long)ids[k] * D.nt];
       float sd;
       pn[lin] = ring_update(D.ring, slot, it, add, &sd);
-      if (dd) dd[lin] = sd;
+      if (dd) dst1(dd, lin, sd, dbf16);
     } else {
       float acc = pn[lin];
       for (int k = k0; k < k1; ++k) {
@@ -102,7 +103,7 @@ __global__ void k_inject_record(const ShotDesc* __restrict__ desc, const long lo
       }
       pn[lin] = acc;
       dn[lin] += add;
-      if (dd) dd[lin] += add;
+      if (dd) dst1(dd, lin, dld1(dd, lin, dbf16) + add, dbf16);
     }
   }
   if (!record) return;
@@ -117,7 +118,7 @@ __global__ void k_inject_record(const ShotDesc* __restrict__ desc, const long lo
 // here (boundary nodes, which the stencil skips, add their full lambda * D).
 __device__ void adj_inject_shot(const ShotDesc& D, const long long* __restrict__ pts, const int* __restrict__ ptr,
                                 const int* __restrict__ ids, const int* __restrict__ bslot, float* lp, float* ld,
-                                const float* dp, float* gp, float* cp, int it);
+                                const float* dp, int dbf16, float* gp, float* cp, int it);
 
 // One block per accumulator group (grp consecutive shots share one gradient
 // pair); the group's shots are handled one after the other, so receivers of
@@ -125,7 +126,7 @@ __device__ void adj_inject_shot(const ShotDesc& D, const long long* __restrict__
 __global__ void k_adj_inject(const ShotDesc* __restrict__ desc, const long long* __restrict__ pts,
                              const int* __restrict__ ptr, const int* __restrict__ ids,
                              const int* __restrict__ bslot, FieldArg lam, FieldArg lamd, FieldArg dcorr, FieldArg g,
-                             FieldArg gc, int it, int nshots, int grp) {
+                             FieldArg gc, int it, int nshots, int grp, int dbf16) {
   float* gp = g.p + (long long)blockIdx.x * g.s;
   float* cp = gc.p + (long long)blockIdx.x * gc.s;
   for (int j = 0; j < grp; ++j) {
@@ -133,13 +134,13 @@ __global__ void k_adj_inject(const ShotDesc* __restrict__ desc, const long long*
     if (shot >= nshots) break;
     if (j > 0) __syncthreads();
     adj_inject_shot(desc[shot], pts, ptr, ids, bslot, lam.p + (long long)shot * lam.s,
-                    lamd.p + (long long)shot * lamd.s, dcorr.p + (long long)shot * dcorr.s, gp, cp, it);
+                    lamd.p + (long long)shot * lamd.s, dptr(dcorr, shot, dbf16), dbf16, gp, cp, it);
   }
 }
 
 __device__ void adj_inject_shot(const ShotDesc& D, const long long* __restrict__ pts, const int* __restrict__ ptr,
                                 const int* __restrict__ ids, const int* __restrict__ bslot, float* lp, float* ld,
-                                const float* dp, float* gp, float* cp, int it) {
+                                const float* dp, int dbf16, float* gp, float* cp, int it) {
   if (it > D.nt) return;
   for (int u = threadIdx.x; u < D.nrp; u += blockDim.x) {
     const long long lin = pts[D.rp_off + u];
@@ -164,7 +165,7 @@ __device__ void adj_inject_shot(const ShotDesc& D, const long long* __restrict__
       corr = add;
     }
     float gv = gp[lin], cv = cp[lin];
-    kahan_add(gv, cv, corr * dp[lin]);
+    kahan_add(gv, cv, corr * dld1(dp, lin, dbf16));
     gp[lin] = gv;
     cp[lin] = cv;
   }
@@ -635,13 +636,14 @@ void ensure_state(sw_wavesim* ws, int S, bool grad, int max_nt) {
     const long long dslots = K == 1 ? max_nt : K;
     if (dslots > ws->d_slots) {
       ws->dbuf.release();
-      dev_alloc(ws->dbuf, (size_t)ws->cap * dslots * F * sizeof(float), "D buffer", st);
+      const size_t esz = ws->gp.snapshot_bf16 >= 1 ? sizeof(__nv_bfloat16) : sizeof(float);
+      dev_alloc(ws->dbuf, (size_t)ws->cap * dslots * F * esz, "D buffer", st);
       ws->d_slots = dslots;
     }
     const long long cks = K == 1 ? 0 : max_nt / K;
     if (cks > ws->ck_slots) {
       ws->ck.release();
-      const bool bf = ws->gp.snapshot_bf16 != 0;
+      const bool bf = ws->gp.snapshot_bf16 >= 2;
       const long long slot = bf ? ws->strip_total : 2 * F + ws->strip_total;
       dev_alloc(ws->ck, (size_t)ws->cap * cks * slot * sizeof(float), "checkpoints", st);
       if (bf) {
@@ -665,9 +667,10 @@ size_t per_shot_bytes(const sw_wavesim* ws, bool grad, int max_nt) {
   if (ws->gradient) floats = 2 * floats + 2 * ws->F;
   if (grad) {
     const int K = ws->gp.check_freq;
-    floats += (K == 1 ? (long long)max_nt : K) * ws->F;
+    const long long dsl = (K == 1 ? (long long)max_nt : K) * ws->F;
+    floats += ws->gp.snapshot_bf16 >= 1 ? (dsl + 1) / 2 : dsl;  // BF16 D slots take half
     if (K > 1) {
-      if (ws->gp.snapshot_bf16)  // BF16 (p, d) = one float's worth per point, plus the FP32 stage
+      if (ws->gp.snapshot_bf16 >= 2)  // BF16 (p, d) = one float's worth per point, plus the FP32 stage
         floats += (long long)(max_nt / K) * (ws->F + ws->strip_total) + 2 * ws->F;
       else
         floats += (long long)(max_nt / K) * (2 * ws->F + ws->strip_total);
@@ -830,7 +833,16 @@ StepArgs base_args(sw_wavesim* ws, const StepCtx& c, int S) {
   a.TZ = c.TZ;
   a.err = ws->ctx->err.as<int>();
   a.pf = ws->pf;
+  a.dbf16 = (ws->gradient && ws->gp.snapshot_bf16 >= 1) ? 1 : 0;
   return a;
+}
+
+// D slot `k` of every shot (the slots of a shot are contiguous; FP32 or BF16 elements).
+FieldArg dslot_arg(const sw_wavesim* ws, long long k) {
+  const long long off = k * ws->F;
+  float* p = ws->gp.snapshot_bf16 >= 1 ? reinterpret_cast<float*>(ws->dbuf.as<__nv_bfloat16>() + off)
+                                       : ws->dbuf.as<float>() + off;
+  return FieldArg{p, ws->d_slots * ws->F};
 }
 
 FieldArg fa(const DevMem& m, long long stride) { return FieldArg{m.as<float>(), stride}; }
@@ -878,7 +890,8 @@ void launch_inject(sw_wavesim* ws, int Sa, const FieldArg& pnew, const FieldArg&
   ws->ctx->prof.begin(st, KK_SRCREC, 0.0, &ev);
   k_inject_record<<<Sa, 128, 0, st>>>(ws->d_desc.as<ShotDesc>(), ws->d_pts.as<long long>(), ws->d_ptr.as<int>(),
                                       ws->d_ids.as<int>(), ws->d_bslot.as<int>(), ws->d_rec.as<long long>(), pnew,
-                                      dnew, Dw, d_first, it, record);
+                                      dnew, Dw, d_first, it, record,
+                                      (ws->gradient && ws->gp.snapshot_bf16 >= 1) ? 1 : 0);
   check_cuda(cudaGetLastError(), "inject/record launch");
   ws->ctx->prof.end(st, KK_SRCREC, ev);
 }
@@ -924,7 +937,7 @@ void forward_group(sw_wavesim* ws, const std::vector<HostShot>& group, bool grad
   const int max_nt = group.front().nt;
   const int K = grad ? ws->gp.check_freq : 0;
   const long long F = ws->F;
-  const bool bf16 = grad && ws->gp.snapshot_bf16;
+  const bool bf16 = grad && ws->gp.snapshot_bf16 >= 2;
   const long long slot = bf16 ? ws->strip_total : 2 * F + ws->strip_total;
   int pc = 0, pk = 0;
   Launcher L{ws, st};
@@ -975,7 +988,7 @@ void forward_group(sw_wavesim* ws, const std::vector<HostShot>& group, bool grad
           if (it - 1 >= group[k].nt / K * K) { d_first = k; break; }
         dslot = (it - 1) % K;
       }
-      a.Dout = FieldArg{ws->dbuf.as<float>() + dslot * F, ws->d_slots * F};
+      a.Dout = dslot_arg(ws, dslot);
       a.d_first = d_first;
     }
     const int n_dwrite = grad ? Sa - d_first : 0;
@@ -997,7 +1010,7 @@ void adjoint_group(sw_wavesim* ws, const std::vector<HostShot>& group) {
   const int max_nt = group.front().nt;
   const int K = ws->gp.check_freq;
   const long long F = ws->F;
-  const bool bf16 = ws->gp.snapshot_bf16 != 0;
+  const bool bf16 = ws->gp.snapshot_bf16 >= 2;
   const long long slot = bf16 ? ws->strip_total : 2 * F + ws->strip_total;
   Launcher L{ws, st};
   zero_state(ws, S, true);
@@ -1044,7 +1057,7 @@ void adjoint_group(sw_wavesim* ws, const std::vector<HostShot>& group) {
           a.xi_out[d] = fa(ws->xi[d], ws->xsz[d]);
         }
         const long long dslot = (t - 1) % K;
-        a.Dout = FieldArg{ws->dbuf.as<float>() + dslot * F, ws->d_slots * F};
+        a.Dout = dslot_arg(ws, dslot);
         a.d_first = 0;
         L.step<MODE_FWD_D>(a, c, stencil_bytes(ws, Sa, MODE_FWD_D, Sa, false), true);
         launch_inject(ws, Sa, a.pnew, a.dout, a.Dout, 0, t, 0);
@@ -1071,7 +1084,7 @@ void adjoint_group(sw_wavesim* ws, const std::vector<HostShot>& group) {
       a.xi_out[d] = a.xi_in[d];
     }
     const long long dslot = K == 1 ? it - 1 : (it - 1) % K;
-    a.dcorr = FieldArg{ws->dbuf.as<float>() + dslot * F, ws->d_slots * F};
+    a.dcorr = dslot_arg(ws, dslot);
     a.g = fa(ws->g, F);
     a.gc = fa(ws->gc, F);
     if (ws->grp == 4) {
@@ -1094,7 +1107,7 @@ void adjoint_group(sw_wavesim* ws, const std::vector<HostShot>& group) {
     ws->ctx->prof.begin(st, KK_SRCREC, 0.0, &ev);
     k_adj_inject<<<(Sa + ws->grp - 1) / ws->grp, 128, 0, st>>>(
         ws->d_desc.as<ShotDesc>(), ws->d_pts.as<long long>(), ws->d_ptr.as<int>(), ws->d_ids.as<int>(),
-        ws->d_bslot.as<int>(), a.pnew, a.dout, a.dcorr, a.g, a.gc, it, Sa, ws->grp);
+        ws->d_bslot.as<int>(), a.pnew, a.dout, a.dcorr, a.g, a.gc, it, Sa, ws->grp, a.dbf16);
     check_cuda(cudaGetLastError(), "adjoint inject launch");
     ws->ctx->prof.end(st, KK_SRCREC, ev);
     apc = 1 - apc;
@@ -1180,6 +1193,7 @@ void wavesim_init(sw_wavesim* ws, sw_ctx* ctx, const sw_acoustic_params* p, int 
     if (ws->gp.check_freq < 1) fail(SW_ERR_ARG, "check_freq must be positive");
     if (ws->gp.mute_radius_src < 0 || ws->gp.mute_radius_rec < 0)
       fail(SW_ERR_ARG, "mutearoundpoint!(): The smoothing radius must be positive.");
+    if (ws->gp.snapshot_bf16 < 0 || ws->gp.snapshot_bf16 > 2) fail(SW_ERR_ARG, "snapshot_bf16 must be 0, 1 or 2");
   }
   ws->N = p->ndim;
   for (int d = 0; d < 3; ++d) ws->n[d] = d < p->ndim ? p->n[d] : 1;
@@ -1279,6 +1293,8 @@ void acoustic_gradient(sw_wavesim* ws, int nshots, const sw_acoustic_shot* shots
     dev_alloc(dmis, sizeof(double), "misfit output", ws->ctx->stream);
     mout = dmis.as<double>();
   }
+  if (ws->gp.snapshot_bf16 >= 1 && ws->N == 2 && (ws->variant & 3) == 1)
+    fail(SW_ERR_UNSUPPORTED, "BF16 snapshots are not available with the TMA stencil variant");
   // the shot sum is fused into the 2D adjoint for batches of 4 or more shots,
   // unless per-shot muting needs each shot's gradient
   ws->grp = (!mute && ws->N == 2 && (ws->variant & 3) != 1 && nshots >= 4) ? 4 : 1;

@@ -34,6 +34,8 @@
 // the stencil, exactly like the reference.
 #pragma once
 
+#include <cuda_bf16.h>
+
 #include "internal.h"
 
 namespace swgb {
@@ -58,6 +60,7 @@ struct StepArgs {
   int tiles_x, tiles_y, tiles_z, TZ;
   int* err;                                        // set to 1 when a bounded wait gives up
   int pf;                                          // 2D stencil: rows ahead prefetched into L2 (0 = off)
+  int dbf16;                                       // Dout / dcorr hold BF16 (the pointers are __nv_bfloat16 arrays)
 };
 
 struct StripIO {
@@ -84,6 +87,45 @@ __device__ __forceinline__ void ld4rw(float (&v)[4], const float* p) {
 }
 __device__ __forceinline__ void st4(float* p, const float (&v)[4]) {
   *reinterpret_cast<float4*>(p) = make_float4(v[0], v[1], v[2], v[3]);
+}
+
+// The D slots (second time differences kept for the gradient) are FP32 or,
+// with BF16 snapshots, __nv_bfloat16 arrays behind the same float* handle;
+// idx counts elements either way.
+__device__ __forceinline__ float* dptr(const FieldArg& f, int shot, int bf) {
+  if (!f.p) return nullptr;
+  if (bf) return reinterpret_cast<float*>(reinterpret_cast<__nv_bfloat16*>(f.p) + (long long)shot * f.s);
+  return f.p + (long long)shot * f.s;
+}
+__device__ __forceinline__ void dld4(float (&v)[4], const float* p, long long idx, int bf) {
+  if (bf) {
+    const uint2 u = __ldg(reinterpret_cast<const uint2*>(reinterpret_cast<const __nv_bfloat16*>(p) + idx));
+    const float2 a = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&u.x));
+    const float2 b = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&u.y));
+    v[0] = a.x; v[1] = a.y; v[2] = b.x; v[3] = b.y;
+  } else {
+    ld4(v, p + idx);
+  }
+}
+__device__ __forceinline__ void dst4(float* p, long long idx, const float (&v)[4], int bf) {
+  if (bf) {
+    const __nv_bfloat162 a = __floats2bfloat162_rn(v[0], v[1]);
+    const __nv_bfloat162 b = __floats2bfloat162_rn(v[2], v[3]);
+    uint2 u;
+    u.x = *reinterpret_cast<const unsigned*>(&a);
+    u.y = *reinterpret_cast<const unsigned*>(&b);
+    *reinterpret_cast<uint2*>(reinterpret_cast<__nv_bfloat16*>(p) + idx) = u;
+  } else {
+    st4(p + idx, v);
+  }
+}
+__device__ __forceinline__ void dst1(float* p, long long idx, float v, int bf) {
+  if (bf) reinterpret_cast<__nv_bfloat16*>(p)[idx] = __float2bfloat16_rn(v);
+  else p[idx] = v;
+}
+__device__ __forceinline__ float dld1(const float* p, long long idx, int bf) {
+  if (bf) return __bfloat162float(reinterpret_cast<const __nv_bfloat16*>(p)[idx]);
+  return p[idx];
 }
 
 // Kahan-compensated g += y (compensation c holds the running rounding error;
@@ -204,8 +246,8 @@ __global__ void __launch_bounds__(32 * NW, (Ac2dBounds<MODE, NW>::MINB - (DP - 1
   float* ckp = fptr(A.ck_p, shot);
   float* ckd = fptr(A.ck_d, shot);
   float* Dw = nullptr;
-  if (MODE == MODE_FWD_D && shot >= A.d_first) Dw = fptr(A.Dout, shot);
-  const float* dcr = MODE == MODE_ADJ ? fptr(A.dcorr, shot) : nullptr;
+  if (MODE == MODE_FWD_D && shot >= A.d_first) Dw = dptr(A.Dout, shot, A.dbf16);
+  const float* dcr = MODE == MODE_ADJ ? dptr(A.dcorr, shot, A.dbf16) : nullptr;
   float* gg = MODE == MODE_ADJ ? fptr(A.g, shot) : nullptr;
   float* gcp = MODE == MODE_ADJ ? fptr(A.gc, shot) : nullptr;
 
@@ -221,7 +263,7 @@ __global__ void __launch_bounds__(32 * NW, (Ac2dBounds<MODE, NW>::MINB - (DP - 1
     ld4rw(o, di + row + xa);
     ld4(f, fa + row + xa);
     if (MODE == MODE_ADJ) {
-      ld4(dv, dcr + row + xa);
+      dld4(dv, dcr, row + xa, A.dbf16);
       ld4rw(g4, gg + row + xa);
       ld4rw(c4, gcp + row + xa);
     }
@@ -247,7 +289,7 @@ __global__ void __launch_bounds__(32 * NW, (Ac2dBounds<MODE, NW>::MINB - (DP - 1
       l2_prefetch(pc + prow + P, seg);
       l2_prefetch(di + prow, seg);
       if (MODE == MODE_ADJ) {
-        l2_prefetch(dcr + prow, seg);
+        if (!A.dbf16) l2_prefetch(dcr + prow, seg);
         l2_prefetch(gg + prow, seg);
         l2_prefetch(gcp + prow, seg);
       }
@@ -267,7 +309,7 @@ __global__ void __launch_bounds__(32 * NW, (Ac2dBounds<MODE, NW>::MINB - (DP - 1
       ld4rw(on, di + nrow + xa);
       ld4(fn, fa + nrow + xa);
       if (MODE == MODE_ADJ) {
-        ld4(dvn, dcr + nrow + xa);
+        dld4(dvn, dcr, nrow + xa, A.dbf16);
         ld4rw(g4n, gg + nrow + xa);
         ld4rw(c4n, gcp + nrow + xa);
       }
@@ -321,7 +363,7 @@ __global__ void __launch_bounds__(32 * NW, (Ac2dBounds<MODE, NW>::MINB - (DP - 1
       if (vec_interior) {
         st4(pn + row + x0, outp);
         st4(dn + row + x0, outd);
-        if (MODE == MODE_FWD_D && Dw) st4(Dw + row + x0, outD);
+        if (MODE == MODE_FWD_D && Dw) dst4(Dw, row + x0, outD, A.dbf16);
       } else {
 #pragma unroll
         for (int e = 0; e < 4; ++e) {
@@ -329,7 +371,7 @@ __global__ void __launch_bounds__(32 * NW, (Ac2dBounds<MODE, NW>::MINB - (DP - 1
           if (x >= 1 && x <= nx - 2) {
             pn[row + x] = outp[e];
             dn[row + x] = outd[e];
-            if (MODE == MODE_FWD_D && Dw) Dw[row + x] = outD[e];
+            if (MODE == MODE_FWD_D && Dw) dst1(Dw, row + x, outD[e], A.dbf16);
           }
         }
       }
@@ -393,7 +435,7 @@ static __global__ void __launch_bounds__(128, 4) k_ac2d_adj_grp(const StepArgs A
   const float* di = fptr(A.din, sh);
   float* dn = fptr(A.dout, sh);
   const float* __restrict__ fa = A.fact;
-  const float* dcr = fptr(A.dcorr, sh);
+  const float* dcr = dptr(A.dcorr, sh, A.dbf16);
   const float* cp = A.cpml + (long long)sh * A.cpml_stride;
   const int na = 2 * H + 2, nh = 2 * H, L = 2 * na + 2 * nh;
   StripIO sx, sz;
@@ -424,7 +466,7 @@ static __global__ void __launch_bounds__(128, 4) k_ac2d_adj_grp(const StepArgs A
     ld4(rp, pc + row + P + xa);
     ld4rw(o, di + row + xa);
     ld4(f, fa + row + xa);
-    ld4(dv, dcr + row + xa);
+    dld4(dv, dcr, row + xa, A.dbf16);
   }
   float gv = 0.f, cv = 0.f;
   if (tin) {
@@ -442,7 +484,7 @@ static __global__ void __launch_bounds__(128, 4) k_ac2d_adj_grp(const StepArgs A
       ld4(rpn, pc + nrow + P + xa);
       ld4rw(on, di + nrow + xa);
       ld4(fn, fa + nrow + xa);
-      ld4(dvn, dcr + nrow + xa);
+      dld4(dvn, dcr, nrow + xa, A.dbf16);
     }
     if (tin && more) {
       gvn = gp[row + P + xt];
@@ -577,8 +619,8 @@ __global__ void __launch_bounds__(128) k_ac3d_step(const StepArgs A) {
   float* ckp = fptr(A.ck_p, shot);
   float* ckd = fptr(A.ck_d, shot);
   float* Dw = nullptr;
-  if (MODE == MODE_FWD_D && shot >= A.d_first) Dw = fptr(A.Dout, shot);
-  const float* dcr = MODE == MODE_ADJ ? fptr(A.dcorr, shot) : nullptr;
+  if (MODE == MODE_FWD_D && shot >= A.d_first) Dw = dptr(A.Dout, shot, A.dbf16);
+  const float* dcr = MODE == MODE_ADJ ? dptr(A.dcorr, shot, A.dbf16) : nullptr;
   float* gg = MODE == MODE_ADJ ? fptr(A.g, shot) : nullptr;
   float* gcp = MODE == MODE_ADJ ? fptr(A.gc, shot) : nullptr;
 
@@ -637,7 +679,7 @@ __global__ void __launch_bounds__(128) k_ac3d_step(const StepArgs A) {
       }
       if (MODE == MODE_ADJ) {
         float dv[4], g4[4], c4[4];
-        ld4(dv, dcr + idx);
+        dld4(dv, dcr, idx, A.dbf16);
         ld4rw(g4, gg + idx);
         ld4rw(c4, gcp + idx);
 #pragma unroll
@@ -655,7 +697,7 @@ __global__ void __launch_bounds__(128) k_ac3d_step(const StepArgs A) {
       if (vec_interior) {
         st4(pn + idx, outp);
         st4(dn + idx, outd);
-        if (MODE == MODE_FWD_D && Dw) st4(Dw + idx, outD);
+        if (MODE == MODE_FWD_D && Dw) dst4(Dw, idx, outD, A.dbf16);
       } else {
 #pragma unroll
         for (int e = 0; e < 4; ++e) {
@@ -663,7 +705,7 @@ __global__ void __launch_bounds__(128) k_ac3d_step(const StepArgs A) {
           if (x >= 1 && x <= nx - 2) {
             pn[idx + e] = outp[e];
             dn[idx + e] = outd[e];
-            if (MODE == MODE_FWD_D && Dw) Dw[idx + e] = outD[e];
+            if (MODE == MODE_FWD_D && Dw) dst1(Dw, idx + e, outD[e], A.dbf16);
           }
         }
       }
@@ -769,7 +811,7 @@ __global__ void __launch_bounds__(160, TmaLayout<MODE>::MIN_BLOCKS) k_ac2d_tma(c
 
   const float* pc = fptr(A.pcur, shot);
   const float* di = fptr(A.din, shot);
-  const float* dcr = MODE == MODE_ADJ ? fptr(A.dcorr, shot) : nullptr;
+  const float* dcr = MODE == MODE_ADJ ? dptr(A.dcorr, shot, A.dbf16) : nullptr;
   float* gg = MODE == MODE_ADJ ? fptr(A.g, shot) : nullptr;
   float* gcp = MODE == MODE_ADJ ? fptr(A.gc, shot) : nullptr;
 
@@ -816,7 +858,7 @@ __global__ void __launch_bounds__(160, TmaLayout<MODE>::MIN_BLOCKS) k_ac2d_tma(c
   float* ckp = fptr(A.ck_p, shot);
   float* ckd = fptr(A.ck_d, shot);
   float* Dw = nullptr;
-  if (MODE == MODE_FWD_D && shot >= A.d_first) Dw = fptr(A.Dout, shot);
+  if (MODE == MODE_FWD_D && shot >= A.d_first) Dw = dptr(A.Dout, shot, A.dbf16);
   StripIO sx, sz;
   sx.psi_in = fptr(A.psi_in[0], shot);  sx.psi_out = fptr(A.psi_out[0], shot);
   sx.xi_in = fptr(A.xi_in[0], shot);    sx.xi_out = fptr(A.xi_out[0], shot);
@@ -924,7 +966,7 @@ __global__ void __launch_bounds__(160, TmaLayout<MODE>::MIN_BLOCKS) k_ac2d_tma(c
       if (vec_interior) {
         st4(pn + row + x0, outp);
         st4(dn + row + x0, outd);
-        if (MODE == MODE_FWD_D && Dw) st4(Dw + row + x0, outD);
+        if (MODE == MODE_FWD_D && Dw) dst4(Dw, row + x0, outD, A.dbf16);
       } else {
 #pragma unroll
         for (int e = 0; e < 4; ++e) {
@@ -932,7 +974,7 @@ __global__ void __launch_bounds__(160, TmaLayout<MODE>::MIN_BLOCKS) k_ac2d_tma(c
           if (x >= 1 && x <= nx - 2) {
             pn[row + x] = outp[e];
             dn[row + x] = outd[e];
-            if (MODE == MODE_FWD_D && Dw) Dw[row + x] = outD[e];
+            if (MODE == MODE_FWD_D && Dw) dst1(Dw, row + x, outD[e], A.dbf16);
           }
         }
       }

@@ -118,7 +118,7 @@ class GpuRun:
         prm.dt, prm.halo, prm.rcoef, prm.freetop = case.dt, case.halo, case.rcoef, int(case.freetop)
         gp = L.SwGradParams()
         gp.check_freq, gp.mute_radius_src, gp.mute_radius_rec = check_freq, mute_src, mute_rec
-        gp.snapshot_bf16 = int(bf16)
+        gp.snapshot_bf16 = int(bf16)  # 0 FP32, 1 BF16 recompute buffer, 2 also BF16 checkpoints
         self.h = ctypes.c_void_p()
         self.ctx.check(self.ctx.lib.sw_wavesim_create(self.ctx.h, ctypes.byref(prm), int(gradient),
                                                       ctypes.byref(gp), ctypes.byref(self.h)), "create")
