@@ -171,6 +171,13 @@ int sw_acoustic_gradient(sw_wavesim* ws, int32_t nshots, const sw_acoustic_shot*
  * rows ahead into L2 (k = 1..15).  Results do not depend on either. */
 int sw_wavesim_set_tuning(sw_wavesim* ws, int32_t tz, int32_t variant);
 
+/* CUDA graphs (on by default): a batch's whole device-side time loop
+ * (forward; for the gradient also misfit, adjoint and shot sum) is captured
+ * into a graph on the second call with the same batch layout and replayed on
+ * later calls.  No reference counterpart (the reference launches every kernel
+ * from its time loop).  on = 0 launches directly. */
+int sw_wavesim_use_graphs(sw_wavesim* ws, int32_t on);
+
 /* Per-kernel timing collected with CUDA events on the context's stream while
  * enabled (0 = off).  kind: 0 = forward stencil, 1 = adjoint stencil (with the
  * correlation on the acoustic path), 2 = source/receiver kernels, 3 = other,

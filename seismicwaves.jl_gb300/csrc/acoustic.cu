@@ -27,6 +27,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <map>
 #include <numeric>
 #include <sstream>
 
@@ -374,6 +375,18 @@ struct sw_wavesim {
   int variant = 0;  // 2D stencil: 0 = register-pipelined, 1 = TMA
   int pf = 0;       // 2D stencil: L2 prefetch distance in rows (0 = off)
   int grp = 1;      // shots per gradient accumulator in the adjoint (4: shot sum fused, 1: per shot)
+  // CUDA graphs of a group's whole time loop, keyed by what the captured launches depend on
+  long long gen = 0;  // bumped whenever a device buffer the kernels see is (re)allocated
+  bool use_graphs = true;
+  std::map<std::vector<long long>, cudaGraphExec_t> graphs;
+  std::map<std::vector<long long>, int> graph_uses;  // calls per key (a key is captured on its second call)
+  DevMem d_gout, d_mout;  // gradient / misfit of the host-buffer path (stable addresses for the graphs)
+  void drop_graphs() {
+    for (auto& kv : graphs) cudaGraphExecDestroy(kv.second);
+    graphs.clear();
+    graph_uses.clear();
+  }
+  ~sw_wavesim() { drop_graphs(); }
 };
 
 namespace {
@@ -389,6 +402,59 @@ void ensure(sw_wavesim* ws, DevMem& m, size_t bytes, const char* what) {
   if (m.bytes >= bytes && m.p) return;
   m.release();
   dev_alloc(m, bytes, what, ws->ctx->stream);
+  ++ws->gen;
+}
+
+// Runs `work` (the device work of one group: launches, memsets, no host
+// synchronisation and no allocation) through a CUDA graph: captured on the
+// second call with `key` (one-off calls run directly), replayed afterwards;
+// at most 32 graphs are kept per simulation, later keys run directly.  Launch-bound cases (small grids, single
+// shots) gain the most.  Work runs directly instead when profiling (the
+// per-kernel events belong to single launches), when the caller's stream is
+// itself being captured (the launches then join the caller's graph), for the
+// TMA stencil variant, or when graphs are switched off.
+template <typename Work>
+void run_graph(sw_wavesim* ws, std::vector<long long> key, Work&& work) {
+  cudaStream_t st = ws->ctx->stream;
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  check_cuda(cudaStreamIsCapturing(st, &cs), "cudaStreamIsCapturing");
+  if (!ws->use_graphs || ws->ctx->prof.on || cs != cudaStreamCaptureStatusNone || (ws->variant & 3) == 1) {
+    work();
+    return;
+  }
+  key.push_back(ws->gen);
+  auto it = ws->graphs.find(key);
+  if (it == ws->graphs.end()) {
+    if (ws->graph_uses.size() > 4096) ws->graph_uses.clear();
+    if (++ws->graph_uses[key] < 2 || ws->graphs.size() >= 32) {
+      work();
+      return;
+    }
+    check_cuda(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal), "begin stream capture");
+    try {
+      work();
+    } catch (...) {
+      cudaGraph_t g = nullptr;
+      cudaStreamEndCapture(st, &g);
+      if (g) cudaGraphDestroy(g);
+      cudaGetLastError();
+      throw;
+    }
+    cudaGraph_t g = nullptr;
+    check_cuda(cudaStreamEndCapture(st, &g), "end stream capture");
+    cudaGraphExec_t ex = nullptr;
+    const cudaError_t e = cudaGraphInstantiate(&ex, g, 0);
+    cudaGraphDestroy(g);
+    check_cuda(e, "graph instantiate");
+    it = ws->graphs.emplace(key, ex).first;
+  }
+  check_cuda(cudaGraphLaunch(it->second, st), "graph launch");
+}
+
+std::vector<long long> group_key(const sw_wavesim* ws, const std::vector<HostShot>& group, bool grad) {
+  std::vector<long long> k = {grad ? 1 : 0, ws->grp, ws->variant, ws->tile_tz, ws->pf, (long long)group.size()};
+  for (const auto& h : group) k.push_back(h.nt);
+  return k;
 }
 
 template <typename T>
@@ -630,6 +696,7 @@ void ensure_state(sw_wavesim* ws, int S, bool grad, int max_nt) {
     ws->cap = S;
     ws->d_slots = 0;
     ws->ck_slots = 0;
+    ++ws->gen;
   }
   if (grad) {
     const int K = ws->gp.check_freq;
@@ -639,6 +706,7 @@ void ensure_state(sw_wavesim* ws, int S, bool grad, int max_nt) {
       const size_t esz = ws->gp.snapshot_bf16 >= 1 ? sizeof(__nv_bfloat16) : sizeof(float);
       dev_alloc(ws->dbuf, (size_t)ws->cap * dslots * F * esz, "D buffer", st);
       ws->d_slots = dslots;
+      ++ws->gen;
     }
     const long long cks = K == 1 ? 0 : max_nt / K;
     if (cks > ws->ck_slots) {
@@ -654,8 +722,12 @@ void ensure_state(sw_wavesim* ws, int S, bool grad, int max_nt) {
         dev_alloc(ws->ck_stage, (size_t)ws->cap * 2 * F * sizeof(float), "checkpoint stage", st);
       }
       ws->ck_slots = cks;
+      ++ws->gen;
     }
-    if (!ws->zero.p) dev_alloc(ws->zero, (size_t)(2 * F + ws->strip_total) * sizeof(float), "zero state", st);
+    if (!ws->zero.p) {
+      dev_alloc(ws->zero, (size_t)(2 * F + ws->strip_total) * sizeof(float), "zero state", st);
+      ++ws->gen;
+    }
   }
 }
 
@@ -1248,7 +1320,7 @@ void acoustic_forward(sw_wavesim* ws, int nshots, const sw_acoustic_shot* shots,
     ensure_state(ws, (int)group.size(), false, group.front().nt);
     Tables T;
     build_tables(ws, shots, group, on_device, false, T);
-    forward_group(ws, group, false);
+    run_graph(ws, group_key(ws, group, false), [&] { forward_group(ws, group, false); });
     download_traces(ws, shots, group, on_device);
   }
   check_cuda(cudaStreamSynchronize(ws->ctx->stream), "forward");
@@ -1281,23 +1353,22 @@ void acoustic_gradient(sw_wavesim* ws, int nshots, const sw_acoustic_shot* shots
     }
   cudaStream_t st = ws->ctx->stream;
   const std::vector<HostShot> order = sorted_order(nshots, shots);
-  DevMem dgrad, dmis;
   double* gout = grad;
   double* mout = misfit;
   if (!on_device) {
-    dev_alloc(dgrad, (size_t)ws->npts * sizeof(double), "gradient output", ws->ctx->stream);
-    gout = dgrad.as<double>();
-    dev_alloc(dmis, sizeof(double), "misfit output", ws->ctx->stream);
-    mout = dmis.as<double>();
-  } else if (!mout) {
-    dev_alloc(dmis, sizeof(double), "misfit output", ws->ctx->stream);
-    mout = dmis.as<double>();
+    ensure(ws, ws->d_gout, (size_t)ws->npts * sizeof(double), "gradient output");
+    gout = ws->d_gout.as<double>();
+  }
+  if (!on_device || !mout) {
+    ensure(ws, ws->d_mout, sizeof(double), "misfit output");
+    mout = ws->d_mout.as<double>();
   }
   if (ws->gp.snapshot_bf16 >= 1 && ws->N == 2 && (ws->variant & 3) == 1)
     fail(SW_ERR_UNSUPPORTED, "BF16 snapshots are not available with the TMA stencil variant");
   // the shot sum is fused into the 2D adjoint for batches of 4 or more shots,
   // unless per-shot muting needs each shot's gradient
   ws->grp = (!mute && ws->N == 2 && (ws->variant & 3) != 1 && nshots >= 4) ? 4 : 1;
+  const int nblk = 64;
   bool first_group = true;
   for (const auto& group : plan_groups(ws, order, true)) {
     const int S = (int)group.size();
@@ -1305,12 +1376,9 @@ void acoustic_gradient(sw_wavesim* ws, int nshots, const sw_acoustic_shot* shots
     ensure_state(ws, S, true, max_nt);
     Tables T;
     build_tables(ws, shots, group, on_device, true, T);
-    forward_group(ws, group, true);
-    download_traces(ws, shots, group, on_device);
-    // misfit and adjoint source
-    const int nblk = 64;
     ensure(ws, ws->d_partial, (size_t)nblk * S * sizeof(double), "misfit partials");
-    {
+    const bool accumulate = !first_group;
+    auto misfit_and_adjsrc = [&] {
       cudaEvent_t ev = nullptr;
       ws->ctx->prof.begin(st, KK_OTHER, 0.0, &ev);
       k_misfit_adjsrc<<<dim3(nblk, S), 256, 0, st>>>(ws->d_desc.as<ShotDesc>(), ws->d_rec.as<long long>(),
@@ -1318,12 +1386,40 @@ void acoustic_gradient(sw_wavesim* ws, int nshots, const sw_acoustic_shot* shots
       check_cuda(cudaGetLastError(), "misfit launch");
       ws->ctx->prof.end(st, KK_OTHER, ev);
       ws->ctx->prof.begin(st, KK_OTHER, 0.0, &ev);
-      k_misfit_sum<<<1, 256, 0, st>>>(ws->d_partial.as<double>(), nblk, S, mout, first_group ? 0 : 1);
+      k_misfit_sum<<<1, 256, 0, st>>>(ws->d_partial.as<double>(), nblk, S, mout, accumulate ? 1 : 0);
       check_cuda(cudaGetLastError(), "misfit sum launch");
       ws->ctx->prof.end(st, KK_OTHER, ev);
+    };
+    auto reduce = [&] {
+      cudaEvent_t ev = nullptr;
+      ws->ctx->prof.begin(st, KK_OTHER, 0.0, &ev);
+      const long long blocks = std::min<long long>((ws->npts + 255) / 256, 8192);
+      k_reduce_grad<<<(unsigned)blocks, 256, 0, st>>>(ws->g.as<float>(), ws->gc.as<float>(), ws->F,
+                                                      (S + ws->grp - 1) / ws->grp,
+                                                      ws->vp.as<float>(), ws->n[0], ws->npts, ws->P,
+                                                      1.0 / (ws->prm.dt * ws->prm.dt), gout, accumulate ? 1 : 0);
+      check_cuda(cudaGetLastError(), "gradient reduction launch");
+      ws->ctx->prof.end(st, KK_OTHER, ev);
+    };
+    if (!mute) {
+      // the whole group -- forward, misfit, adjoint, shot sum -- as one graph
+      std::vector<long long> key = group_key(ws, group, true);
+      key.insert(key.end(), {accumulate ? 1 : 0, (long long)(uintptr_t)gout, (long long)(uintptr_t)mout});
+      run_graph(ws, key, [&] {
+        forward_group(ws, group, true);
+        misfit_and_adjsrc();
+        adjoint_group(ws, group);
+        reduce();
+      });
+      download_traces(ws, shots, group, on_device);
+      first_group = false;
+      continue;
     }
+    forward_group(ws, group, true);
+    download_traces(ws, shots, group, on_device);
+    misfit_and_adjsrc();
     adjoint_group(ws, group);
-    if (mute) {
+    {
       // sources first, then receivers, like the reference; rmax depends on the radius
       double hmax = 0;
       for (int d = 0; d < ws->N; ++d) hmax = std::max(hmax, ws->prm.h[d]);
@@ -1362,18 +1458,7 @@ void acoustic_gradient(sw_wavesim* ws, int nshots, const sw_acoustic_shot* shots
         check_cuda(cudaStreamSynchronize(st), "mute");
       }
     }
-    {
-      cudaEvent_t ev = nullptr;
-      ws->ctx->prof.begin(st, KK_OTHER, 0.0, &ev);
-      const long long blocks = std::min<long long>((ws->npts + 255) / 256, 8192);
-      k_reduce_grad<<<(unsigned)blocks, 256, 0, st>>>(ws->g.as<float>(), ws->gc.as<float>(), ws->F,
-                                                      (S + ws->grp - 1) / ws->grp,
-                                                      ws->vp.as<float>(), ws->n[0], ws->npts, ws->P,
-                                                      1.0 / (ws->prm.dt * ws->prm.dt), gout,
-                                                      first_group ? 0 : 1);
-      check_cuda(cudaGetLastError(), "gradient reduction launch");
-      ws->ctx->prof.end(st, KK_OTHER, ev);
-    }
+    reduce();
     first_group = false;
   }
   if (!on_device) {
@@ -1389,6 +1474,10 @@ void wavesim_set_tuning(sw_wavesim* ws, int tz, int variant) {
   ws->tile_tz = tz;
   ws->variant = variant % 16;
   ws->pf = variant / 16;
+}
+void wavesim_use_graphs(sw_wavesim* ws, bool on) {
+  ws->use_graphs = on;
+  if (!on) ws->drop_graphs();
 }
 sw_ctx* wavesim_ctx(sw_wavesim* ws) { return ws->ctx; }
 sw_wavesim* wavesim_new() { return new sw_wavesim(); }

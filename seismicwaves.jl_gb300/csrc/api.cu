@@ -17,6 +17,7 @@ void acoustic_forward(sw_wavesim* ws, int nshots, const sw_acoustic_shot* shots,
 void acoustic_gradient(sw_wavesim* ws, int nshots, const sw_acoustic_shot* shots, bool on_device, double* grad,
                        double* misfit);
 void wavesim_set_tuning(sw_wavesim* ws, int tz, int variant);
+void wavesim_use_graphs(sw_wavesim* ws, bool on);
 sw_ctx* wavesim_ctx(sw_wavesim* ws);
 sw_wavesim* wavesim_new();
 void wavesim_delete(sw_wavesim* ws);
@@ -346,6 +347,12 @@ int sw_elastic_set_tuning(sw_elastic* es, int32_t tz) {
   if (!es) return SW_ERR_ARG;
   sw_ctx* ctx = swgb::elastic_ctx(es);
   return guarded(ctx, [&] { swgb::elastic_set_tuning(es, tz); });
+}
+
+int sw_wavesim_use_graphs(sw_wavesim* ws, int32_t on) {
+  if (!ws) return SW_ERR_ARG;
+  sw_ctx* ctx = swgb::wavesim_ctx(ws);
+  return guarded(ctx, [&] { swgb::wavesim_use_graphs(ws, on != 0); });
 }
 
 }  // extern "C"

@@ -299,3 +299,23 @@ def test_2d_stencil_variants_match_oracle(sw, oracle, tz):
         assert rel_l2(fw, tref) < TRACE_TOL
         assert abs(msf - mref) / abs(mref) < MISFIT_TOL
         assert rel_l2(g, gref) < GRAD_TOL
+
+
+def test_graph_replay_is_bitwise_identical(sw, oracle):
+    """Calls 1 (direct), 2 (captured) and 3 (replayed) give the same bits as
+    a simulation with graphs switched off, for the forward and the gradient."""
+    case, shot = _grad_case(sw, oracle, nt=300)
+    shots = [shot] * 5
+    off = GpuRun(sw, case, gradient=True, check_freq=10)
+    off.ctx.check(off.ctx.lib.sw_wavesim_use_graphs(off.h, 0), "use_graphs")
+    g0, m0, t0 = off.gradient(shots)
+    f0 = off.forward(shots)
+    off.close()
+    on = GpuRun(sw, case, gradient=True, check_freq=10)
+    for _ in range(3):
+        g, m, t = on.gradient(shots)
+        assert np.array_equal(g, g0) and m == m0
+        assert all(np.array_equal(a, b) for a, b in zip(t, t0))
+        f = on.forward(shots)
+        assert all(np.array_equal(a, b) for a, b in zip(f, f0))
+    on.close()
