@@ -50,6 +50,8 @@ def _args():
     p.add_argument("--tz", type=int, default=0, help="stencil tile height (0 = library heuristic)")
     p.add_argument("--variant", type=int, default=-1, help="2D stencil variant (-1 = library default)")
     p.add_argument("--autotune", action="store_true", help="pick variant and band height with the autotuner")
+    p.add_argument("--bf16", type=int, default=0, help="acoustic snapshot_bf16 (0 FP32, 1 BF16 recompute buffer, "
+                                                      "2 also BF16 checkpoints)")
     return p.parse_args()
 
 
@@ -130,7 +132,7 @@ class ClockSampler:
 class GradientRun:
     """The workload's shots as C-ABI structs over device (or pinned host) buffers."""
 
-    def __init__(self, sw, w, device, on_device=True):
+    def __init__(self, sw, w, device, on_device=True, bf16=0):
         import torch
 
         L = sw._lib
@@ -146,6 +148,7 @@ class GradientRun:
         prm.dt, prm.halo, prm.rcoef, prm.freetop = w.dt, w.halo, 1e-4, int(w.freetop)
         gp = L.SwGradParams()
         gp.check_freq = w.check_freq
+        gp.snapshot_bf16 = bf16
         self.h = ctypes.c_void_p()
         self.ctx.check(self.lib.sw_wavesim_create(self.ctx.h, ctypes.byref(prm), 1, ctypes.byref(gp),
                                                   ctypes.byref(self.h)), "sw_wavesim_create")
@@ -339,6 +342,7 @@ class ElasticRun:
 def _elastic_cpu_baseline(sw, w, nt_sample):
     import oracle
 
+    nt_sample = _sample_nt(w, nt_sample)
     E = sys.modules[sw.__name__ + ".elastic"]
     s = w.shots[0]
     nx, nz = w.lam.shape
@@ -384,9 +388,15 @@ def _traffic_from_profiles(kernel, workload):
     return None
 
 
+def _sample_nt(w, nt_sample):
+    """CPU sample length: the requested steps, fewer on large grids (about 2e9 point-steps at most)."""
+    return int(max(20, min(nt_sample, 2e9 // max(w.gridpoints, 1))))
+
+
 def _cpu_baseline(sw, w, nt_sample):
     import oracle
 
+    nt_sample = _sample_nt(w, nt_sample)
     s = w.shots[0]
     si = sw.nearest_grid_points(s.src_pos, w.h)
     ri = sw.nearest_grid_points(s.rec_pos, w.h)
@@ -440,7 +450,7 @@ def run_gb300(a):
         torch.cuda.set_device(local)
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     sw, w = _workload(a.workload, a.shots, a.nt)
-    R = GradientRun(sw, w, local)
+    R = GradientRun(sw, w, local, bf16=a.bf16)
     if a.tz or a.variant >= 0:
         R.ctx.check(R.lib.sw_wavesim_set_tuning(R.h, a.tz, max(a.variant, 0)), "sw_wavesim_set_tuning")
     R.make_observed()
@@ -531,7 +541,9 @@ def run_gb300(a):
                                            max(s.rec_pos.shape[0] for s in w.shots)],
                        "check_freq": w.check_freq, "halo": w.halo,
                        "cache": "inputs larger than L2 (each step streams tens of GB of wavefield state)",
-                       "precision": "fp32 wavefields and stencil, Kahan fp32 correlation, fp64 misfit and shot sum",
+                       "precision": "fp32 wavefields and stencil, Kahan fp32 correlation, fp64 misfit and shot sum"
+                                    + (", bf16 recompute buffer" if a.bf16 >= 1 else "")
+                                    + (", bf16 checkpoints" if a.bf16 >= 2 else ""),
                        "parallelism": f"replicas x{world}" if world > 1 else "1 GPU, all shots batched"},
             "shots_per_s": shots_per_s,
             "plain": plain,
