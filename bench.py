@@ -50,6 +50,7 @@ def _args():
     p.add_argument("--tz", type=int, default=0, help="stencil tile height (0 = library heuristic)")
     p.add_argument("--variant", type=int, default=-1, help="2D stencil variant (-1 = library default)")
     p.add_argument("--autotune", action="store_true", help="pick variant and band height with the autotuner")
+    p.add_argument("--forward-only", action="store_true", help="time the batched forward instead of the gradient")
     p.add_argument("--bf16", type=int, default=0, help="acoustic snapshot_bf16 (0 FP32, 1 BF16 recompute buffer, "
                                                       "2 also BF16 checkpoints)")
     return p.parse_args()
@@ -197,6 +198,10 @@ class GradientRun:
         self.ctx.check(self.lib.sw_acoustic_forward(self.hf, len(idx), arr, 1), "observed forward")
         self.lib.sw_wavesim_destroy(self.hf)
         self.ctx.check(self.lib.sw_wavesim_set_vp(self.h, self.vp_d.data_ptr(), 1), "set_vp")
+
+    def forward_device(self, idx):
+        arr = self.structs(idx, [x.data_ptr() for x in self.tf_d], [x.data_ptr() for x in self.tr_d], None)
+        self.ctx.check(self.lib.sw_acoustic_forward(self.h, len(idx), arr, 1), "sw_acoustic_forward")
 
     def gradient_device(self, idx):
         arr = self.structs(idx, [x.data_ptr() for x in self.tf_d], [x.data_ptr() for x in self.tr_d],
@@ -467,6 +472,26 @@ def run_gb300(a):
     nshots = len(w.shots)
     allidx = list(range(nshots))
     pts = float(w.point_steps())
+    if a.forward_only:
+        for _ in range(a.warmup):
+            R.forward_device(allidx)
+        clocks = ClockSampler(local)
+        clocks.start()
+        t_f = R.timed(lambda: R.forward_device(allidx), a.steps)
+        clk = clocks.stop()
+        R.ctx.profile(True)
+        R.timed(lambda: R.forward_device(allidx), 1)
+        R.ctx.profile(False)
+        ms, nl, by = R.ctx.profile_read(0)
+        peak, peak_kind = _peak()
+        if rank == 0:
+            print(json.dumps({"mode": "forward", "value": pts * a.steps / t_f / 1e9, "unit": UNIT,
+                              "ms_per_step": t_f * 1e3 / a.steps, "steps": a.steps, "warmup": a.warmup,
+                              "config": {"workload": w.name, "shots": nshots, "nt": max(s.nt for s in w.shots)},
+                              "clocks": clk, "stencil": {"ms": ms, "launches": nl, "GB_per_s": by / (ms / 1e3) / 1e9,
+                                                         "frac": by / (ms / 1e3) / 1e9 / peak, "peak": peak,
+                                                         "peak_kind": peak_kind}}), flush=True)
+        return
 
     def barrier():
         torch.cuda.synchronize(R.dev)

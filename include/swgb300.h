@@ -167,8 +167,10 @@ int sw_acoustic_gradient(sw_wavesim* ws, int32_t nshots, const sw_acoustic_shot*
  * the 2D stencil implementation: 0, 2, 3 = register-pipelined loads with 4,
  * 8 or 16 warps per block, 1 = TMA bulk copies through shared memory with a
  * producer warp; + 4 keeps a second row of loads in flight in the forward
- * kernels of the 4-warp stencil; + 16*k additionally prefetches the rows k
- * rows ahead into L2 (k = 1..15).  Results do not depend on either. */
+ * kernels of the 4-warp stencil; + 8 runs the grouped 2D adjoint (4+ shots)
+ * with 5 resident blocks per SM instead of 4 (registers capped at 102);
+ * + 16*k additionally prefetches the rows k rows ahead into L2 (k = 1..15).
+ * Results do not depend on any of them. */
 int sw_wavesim_set_tuning(sw_wavesim* ws, int32_t tz, int32_t variant);
 
 /* CUDA graphs (on by default): a batch's whole device-side time loop

@@ -74,6 +74,11 @@ def _box_smooth(a, w):
 
 def _gauss_smooth(a, sigma):
     """Separable Gaussian filter (truncated at 4 sigma, edges replicated)."""
+    try:  # same filter, much faster on large grids
+        from scipy.ndimage import gaussian_filter
+        return gaussian_filter(a, sigma, mode="nearest", truncate=4.0)
+    except ImportError:
+        pass
     r = int(4 * sigma + 0.5)
     x = np.arange(-r, r + 1)
     k = np.exp(-0.5 * (x / sigma) ** 2)

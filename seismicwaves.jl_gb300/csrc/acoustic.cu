@@ -1169,7 +1169,10 @@ void adjoint_group(sw_wavesim* ws, const std::vector<HostShot>& group) {
       check_vector_alignment(b);
       cudaEvent_t ev0 = nullptr;
       ws->ctx->prof.begin(st, KK_ADJOINT, stencil_bytes(ws, Sa, MODE_ADJ, 0, false, ngrp), &ev0);
-      k_ac2d_adj_grp<<<(unsigned)blocks, 128, 0, st>>>(b);
+      if (ws->variant & 8)
+        k_ac2d_adj_grp<5><<<(unsigned)blocks, 128, 0, st>>>(b);
+      else
+        k_ac2d_adj_grp<4><<<(unsigned)blocks, 128, 0, st>>>(b);
       check_cuda(cudaGetLastError(), "adjoint stencil launch");
       ws->ctx->prof.end(st, KK_ADJOINT, ev0);
     } else {

@@ -409,7 +409,8 @@ __global__ void __launch_bounds__(32 * NW, (Ac2dBounds<MODE, NW>::MINB - (DP - 1
 // keeps the result deterministic.  Warps of inactive shots (it > nt) only
 // take part in the block barriers.
 // ---------------------------------------------------------------------------
-static __global__ void __launch_bounds__(128, 4) k_ac2d_adj_grp(const StepArgs A) {
+template <int MINB>
+__global__ void __launch_bounds__(128, MINB) k_ac2d_adj_grp(const StepArgs A) {
   constexpr unsigned FULL = 0xffffffffu;
   __shared__ float4 prod[2][4][32];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -570,6 +571,29 @@ static __global__ void __launch_bounds__(128, 4) k_ac2d_adj_grp(const StepArgs A
 // points per warp); tile = 128 x 4 y x TZ z.  y neighbours come through L1.
 // psi_0/xi_0: [z][y][q];  psi_1/xi_1: [z][q][P];  psi_2/xi_2: [q][y][P].
 // ---------------------------------------------------------------------------
+// C-PML strip descriptor of axis d for one shot (built where it is needed).
+__device__ __forceinline__ StripIO strip_io(const StepArgs& A, int d, int shot, long long step) {
+  const int H = A.halo;
+  const int na = 2 * H + 2, nh = 2 * H, L = 2 * na + 2 * nh;
+  const float* cp = A.cpml + (long long)shot * A.cpml_stride + (long long)d * L;
+  StripIO s;
+  s.psi_in = fptr(A.psi_in[d], shot);
+  s.psi_out = fptr(A.psi_out[d], shot);
+  s.xi_in = fptr(A.xi_in[d], shot);
+  s.xi_out = fptr(A.xi_out[d], shot);
+  s.ck_psi = fptr(A.ck_psi[d], shot);
+  s.ck_xi = fptr(A.ck_xi[d], shot);
+  s.a = cp;
+  s.ah = cp + na;
+  s.b = cp + na + nh;
+  s.bh = cp + 2 * na + nh;
+  s.psi_step = step;
+  s.xi_step = step;
+  s.psi_base = 0;
+  s.xi_base = 0;
+  return s;
+}
+
 template <int MODE>
 __global__ void __launch_bounds__(128) k_ac3d_step(const StepArgs A) {
   constexpr unsigned FULL = 0xffffffffu;
@@ -596,22 +620,7 @@ __global__ void __launch_bounds__(128) k_ac3d_step(const StepArgs A) {
   const float* di = fptr(A.din, shot);
   float* dn = fptr(A.dout, shot);
   const float* __restrict__ fa = A.fact;
-  const float* cp = A.cpml + (long long)shot * A.cpml_stride;
-  const int na = 2 * H + 2, nh = 2 * H, L = 2 * na + 2 * nh;
-
-  StripIO s0, s1, s2;
-  StripIO* ss[3] = {&s0, &s1, &s2};
-#pragma unroll
-  for (int d = 0; d < 3; ++d) {
-    StripIO& s = *ss[d];
-    s.psi_in = fptr(A.psi_in[d], shot);  s.psi_out = fptr(A.psi_out[d], shot);
-    s.xi_in = fptr(A.xi_in[d], shot);    s.xi_out = fptr(A.xi_out[d], shot);
-    s.ck_psi = fptr(A.ck_psi[d], shot);  s.ck_xi = fptr(A.ck_xi[d], shot);
-    s.a = cp + d * L; s.ah = cp + d * L + na; s.b = cp + d * L + na + nh; s.bh = cp + d * L + 2 * na + nh;
-  }
-  s0.psi_step = 1; s0.xi_step = 1;
-  s1.psi_step = P; s1.xi_step = P;
-  s2.psi_step = (long long)ny * P; s2.xi_step = (long long)ny * P;
+  const int na = 2 * H + 2, nh = 2 * H;
 
   const bool xstrip = inb && (x0 < H || x0 + 3 >= nx - H);
   const bool ystrip = (y < H) || (y >= ny - H);
@@ -624,27 +633,40 @@ __global__ void __launch_bounds__(128) k_ac3d_step(const StepArgs A) {
   float* gg = MODE == MODE_ADJ ? fptr(A.g, shot) : nullptr;
   float* gcp = MODE == MODE_ADJ ? fptr(A.gc, shot) : nullptr;
 
+  // Software-pipelined z march: the loads of plane z+1 (p of z+2, the y
+  // neighbours, d and fact) are issued before plane z is computed.  The
+  // C-PML strip descriptors are built only where a strip is met (they would
+  // otherwise hold ~60 registers for the whole kernel).
   const long long rowoff = (long long)y * P + xa;
-  float rm[4], r0[4], rp[4];
-  ld4(rm, pc + (long long)(z_begin - 1) * plane + rowoff);
-  ld4(r0, pc + (long long)z_begin * plane + rowoff);
+  float rm[4], r0[4], rp[4], ym[4], yp[4], o[4], f[4];
+  {
+    const long long idx = (long long)z_begin * plane + rowoff;
+    ld4(rm, pc + idx - plane);
+    ld4(r0, pc + idx);
+    ld4(rp, pc + idx + plane);
+    ld4(ym, pc + idx - P);
+    ld4(yp, pc + idx + P);
+    ld4rw(o, di + idx);
+    ld4(f, fa + idx);
+  }
   for (int z = z_begin; z < z_end; ++z) {
     const long long base = (long long)z * plane;
     const long long idx = base + rowoff;
-    ld4(rp, pc + idx + plane);
-    float ym[4], yp[4];
-    ld4(ym, pc + idx - P);
-    ld4(yp, pc + idx + P);
+    const bool more = z + 1 < z_end;
+    float rpn[4], ymn[4], ypn[4], on[4], fn[4];
+    if (more) {
+      const long long nidx = idx + plane;
+      ld4(rpn, pc + nidx + plane);
+      ld4(ymn, pc + nidx - P);
+      ld4(ypn, pc + nidx + P);
+      ld4rw(on, di + nidx);
+      ld4(fn, fa + nidx);
+    }
     float left = __shfl_up_sync(FULL, r0[3], 1);
     float right = __shfl_down_sync(FULL, r0[0], 1);
     if (lane == 0) left = xa > 0 ? pc[idx - 1] : 0.f;
     if (lane == 31) right = xa + 4 < P ? pc[idx + 4] : 0.f;
-    float o[4], f[4];
-    ld4rw(o, di + idx);
-    ld4(f, fa + idx);
     const bool zstrip = (z < H) || (z >= nz - H);
-    s0.psi_base = ((long long)z * ny + y) * nh;
-    s0.xi_base = ((long long)z * ny + y) * na;
     float outp[4], outd[4], outD[4];
 #pragma unroll
     for (int e = 0; e < 4; ++e) {
@@ -656,13 +678,20 @@ __global__ void __launch_bounds__(128) k_ac3d_step(const StepArgs A) {
       float tz = (rm[e] - 2.f * c + rp[e]) * A.ih2[2];
       const int x = x0 + e;
       const bool pin = inb && x >= 1 && x <= nx - 2;
-      if (xstrip && pin) tx = cpml_axis_term(tx, xm, c, xp, x, nx, H, A.ih[0], s0);
+      if (xstrip && pin) {
+        StripIO s0 = strip_io(A, 0, shot, 1);
+        s0.psi_base = ((long long)z * ny + y) * nh;
+        s0.xi_base = ((long long)z * ny + y) * na;
+        tx = cpml_axis_term(tx, xm, c, xp, x, nx, H, A.ih[0], s0);
+      }
       if (ystrip && pin) {
+        StripIO s1 = strip_io(A, 1, shot, P);
         s1.psi_base = (long long)z * nh * P + x;
         s1.xi_base = (long long)z * na * P + x;
         ty = cpml_axis_term(ty, ym[e], c, yp[e], y, ny, H, A.ih[1], s1);
       }
       if (zstrip && pin) {
+        StripIO s2 = strip_io(A, 2, shot, (long long)ny * P);
         s2.psi_base = (long long)y * P + x;
         s2.xi_base = (long long)y * P + x;
         tz = cpml_axis_term(tz, rm[e], c, rp[e], z, nz, H, A.ih[2], s2);
@@ -711,7 +740,17 @@ __global__ void __launch_bounds__(128) k_ac3d_step(const StepArgs A) {
       }
     }
 #pragma unroll
-    for (int e = 0; e < 4; ++e) { rm[e] = r0[e]; r0[e] = rp[e]; }
+    for (int e = 0; e < 4; ++e) {
+      rm[e] = r0[e];
+      r0[e] = rp[e];
+      if (more) {
+        rp[e] = rpn[e];
+        ym[e] = ymn[e];
+        yp[e] = ypn[e];
+        o[e] = on[e];
+        f[e] = fn[e];
+      }
+    }
   }
 }
 

@@ -319,3 +319,16 @@ def test_graph_replay_is_bitwise_identical(sw, oracle):
         f = on.forward(shots)
         assert all(np.array_equal(a, b) for a, b in zip(f, f0))
     on.close()
+
+
+@pytest.mark.parametrize("variant", [0, 8])
+def test_gradient_grouped_adjoint_variants(sw, oracle, variant):
+    """The grouped 2D adjoint (4+ shots, one Kahan update per group) with 4 or
+    5 resident blocks per SM matches the oracle's shot sum."""
+    case, shot = _grad_case(sw, oracle, nt=300)
+    run = GpuRun(sw, case, gradient=True, check_freq=10, variant=variant)
+    g, msf, _ = run.gradient([shot] * 5)
+    run.close()
+    gref, mref, _ = oracle_gradient(oracle, sw, case, shot, check_freq=10)
+    assert abs(msf - 5 * mref) / abs(5 * mref) < MISFIT_TOL
+    assert rel_l2(g, 5 * gref) < GRAD_TOL
