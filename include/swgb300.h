@@ -162,6 +162,16 @@ int sw_acoustic_forward(sw_wavesim* ws, int32_t nshots, const sw_acoustic_shot* 
 int sw_acoustic_gradient(sw_wavesim* ws, int32_t nshots, const sw_acoustic_shot* shots, int32_t on_device,
                          double* grad, double* misfit);
 
+/* sw_acoustic_forward with snapshots (RunParameters.snapevery): after every
+ * time step it with it % snapevery == 0 the pressure field p[it] of each shot
+ * is copied (unpadded, column-major, prod(n) floats) into snapshots[k] +
+ * (it/snapevery - 1) * prod(n); snapshots[k] (host or device memory) holds
+ * floor(nt_k / snapevery) fields.  Replaces LinearSnapshotter + savesnapshot!
+ * in swforward_1shot! (src/utils/snapshotter.jl:1-41,
+ * src/models/acoustic/acou_forward.jl:54-57).  snapevery < nt as the reference asserts. */
+int sw_acoustic_forward_snapshots(sw_wavesim* ws, int32_t nshots, const sw_acoustic_shot* shots, int32_t on_device,
+                                  int32_t snapevery, float* const* snapshots);
+
 /* Stencil tuning knobs used by the autotuner: tz = height (in planes of the
  * marching axis) of a block's tile, 0 = built-in heuristic; variant selects
  * the 2D stencil implementation: 0, 2, 3 = register-pipelined loads with 4,
@@ -254,6 +264,16 @@ int sw_elastic_forward(sw_elastic* es, int32_t nshots, const sw_elastic_shot* sh
  * outputs are device pointers. */
 int sw_elastic_gradient(sw_elastic* es, int32_t nshots, const sw_elastic_shot* shots, int32_t on_device,
                         double* grad_rho, double* grad_lambda, double* grad_mu, double* misfit);
+/* sw_elastic_forward with snapshots (RunParameters.snapevery): after every
+ * step it with it % snapevery == 0, each shot's ucur and sigma fields are
+ * copied into snapshots[k] + (it/snapevery - 1) * B as one block of
+ * B = (nx-1)nz + nx(nz-1) + 2 nx nz + (nx-1)(nz-1) floats: ux (nx-1, nz),
+ * uz (nx, nz-1), sigma_xx, sigma_zz (nx, nz), sigma_xz (nx-1, nz-1), each
+ * column-major.  Replaces savesnapshot! in swforward_1shot!
+ * (src/models/elastic/ela_forward.jl:74-78, src/utils/snapshotter.jl:1-41). */
+int sw_elastic_forward_snapshots(sw_elastic* es, int32_t nshots, const sw_elastic_shot* shots, int32_t on_device,
+                                 int32_t snapevery, float* const* snapshots);
+
 /* Rows per thread block of the elastic stencil kernels: 8, 16 or 32 (0 =
  * default 8).  A tuning knob of this backend; no reference counterpart. */
 int sw_elastic_set_tuning(sw_elastic* es, int32_t tz);

@@ -59,6 +59,11 @@ def load():
         lib.oracle_spread_positions.restype = ctypes.c_long
         lib.oracle_bessel_i0.argtypes = [d]
         lib.oracle_bessel_i0.restype = d
+        lib.oracle_acoustic_forward_snap.argtypes = [i, P, P, d, i, P, P, i, i, P, P, i, P, P, i, i, P]
+        lib.oracle_acoustic_forward_snap.restype = i
+        lib.oracle_elastic_forward_snap.argtypes = [P, P, d, i, i, P, P, P, i, i, P, i, i, i, P, P, P, P, P, i, P,
+                                                    P, P, P, i, i, P]
+        lib.oracle_elastic_forward_snap.restype = i
         lib.oracle_interp.argtypes = [P, i, i, i, i, i, P]
         lib.oracle_interp.restype = None
         lib.oracle_back_interp.argtypes = [P, i, i, P, i, i, i, P]
@@ -304,3 +309,44 @@ def elastic_gradient(lam, mu, rho, h, dt, halo, freetop, cpml, shot, observed, *
     if rc != 0:
         raise RuntimeError(f"oracle_elastic_gradient failed ({rc})")
     return g, float(misfit[0]), traces
+
+
+def acoustic_forward_snapshots(vp, h, dt, halo, cpml, srctf, src_idx, rec_idx, snapevery, *, nthreads=0):
+    """swforward_1shot! with a LinearSnapshotter: (traces, snapshots (nsnap, *vp.shape))."""
+    vp = np.asfortranarray(vp, dtype=np.float64)
+    N, n, hh = _grid(vp, h)
+    srctf = np.asfortranarray(srctf, dtype=np.float64)
+    nt, nsrc = srctf.shape
+    src_idx = np.asfortranarray(src_idx, dtype=np.int32)
+    rec_idx = np.asfortranarray(rec_idx, dtype=np.int32)
+    nrec = rec_idx.shape[0]
+    cpml = np.ascontiguousarray(cpml, dtype=np.float64)
+    traces = np.zeros((nt, nrec), dtype=np.float64, order="F")
+    nsnap = nt // snapevery
+    snaps = np.zeros((nsnap, vp.size), dtype=np.float64)
+    rc = load().oracle_acoustic_forward_snap(N, _p(n), _p(hh), float(dt), int(halo), _p(vp), _p(cpml), nt, nsrc,
+                                             _p(src_idx), _p(srctf), nrec, _p(rec_idx), _p(traces),
+                                             int(nthreads or max_threads()), int(snapevery), _p(snaps))
+    if rc != 0:
+        raise RuntimeError(f"oracle_acoustic_forward_snap failed ({rc})")
+    return traces, np.stack([s.reshape(vp.shape, order="F") for s in snaps]) if nsnap else snaps
+
+
+def elastic_forward_snapshots(lam, mu, rho, h, dt, halo, freetop, cpml, shot, snapevery, *, interp_rho=0,
+                              interp_mu=0, nthreads=0):
+    """Elastic swforward_1shot! with snapshots: (traces, blocks (nsnap, B)) with B the
+    concatenated ux, uz, sxx, szz, sxz fields (column-major)."""
+    (lam, mu, rho, n, hh, kind, tf, nt, nsrc, mt, sc, sij, scoef, nrec, rcn, rij, rcoef,
+     cp) = _elastic_common(lam, mu, rho, h, cpml, shot)
+    nx, nz = lam.shape
+    B = (nx - 1) * nz + nx * (nz - 1) + 2 * nx * nz + (nx - 1) * (nz - 1)
+    traces = np.zeros((nt, 2, nrec), dtype=np.float64, order="F")
+    snaps = np.zeros((nt // snapevery, B), dtype=np.float64)
+    rc = load().oracle_elastic_forward_snap(_p(n), _p(hh), float(dt), int(halo), int(bool(freetop)), _p(lam),
+                                            _p(mu), _p(rho), int(interp_rho), int(interp_mu), _p(cp), nt, kind,
+                                            nsrc, _p(tf), _p(mt), _p(sc), _p(sij), _p(scoef), nrec, _p(rcn), _p(rij),
+                                            _p(rcoef), _p(traces), int(nthreads or max_threads()), int(snapevery),
+                                            _p(snaps))
+    if rc != 0:
+        raise RuntimeError(f"oracle_elastic_forward_snap failed ({rc})")
+    return traces, snaps

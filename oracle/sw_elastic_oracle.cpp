@@ -540,7 +540,7 @@ ElShot make_shot(int nt, int kind, int nsrc, const double* srctf, const double* 
 template <typename T>
 int run_forward(const int* n, const double* h, double dt, int halo, int freetop, const double* lam,
                 const double* mu, const double* rho, int irho, int imu, const double* cpml, const ElShot& sh,
-                double* traces, int nthreads) {
+                double* traces, int nthreads, int snapevery = 0, double* snaps = nullptr) {
   ElasticSim<T> sim(n[0], n[1], h, dt, halo, freetop != 0, nthreads);
   set_material(sim, lam, mu, rho, irho, imu);
   const int blk = 2 * (2 * (halo + 1)) + 2 * (2 * halo);
@@ -549,7 +549,16 @@ int run_forward(const int* n, const double* h, double dt, int halo, int freetop,
   sim.reset_fields();
   Runner<T> run(sim, sh);
   std::vector<T> tr((size_t)sh.nt * 2 * sh.nrec, T(0));
-  for (int it = 1; it <= sh.nt; ++it) run.step(it, tr.data());
+  const long sblk = (long)(n[0] - 1) * n[1] + (long)n[0] * (n[1] - 1) + 2L * n[0] * n[1] + (long)(n[0] - 1) * (n[1] - 1);
+  for (int it = 1; it <= sh.nt; ++it) {
+    run.step(it, tr.data());
+    // savesnapshot!("ucur" => ..., "σ" => ...) (ela_forward.jl:74-78): ux, uz, sxx, szz, sxz
+    if (snaps && snapevery > 0 && it % snapevery == 0) {
+      double* o = snaps + (long)(it / snapevery - 1) * sblk;
+      for (const std::vector<T>* v : {&sim.ux[sim.icur].v, &sim.uz[sim.icur].v, &sim.sxx.v, &sim.szz.v, &sim.sxz.v})
+        for (T x : *v) *o++ = (double)x;
+    }
+  }
   for (size_t q = 0; q < tr.size(); ++q) traces[q] = (double)tr[q];
   return 0;
 }
@@ -765,6 +774,19 @@ int oracle_elastic_forward(int use_f32, const int* n, const double* h, double dt
   if (use_f32)
     return run_forward<float>(n, h, dt, halo, freetop, lam, mu, rho, irho, imu, cpml, sh, traces, nthreads);
   return run_forward<double>(n, h, dt, halo, freetop, lam, mu, rho, irho, imu, cpml, sh, traces, nthreads);
+}
+
+int oracle_elastic_forward_snap(const int* n, const double* h, double dt, int halo, int freetop, const double* lam,
+                                const double* mu, const double* rho, int irho, int imu, const double* cpml, int nt,
+                                int kind, int nsrc, const double* srctf, const double* momtens, const int* src_cnt,
+                                const int* src_ij, const double* src_coef, int nrec, const int* rec_cnt,
+                                const int* rec_ij, const double* rec_coef, double* traces, int nthreads,
+                                int snapevery, double* snaps) {
+  if (n[0] < 5 || n[1] < 5 || (kind != 0 && kind != 1)) return 1;
+  ElShot sh = make_shot<double>(nt, kind, nsrc, srctf, momtens, src_cnt, src_ij, src_coef, nrec, rec_cnt,
+                                rec_ij, rec_coef);
+  return run_forward<double>(n, h, dt, halo, freetop, lam, mu, rho, irho, imu, cpml, sh, traces, nthreads,
+                             snapevery, snaps);
 }
 
 int oracle_elastic_gradient(int use_f32, const int* n, const double* h, double dt, int halo, int freetop,

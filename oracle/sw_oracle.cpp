@@ -252,7 +252,8 @@ Snap<T> snap_p(const AcousticSim<T>& s, int which) { return Snap<T>{s.buf[which]
 template <typename T>
 int run_forward(int N, const int* n, const double* h, double dt, int halo, const double* vp,
                 const double* cpml, int nt, int nsrc, const int* src_idx, const double* srctf,
-                int nrec, const int* rec_idx, double* traces, int nthreads) {
+                int nrec, const int* rec_idx, double* traces, int nthreads, int snapevery = 0,
+                double* snaps = nullptr) {
   AcousticSim<T> sim(N, n, h, halo, nthreads);
   prepare_sim(sim, vp, dt, cpml);
   std::vector<long> sl(nsrc), rl(nrec);
@@ -269,8 +270,14 @@ int run_forward(int N, const int* n, const double* h, double dt, int halo, const
   std::vector<T> tf((long)nt * nsrc), tr((long)nt * nrec, T(0));
   for (long q = 0; q < (long)nt * nsrc; ++q) tf[q] = (T)srctf[q];
   sim.reset_fields();
-  for (int it = 1; it <= nt; ++it)
+  for (int it = 1; it <= nt; ++it) {
     sim.step(it, nsrc, sl.data(), tf.data(), nt, nrec, rl.data(), tr.data(), nt);
+    // savesnapshot!("pcur" => p[it]) (acou_forward.jl:54-57, snapshotter.jl:35-41)
+    if (snaps && snapevery > 0 && it % snapevery == 0) {
+      double* o = snaps + (long)(it / snapevery - 1) * sim.npts;
+      for (long c = 0; c < sim.npts; ++c) o[c] = (double)sim.buf[sim.icur][c];
+    }
+  }
   for (long q = 0; q < (long)nt * nrec; ++q) traces[q] = (double)tr[q];
   return 0;
 }
@@ -442,6 +449,15 @@ int oracle_acoustic_forward(int use_f32, int N, const int* n, const double* h, d
   if (use_f32)
     return run_forward<float>(N, n, h, dt, halo, vp, cpml, nt, nsrc, src_idx, srctf, nrec, rec_idx, traces, nthreads);
   return run_forward<double>(N, n, h, dt, halo, vp, cpml, nt, nsrc, src_idx, srctf, nrec, rec_idx, traces, nthreads);
+}
+
+int oracle_acoustic_forward_snap(int N, const int* n, const double* h, double dt, int halo, const double* vp,
+                                 const double* cpml, int nt, int nsrc, const int* src_idx, const double* srctf,
+                                 int nrec, const int* rec_idx, double* traces, int nthreads, int snapevery,
+                                 double* snaps) {
+  if (N != 2 && N != 3) return 1;
+  return run_forward<double>(N, n, h, dt, halo, vp, cpml, nt, nsrc, src_idx, srctf, nrec, rec_idx, traces, nthreads,
+                             snapevery, snaps);
 }
 
 int oracle_acoustic_gradient(int use_f32, int N, const int* n, const double* h, double dt, int halo,

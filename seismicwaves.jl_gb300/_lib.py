@@ -26,7 +26,7 @@ EXPORTS = [
     "sw_acoustic_forward", "sw_acoustic_gradient", "sw_wavesim_set_tuning", "sw_profile_enable",
     "sw_profile_read", "sw_acoustic2d_forward_noalloc", "sw_elastic_create", "sw_elastic_destroy",
     "sw_elastic_set_material", "sw_elastic_forward", "sw_elastic_gradient", "sw_elastic_set_tuning",
-    "sw_wavesim_use_graphs",
+    "sw_wavesim_use_graphs", "sw_acoustic_forward_snapshots", "sw_elastic_forward_snapshots",
 ]
 
 i32, f64, vp_ = ctypes.c_int32, ctypes.c_double, ctypes.c_void_p
@@ -108,6 +108,8 @@ def load() -> ctypes.CDLL:
     lib.sw_elastic_gradient.argtypes = [vp_, i32, P(SwElasticShot), i32, vp_, vp_, vp_, vp_]
     lib.sw_elastic_set_tuning.argtypes = [vp_, i32]
     lib.sw_wavesim_use_graphs.argtypes = [vp_, i32]
+    lib.sw_acoustic_forward_snapshots.argtypes = [vp_, i32, P(SwAcousticShot), i32, i32, P(vp_)]
+    lib.sw_elastic_forward_snapshots.argtypes = [vp_, i32, P(SwElasticShot), i32, i32, P(vp_)]
     _lib = lib
     return lib
 

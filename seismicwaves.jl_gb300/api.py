@@ -299,7 +299,7 @@ class AcousticCDCPMLWaveSimulation:
             raise ValueError(f"No backend found for model of type AcousticCDCPMLWaveSimulation and "
                              f"`parall =` {runparams.parall}. Argument `parall` must be {_BACKEND}.")
         if runparams.snapevery is not None:
-            raise NotImplementedError("snapshots (snapevery) are not produced by the GB300 backend")
+            assert 1 <= runparams.snapevery < nt, "Checkpointing frequency must be smaller than the number of timesteps!"
         if runparams.infoevery is not None:
             assert 1 <= runparams.infoevery <= nt, "Infoevery parameter must be positive and less then nt!"
         self.params, self.cpmlparams, self.nt, self.dt = params, cpmlparams, nt, params.dt
@@ -446,11 +446,29 @@ class AcousticCDCPMLWaveSimulation:
             self.check_positions(shot.recs.positions)
 
     def run_forward(self, shots):
+        """Fills the seismograms; with RunParameters.snapevery returns, per shot, the
+        reference's snapshot Dict {it: {"pcur": p[it]}} (run_swforward!, forward.jl:90-114)."""
         self.init_shots(shots)
         structs, keep = self._shot_structs(shots)
-        self.ctx.check(self.ctx.lib.sw_acoustic_forward(self._h, len(shots), structs, 0), "sw_acoustic_forward")
+        snapevery = self.runparams.snapevery
+        if snapevery:
+            npts = int(np.prod(self.grid.size))
+            bufs = [np.zeros((k[0].shape[0] // snapevery) * npts, dtype=np.float32) for k in keep]
+            ptrs = (ctypes.c_void_p * len(bufs))(*[b.ctypes.data for b in bufs])
+            self.ctx.check(self.ctx.lib.sw_acoustic_forward_snapshots(self._h, len(shots), structs, 0, snapevery,
+                                                                      ptrs), "sw_acoustic_forward_snapshots")
+        else:
+            self.ctx.check(self.ctx.lib.sw_acoustic_forward(self._h, len(shots), structs, 0), "sw_acoustic_forward")
         for shot, (traces, _) in zip(shots, keep):
             shot.recs.seismograms[...] = traces
+        if not snapevery:
+            return None
+        out = []
+        for b in bufs:
+            snaps = b.reshape(-1, npts)
+            out.append({(q + 1) * snapevery: {"pcur": snaps[q].reshape(self.grid.size, order="F").copy()}
+                        for q in range(snaps.shape[0])})
+        return out
 
     def run_gradient(self, shots, misfits):
         assert self.gradient, "The wavesim object was not built for gradient computations. (Was `gradient=true` specified?)"
@@ -530,12 +548,12 @@ def _prepare(params_or_wavesim, matprop, runparams, gradient, gradparams=None):
 
 def swforward(params_or_wavesim, matprop: VpAcousticCDMaterialProperties, shots: Sequence[ScalarShot], *,
               runparams: RunParameters | None = None):
-    """swforward! (src/apis/forward.jl:24-66): fills shot.recs.seismograms of every shot."""
+    """swforward! (src/apis/forward.jl:24-66): fills shot.recs.seismograms of every shot; with
+    RunParameters.snapevery returns the snapshots of every shot (a list of Dicts {it: fields})."""
     ws = _prepare(params_or_wavesim, matprop, runparams, False)
     _check_sim_consistency(matprop, shots)
     ws.set_matprop(matprop)
-    ws.run_forward(list(shots))
-    return None
+    return ws.run_forward(list(shots))
 
 
 def swmisfit(params_or_wavesim, matprop: VpAcousticCDMaterialProperties, shots: Sequence[ScalarShot],

@@ -381,6 +381,9 @@ struct sw_wavesim {
   std::map<std::vector<long long>, cudaGraphExec_t> graphs;
   std::map<std::vector<long long>, int> graph_uses;  // calls per key (a key is captured on its second call)
   DevMem d_gout, d_mout;  // gradient / misfit of the host-buffer path (stable addresses for the graphs)
+  // snapshots requested by the current forward call (snapevery = 0: none)
+  int snapevery = 0;
+  float* const* snap_out = nullptr;  // per caller shot: host buffer of nt/snapevery fields
   void drop_graphs() {
     for (auto& kv : graphs) cudaGraphExecDestroy(kv.second);
     graphs.clear();
@@ -1071,6 +1074,17 @@ void forward_group(sw_wavesim* ws, const std::vector<HostShot>& group, bool grad
       L.step<MODE_FWD>(a, c, bytes);
     launch_inject(ws, Sa, a.pnew, a.dout, grad ? a.Dout : FieldArg{nullptr, 0}, d_first, it, 1);
     if (ck_slot >= 0) pack_checkpoint(ws, Sa, ck_slot);
+    if (!grad && ws->snapevery > 0 && it % ws->snapevery == 0) {
+      // savesnapshot!("pcur" => p[it]): unpadded copy into the caller's buffer of each active shot
+      const long long rows = (long long)ws->n[1] * (ws->N == 3 ? ws->n[2] : 1);
+      for (int k = 0; k < Sa; ++k) {
+        float* dst = ws->snap_out[group[k].orig] + (long long)(it / ws->snapevery - 1) * ws->npts;
+        check_cuda(cudaMemcpy2DAsync(dst, (size_t)ws->n[0] * sizeof(float), a.pnew.p + (long long)k * a.pnew.s,
+                                     (size_t)ws->P * sizeof(float), (size_t)ws->n[0] * sizeof(float), (size_t)rows,
+                                     cudaMemcpyDefault, st),
+                   "snapshot copy");
+      }
+    }
     pc = 1 - pc;
     pk = 1 - pk;
   }
@@ -1323,12 +1337,36 @@ void acoustic_forward(sw_wavesim* ws, int nshots, const sw_acoustic_shot* shots,
     ensure_state(ws, (int)group.size(), false, group.front().nt);
     Tables T;
     build_tables(ws, shots, group, on_device, false, T);
-    run_graph(ws, group_key(ws, group, false), [&] { forward_group(ws, group, false); });
+    if (ws->snapevery > 0)
+      forward_group(ws, group, false);  // host copies inside the loop: no graph
+    else
+      run_graph(ws, group_key(ws, group, false), [&] { forward_group(ws, group, false); });
     download_traces(ws, shots, group, on_device);
   }
   check_cuda(cudaStreamSynchronize(ws->ctx->stream), "forward");
   check_timeout(ws);
   ws->ctx->prof.resolve();
+}
+
+void acoustic_forward_snapshots(sw_wavesim* ws, int nshots, const sw_acoustic_shot* shots, bool on_device,
+                                int snapevery, float* const* snapshots) {
+  if (snapevery < 1 || !snapshots) fail(SW_ERR_ARG, "snapevery must be positive and snapshots non-NULL");
+  for (int k = 0; k < nshots; ++k) {
+    if (shots && snapevery >= shots[k].nt)
+      fail(SW_ERR_ARG, "Checkpointing frequency must be smaller than the number of timesteps!");
+    if (!snapshots[k]) fail(SW_ERR_ARG, "snapshot buffer is NULL");
+  }
+  ws->snapevery = snapevery;
+  ws->snap_out = snapshots;
+  try {
+    acoustic_forward(ws, nshots, shots, on_device);
+  } catch (...) {
+    ws->snapevery = 0;
+    ws->snap_out = nullptr;
+    throw;
+  }
+  ws->snapevery = 0;
+  ws->snap_out = nullptr;
 }
 
 void acoustic_gradient(sw_wavesim* ws, int nshots, const sw_acoustic_shot* shots, bool on_device, double* grad,

@@ -18,6 +18,8 @@ void acoustic_gradient(sw_wavesim* ws, int nshots, const sw_acoustic_shot* shots
                        double* misfit);
 void wavesim_set_tuning(sw_wavesim* ws, int tz, int variant);
 void wavesim_use_graphs(sw_wavesim* ws, bool on);
+void acoustic_forward_snapshots(sw_wavesim* ws, int nshots, const sw_acoustic_shot* shots, bool on_device,
+                                int snapevery, float* const* snapshots);
 sw_ctx* wavesim_ctx(sw_wavesim* ws);
 sw_wavesim* wavesim_new();
 void wavesim_delete(sw_wavesim* ws);
@@ -27,6 +29,8 @@ void elastic_forward(sw_elastic* es, int nshots, const sw_elastic_shot* shots, b
 void elastic_gradient(sw_elastic* es, int nshots, const sw_elastic_shot* shots, bool on_device, double* g_rho,
                       double* g_lam, double* g_mu, double* misfit);
 void elastic_set_tuning(sw_elastic* es, int tz);
+void elastic_forward_snapshots(sw_elastic* es, int nshots, const sw_elastic_shot* shots, bool on_device,
+                               int snapevery, float* const* snapshots);
 sw_ctx* elastic_ctx(sw_elastic* es);
 sw_elastic* elastic_new();
 void elastic_delete(sw_elastic* es);
@@ -353,6 +357,26 @@ int sw_wavesim_use_graphs(sw_wavesim* ws, int32_t on) {
   if (!ws) return SW_ERR_ARG;
   sw_ctx* ctx = swgb::wavesim_ctx(ws);
   return guarded(ctx, [&] { swgb::wavesim_use_graphs(ws, on != 0); });
+}
+
+int sw_acoustic_forward_snapshots(sw_wavesim* ws, int32_t nshots, const sw_acoustic_shot* shots, int32_t on_device,
+                                  int32_t snapevery, float* const* snapshots) {
+  if (!ws) return SW_ERR_ARG;
+  sw_ctx* ctx = swgb::wavesim_ctx(ws);
+  return guarded(ctx, [&] {
+    swgb::check_cuda(cudaSetDevice(ctx->device), "cudaSetDevice");
+    swgb::acoustic_forward_snapshots(ws, nshots, shots, on_device != 0, snapevery, snapshots);
+  });
+}
+
+int sw_elastic_forward_snapshots(sw_elastic* es, int32_t nshots, const sw_elastic_shot* shots, int32_t on_device,
+                                 int32_t snapevery, float* const* snapshots) {
+  if (!es) return SW_ERR_ARG;
+  sw_ctx* ctx = swgb::elastic_ctx(es);
+  return guarded(ctx, [&] {
+    swgb::check_cuda(cudaSetDevice(ctx->device), "cudaSetDevice");
+    swgb::elastic_forward_snapshots(es, nshots, shots, on_device != 0, snapevery, snapshots);
+  });
 }
 
 }  // extern "C"

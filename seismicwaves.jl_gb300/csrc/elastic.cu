@@ -732,6 +732,8 @@ struct sw_elastic {
   // tables
   DevMem d_desc, d_ll, d_int, d_flt, d_tf, d_tr, d_obs, d_ic, d_mask, d_adj, d_mt, d_cp;
   DevMem d_partial, d_amax, d_balls, d_ball_ptr, d_cs;
+  int snapevery = 0;                 // snapshots requested by the current forward call
+  float* const* snap_out = nullptr;  // per caller shot: nt/snapevery blocks [ux, uz, sxx, szz, sxz]
   int tz = 8;  // rows per block of the stencil kernels (8, 16 or 32; 8 measured fastest)
 };
 
@@ -1211,6 +1213,30 @@ void adjoint_step(Run& R, int S, int it, float sa) {
   R.inject_force(S, it, true, sa, nullptr);
 }
 
+// savesnapshot!("ucur" => ..., "σ" => ...) of ela_forward.jl:74-78 for the active shots:
+// one block per snapshot, [ux (nx-1, nz), uz (nx, nz-1), sxx, szz (nx, nz), sxz (nx-1, nz-1)].
+long long snapshot_floats(const sw_elastic* es) {
+  const long long nx = es->g.nx, nz = es->g.nz;
+  return (nx - 1) * nz + nx * (nz - 1) + 2 * nx * nz + (nx - 1) * (nz - 1);
+}
+
+void save_snapshots(sw_elastic* es, const std::vector<HostShot>& group, int A, int it) {
+  const Geo& g = es->g;
+  const int w[5] = {g.nx - 1, g.nx, g.nx, g.nx, g.nx - 1};
+  const int h[5] = {g.nz, g.nz - 1, g.nz, g.nz, g.nz - 1};
+  const int field[5] = {0, 1, 4, 5, 6};
+  for (int k = 0; k < A; ++k) {
+    float* dst = es->snap_out[group[k].orig] + (long long)(it / es->snapevery - 1) * snapshot_floats(es);
+    for (int q = 0; q < 5; ++q) {
+      const float* src = es->st[field[q]].as<float>() + (long long)k * g.F + g.lin(1, 1);
+      check_cuda(cudaMemcpy2DAsync(dst, (size_t)w[q] * sizeof(float), src, (size_t)g.P * sizeof(float),
+                                   (size_t)w[q] * sizeof(float), (size_t)h[q], cudaMemcpyDefault, es->ctx->stream),
+                 "snapshot copy");
+      dst += (long long)w[q] * h[q];
+    }
+  }
+}
+
 std::vector<HostShot> sorted_order(int nshots, const sw_elastic_shot* shots) {
   std::vector<HostShot> order(nshots);
   for (int k = 0; k < nshots; ++k) order[k] = HostShot{k, shots[k].nt};
@@ -1395,11 +1421,36 @@ void elastic_forward(sw_elastic* es, int nshots, const sw_elastic_shot* shots, b
     const float sf_ref = set_forward_scales(es, shots, group, desc);
     Run R{es, es->ctx->stream, es->d_desc.as<ShotDesc>(), sf_ref};
     zero_state(es, S, false);
-    for (int it = 1; it <= group.front().nt; ++it) full_step(R, active_count(group, it), it, true, KK_STENCIL, nullptr, nullptr);
+    for (int it = 1; it <= group.front().nt; ++it) {
+      const int A = active_count(group, it);
+      full_step(R, A, it, true, KK_STENCIL, nullptr, nullptr);
+      if (es->snapevery > 0 && it % es->snapevery == 0) save_snapshots(es, group, A, it);
+    }
     download_traces(es, shots, group, desc, on_device);
   }
   check_cuda(cudaStreamSynchronize(es->ctx->stream), "elastic forward");
   es->ctx->prof.resolve();
+}
+
+void elastic_forward_snapshots(sw_elastic* es, int nshots, const sw_elastic_shot* shots, bool on_device,
+                               int snapevery, float* const* snapshots) {
+  if (snapevery < 1 || !snapshots) fail(SW_ERR_ARG, "snapevery must be positive and snapshots non-NULL");
+  for (int k = 0; k < nshots; ++k) {
+    if (shots && snapevery >= shots[k].nt)
+      fail(SW_ERR_ARG, "Checkpointing frequency must be smaller than the number of timesteps!");
+    if (!snapshots[k]) fail(SW_ERR_ARG, "snapshot buffer is NULL");
+  }
+  es->snapevery = snapevery;
+  es->snap_out = snapshots;
+  try {
+    elastic_forward(es, nshots, shots, on_device);
+  } catch (...) {
+    es->snapevery = 0;
+    es->snap_out = nullptr;
+    throw;
+  }
+  es->snapevery = 0;
+  es->snap_out = nullptr;
 }
 
 void elastic_gradient(sw_elastic* es, int nshots, const sw_elastic_shot* shots, bool on_device, double* g_rho,

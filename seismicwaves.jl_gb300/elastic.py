@@ -232,7 +232,8 @@ class ElasticIsoCPMLWaveSimulation:
             raise ValueError(f"No backend found for model of type ElasticIsoCPMLWaveSimulation and "
                              f"`parall =` {runparams.parall}. Argument `parall` must be {_BACKEND}.")
         if runparams.snapevery is not None:
-            raise NotImplementedError("snapshots (snapevery) are not produced by the GB300 backend")
+            assert 1 <= runparams.snapevery < params.ntimesteps, \
+                "Checkpointing frequency must be smaller than the number of timesteps!"
         self.params, self.cpmlparams, self.nt, self.dt = params, cpmlparams, nt, params.dt
         self.grid = UniformFiniteDifferenceGrid(params.gridsize, params.gridspacing)
         self.runparams, self.gradient, self.sincinterp = runparams, gradient, sincinterp
@@ -409,11 +410,36 @@ class ElasticIsoCPMLWaveSimulation:
             self.check_positions(shot.recs.positions)
 
     def run_forward(self, shots):
+        """Fills the seismograms; with RunParameters.snapevery returns, per shot,
+        {it: {"ucur": [ux, uz], "σ": [σxx, σzz, σxz]}} (ela_forward.jl:74-78)."""
         self.init_shots(shots)
         structs, keep = self._shot_structs(shots)
-        self.ctx.check(self.ctx.lib.sw_elastic_forward(self._h, len(shots), structs, 0), "sw_elastic_forward")
+        snapevery = self.runparams.snapevery
+        nx, nz = self.grid.size
+        shapes = [(nx - 1, nz), (nx, nz - 1), (nx, nz), (nx, nz), (nx - 1, nz - 1)]
+        B = sum(a * b for a, b in shapes)
+        if snapevery:
+            bufs = [np.zeros((k[0].shape[0] // snapevery) * B, dtype=np.float32) for k in keep]
+            ptrs = (ctypes.c_void_p * len(bufs))(*[b.ctypes.data for b in bufs])
+            self.ctx.check(self.ctx.lib.sw_elastic_forward_snapshots(self._h, len(shots), structs, 0, snapevery,
+                                                                     ptrs), "sw_elastic_forward_snapshots")
+        else:
+            self.ctx.check(self.ctx.lib.sw_elastic_forward(self._h, len(shots), structs, 0), "sw_elastic_forward")
         for shot, (traces, _) in zip(shots, keep):
             shot.recs.seismograms[...] = traces
+        if not snapevery:
+            return None
+        out = []
+        for b in bufs:
+            d = {}
+            for q, blk in enumerate(b.reshape(-1, B)):
+                parts, o = [], 0
+                for a_, b_ in shapes:
+                    parts.append(blk[o:o + a_ * b_].reshape((a_, b_), order="F").copy())
+                    o += a_ * b_
+                d[(q + 1) * snapevery] = {"ucur": parts[:2], "σ": parts[2:]}
+            out.append(d)
+        return out
 
     def run_gradient(self, shots, misfits):
         assert self.gradient, "The wavesim object was not built for gradient computations. (Was `gradient=true` specified?)"
