@@ -603,6 +603,31 @@ __global__ void __launch_bounds__(BX) k_el_corr(const CorrArgs A) {
   }
 }
 
+// One snapshot block per shot (blockIdx.y): ux, uz, sxx, szz, sxz unpadded and
+// scaled back from the shot's source scale, into stage + shot * B.
+__global__ void k_el_snapshot(Geo g, const ShotDesc* __restrict__ desc, const float* __restrict__ ux,
+                              const float* __restrict__ uz, const float* __restrict__ sxx,
+                              const float* __restrict__ szz, const float* __restrict__ sxz, long long B,
+                              float* __restrict__ stage) {
+  const int s = blockIdx.y;
+  const float inv = 1.0f / desc[s].sf;
+  const long long so = (long long)s * g.F;
+  const long long n0 = (long long)(g.nx - 1) * g.nz, n1 = (long long)g.nx * (g.nz - 1);
+  const long long n2 = (long long)g.nx * g.nz, n4 = (long long)(g.nx - 1) * (g.nz - 1);
+  for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < B; q += (long long)gridDim.x * blockDim.x) {
+    const float* f;
+    long long r = q;
+    int w;
+    if (r < n0) { f = ux; w = g.nx - 1; }
+    else if ((r -= n0) < n1) { f = uz; w = g.nx; }
+    else if ((r -= n1) < n2) { f = sxx; w = g.nx; }
+    else if ((r -= n2) < n2) { f = szz; w = g.nx; }
+    else { r -= n2; f = sxz; w = g.nx - 1; (void)n4; }
+    const int i = (int)(r % w) + 1, j = (int)(r / w) + 1;
+    stage[(long long)s * B + q] = f[so + g.lin(i, j)] * inv;
+  }
+}
+
 // Mute ball of one position (mutearoundpoint!, src/utils/mute_grad.jl:13-80).
 struct MuteBall {
   int lo[2], hi[2];
@@ -732,6 +757,7 @@ struct sw_elastic {
   // tables
   DevMem d_desc, d_ll, d_int, d_flt, d_tf, d_tr, d_obs, d_ic, d_mask, d_adj, d_mt, d_cp;
   DevMem d_partial, d_amax, d_balls, d_ball_ptr, d_cs;
+  DevMem d_snap;                     // snapshot stage (one block per shot)
   int snapevery = 0;                 // snapshots requested by the current forward call
   float* const* snap_out = nullptr;  // per caller shot: nt/snapevery blocks [ux, uz, sxx, szz, sxz]
   int tz = 8;  // rows per block of the stencil kernels (8, 16 or 32; 8 measured fastest)
@@ -1221,19 +1247,19 @@ long long snapshot_floats(const sw_elastic* es) {
 }
 
 void save_snapshots(sw_elastic* es, const std::vector<HostShot>& group, int A, int it) {
-  const Geo& g = es->g;
-  const int w[5] = {g.nx - 1, g.nx, g.nx, g.nx, g.nx - 1};
-  const int h[5] = {g.nz, g.nz - 1, g.nz, g.nz, g.nz - 1};
-  const int field[5] = {0, 1, 4, 5, 6};
+  const long long B = snapshot_floats(es);
+  cudaStream_t st = es->ctx->stream;
+  ensure(es, es->d_snap, (size_t)es->cap * B * sizeof(float), "snapshot stage");
+  const dim3 grid((unsigned)std::min<long long>((B + 255) / 256, 1024), A);
+  k_el_snapshot<<<grid, 256, 0, st>>>(es->g, es->d_desc.as<ShotDesc>(), es->st[0].as<float>(), es->st[1].as<float>(),
+                                      es->st[4].as<float>(), es->st[5].as<float>(), es->st[6].as<float>(), B,
+                                      es->d_snap.as<float>());
+  check_cuda(cudaGetLastError(), "snapshot launch");
   for (int k = 0; k < A; ++k) {
-    float* dst = es->snap_out[group[k].orig] + (long long)(it / es->snapevery - 1) * snapshot_floats(es);
-    for (int q = 0; q < 5; ++q) {
-      const float* src = es->st[field[q]].as<float>() + (long long)k * g.F + g.lin(1, 1);
-      check_cuda(cudaMemcpy2DAsync(dst, (size_t)w[q] * sizeof(float), src, (size_t)g.P * sizeof(float),
-                                   (size_t)w[q] * sizeof(float), (size_t)h[q], cudaMemcpyDefault, es->ctx->stream),
-                 "snapshot copy");
-      dst += (long long)w[q] * h[q];
-    }
+    float* dst = es->snap_out[group[k].orig] + (long long)(it / es->snapevery - 1) * B;
+    check_cuda(cudaMemcpyAsync(dst, es->d_snap.as<float>() + (long long)k * B, (size_t)B * sizeof(float),
+                               cudaMemcpyDefault, st),
+               "snapshot copy");
   }
 }
 
