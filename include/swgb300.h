@@ -275,7 +275,9 @@ int sw_elastic_forward_snapshots(sw_elastic* es, int32_t nshots, const sw_elasti
                                  int32_t snapevery, float* const* snapshots);
 
 /* Rows per thread block of the elastic stencil kernels: 8, 16 or 32 (0 =
- * default 8).  A tuning knob of this backend; no reference counterpart. */
+ * default 8); + 64 selects the one-point-per-thread kernels instead of the
+ * four-points-per-thread ones.  A tuning knob of this backend; no reference
+ * counterpart. */
 int sw_elastic_set_tuning(sw_elastic* es, int32_t tz);
 
 /* 2D forward of one shot that allocates no device memory.  Has no

@@ -325,6 +325,328 @@ __global__ void __launch_bounds__(BX) k_el_disp(const Args A) {
 }
 
 // ---------------------------------------------------------------------------
+// Vector forms of the two update kernels: four consecutive x points per thread
+// (one float4 per row and field), a warp covers 128 points and a block of four
+// warps 512.  Same arithmetic per point as k_el_stress / k_el_disp; the z
+// neighbours are float4 windows in registers, the x neighbours the adjacent
+// lanes' elements (loaded at the warp edges).  Points outside a node range
+// are computed but not stored.
+// ---------------------------------------------------------------------------
+struct F4 {
+  float v[4];
+};
+__device__ __forceinline__ F4 ld4z(const float* __restrict__ p, long long c, bool ok) {
+  F4 r;
+  if (ok) {
+    const float4 t = __ldg(reinterpret_cast<const float4*>(p + c));
+    r.v[0] = t.x; r.v[1] = t.y; r.v[2] = t.z; r.v[3] = t.w;
+  } else {
+    r.v[0] = r.v[1] = r.v[2] = r.v[3] = 0.0f;
+  }
+  return r;
+}
+__device__ __forceinline__ F4 ld4rwz(const float* p, long long c) {
+  const float4 t = *reinterpret_cast<const float4*>(p + c);
+  F4 r;
+  r.v[0] = t.x; r.v[1] = t.y; r.v[2] = t.z; r.v[3] = t.w;
+  return r;
+}
+__device__ __forceinline__ void st4v(float* p, long long c, const float (&v)[4]) {
+  *reinterpret_cast<float4*>(p + c) = make_float4(v[0], v[1], v[2], v[3]);
+}
+
+template <int TZ>
+__global__ void __launch_bounds__(BX) k_el_stress4(const Args A) {
+  const Geo g = A.g;
+  const int s = blockIdx.z;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int wx0 = (blockIdx.x * 4 + warp) * 128;
+  const int j0 = blockIdx.y * TZ + 1;
+  const int j1 = min(j0 + TZ - 1, g.nz - 1);
+  if (j0 > j1 || wx0 >= g.nx) return;  // block / warp uniform
+  const int i0 = wx0 + lane * 4 + 1;
+  const bool ldok = i0 <= g.nx + 2;
+  const long long so = (long long)s * g.F;
+  const float* __restrict__ ux = A.ux + so;
+  const float* __restrict__ uz = A.uz + so;
+  float* __restrict__ sxx = A.sxx + so;
+  float* __restrict__ szz = A.szz + so;
+  float* __restrict__ sxz = A.sxz + so;
+  const int na = 2 * g.halo + 2, nh = 2 * g.halo;
+  const float* cx = A.cp + (long long)s * A.cps;
+  const float* cz = cx + 2 * na + 2 * nh;
+  const int jlo = g.ft ? 1 : 2;
+  const int P = g.P;
+  // x strips touch this thread's points only near the left and right edges
+  const bool xstrip = i0 <= g.halo + 1 || i0 + 3 >= g.nx - 1 - g.halo;
+  const bool xx_all = i0 >= 2 && i0 + 3 <= g.nx - 1;  // all four points are sigma_xx nodes
+  const bool xz_all = i0 + 3 <= g.nx - 1;             // all four points are sigma_xz nodes
+  long long c = g.lin(i0, j0);
+  F4 xu0 = ld4z(ux, c - P, ldok), xu1 = ld4z(ux, c, ldok), xu2 = ld4z(ux, c + P, ldok), xu3 = ld4z(ux, c + 2 * P, ldok);
+  F4 zu0 = ld4z(uz, c - 2 * P, ldok), zu1 = ld4z(uz, c - P, ldok), zu2 = ld4z(uz, c, ldok), zu3 = ld4z(uz, c + P, ldok);
+  for (int j = j0; j <= j1; ++j, c += P) {
+    const bool more = j + 1 <= j1;
+    F4 xun = ld4z(ux, c + 3 * P, ldok && more);
+    F4 zun = ld4z(uz, c + 2 * P, ldok && more);
+    // ux at i0-2 .. i0+4, uz at i0-1 .. i0+5 (row j)
+    float ua[7], za[7];
+    ua[0] = __shfl_up_sync(FULL, xu1.v[2], 1);
+    ua[1] = __shfl_up_sync(FULL, xu1.v[3], 1);
+    ua[6] = __shfl_down_sync(FULL, xu1.v[0], 1);
+    za[0] = __shfl_up_sync(FULL, zu2.v[3], 1);
+    za[5] = __shfl_down_sync(FULL, zu2.v[0], 1);
+    za[6] = __shfl_down_sync(FULL, zu2.v[1], 1);
+    if (lane == 0) {
+      ua[0] = ldz(ux, c - 2, ldok);
+      ua[1] = ldz(ux, c - 1, ldok);
+      za[0] = ldz(uz, c - 1, ldok);
+    }
+    if (lane == 31) {
+      ua[6] = ldz(ux, c + 4, ldok);
+      za[5] = ldz(uz, c + 4, ldok);
+      za[6] = ldz(uz, c + 5, ldok);
+    }
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+      ua[2 + e] = xu1.v[e];
+      za[1 + e] = zu2.v[e];
+    }
+    const F4 L4 = ld4z(A.lam, c, ldok), M4 = ld4z(A.mu, c, ldok), MIJ = ld4z(A.mu_ij, c, ldok);
+    int colF = 0, colH = 0;
+    const int kF = cpml_full(j, g.nz, g.halo, colF);  // duz/dz at sigma_xx nodes (uz has nz-1 points)
+    const int kH = cpml_half(j, g.nz, g.halo, colH);  // dux/dz at sigma_xz nodes (ux has nz points)
+    float oxx[4], ozz[4], oxz[4];
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+      const int i = i0 + e;
+      const float l = L4.v[e], m = M4.v[e];
+      const float l2m = l + 2.0f * m;
+      // sigma_xx, sigma_zz
+      const float dux = d4(ua[e], ua[e + 1], ua[e + 2], ua[e + 3], g.idx);
+      float duz;
+      if (g.ft && j == 1) duz = (-l / l2m) * dux;
+      else if (g.ft && j == 2) duz = d4(zu1.v[e], zu1.v[e], zu2.v[e], zu3.v[e], g.idz);
+      else duz = d4(zu0.v[e], zu1.v[e], zu2.v[e], zu3.v[e], g.idz);
+      const bool xx = i >= 2 && i <= g.nx - 1 && j >= jlo;
+      float duxc = dux, duzc = duz;
+      if (xstrip && xx) {
+        int colE = 0;
+        const int kE = cpml_full(i, g.nx, g.halo, colE);
+        if (kE) duxc = cpml_upd(A.px[2] + (long long)s * A.xs + (long long)(j - 1) * g.W + colE, cx[kE - 1],
+                                cx[na + nh + kE - 1], dux);
+      }
+      if (kF && xx)
+        duzc = cpml_upd(A.pz[3] + (long long)s * A.zs + (long long)colF * P + (i - 1), cz[kF - 1],
+                        cz[na + nh + kF - 1], duz);
+      oxx[e] = l2m * duxc + l * duzc;
+      ozz[e] = (j == 1) ? 0.0f : l * duxc + l2m * duzc;
+      // sigma_xz
+      const float dzx = d4(za[e], za[e + 1], za[e + 2], za[e + 3], g.idx);
+      const float dxz = (g.ft && j == 1) ? d4(xu2.v[e], xu1.v[e], xu2.v[e], xu3.v[e], g.idz)
+                                         : d4(xu0.v[e], xu1.v[e], xu2.v[e], xu3.v[e], g.idz);
+      const bool xz = i <= g.nx - 1;
+      float dzxc = dzx, dxzc = dxz;
+      if (xstrip && xz) {
+        int colG = 0;
+        const int kG = cpml_half(i, g.nx, g.halo, colG);
+        if (kG) dzxc = cpml_upd(A.px[3] + (long long)s * A.xs + (long long)(j - 1) * g.W + colG, cx[na + kG - 1],
+                                cx[2 * na + nh + kG - 1], dzx);
+      }
+      if (kH && xz)
+        dxzc = cpml_upd(A.pz[2] + (long long)s * A.zs + (long long)colH * P + (i - 1), cz[na + kH - 1],
+                        cz[2 * na + nh + kH - 1], dxz);
+      oxz[e] = MIJ.v[e] * (dzxc + dxzc);
+    }
+    if (ldok) {
+      if (xx_all && j >= jlo) {
+        st4v(sxx, c, oxx);
+        st4v(szz, c, ozz);
+      } else {
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+          const int i = i0 + e;
+          if (i >= 2 && i <= g.nx - 1 && j >= jlo) {
+            sxx[c + e] = oxx[e];
+            szz[c + e] = ozz[e];
+          }
+        }
+      }
+      if (xz_all) {
+        st4v(sxz, c, oxz);
+      } else {
+#pragma unroll
+        for (int e = 0; e < 4; ++e)
+          if (i0 + e <= g.nx - 1) sxz[c + e] = oxz[e];
+      }
+    }
+    xu0 = xu1; xu1 = xu2; xu2 = xu3; xu3 = xun;
+    zu0 = zu1; zu1 = zu2; zu2 = zu3; zu3 = zun;
+  }
+}
+
+template <int TZ>
+__global__ void __launch_bounds__(BX) k_el_disp4(const Args A) {
+  const Geo g = A.g;
+  const int s = blockIdx.z;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int wx0 = (blockIdx.x * 4 + warp) * 128;
+  const int j0 = blockIdx.y * TZ + 1;
+  const int j1 = min(j0 + TZ - 1, g.nz);
+  if (j0 > j1 || wx0 >= g.nx) return;
+  const int i0 = wx0 + lane * 4 + 1;
+  const bool ldok = i0 <= g.nx + 2;
+  const long long so = (long long)s * g.F;
+  float* __restrict__ ux = A.ux + so;
+  float* __restrict__ uz = A.uz + so;
+  float* __restrict__ dux = A.dux + so;
+  float* __restrict__ duz = A.duz + so;
+  const float* __restrict__ sxx = A.sxx + so;
+  const float* __restrict__ szz = A.szz + so;
+  const float* __restrict__ sxz = A.sxz + so;
+  const int na = 2 * g.halo + 2, nh = 2 * g.halo;
+  const float* cx = A.cp + (long long)s * A.cps;
+  const float* cz = cx + 2 * na + 2 * nh;
+  const bool slots = A.sUx != nullptr;
+  const int P = g.P;
+  const bool xstrip = i0 <= g.halo + 1 || i0 + 3 >= g.nx - 1 - g.halo;
+  const bool ux_all = i0 + 3 <= g.nx - 1;  // all four points are ux nodes
+  const bool uz_all = i0 + 3 <= g.nx;      // all four points are uz nodes
+  long long c = g.lin(i0, j0);
+  F4 q0 = ld4z(sxz, c - 2 * P, ldok), q1 = ld4z(sxz, c - P, ldok), q2 = ld4z(sxz, c, ldok), q3 = ld4z(sxz, c + P, ldok);
+  F4 w0 = ld4z(szz, c - P, ldok), w1 = ld4z(szz, c, ldok), w2 = ld4z(szz, c + P, ldok), w3 = ld4z(szz, c + 2 * P, ldok);
+  F4 xc = ld4z(sxx, c, ldok);
+  for (int j = j0; j <= j1; ++j, c += P) {
+    const bool more = j + 1 <= j1;
+    F4 qn = ld4z(sxz, c + 2 * P, ldok && more);
+    F4 wn = ld4z(szz, c + 3 * P, ldok && more);
+    F4 xcn = ld4z(sxx, c + P, ldok && more);
+    // sigma_xx at i0-1 .. i0+5, sigma_xz at i0-2 .. i0+4 (row j)
+    float xa[7], qa[7];
+    xa[0] = __shfl_up_sync(FULL, xc.v[3], 1);
+    xa[5] = __shfl_down_sync(FULL, xc.v[0], 1);
+    xa[6] = __shfl_down_sync(FULL, xc.v[1], 1);
+    qa[0] = __shfl_up_sync(FULL, q2.v[2], 1);
+    qa[1] = __shfl_up_sync(FULL, q2.v[3], 1);
+    qa[6] = __shfl_down_sync(FULL, q2.v[0], 1);
+    if (lane == 0) {
+      xa[0] = ldz(sxx, c - 1, ldok);
+      qa[0] = ldz(sxz, c - 2, ldok);
+      qa[1] = ldz(sxz, c - 1, ldok);
+    }
+    if (lane == 31) {
+      xa[5] = ldz(sxx, c + 4, ldok);
+      xa[6] = ldz(sxx, c + 5, ldok);
+      qa[6] = ldz(sxz, c + 4, ldok);
+    }
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+      xa[1 + e] = xc.v[e];
+      qa[2 + e] = q2.v[e];
+    }
+    int colB = 0, colD = 0;
+    const int kB = cpml_full(j, g.nz, g.halo, colB);  // dsxz/dz at ux nodes (sigma_xz has nz-1 points)
+    const int kD = cpml_half(j, g.nz, g.halo, colD);  // dszz/dz at uz nodes (sigma_zz has nz points)
+    if (ldok) {
+      // ux nodes
+      const F4 R = ld4z(A.dtr_i, c, true);
+      F4 U = ld4rwz(ux, c), DU = ld4rwz(dux, c);
+      float nu[4], ndu[4], Dv[4];
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        const int i = i0 + e;
+        const float d1 = d4(xa[e], xa[e + 1], xa[e + 2], xa[e + 3], g.idx);
+        float d2;
+        if (g.ft && j == 1) d2 = d4(-q3.v[e], -q2.v[e], q2.v[e], q3.v[e], g.idz);
+        else if (g.ft && j == 2) d2 = d4(-q1.v[e], q1.v[e], q2.v[e], q3.v[e], g.idz);
+        else d2 = d4(q0.v[e], q1.v[e], q2.v[e], q3.v[e], g.idz);
+        const bool on = i <= g.nx - 1;
+        float d1c = d1, d2c = d2;
+        if (xstrip && on) {
+          int colA = 0;
+          const int kA = cpml_half(i, g.nx, g.halo, colA);
+          if (kA) d1c = cpml_upd(A.px[0] + (long long)s * A.xs + (long long)(j - 1) * g.W + colA, cx[na + kA - 1],
+                                 cx[2 * na + nh + kA - 1], d1);
+        }
+        if (kB && on)
+          d2c = cpml_upd(A.pz[1] + (long long)s * A.zs + (long long)colB * P + (i - 1), cz[kB - 1],
+                         cz[na + nh + kB - 1], d2);
+        Dv[e] = R.v[e] * (d1c + d2c);
+        ndu[e] = DU.v[e] + Dv[e];
+        nu[e] = U.v[e] + ndu[e];
+      }
+      if (ux_all) {
+        if (slots) {
+          st4v(A.sUx + so, c, U.v);
+          st4v(A.sDx + so, c, Dv);
+        }
+        st4v(ux, c, nu);
+        st4v(dux, c, ndu);
+      } else {
+#pragma unroll
+        for (int e = 0; e < 4; ++e)
+          if (i0 + e <= g.nx - 1) {
+            if (slots) {
+              A.sUx[so + c + e] = U.v[e];
+              A.sDx[so + c + e] = Dv[e];
+            }
+            ux[c + e] = nu[e];
+            dux[c + e] = ndu[e];
+          }
+      }
+      // uz nodes
+      if (j <= g.nz - 1) {
+        const F4 Rj = ld4z(A.dtr_j, c, true);
+        F4 V = ld4rwz(uz, c), DV = ld4rwz(duz, c);
+        float nv[4], ndv[4], Dz[4];
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+          const int i = i0 + e;
+          const float d1 = d4(qa[e], qa[e + 1], qa[e + 2], qa[e + 3], g.idx);
+          const float d2 = (g.ft && j == 1) ? d4(-w2.v[e], w1.v[e], w2.v[e], w3.v[e], g.idz)
+                                            : d4(w0.v[e], w1.v[e], w2.v[e], w3.v[e], g.idz);
+          const bool on = i <= g.nx;
+          float d1c = d1, d2c = d2;
+          if (xstrip && on) {
+            int colC = 0;
+            const int kC = cpml_full(i, g.nx, g.halo, colC);
+            if (kC) d1c = cpml_upd(A.px[1] + (long long)s * A.xs + (long long)(j - 1) * g.W + colC, cx[kC - 1],
+                                   cx[na + nh + kC - 1], d1);
+          }
+          if (kD && on)
+            d2c = cpml_upd(A.pz[0] + (long long)s * A.zs + (long long)colD * P + (i - 1), cz[na + kD - 1],
+                           cz[2 * na + nh + kD - 1], d2);
+          Dz[e] = Rj.v[e] * (d1c + d2c);
+          ndv[e] = DV.v[e] + Dz[e];
+          nv[e] = V.v[e] + ndv[e];
+        }
+        if (uz_all) {
+          if (slots) {
+            st4v(A.sUz + so, c, V.v);
+            st4v(A.sDz + so, c, Dz);
+          }
+          st4v(uz, c, nv);
+          st4v(duz, c, ndv);
+        } else {
+#pragma unroll
+          for (int e = 0; e < 4; ++e)
+            if (i0 + e <= g.nx) {
+              if (slots) {
+                A.sUz[so + c + e] = V.v[e];
+                A.sDz[so + c + e] = Dz[e];
+              }
+              uz[c + e] = nv[e];
+              duz[c + e] = ndv[e];
+            }
+        }
+      }
+    }
+    q0 = q1; q1 = q2; q2 = q3; q3 = qn;
+    w0 = w1; w1 = w2; w2 = w3; w3 = wn;
+    xc = xcn;
+  }
+}
+
+// ---------------------------------------------------------------------------
 // Sources, receivers, misfit
 // ---------------------------------------------------------------------------
 // Unique-point CSR of one injection table: point p (padded index lin[p]) gets
@@ -761,6 +1083,7 @@ struct sw_elastic {
   int snapevery = 0;                 // snapshots requested by the current forward call
   float* const* snap_out = nullptr;  // per caller shot: nt/snapevery blocks [ux, uz, sxx, szz, sxz]
   int tz = 8;  // rows per block of the stencil kernels (8, 16 or 32; 8 measured fastest)
+  bool vec = true;  // four x points per thread (k_el_*4) instead of one
 };
 
 namespace {
@@ -1125,6 +1448,7 @@ struct Run {
   cudaStream_t st;
   const ShotDesc* ddesc;
   float sf_ref = 1.0f;  // the largest source scale of the group (the gradient's common scale)
+  bool any_mt = true, any_force = true;  // source kinds present in the group (skip empty launches)
 
   Args args(bool adjoint) const {
     Args a{};
@@ -1197,9 +1521,15 @@ void zero_state(sw_elastic* es, int S, bool adjoint) {
 
 template <int TZ>
 void launch_stencil_tz(const sw_elastic* es, cudaStream_t st, const Args& a, int S, bool stress) {
-  const dim3 grid((es->g.nx + BX - 1) / BX, (es->g.nz + TZ - 1) / TZ, S);
-  if (stress) k_el_stress<TZ><<<grid, BX, 0, st>>>(a);
-  else k_el_disp<TZ><<<grid, BX, 0, st>>>(a);
+  if (es->vec) {  // four points per thread: 512 per block
+    const dim3 grid((es->g.nx + 511) / 512, (es->g.nz + TZ - 1) / TZ, S);
+    if (stress) k_el_stress4<TZ><<<grid, BX, 0, st>>>(a);
+    else k_el_disp4<TZ><<<grid, BX, 0, st>>>(a);
+  } else {
+    const dim3 grid((es->g.nx + BX - 1) / BX, (es->g.nz + TZ - 1) / TZ, S);
+    if (stress) k_el_stress<TZ><<<grid, BX, 0, st>>>(a);
+    else k_el_disp<TZ><<<grid, BX, 0, st>>>(a);
+  }
   check_cuda(cudaGetLastError(), stress ? "stress launch" : "displacement launch");
 }
 
@@ -1219,11 +1549,11 @@ void full_step(Run& R, int S, int it, bool record, int kind, float* sU[2], float
   es->ctx->prof.begin(R.st, kind, 0.0, &ev);
   launch_stencil(es, R.st, a, S, true);
   es->ctx->prof.end(R.st, kind, ev);
-  R.inject_sigma(S, it);
+  if (R.any_mt) R.inject_sigma(S, it);
   es->ctx->prof.begin(R.st, kind, R.step_bytes(S, sU != nullptr), &ev);
   launch_stencil(es, R.st, a, S, false);
   es->ctx->prof.end(R.st, kind, ev);
-  R.inject_force(S, it, false, 1.0f, sD);
+  if (R.any_force) R.inject_force(S, it, false, 1.0f, sD);
   if (record) R.record(S, it);
 }
 
@@ -1362,7 +1692,7 @@ void elastic_init(sw_elastic* es, sw_ctx* ctx, const sw_elastic_params* p, int g
   g.nz = p->n[1];
   g.halo = p->halo;
   g.ft = p->freetop ? 1 : 0;
-  g.P = (int)round_up(g.nx + XPAD + 4, 32);
+  g.P = (int)round_up(g.nx + XPAD + 8, 32);  // the vector kernels read up to column nx + 36
   g.F = (long long)g.P * (g.nz + 2 * ZPAD);
   g.W = (int)round_up(2 * g.halo + 3, 4);
   g.idx = (float)(1.0 / p->h[0]);
@@ -1446,6 +1776,8 @@ void elastic_forward(sw_elastic* es, int nshots, const sw_elastic_shot* shots, b
     build_tables(es, shots, group, on_device, false, desc);
     const float sf_ref = set_forward_scales(es, shots, group, desc);
     Run R{es, es->ctx->stream, es->d_desc.as<ShotDesc>(), sf_ref};
+    R.any_mt = R.any_force = false;
+    for (const auto& h : group) (shots[h.orig].kind == 0 ? R.any_mt : R.any_force) = true;
     zero_state(es, S, false);
     for (int it = 1; it <= group.front().nt; ++it) {
       const int A = active_count(group, it);
@@ -1520,6 +1852,8 @@ void elastic_gradient(sw_elastic* es, int nshots, const sw_elastic_shot* shots, 
     build_tables(es, shots, group, on_device, true, desc);
     const float sf_ref = set_forward_scales(es, shots, group, desc);
     Run R{es, st, es->d_desc.as<ShotDesc>(), sf_ref};
+    R.any_mt = R.any_force = false;
+    for (const auto& h : group) (shots[h.orig].kind == 0 ? R.any_mt : R.any_force) = true;
     const long long F = g.F;
     const int cap = es->cap;
     float* slots = es->slots.as<float>();
@@ -1709,8 +2043,12 @@ void elastic_gradient(sw_elastic* es, int nshots, const sw_elastic_shot* shots, 
 }
 
 void elastic_set_tuning(sw_elastic* es, int tz) {
-  if (tz != 0 && tz != 8 && tz != 16 && tz != 32) fail(SW_ERR_ARG, "tz must be 0 (default), 8, 16 or 32");
-  es->tz = tz == 0 ? 8 : tz;
+  // tz = rows per block (8, 16, 32; 0 = 8); + 64 selects the one-point-per-thread kernels
+  const int rows = tz % 64;
+  if (tz < 0 || tz >= 128 || (rows != 0 && rows != 8 && rows != 16 && rows != 32))
+    fail(SW_ERR_ARG, "tz must be 0, 8, 16 or 32, optionally + 64");
+  es->tz = rows == 0 ? 8 : rows;
+  es->vec = tz < 64;
 }
 sw_ctx* elastic_ctx(sw_elastic* es) { return es->ctx; }
 sw_elastic* elastic_new() { return new sw_elastic(); }
