@@ -12,7 +12,7 @@
  * 1-based; traces are (nt, nrec) column-major with time fastest; positions are
  * (npos, ndim) column-major.  Unless a call takes an `on_device` flag set to
  * 1, every pointer is a host pointer and the call copies in and out.  With
- * on_device = 1 the bulk arrays (vp, srctf, traces, observed, invcov_diag,
+ * on_device = 1 the bulk arrays (vp, srctf, traces, observed, invcov_diag, invcov,
  * grad, misfit) are device pointers; the small tables (grid indices, C-PML
  * coefficients, windows, positions) are always host memory.
  *
@@ -129,6 +129,8 @@ typedef struct {
   const int32_t* windows;   /* (2, nwin): 1-based inclusive [first, last] pairs (host memory) */
   const double* src_pos;    /* (nsrc, ndim) metres, muting only (host memory) */
   const double* rec_pos;    /* (nrec, ndim) metres, muting only (host memory) */
+  const float* invcov;      /* gradient: NULL, or the full inverse covariance (nt, nt) column-major
+                               (L2Misfit.invcov as a dense matrix); takes precedence over invcov_diag */
 } sw_acoustic_shot;
 
 /* GradParameters. */
@@ -245,6 +247,8 @@ typedef struct {
   const int32_t* windows;  /* (2, nwin) 1-based inclusive time windows; host memory */
   const double* src_pos;   /* (nsrc, 2) metres, for muting; host memory */
   const double* rec_pos;   /* (nrec, 2) metres, for muting; host memory */
+  const float* invcov;     /* gradient: NULL, or the full inverse covariance (nt, nt) column-major, applied to
+                              each component; takes precedence over invcov_diag */
 } sw_elastic_shot;
 
 /* One elastic simulation (a set of preallocated device fields).  gradient = 1

@@ -40,7 +40,8 @@ class SwAcousticParams(ctypes.Structure):
 class SwAcousticShot(ctypes.Structure):
     _fields_ = [("nt", i32), ("nsrc", i32), ("src_idx", vp_), ("srctf", vp_), ("nrec", i32),
                 ("rec_idx", vp_), ("traces", vp_), ("cpml", vp_), ("observed", vp_),
-                ("invcov_diag", vp_), ("nwin", i32), ("windows", vp_), ("src_pos", vp_), ("rec_pos", vp_)]
+                ("invcov_diag", vp_), ("nwin", i32), ("windows", vp_), ("src_pos", vp_), ("rec_pos", vp_),
+                ("invcov", vp_)]
 
 
 class SwGradParams(ctypes.Structure):
@@ -61,7 +62,7 @@ class SwElasticShot(ctypes.Structure):
     _fields_ = [("nt", i32), ("kind", i32), ("nsrc", i32), ("srctf", vp_), ("momtens", vp_),
                 ("src", SwPointTable * 2), ("nrec", i32), ("rec", SwPointTable * 2), ("traces", vp_),
                 ("cpml", vp_), ("observed", vp_), ("invcov_diag", vp_), ("nwin", i32), ("windows", vp_),
-                ("src_pos", vp_), ("rec_pos", vp_)]
+                ("src_pos", vp_), ("rec_pos", vp_), ("invcov", vp_)]
 
 
 class SwError(RuntimeError):

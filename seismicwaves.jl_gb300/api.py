@@ -132,8 +132,8 @@ class L2Misfit:
     """src/inversion/misfits/L2Misfit.jl:2-20.
 
     ``invcov`` may be None (identity), a vector (its diagonal) or a square
-    matrix; the GPU gradient takes diagonal inverse covariances (a dense
-    matrix that is diagonal is accepted).
+    matrix (applied on the GPU by a cuBLAS product when it has off-diagonal
+    terms).
     """
 
     def __init__(self, observed=None, invcov=None, windows: Sequence[tuple[int, int]] = ()):
@@ -154,17 +154,21 @@ class L2Misfit:
         self.windows = windows
 
     def invcov_diagonal(self):
-        """Diagonal of C^-1 (None = identity); raises for a non-diagonal matrix."""
+        """Diagonal of C^-1 (None = identity or a non-diagonal matrix, see invcov_dense)."""
         ic = self.invcov
         if ic is None:
             return None
         if ic.ndim == 1:
             return ic
         d = np.diag(ic)
-        if np.count_nonzero(ic - np.diag(d)) != 0:
-            raise NotImplementedError("the GB300 gradient takes a diagonal inverse covariance; "
-                                      "this one has off-diagonal terms")
-        return d
+        return d if np.count_nonzero(ic - np.diag(d)) == 0 else None
+
+    def invcov_dense(self):
+        """C^-1 as a dense (nt, nt) matrix when it has off-diagonal terms, else None."""
+        ic = self.invcov
+        if ic is None or ic.ndim == 1 or self.invcov_diagonal() is not None:
+            return None
+        return ic
 
     def _masked_residuals(self, seismograms):
         res = np.asarray(seismograms, dtype=np.float64) - self.observed
@@ -428,6 +432,11 @@ class AcousticCDCPMLWaveSimulation:
                     diag = np.ascontiguousarray(diag, dtype=np.float32)
                     st.invcov_diag = diag.ctypes.data
                     arrs.append(diag)
+                dense = m.invcov_dense()
+                if dense is not None:
+                    dense = np.asfortranarray(dense, dtype=np.float32)
+                    st.invcov = dense.ctypes.data
+                    arrs.append(dense)
                 if m.windows:
                     win = np.ascontiguousarray(np.array(m.windows, dtype=np.int32).reshape(-1))
                     st.nwin, st.windows = len(m.windows), win.ctypes.data

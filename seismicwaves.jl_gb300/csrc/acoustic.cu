@@ -55,6 +55,9 @@ struct ShotDesc {
   const float* mask;         // (nt) or nullptr
   float* adj;                // (nt, nrec) adjoint source (prescaled)
   float* ring;               // 3 values per boundary injection point (see k_inject_record)
+  const float* icd;          // dense inverse covariance (nt, nt) or nullptr
+  float* resid;              // dense case: masked residuals (nt, nrec)
+  const float* cres;         // dense case: C^-1 r (nt, nrec), from cuBLAS
 };
 
 // Boundary injection points.  The reference never updates the outermost grid
@@ -172,6 +175,20 @@ __device__ void adj_inject_shot(const ShotDesc& D, const long long* __restrict__
   }
 }
 
+// Masked residuals of the shots with a dense inverse covariance (the input of
+// the cuBLAS product C^-1 r).  gridDim = (blocks per shot, shots).
+__global__ void k_residual_dense(const ShotDesc* __restrict__ desc) {
+  const ShotDesc& D = desc[blockIdx.y];
+  if (!D.icd) return;
+  const long long total = (long long)D.nt * D.nrec;
+  for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < total;
+       q += (long long)gridDim.x * blockDim.x) {
+    float res = D.tr[q] - D.obs[q];
+    if (D.mask) res *= D.mask[q % D.nt];
+    D.resid[q] = res;
+  }
+}
+
 // Residuals, window mask, C^-1 r, misfit (FP64) and the prescaled adjoint
 // source -C^-1 r * fact(rec).  gridDim = (blocks per shot, shots).
 __global__ void k_misfit_adjsrc(const ShotDesc* __restrict__ desc, const long long* __restrict__ rec_lin,
@@ -186,7 +203,7 @@ __global__ void k_misfit_adjsrc(const ShotDesc* __restrict__ desc, const long lo
     const int r = (int)(q / D.nt);
     float res = D.tr[q] - D.obs[q];
     if (D.mask) res *= D.mask[t];
-    const float cres = D.ic ? D.ic[t] * res : res;
+    const float cres = D.cres ? D.cres[q] : (D.ic ? D.ic[t] * res : res);
     acc += (double)res * (double)cres;
     D.adj[q] = (-cres) * fact[rec_lin[D.rec_off + r]];
   }
@@ -370,6 +387,7 @@ struct sw_wavesim {
   // tables
   DevMem d_desc, d_pts, d_ptr, d_ids, d_bslot, d_rec, d_tf, d_tr, d_obs, d_ic, d_mask, d_adj, d_cpml, d_partial, d_mis;
   DevMem d_ring;  // boundary-injection rings (3 floats per point)
+  DevMem d_icd, d_dres;  // dense inverse covariances; residuals and C^-1 r of those shots
   DevMem d_mute, d_mute_ptr;
   int tile_tz = 0;  // 0 = heuristic
   int variant = 0;  // 2D stencil: 0 = register-pipelined, 1 = TMA
@@ -587,12 +605,16 @@ void build_tables(sw_wavesim* ws, const sw_acoustic_shot* shots, const std::vect
   T.pts.clear(); T.rec.clear(); T.ptr.clear(); T.ids.clear(); T.bslot.clear();
   T.nring = 0;
   std::vector<int> ring_off(S);
-  long long tf_total = 0, tr_total = 0, ic_total = 0, mask_total = 0;
+  long long tf_total = 0, tr_total = 0, ic_total = 0, mask_total = 0, icd_total = 0, dres_total = 0;
   for (int k = 0; k < S; ++k) {
     const sw_acoustic_shot& s = shots[group[k].orig];
     tf_total += (long long)s.nt * s.nsrc;
     tr_total += (long long)s.nt * s.nrec;
     if (s.invcov_diag) ic_total += s.nt;
+    if (grad && s.invcov) {
+      icd_total += (long long)s.nt * s.nt;
+      dres_total += (long long)s.nt * s.nrec;
+    }
     if (s.nwin > 0) mask_total += s.nt;
   }
   // device staging
@@ -605,7 +627,12 @@ void build_tables(sw_wavesim* ws, const sw_acoustic_shot* shots, const std::vect
     }
     ensure(ws, ws->d_mask, std::max<long long>(mask_total, 4) * sizeof(float), "window mask");
     ensure(ws, ws->d_adj, std::max<long long>(tr_total, 4) * sizeof(float), "adjoint source");
+    if (dres_total) {
+      if (!on_device) ensure(ws, ws->d_icd, icd_total * sizeof(float), "dense inverse covariance");
+      ensure(ws, ws->d_dres, 2 * dres_total * sizeof(float), "dense residuals");
+    }
   }
+  long long icd_o = 0, dres_o = 0;
   const int na = 2 * ws->prm.halo + 2, nh = 2 * ws->prm.halo;
   const int cstride = ws->N * (2 * na + 2 * nh);
   std::vector<float> cpml((size_t)S * cstride);
@@ -651,6 +678,20 @@ void build_tables(sw_wavesim* ws, const sw_acoustic_shot* shots, const std::vect
       }
     }
     D.tr = ws->d_tr.as<float>() + tr_o;
+    if (grad && s.invcov) {
+      if (on_device) {
+        D.icd = s.invcov;
+      } else {
+        float* cp = ws->d_icd.as<float>() + icd_o;
+        check_cuda(cudaMemcpyAsync(cp, s.invcov, (size_t)s.nt * s.nt * sizeof(float), cudaMemcpyHostToDevice, st),
+                   "invcov upload");
+        D.icd = cp;
+        icd_o += (long long)s.nt * s.nt;
+      }
+      D.resid = ws->d_dres.as<float>() + dres_o;
+      D.cres = ws->d_dres.as<float>() + dres_total + dres_o;
+      dres_o += (long long)s.nt * s.nrec;
+    }
     if (grad) {
       D.adj = ws->d_adj.as<float>() + tr_o;
       if (s.nwin > 0) {
@@ -1419,8 +1460,18 @@ void acoustic_gradient(sw_wavesim* ws, int nshots, const sw_acoustic_shot* shots
     build_tables(ws, shots, group, on_device, true, T);
     ensure(ws, ws->d_partial, (size_t)nblk * S * sizeof(double), "misfit partials");
     const bool accumulate = !first_group;
+    bool any_dense = false;
+    for (const auto& h : group) any_dense = any_dense || shots[h.orig].invcov;
     auto misfit_and_adjsrc = [&] {
       cudaEvent_t ev = nullptr;
+      if (any_dense) {  // C^-1 r of the shots with a dense inverse covariance (cuBLAS)
+        k_residual_dense<<<dim3(nblk, S), 256, 0, st>>>(ws->d_desc.as<ShotDesc>());
+        check_cuda(cudaGetLastError(), "residual launch");
+        for (int k = 0; k < S; ++k)
+          if (T.desc[k].icd)
+            dense_invcov(ws->ctx, T.desc[k].nt, T.desc[k].nrec, T.desc[k].icd, T.desc[k].resid,
+                         const_cast<float*>(T.desc[k].cres));
+      }
       ws->ctx->prof.begin(st, KK_OTHER, 0.0, &ev);
       k_misfit_adjsrc<<<dim3(nblk, S), 256, 0, st>>>(ws->d_desc.as<ShotDesc>(), ws->d_rec.as<long long>(),
                                                      ws->fact.as<float>(), ws->d_partial.as<double>());
@@ -1442,7 +1493,7 @@ void acoustic_gradient(sw_wavesim* ws, int nshots, const sw_acoustic_shot* shots
       check_cuda(cudaGetLastError(), "gradient reduction launch");
       ws->ctx->prof.end(st, KK_OTHER, ev);
     };
-    if (!mute) {
+    if (!mute && !any_dense) {
       // the whole group -- forward, misfit, adjoint, shot sum -- as one graph
       std::vector<long long> key = group_key(ws, group, true);
       key.insert(key.end(), {accumulate ? 1 : 0, (long long)(uintptr_t)gout, (long long)(uintptr_t)mout});

@@ -674,6 +674,9 @@ struct ShotDesc {
   const float* ic;           // diagonal inverse covariance or null
   const float* mask;         // window mask (nt) or null
   float* adjsrc;             // adjoint source (nt, 2, nrec)
+  const float* icd;          // dense inverse covariance (nt, nt) or null
+  float* resid;              // dense case: masked residuals (nt, 2 nrec)
+  const float* cres;         // dense case: C^-1 r (nt, 2 nrec), from cuBLAS
 };
 
 // sigma_xx += Mxx w tf, sigma_zz += Mzz w tf (table 0), sigma_xz += Mxz w tf (table 1)
@@ -775,7 +778,7 @@ __global__ void k_el_misfit(const ShotDesc* __restrict__ desc, double* __restric
     const int t = (int)(q % D.nt);
     float res = D.tr[q] - D.obs[q];
     if (D.mask) res *= D.mask[t];
-    const float cres = D.ic ? D.ic[t] * res : res;
+    const float cres = D.cres ? D.cres[q] : (D.ic ? D.ic[t] * res : res);
     acc += (double)res * (double)cres;
     D.adjsrc[q] = -cres;
     mx = fmaxf(mx, fabsf(cres));
@@ -795,6 +798,19 @@ __global__ void k_el_misfit(const ShotDesc* __restrict__ desc, double* __restric
   if (threadIdx.x == 0) {
     partial[(long long)shot * gridDim.x + blockIdx.x] = red[0];
     atomicMax(amax, __float_as_uint(redm[0]));  // non-negative floats order like their bits
+  }
+}
+
+// Masked residuals of the shots with a dense inverse covariance.
+__global__ void k_el_residual_dense(const ShotDesc* __restrict__ desc) {
+  const ShotDesc& D = desc[blockIdx.y];
+  if (!D.icd) return;
+  const long long total = (long long)D.nt * 2 * D.nrec;
+  for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < total;
+       q += (long long)gridDim.x * blockDim.x) {
+    float res = D.tr[q] - D.obs[q];
+    if (D.mask) res *= D.mask[q % D.nt];
+    D.resid[q] = res;
   }
 }
 
@@ -1079,6 +1095,7 @@ struct sw_elastic {
   // tables
   DevMem d_desc, d_ll, d_int, d_flt, d_tf, d_tr, d_obs, d_ic, d_mask, d_adj, d_mt, d_cp;
   DevMem d_partial, d_amax, d_balls, d_ball_ptr, d_cs;
+  DevMem d_icd, d_dres;  // dense inverse covariances; residuals and C^-1 r of those shots
   DevMem d_snap;                     // snapshot stage (one block per shot)
   int snapevery = 0;                 // snapshots requested by the current forward call
   float* const* snap_out = nullptr;  // per caller shot: nt/snapevery blocks [ux, uz, sxx, szz, sxz]
@@ -1346,6 +1363,18 @@ void build_tables(sw_elastic* es, const sw_elastic_shot* shots, const std::vecto
     ensure(es, es->d_obs, (size_t)tr_total * sizeof(float), "observed traces");
     ensure(es, es->d_adj, (size_t)tr_total * sizeof(float), "adjoint sources");
   }
+  long long icd_total = 0, dres_total = 0;
+  for (int k = 0; k < S; ++k) {
+    const sw_elastic_shot& s = shots[group[k].orig];
+    if (grad && s.invcov) {
+      icd_total += (long long)s.nt * s.nt;
+      dres_total += (long long)s.nt * 2 * s.nrec;
+    }
+  }
+  if (dres_total) {
+    if (!on_device) ensure(es, es->d_icd, icd_total * sizeof(float), "dense inverse covariance");
+    ensure(es, es->d_dres, 2 * dres_total * sizeof(float), "dense residuals");
+  }
   long long ic_total = 0;
   std::vector<long long> ic_off(S, -1);
   for (int k = 0; k < S; ++k) {
@@ -1399,6 +1428,24 @@ void build_tables(sw_elastic* es, const sw_elastic_shot* shots, const std::vecto
     D.ic = (grad && s.invcov_diag) ? es->d_ic.as<float>() + ic_off[k] : nullptr;
     D.mask = o.has_mask ? FL + o.mask : nullptr;
     D.adjsrc = grad ? es->d_adj.as<float>() + tr_off[k] : nullptr;
+  }
+  long long icd_o = 0, dres_o = 0;
+  for (int k = 0; k < S; ++k) {
+    const sw_elastic_shot& s = shots[group[k].orig];
+    if (!(grad && s.invcov)) continue;
+    ShotDesc& D = desc[k];
+    if (on_device) {
+      D.icd = s.invcov;
+    } else {
+      float* cp = es->d_icd.as<float>() + icd_o;
+      check_cuda(cudaMemcpyAsync(cp, s.invcov, (size_t)s.nt * s.nt * sizeof(float), cudaMemcpyHostToDevice, st),
+                 "invcov upload");
+      D.icd = cp;
+      icd_o += (long long)s.nt * s.nt;
+    }
+    D.resid = es->d_dres.as<float>() + dres_o;
+    D.cres = es->d_dres.as<float>() + dres_total + dres_o;
+    dres_o += (long long)s.nt * 2 * s.nrec;
   }
   upload(es, es->d_desc, desc, "shot descriptors");
 }
@@ -1925,6 +1972,14 @@ void elastic_gradient(sw_elastic* es, int nshots, const sw_elastic_shot* shots, 
     check_cuda(cudaMemsetAsync(es->d_amax.p, 0, sizeof(unsigned), st), "max clear");
     {
       cudaEvent_t ev = nullptr;
+      bool any_dense = false;
+      for (const auto& d : desc) any_dense = any_dense || d.icd;
+      if (any_dense) {  // C^-1 r of the shots with a dense inverse covariance (cuBLAS), per component
+        k_el_residual_dense<<<dim3(nblk, S), 256, 0, st>>>(R.ddesc);
+        check_cuda(cudaGetLastError(), "residual launch");
+        for (const auto& d : desc)
+          if (d.icd) dense_invcov(es->ctx, d.nt, 2 * d.nrec, d.icd, d.resid, const_cast<float*>(d.cres));
+      }
       es->ctx->prof.begin(st, KK_OTHER, 0.0, &ev);
       k_el_misfit<<<dim3(nblk, S), 256, 0, st>>>(R.ddesc, es->d_partial.as<double>(), es->d_amax.as<unsigned>());
       check_cuda(cudaGetLastError(), "misfit launch");

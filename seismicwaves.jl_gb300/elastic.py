@@ -392,6 +392,11 @@ class ElasticIsoCPMLWaveSimulation:
                     diag = np.ascontiguousarray(diag, dtype=np.float32)
                     st.invcov_diag = diag.ctypes.data
                     arrs.append(diag)
+                dense = m.invcov_dense()
+                if dense is not None:
+                    dense = np.asfortranarray(dense, dtype=np.float32)
+                    st.invcov = dense.ctypes.data
+                    arrs.append(dense)
                 if m.windows:
                     win = np.ascontiguousarray(np.array(m.windows, dtype=np.int32).reshape(-1))
                     st.nwin, st.windows = len(m.windows), win.ctypes.data

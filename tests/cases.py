@@ -144,7 +144,10 @@ class GpuRun:
                 obs = np.asfortranarray(shot.observed, dtype=np.float32)
                 st.observed = obs.ctypes.data
                 items.append(obs)
-                if shot.invcov is not None:
+                if shot.invcov is not None and np.ndim(shot.invcov) == 2:  # dense (nt, nt)
+                    ic = np.asfortranarray(shot.invcov, dtype=np.float32)
+                    st.invcov = ic.ctypes.data
+                elif shot.invcov is not None:
                     ic = np.ascontiguousarray(shot.invcov, dtype=np.float32)
                     st.invcov_diag = ic.ctypes.data
                     items.append(ic)

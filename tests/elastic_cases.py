@@ -192,8 +192,12 @@ class GpuElastic:
                 st.observed = obs.ctypes.data
                 arrs.append(obs)
                 if invcov is not None and invcov[k] is not None:
-                    ic = np.ascontiguousarray(invcov[k], dtype=np.float32)
-                    st.invcov_diag = ic.ctypes.data
+                    if np.ndim(invcov[k]) == 2:  # dense (nt, nt)
+                        ic = np.asfortranarray(invcov[k], dtype=np.float32)
+                        st.invcov = ic.ctypes.data
+                    else:
+                        ic = np.ascontiguousarray(invcov[k], dtype=np.float32)
+                        st.invcov_diag = ic.ctypes.data
                     arrs.append(ic)
                 if windows is not None and windows[k]:
                     w = np.ascontiguousarray(np.array(windows[k], dtype=np.int32).reshape(-1))

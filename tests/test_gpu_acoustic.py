@@ -332,3 +332,25 @@ def test_gradient_grouped_adjoint_variants(sw, oracle, variant):
     gref, mref, _ = oracle_gradient(oracle, sw, case, shot, check_freq=10)
     assert abs(msf - 5 * mref) / abs(5 * mref) < MISFIT_TOL
     assert rel_l2(g, 5 * gref) < GRAD_TOL
+
+
+def _dense_invcov(nt, seed=0):
+    """A symmetric positive-definite inverse covariance with off-diagonal terms
+    (exponentially correlated noise)."""
+    i = np.arange(nt)
+    c = np.exp(-np.abs(i[:, None] - i[None, :]) / 3.0)
+    return np.linalg.inv(c + 0.1 * np.eye(nt))
+
+
+def test_gradient_dense_invcov(sw, oracle):
+    """A full inverse covariance (cuBLAS product on the device) against the oracle's dense C^-1 r."""
+    case, shot = _grad_case(sw, oracle, nt=300)
+    ic = _dense_invcov(shot.nt)
+    shot.invcov = ic
+    run = GpuRun(sw, case, gradient=True, check_freq=10)
+    g, msf, _ = run.gradient([shot])
+    run.close()
+    gref, mref, _ = oracle_gradient(oracle, sw, case, shot, check_freq=10)
+    print(f"dense invcov: misfit {abs(msf - mref) / abs(mref):.2e} gradient {rel_l2(g, gref):.2e}")
+    assert abs(msf - mref) / abs(mref) < MISFIT_TOL
+    assert rel_l2(g, gref) < GRAD_TOL

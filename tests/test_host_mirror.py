@@ -36,9 +36,10 @@ def test_l2_misfit(sw):
     assert np.isclose(m.calcmisfit(recs), 0.5 * np.sum(r * ic[:, None] * r))
     np.testing.assert_allclose(m.dchi_du(recs), ic[:, None] * r)
     np.testing.assert_allclose(m.invcov_diagonal(), ic)
+    assert m.invcov_dense() is None
     dense = sw.L2Misfit(observed=obs, invcov=np.ones((50, 50)))
-    with pytest.raises(NotImplementedError):
-        dense.invcov_diagonal()
+    assert dense.invcov_diagonal() is None
+    assert dense.invcov_dense().shape == (50, 50)
     with pytest.raises(AssertionError):
         sw.L2Misfit(observed=obs, windows=[(0, 3)])
 
