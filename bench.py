@@ -344,6 +344,184 @@ class ElasticRun:
     timed = GradientRun.timed
 
 
+class VDRun(GradientRun):
+    """The variable-density workload's shots as C-ABI structs (sw_acoustic_vd_*)."""
+
+    def __init__(self, sw, w, device):
+        import torch
+
+        L = sw._lib
+        V = sys.modules[sw.__name__ + ".vd"]
+        self.sw, self.w, self.L, self.torch = sw, w, L, torch
+        self.dev = torch.device("cuda", device)
+        self.ctx = L.Context(device)
+        self.lib = self.ctx.lib
+        prm = L.SwAcousticParams()
+        prm.ndim = 2
+        for d in range(2):
+            prm.n[d], prm.h[d] = w.vp.shape[d], w.h[d]
+        prm.n[2], prm.h[2] = 1, 1.0
+        prm.dt, prm.halo, prm.rcoef, prm.freetop = w.dt, w.halo, 1e-4, int(w.freetop)
+        gp = L.SwGradParams()
+        gp.check_freq = w.check_freq
+        self.h = ctypes.c_void_p()
+        self.ctx.check(self.lib.sw_acoustic_vd_create(self.ctx.h, ctypes.byref(prm), 0, 1, ctypes.byref(gp),
+                                                      ctypes.byref(self.h)), "sw_acoustic_vd_create")
+        self.stream = torch.cuda.ExternalStream(self.ctx.stream, device=self.dev)
+        vmax = float(np.max(w.vp))
+        self.host = []
+        for s in w.shots:
+            si = sw.nearest_grid_points(s.src_pos, w.h)
+            ri = sw.nearest_grid_points(s.rec_pos, w.h)
+            tf = V.scale_srctf_vd(s.stf(w.dt), si, w.vp, w.rho, w.h, w.dt)
+            parts = []
+            for d in range(2):
+                parts += L.cpml_coefficients(vmax, w.dt, w.halo, 1e-4, w.h[d], s.f0, w.freetop and d == 1)
+            self.host.append((si, ri, tf, np.concatenate(parts).astype(np.float32)))
+        t = torch
+        self.tf_d = [t.from_numpy(np.ascontiguousarray(h[2].ravel(order="F"))).to(self.dev) for h in self.host]
+        self.tr_d = [t.zeros(s.nt * h[1].shape[0], dtype=t.float32, device=self.dev) for s, h in zip(w.shots, self.host)]
+        self.obs_d = [t.zeros_like(x) for x in self.tr_d]
+        self.grad_d = t.zeros(2 * int(np.prod(w.vp.shape)), dtype=t.float64, device=self.dev)
+        self.mis_d = t.zeros(1, dtype=t.float64, device=self.dev)
+
+    def set_material(self, vp, rho):
+        a = [np.asfortranarray(x, dtype=np.float32) for x in (vp, rho)]
+        self.ctx.check(self.lib.sw_acoustic_vd_set_material(self.h, a[0].ctypes.data, a[1].ctypes.data),
+                       "sw_acoustic_vd_set_material")
+
+    def make_observed(self):
+        self.set_material(self.w.vp_observed, self.w.rho_observed)
+        idx = list(range(len(self.w.shots)))
+        arr = self.structs(idx, [x.data_ptr() for x in self.tf_d], [x.data_ptr() for x in self.obs_d], None)
+        self.ctx.check(self.lib.sw_acoustic_vd_forward(self.h, len(idx), arr, 1), "observed forward")
+        self.set_material(self.w.vp, self.w.rho)
+
+    def gradient_device(self, idx):
+        arr = self.structs(idx, [x.data_ptr() for x in self.tf_d], [x.data_ptr() for x in self.tr_d],
+                           [x.data_ptr() for x in self.obs_d])
+        n = self.grad_d.numel() // 2
+        p = self.grad_d.data_ptr()
+        self.ctx.check(self.lib.sw_acoustic_vd_gradient(self.h, len(idx), arr, 1, p, p + 8 * n,
+                                                         self.mis_d.data_ptr()), "sw_acoustic_vd_gradient")
+
+    def setup_host(self):
+        t = self.torch
+        self.tf_h = [x.cpu().pin_memory() for x in self.tf_d]
+        self.obs_h = [x.cpu().pin_memory() for x in self.obs_d]
+        self.tr_h = [t.zeros(x.numel(), dtype=t.float32).pin_memory() for x in self.tr_d]
+        self.grad_h = t.zeros(self.grad_d.numel(), dtype=t.float64).pin_memory()
+        self.mis_h = t.zeros(1, dtype=t.float64).pin_memory()
+        h2d = sum(x.numel() * 4 for x in self.tf_h) + sum(x.numel() * 4 for x in self.obs_h)
+        d2h = sum(x.numel() * 4 for x in self.tr_h) + self.grad_h.numel() * 8 + 8
+        return h2d, d2h
+
+    def gradient_host(self):
+        idx = list(range(len(self.w.shots)))
+        arr = self.structs(idx, [x.data_ptr() for x in self.tf_h], [x.data_ptr() for x in self.tr_h],
+                           [x.data_ptr() for x in self.obs_h])
+        n = self.grad_h.numel() // 2
+        p = self.grad_h.data_ptr()
+        self.ctx.check(self.lib.sw_acoustic_vd_gradient(self.h, len(idx), arr, 0, p, p + 8 * n,
+                                                         self.mis_h.data_ptr()), "sw_acoustic_vd_gradient")
+
+
+def _vd_cpu_baseline(sw, w, nt_sample):
+    import oracle
+
+    V = sys.modules[sw.__name__ + ".vd"]
+    nt_sample = _sample_nt(w, nt_sample)
+    s = w.shots[0]
+    si = sw.nearest_grid_points(s.src_pos, w.h)
+    ri = sw.nearest_grid_points(s.rec_pos, w.h)
+    tf = V.scale_srctf_vd(s.stf(w.dt)[:nt_sample], si, w.vp, w.rho, w.h, w.dt).astype(np.float64)
+    cp = oracle.cpml_blocks(w.vp, w.h, w.dt, w.halo, 1e-4, s.f0, w.freetop)
+    obs = np.zeros((nt_sample, ri.shape[0]))
+    threads = os.cpu_count() or 1
+    K = min(w.check_freq, nt_sample - 1)
+    t0 = time.perf_counter()
+    oracle.vd_gradient(w.vp, w.rho, w.h, w.dt, w.halo, cp, tf, si, ri, obs, check_freq=K, nthreads=threads)
+    dt = time.perf_counter() - t0
+    nx, nz = w.vp.shape
+    sample = (f"one shot of {w.name}, {nt_sample} time steps, checkpoint period {K}, "
+              "FP64 gradient (forward + recompute + adjoint)")
+    return float(nx * nz) * nt_sample / dt / 1e9, threads, sample, dt
+
+
+VD_KINDS = {0: "k_vd_p + k_vd_v forward", 4: "k_vd_p + k_vd_v recompute (writes slots)",
+            1: "k_vd_v + k_vd_p<corr> adjoint with fused correlation"}
+
+
+def measure_vd(a, name="acoustic_vd2d_2001x801", shots=0, nt_cap=0, steps=None, warmup=None, plain=True, cpu=True,
+               device=0):
+    """Batched variable-density gradient: Gpts/s, shots/s, e2e, plain per-shot path, roofline of the dominant kind."""
+    import torch
+
+    steps = a.steps if steps is None else steps
+    warmup = a.warmup if warmup is None else warmup
+    sw, w = _workload(name, shots, nt_cap)
+    R = VDRun(sw, w, device)
+    if a.tz:
+        R.ctx.check(R.lib.sw_acoustic_vd_set_tuning(R.h, a.tz), "sw_acoustic_vd_set_tuning")
+    R.make_observed()
+    nshots = len(w.shots)
+    allidx = list(range(nshots))
+    pts = float(w.point_steps())
+    for _ in range(warmup):
+        R.gradient_device(allidx)
+    torch.cuda.synchronize(R.dev)
+    clocks = ClockSampler(device)
+    clocks.start()
+    t_dev = R.timed(lambda: R.gradient_device(allidx), steps)
+    clk = clocks.stop()
+    R.ctx.profile(True)
+    R.timed(lambda: R.gradient_device(allidx), 1)
+    R.ctx.profile(False)
+    prof = {k: R.ctx.profile_read(k) for k in range(6)}
+    h2d, d2h = R.setup_host()
+    R.gradient_host()
+    t_e2e = R.timed(R.gradient_host, steps)
+    pl = None
+    if plain:
+        R.gradient_device([0])
+        t_plain = R.timed(lambda: [R.gradient_device([i]) for i in allidx], 1)
+        pl = {"value": pts / t_plain / 1e9, "unit": UNIT, "shots_per_s": nshots / t_plain,
+              "ms_per_step": t_plain * 1e3, "what": "same kernels, one shot per call"}
+    dom = max(VD_KINDS, key=lambda k: prof[k][0])
+    ms_tot, launches, bytes_tot = prof[dom]
+    achieved = bytes_tot / (ms_tot / 1e3) / 1e9 if ms_tot > 0 else None
+    peak, peak_kind = _peak()
+    roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak if achieved else None, "traffic": None, "kernel": VD_KINDS[dom],
+            "peak_kind": peak_kind,
+            "kernels": {VD_KINDS[k]: {"ms": prof[k][0], "launches": prof[k][1],
+                                      "GB_per_s": (prof[k][2] / (prof[k][0] / 1e3) / 1e9) if prof[k][0] else None}
+                        for k in VD_KINDS}}
+    out = {"metric": METRIC, "value": pts * steps / t_dev / 1e9, "unit": UNIT, "n_gpus": 1, "steps": steps,
+           "warmup": warmup, "ms_per_step": t_dev * 1e3 / steps, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+           "config": {"workload": w.name, "grid": list(w.vp.shape), "h_m": w.h[0], "shots": nshots,
+                      "nt": max(s.nt for s in w.shots), "check_freq": w.check_freq, "halo": w.halo,
+                      "tz": a.tz or 8,
+                      "cache": "inputs larger than L2 (each step streams several GB of wavefield state)",
+                      "precision": "fp32 wavefields and stencil, fp32 sums over one checkpoint window, "
+                                   "fp64 window totals, misfit and shot sum"},
+           "shots_per_s": nshots * steps / t_dev, "plain": pl,
+           "batched_vs_plain": (nshots * steps / t_dev / pl["shots_per_s"]) if pl else None,
+           "clocks": clk,
+           "e2e": {"value": pts * steps / t_e2e / 1e9, "unit": UNIT, "h2d_bytes_per_step": h2d,
+                   "d2h_bytes_per_step": d2h},
+           "gpu_launches": sum(prof[k][1] for k in range(6)) * steps, "roofline": roof}
+    if cpu:
+        import oracle
+
+        oracle.load()
+        v, threads, sample, _ = _vd_cpu_baseline(sw, w, a.cpu_sample_nt)
+        out["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample}
+    R.lib.sw_acoustic_vd_destroy(R.h)
+    return out
+
+
 def _elastic_cpu_baseline(sw, w, nt_sample):
     import oracle
 
@@ -428,9 +606,14 @@ def run_reference(a):
     import oracle
 
     oracle.load()
+    base = _cpu_baseline
+    if a.workload.startswith("acoustic_vd"):
+        base = _vd_cpu_baseline
+    elif a.workload.startswith("elastic"):
+        base = _elastic_cpu_baseline
     vals = []
     for i in range(a.warmup + a.steps):
-        v, threads, sample, dt = _cpu_baseline(sw, w, a.cpu_sample_nt)
+        v, threads, sample, dt = base(sw, w, a.cpu_sample_nt)
         if i >= a.warmup:
             vals.append((v, dt))
     value = statistics.mean(v for v, _ in vals)
@@ -669,6 +852,11 @@ def main():
         run_reference(a)
         return
     try:
+        if a.workload.startswith("acoustic_vd"):
+            if int(os.environ.get("RANK", "0")) == 0:
+                print(json.dumps(measure_vd(a, a.workload, a.shots, a.nt, plain=not a.no_plain,
+                                            cpu=not a.no_cpu)), flush=True)
+            return
         if a.workload.startswith("elastic"):
             if int(os.environ.get("RANK", "0")) == 0:
                 print(json.dumps(measure_elastic(a, a.workload, a.shots, a.nt, plain=not a.no_plain,

@@ -43,6 +43,21 @@
  *       src/models/acoustic/acou_gradient.jl:4-95, src/utils/checkpointers.jl:1-107,
  *       src/inversion/misfits/L2Misfit.jl:24-77, acoustic2D_xPU.jl:64-76 and :128-169,
  *       correlate_gradient_xPU.jl:1-10, src/utils/mute_grad.jl:13-80)
+ *   sw_acoustic_vd_create / sw_acoustic_vd_destroy
+ *       build_wavesim -> AcousticVDStaggeredCPMLWaveSimulation (src/apis/build.jl:60-72,
+ *       src/models/acoustic/acou_models.jl:311-454)
+ *   sw_acoustic_vd_set_material
+ *       update_matprop! -> precompute_fact! (acou_models.jl:283-300)
+ *   sw_acoustic_vd_forward
+ *       run_swforward! + swforward_1shot! (VD) + forward_onestep_CPML!
+ *       (src/models/acoustic/acou_forward.jl:83-128,
+ *       src/models/acoustic/backends/shared/acoustic2D_VD_xPU.jl:1-125)
+ *   sw_acoustic_vd_gradient
+ *       run_swgradient! + swgradient_1shot! (VD) with LinearCheckpointer, L2 misfit,
+ *       prescale_residuals!, adjoint_onestep_CPML!, correlate_gradient_m0! /
+ *       correlate_gradient_m1!, back_interp, muting and the vp / rho chain rule
+ *       (src/models/acoustic/acou_gradient.jl:97-202, acoustic2D_VD_xPU.jl:64-192,
+ *       src/models/acoustic/backends/shared/correlate_gradient_xPU.jl:12-21)
  *   sw_elastic_create / sw_elastic_destroy
  *       build_wavesim -> ElasticIsoCPMLWaveSimulation (src/models/elastic/ela_models.jl:177-420)
  *   sw_elastic_set_material
@@ -82,6 +97,7 @@ enum {
 typedef struct sw_ctx sw_ctx;
 typedef struct sw_wavesim sw_wavesim;
 typedef struct sw_elastic sw_elastic;
+typedef struct sw_acoustic_vd sw_acoustic_vd;
 
 /* Library version (major*10000 + minor*100 + patch). */
 int sw_version(void);
@@ -283,6 +299,43 @@ int sw_elastic_forward_snapshots(sw_elastic* es, int32_t nshots, const sw_elasti
  * four-points-per-thread ones.  A tuning knob of this backend; no reference
  * counterpart. */
 int sw_elastic_set_tuning(sw_elastic* es, int32_t tz);
+
+/* ---------------------------------------------------------------------------
+ * Variable-density acoustic 2D, 4th-order staggered pressure-velocity scheme
+ * with C-PML (AcousticVDStaggeredCPMLWaveSimulation).  p, vp and rho live on
+ * the (nx, nz) nodes, vx on (nx-1, nz), vz on (nx, nz-1).  Shots use
+ * sw_acoustic_shot, with srctf already scaled by dt vp(src)^2 rho(src) /
+ * (dx dz) as possrcrec_scaletf does for this simulation
+ * (src/models/acoustic/acou_forward.jl:66-80).
+ * ------------------------------------------------------------------------- */
+/* params->ndim must be 2.  interp_rho: 1/rho at the half points, 0 =
+ * arithmetic average (the reference's default), 1 = harmonic.  gradient = 1
+ * prepares the adjoint fields and the checkpointing (gparams as for the
+ * constant-density path; snapshot_bf16 must be 0). */
+int sw_acoustic_vd_create(sw_ctx* ctx, const sw_acoustic_params* params, int32_t interp_rho, int32_t gradient,
+                          const sw_grad_params* gparams, sw_acoustic_vd** out);
+int sw_acoustic_vd_destroy(sw_acoustic_vd* vd);
+/* vp, rho: host arrays of (nx, nz) floats (check_matprop's conditions apply). */
+int sw_acoustic_vd_set_material(sw_acoustic_vd* vd, const float* vp, const float* rho);
+/* Forward modelling of nshots shots in one batch; traces (pressure after
+ * injection) written per shot.  on_device = 1: srctf and traces are device pointers. */
+int sw_acoustic_vd_forward(sw_acoustic_vd* vd, int32_t nshots, const sw_acoustic_shot* shots, int32_t on_device);
+/* sw_acoustic_vd_forward with snapshots: after every step it with
+ * it % snapevery == 0, each shot's pcur and vcur are copied into
+ * snapshots[k] + (it/snapevery - 1) * B as one block of B = nx nz + (nx-1) nz
+ * + nx (nz-1) floats: p (nx, nz), vx (nx-1, nz), vz (nx, nz-1), each
+ * column-major (savesnapshot! in acou_forward.jl:118-121). */
+int sw_acoustic_vd_forward_snapshots(sw_acoustic_vd* vd, int32_t nshots, const sw_acoustic_shot* shots,
+                                     int32_t on_device, int32_t snapevery, float* const* snapshots);
+/* Gradient of the summed L2 misfit with respect to vp and rho, each (nx, nz)
+ * FP64 summed over the shots, with the reference's sign convention; misfit
+ * (may be NULL) = sum of the shots' misfits.  on_device = 1: srctf, traces,
+ * observed, invcov_diag, invcov and the outputs are device pointers. */
+int sw_acoustic_vd_gradient(sw_acoustic_vd* vd, int32_t nshots, const sw_acoustic_shot* shots, int32_t on_device,
+                            double* grad_vp, double* grad_rho, double* misfit);
+/* Rows per thread block of the VD stencil kernels: 8, 16 or 32 (0 = default
+ * 8).  A tuning knob of this backend; results do not depend on it. */
+int sw_acoustic_vd_set_tuning(sw_acoustic_vd* vd, int32_t tz);
 
 /* 2D forward of one shot that allocates no device memory.  Has no
  * counterpart in the reference: it exists for callers that cannot let a

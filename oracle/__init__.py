@@ -1,10 +1,11 @@
 """TEST INFRASTRUCTURE ONLY: Python bindings of the CPU oracle (sw_oracle.cpp,
-sw_elastic_oracle.cpp).
+sw_elastic_oracle.cpp, sw_vd_oracle.cpp).
 
 The oracle is a plain C++ restatement of SeismicWaves.jl's acoustic
-constant-density C-PML algorithm and of its isotropic elastic 2D (P-SV) C-PML
-algorithm (FP64, plus an FP32 instantiation used to study single-precision
-error).  Only the test-suite, ``__graft_entry__.smoke``
+constant-density C-PML algorithm, of its variable-density acoustic 2D
+(staggered pressure-velocity) C-PML algorithm and of its isotropic elastic 2D
+(P-SV) C-PML algorithm (FP64, plus an FP32 instantiation used to study
+single-precision error).  Only the test-suite, ``__graft_entry__.smoke``
 and the CPU-baseline leg of ``bench.py`` may import this module; the product
 (``seismicwaves.jl_gb300``) never does.
 
@@ -22,7 +23,7 @@ from pathlib import Path
 import numpy as np
 
 HERE = Path(__file__).resolve().parent
-SRCS = [HERE / "sw_oracle.cpp", HERE / "sw_elastic_oracle.cpp"]
+SRCS = [HERE / "sw_oracle.cpp", HERE / "sw_elastic_oracle.cpp", HERE / "sw_vd_oracle.cpp"]
 DEPS = SRCS + [HERE / "oracle_common.h"]
 LIB = HERE / "_build" / "libsworacle.so"
 
@@ -74,6 +75,11 @@ def load():
         lib.oracle_elastic_gradient.argtypes = [i, P, P, d, i, i, P, P, P, i, i, P, i, i, i, P, P, P, P, P, i, P,
                                                 P, P, P, P, i, i, P, i, i, i, P, P, P, P, P, P, P, i]
         lib.oracle_elastic_gradient.restype = i
+        lib.oracle_vd_forward.argtypes = [i, P, P, d, i, P, P, i, P, i, i, P, P, i, P, P, i, i, P]
+        lib.oracle_vd_forward.restype = i
+        lib.oracle_vd_gradient.argtypes = [i, P, P, d, i, P, P, i, P, i, i, P, P, i, P, P, P, i, i, P, i, i, i, P,
+                                           P, P, P, P, P, i]
+        lib.oracle_vd_gradient.restype = i
         _lib = lib
     return _lib
 
@@ -350,3 +356,89 @@ def elastic_forward_snapshots(lam, mu, rho, h, dt, halo, freetop, cpml, shot, sn
     if rc != 0:
         raise RuntimeError(f"oracle_elastic_forward_snap failed ({rc})")
     return traces, snaps
+
+
+# ---------------------------------------------------------------------------
+# variable-density acoustic 2D
+# ---------------------------------------------------------------------------
+def _vd_common(vp, rho, h, cpml, srctf, src_idx, rec_idx):
+    vp = np.asfortranarray(vp, dtype=np.float64)
+    rho = np.asfortranarray(rho, dtype=np.float64)
+    assert vp.ndim == 2 and vp.shape == rho.shape
+    n = np.array(vp.shape, dtype=np.int32)
+    hh = np.array(h[:2], dtype=np.float64)
+    srctf = np.asfortranarray(srctf, dtype=np.float64)
+    src_idx = np.asfortranarray(src_idx, dtype=np.int32)
+    rec_idx = np.asfortranarray(rec_idx, dtype=np.int32)
+    cpml = np.ascontiguousarray(cpml, dtype=np.float64)
+    return vp, rho, n, hh, srctf, src_idx, rec_idx, cpml
+
+
+def vd_forward(vp, rho, h, dt, halo, cpml, srctf, src_idx, rec_idx, *, interp=0, f32=False, nthreads=0,
+               snapevery=0):
+    """swforward_1shot! of AcousticVDStaggeredCPMLWaveSimulation (2D) for one shot.
+
+    ``srctf`` (nt, nsrc) is already scaled by dt vp(src)^2 rho(src) / (dx dz).
+    Returns traces (nt, nrec); with ``snapevery`` > 0 also a list of
+    (p, vx, vz) snapshots after the steps it = snapevery, 2 snapevery, ...
+    """
+    vp, rho, n, hh, srctf, src_idx, rec_idx, cpml = _vd_common(vp, rho, h, cpml, srctf, src_idx, rec_idx)
+    nt, nsrc = srctf.shape
+    nrec = rec_idx.shape[0]
+    nx, nz = vp.shape
+    traces = np.zeros((nt, nrec), dtype=np.float64, order="F")
+    B = nx * nz + (nx - 1) * nz + nx * (nz - 1)
+    nsnap = nt // snapevery if snapevery > 0 else 0
+    snaps = np.zeros(max(nsnap, 1) * B, dtype=np.float64)
+    rc = load().oracle_vd_forward(int(f32), _p(n), _p(hh), float(dt), int(halo), _p(vp), _p(rho), int(interp),
+                                  _p(cpml), nt, nsrc, _p(src_idx), _p(srctf), nrec, _p(rec_idx), _p(traces),
+                                  int(nthreads or max_threads()), int(snapevery), _p(snaps))
+    if rc != 0:
+        raise RuntimeError(f"oracle_vd_forward failed ({rc})")
+    if snapevery <= 0:
+        return traces
+    out = []
+    for k in range(nsnap):
+        b = snaps[k * B:(k + 1) * B]
+        p = b[:nx * nz].reshape((nx, nz), order="F")
+        vx = b[nx * nz:nx * nz + (nx - 1) * nz].reshape((nx - 1, nz), order="F")
+        vz = b[nx * nz + (nx - 1) * nz:].reshape((nx, nz - 1), order="F")
+        out.append((p, vx, vz))
+    return traces, out
+
+
+def vd_gradient(vp, rho, h, dt, halo, cpml, srctf, src_idx, rec_idx, observed, *, interp=0, invcov=None,
+                windows=(), check_freq=1, mute_src=0, mute_rec=0, src_pos=None, rec_pos=None, f32=False,
+                nthreads=0):
+    """swgradient_1shot! of the VD simulation plus calcmisfit for one shot.
+
+    Returns ({"vp": ..., "rho": ...}, misfit, traces).
+    """
+    vp, rho, n, hh, srctf, src_idx, rec_idx, cpml = _vd_common(vp, rho, h, cpml, srctf, src_idx, rec_idx)
+    nt, nsrc = srctf.shape
+    nrec = rec_idx.shape[0]
+    observed = np.asfortranarray(observed, dtype=np.float64)
+    assert observed.shape == (nt, nrec)
+    if invcov is None:
+        kind, ic = 0, np.zeros(1)
+    else:
+        ic = np.asfortranarray(invcov, dtype=np.float64)
+        kind = 1 if ic.ndim == 1 else 2
+    win = np.array(list(windows), dtype=np.int32).reshape(-1)
+    nwin = len(win) // 2
+    if win.size == 0:
+        win = np.zeros(2, dtype=np.int32)
+    sp = np.asfortranarray(src_pos if src_pos is not None else np.zeros((nsrc, 2)), dtype=np.float64)
+    rp = np.asfortranarray(rec_pos if rec_pos is not None else np.zeros((nrec, 2)), dtype=np.float64)
+    traces = np.zeros((nt, nrec), dtype=np.float64, order="F")
+    gvp = np.zeros(vp.shape, dtype=np.float64, order="F")
+    grho = np.zeros(vp.shape, dtype=np.float64, order="F")
+    misfit = np.zeros(1, dtype=np.float64)
+    rc = load().oracle_vd_gradient(int(f32), _p(n), _p(hh), float(dt), int(halo), _p(vp), _p(rho), int(interp),
+                                   _p(cpml), nt, nsrc, _p(src_idx), _p(srctf), nrec, _p(rec_idx), _p(observed),
+                                   _p(ic), kind, nwin, _p(win), int(check_freq), int(mute_src), int(mute_rec),
+                                   _p(sp), _p(rp), _p(traces), _p(gvp), _p(grho), _p(misfit),
+                                   int(nthreads or max_threads()))
+    if rc != 0:
+        raise RuntimeError(f"oracle_vd_gradient failed ({rc})")
+    return {"vp": gvp, "rho": grho}, float(misfit[0]), traces

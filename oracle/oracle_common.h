@@ -61,12 +61,54 @@ inline void cpml_axis(double vel_max, double dt, int halo, double rcoef, double 
   }
 }
 
+// ---------------------------------------------------------------------------
+// Half-point interpolation and its chain rule, interpolations.jl:1-47
+// ---------------------------------------------------------------------------
+// Value at the half point whose lower corner is node (i, j) (1-based): the
+// average over the 2 (di + dj = 1) or 4 corners, arithmetic (method 0) or
+// harmonic (method 1).
+inline double interp_at(const double* m, int nx, int i, int j, int di, int dj, int method) {
+  // (i, j) 1-based lower corner; averages over the 2 or 4 corners
+  double s = 0;
+  int cnt = 0;
+  for (int b = 0; b <= dj; ++b)
+    for (int a = 0; a <= di; ++a) {
+      const double v = m[(size_t)(i - 1 + a) + (size_t)(j - 1 + b) * nx];
+      s += method == 1 ? 1.0 / v : v;
+      ++cnt;
+    }
+  s /= cnt;
+  return method == 1 ? 1.0 / s : s;
+}
+
+// back_interp, interpolations.jl:15-47: chain rule of the half-point
+// interpolation back onto the (nx, nz) nodes.
+inline void back_interp(const double* m, int nx, int nz, const double* g, int gx, int di, int dj, int method,
+                        double* res) {
+  const int gz = nz - dj;
+  const double w0 = 1.0 / double((di + 1) * (dj + 1));
+  for (int j = 1; j <= gz; ++j)
+    for (int i = 1; i <= gx; ++i) {
+      const double gv = g[(size_t)(i - 1) + (size_t)(j - 1) * gx];
+      const double itp = method == 1 ? interp_at(m, nx, i, j, di, dj, 1) : 0.0;
+      for (int pb = 0; pb <= dj; ++pb)
+        for (int pa = 0; pa <= di; ++pa) {
+          const size_t c = (size_t)(i - 1 + pa) + (size_t)(j - 1 + pb) * nx;
+          double w = w0;
+          if (method == 1) w = itp * itp / (m[c] * m[c]) * w0;
+          res[c] += gv * w;
+        }
+    }
+}
+
 template <typename T>
 using Snap = std::vector<std::vector<T>>;
 
 // LinearCheckpointer, checkpointers.jl:1-107.  One field (`bname`: "pcur" for
-// the acoustic path, "ucur" for the elastic one) is buffered with width 2 and a
-// K+1 buffer; the others are checkpointed with width 1.
+// the acoustic paths, "ucur" for the elastic one) is buffered in a K+1 buffer
+// and checkpointed with width `bwidth` (2 for the constant-density acoustic and
+// the elastic simulations, 1 for the variable-density one); the others are
+// checkpointed with width 1.
 template <typename T>
 struct LinearCheckpointer {
   int nt, K, last_checkpoint, curr_checkpoint;
@@ -74,16 +116,17 @@ struct LinearCheckpointer {
   std::vector<Snap<T>> buffer;  // buffers[bname], K+1 entries
 
   std::string bname;
+  int bwidth;
 
   LinearCheckpointer(int nt_, int K_, const std::map<std::string, Snap<T>>& proto,
-                     const std::string& buffered = "pcur")
-      : nt(nt_), K(K_), bname(buffered) {
+                     const std::string& buffered = "pcur", int buffered_width = 2)
+      : nt(nt_), K(K_), bname(buffered), bwidth(buffered_width) {
     last_checkpoint = (nt / K) * K;
     curr_checkpoint = last_checkpoint;
     for (int it = 0; it <= nt + 1; ++it) {
       if (it % K != 0) continue;
       for (auto& kv : proto) {
-        const int w = kv.first == bname ? 2 : 1;
+        const int w = kv.first == bname ? bwidth : 1;
         for (int itw = it; itw >= it - w + 1; --itw) {
           Snap<T> z = kv.second;
           for (auto& v : z) std::fill(v.begin(), v.end(), T(0));
@@ -97,7 +140,7 @@ struct LinearCheckpointer {
   }
 
   void save(const std::string& name, const Snap<T>& f, int it) {
-    const int w = name == bname ? 2 : 1;
+    const int w = name == bname ? bwidth : 1;
     for (int itw = it; itw <= it + w - 1; ++itw)
       if (itw % K == 0) checkpoints[it][name] = f;
     if (name == bname && it >= last_checkpoint) buffer[it - last_checkpoint] = f;

@@ -43,6 +43,8 @@
 
 namespace {
 
+using oracle::back_interp;
+using oracle::interp_at;
 using oracle::LinearCheckpointer;
 using oracle::mute_around_point;
 using oracle::Snap;
@@ -297,20 +299,6 @@ struct ElasticSim {
 // Material set-up: precomp_elaprop!, ela_models.jl:156-173 with the
 // interpolations of interpolations.jl:30-43 (0 = arithmetic, 1 = harmonic).
 // ---------------------------------------------------------------------------
-inline double interp_at(const double* m, int nx, int i, int j, int di, int dj, int method) {
-  // (i, j) 1-based lower corner; averages over the 2 or 4 corners
-  double s = 0;
-  int cnt = 0;
-  for (int b = 0; b <= dj; ++b)
-    for (int a = 0; a <= di; ++a) {
-      const double v = m[(size_t)(i - 1 + a) + (size_t)(j - 1 + b) * nx];
-      s += method == 1 ? 1.0 / v : v;
-      ++cnt;
-    }
-  s /= cnt;
-  return method == 1 ? 1.0 / s : s;
-}
-
 template <typename T>
 void set_material(ElasticSim<T>& sim, const double* lam, const double* mu, const double* rho, int irho, int imu) {
   const int nx = sim.nx, nz = sim.nz;
@@ -325,26 +313,6 @@ void set_material(ElasticSim<T>& sim, const double* lam, const double* mu, const
     for (int i = 1; i <= nx; ++i) sim.rho_j(i, j) = (T)interp_at(rho, nx, i, j, 0, 1, irho);
   for (int j = 1; j <= nz - 1; ++j)
     for (int i = 1; i <= nx - 1; ++i) sim.mu_ij(i, j) = (T)interp_at(mu, nx, i, j, 1, 1, imu);
-}
-
-// back_interp, interpolations.jl:15-47: chain rule of the half-point
-// interpolation back onto the (nx, nz) nodes.
-inline void back_interp(const double* m, int nx, int nz, const double* g, int gx, int di, int dj, int method,
-                        double* res) {
-  const int gz = nz - dj;
-  const double w0 = 1.0 / double((di + 1) * (dj + 1));
-  for (int j = 1; j <= gz; ++j)
-    for (int i = 1; i <= gx; ++i) {
-      const double gv = g[(size_t)(i - 1) + (size_t)(j - 1) * gx];
-      const double itp = method == 1 ? interp_at(m, nx, i, j, di, dj, 1) : 0.0;
-      for (int pb = 0; pb <= dj; ++pb)
-        for (int pa = 0; pa <= di; ++pa) {
-          const size_t c = (size_t)(i - 1 + pa) + (size_t)(j - 1 + pb) * nx;
-          double w = w0;
-          if (method == 1) w = itp * itp / (m[c] * m[c]) * w0;
-          res[c] += gv * w;
-        }
-    }
 }
 
 // ---------------------------------------------------------------------------

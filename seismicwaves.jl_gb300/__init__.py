@@ -15,6 +15,7 @@ from .api import (AcousticCDCPMLWaveSimulation, CPMLBoundaryConditionParameters,
 from .elastic import (ArithmeticAverageInterpolation, ElasticIsoCPMLWaveSimulation, ElasticIsoMaterialProperties,
                       ExternalForceShot, ExternalForceSources, HarmonicAverageInterpolation, InputParametersElastic,
                       MomentTensor2D, MomentTensorShot, MomentTensorSources, VectorReceivers, spread_positions)
+from .vd import AcousticVDStaggeredCPMLWaveSimulation, VpRhoAcousticVDMaterialProperties
 
 __all__ = [
     "AcousticCDCPMLWaveSimulation", "CPMLBoundaryConditionParameters", "GradParameters", "InputParametersAcoustic",
@@ -24,5 +25,5 @@ __all__ = [
     "swgradient", "swmisfit", "_lib", "ArithmeticAverageInterpolation", "ElasticIsoCPMLWaveSimulation",
     "ElasticIsoMaterialProperties", "ExternalForceShot", "ExternalForceSources", "HarmonicAverageInterpolation",
     "InputParametersElastic", "MomentTensor2D", "MomentTensorShot", "MomentTensorSources", "VectorReceivers",
-    "spread_positions",
+    "spread_positions", "AcousticVDStaggeredCPMLWaveSimulation", "VpRhoAcousticVDMaterialProperties",
 ]

@@ -27,6 +27,8 @@ EXPORTS = [
     "sw_profile_read", "sw_acoustic2d_forward_noalloc", "sw_elastic_create", "sw_elastic_destroy",
     "sw_elastic_set_material", "sw_elastic_forward", "sw_elastic_gradient", "sw_elastic_set_tuning",
     "sw_wavesim_use_graphs", "sw_acoustic_forward_snapshots", "sw_elastic_forward_snapshots",
+    "sw_acoustic_vd_create", "sw_acoustic_vd_destroy", "sw_acoustic_vd_set_material", "sw_acoustic_vd_forward",
+    "sw_acoustic_vd_forward_snapshots", "sw_acoustic_vd_gradient", "sw_acoustic_vd_set_tuning",
 ]
 
 i32, f64, vp_ = ctypes.c_int32, ctypes.c_double, ctypes.c_void_p
@@ -111,6 +113,13 @@ def load() -> ctypes.CDLL:
     lib.sw_wavesim_use_graphs.argtypes = [vp_, i32]
     lib.sw_acoustic_forward_snapshots.argtypes = [vp_, i32, P(SwAcousticShot), i32, i32, P(vp_)]
     lib.sw_elastic_forward_snapshots.argtypes = [vp_, i32, P(SwElasticShot), i32, i32, P(vp_)]
+    lib.sw_acoustic_vd_create.argtypes = [vp_, P(SwAcousticParams), i32, i32, P(SwGradParams), P(vp_)]
+    lib.sw_acoustic_vd_destroy.argtypes = [vp_]
+    lib.sw_acoustic_vd_set_material.argtypes = [vp_, vp_, vp_]
+    lib.sw_acoustic_vd_forward.argtypes = [vp_, i32, P(SwAcousticShot), i32]
+    lib.sw_acoustic_vd_forward_snapshots.argtypes = [vp_, i32, P(SwAcousticShot), i32, i32, P(vp_)]
+    lib.sw_acoustic_vd_gradient.argtypes = [vp_, i32, P(SwAcousticShot), i32, vp_, vp_, vp_]
+    lib.sw_acoustic_vd_set_tuning.argtypes = [vp_, i32]
     _lib = lib
     return lib
 

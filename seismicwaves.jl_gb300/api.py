@@ -497,8 +497,14 @@ class AcousticCDCPMLWaveSimulation:
 
 
 def _check_sim_consistency(matprop, shots):
-    """src/utils/checks.jl:2-41 for the acoustic CD and the elastic isotropic 2D cases."""
+    """src/utils/checks.jl:2-41 for the acoustic CD / VD and the elastic isotropic 2D cases."""
     from . import elastic as E
+    from . import vd as V
+    if isinstance(matprop, V.VpRhoAcousticVDMaterialProperties):
+        for s in shots:
+            if not (isinstance(s.srcs, ScalarSources) and isinstance(s.recs, ScalarReceivers)):
+                raise TypeError("Types of shots are inconsistent.")
+        return
     if isinstance(matprop, E.ElasticIsoMaterialProperties):
         kinds = {type(s) for s in shots}
         if len(kinds) != 1:
@@ -518,7 +524,8 @@ def _check_sim_consistency(matprop, shots):
 
 def build_wavesim(params, matprop, *, runparams: RunParameters, gradparams: GradParameters | None = None,
                   gradient: bool | None = None, device: int = 0, sincinterp: bool = True):
-    """src/apis/build.jl:18-95: AcousticCDCPMLWaveSimulation or ElasticIsoCPMLWaveSimulation."""
+    """src/apis/build.jl:18-95: AcousticCDCPMLWaveSimulation, AcousticVDStaggeredCPMLWaveSimulation or
+    ElasticIsoCPMLWaveSimulation."""
     from . import elastic as E
     if gradparams is None and gradient:
         gradparams = GradParameters()
@@ -535,10 +542,13 @@ def build_wavesim(params, matprop, *, runparams: RunParameters, gradparams: Grad
         return E.ElasticIsoCPMLWaveSimulation(params, matprop, params.boundcond, runparams=runparams,
                                               gradparams=gradparams, gradient=bool(gradient), sincinterp=sincinterp,
                                               device=device)
+    from . import vd as V
+    if isinstance(matprop, V.VpRhoAcousticVDMaterialProperties):
+        return V.AcousticVDStaggeredCPMLWaveSimulation(params, matprop, params.boundcond, runparams=runparams,
+                                                       gradparams=gradparams, gradient=bool(gradient), device=device)
     if not isinstance(matprop, VpAcousticCDMaterialProperties):
-        raise NotImplementedError("the GB300 backend implements the acoustic constant-density simulation")
-    if runparams.parall == "threadpersrc":
-        raise ValueError("`parall = :threadpersrc` is a CPU-threads mode; the GB300 backend batches shots itself")
+        raise NotImplementedError("the GB300 backend implements the acoustic constant- and variable-density "
+                                  "and the elastic isotropic simulations")
     return AcousticCDCPMLWaveSimulation(params, matprop, params.boundcond, runparams=runparams,
                                         gradparams=gradparams, gradient=bool(gradient), device=device)
 
@@ -577,7 +587,7 @@ def swgradient(params_or_wavesim, matprop: VpAcousticCDMaterialProperties, shots
                gradparams: GradParameters | None = None):
     """swgradient! (src/apis/gradient.jl:31-136).
 
-    Acoustic: returns {"vp": gradient}; elastic: {"rho": , "lambda": , "mu": }
+    Acoustic CD: returns {"vp": gradient}; acoustic VD: {"vp": , "rho": }; elastic: {"rho": , "lambda": , "mu": }
     (float64), with the summed misfit as a second value when
     gradparams.compute_misfit is true.
     """

@@ -17,7 +17,7 @@ INCLUDE = HERE.parent / "include"
 BUILD = HERE / "_build"
 LIB = HERE / "libswgb300.so"
 
-SOURCES = ["api.cu", "acoustic.cu", "elastic.cu", "cpml.cpp", "noalloc.cu"]
+SOURCES = ["api.cu", "acoustic.cu", "elastic.cu", "vd.cu", "cpml.cpp", "noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -10,6 +10,8 @@ exactly what a SeismicWaves.jl user passes to ScalarSources/ScalarReceivers.
   acoustic2d_801       801 x 801, h = 5 m, gradient + 8 blobs, 1 shot, 401 receivers, nt = 3000, K = 50
   acoustic2d_2001x801  2001 x 801, h = 10 m, 12 layers, 64 shots, 50-300 receivers, nt in [2000, 4000], K = 50
   acoustic3d_400       400^3, h = 10 m, smooth random 1800-4000 m/s, 16 shots, 40 x 40 receivers, nt = 2000, K = 100
+  acoustic_vd2d_2001x801  the acoustic2d_2001x801 model and shots with a density from Gardner's relation
+                       rho = 310 vp^0.25 (kg/m^3) and the variable-density scheme's CFL (7/6 factor)
   elastic2d_1200x600   1200 x 600, h = 5 m, vp 2000-4500, vs = vp/sqrt(3) * U(0.9, 1.0), rho 1800-2700 (smooth
                        seeded fields), 32 explosive moment-tensor shots, 300 receivers, nt = 4000, 15 Hz, K = 50
 """
@@ -45,6 +47,8 @@ class Workload:
     check_freq: int
     shots: list = field(default_factory=list)
     vp_observed: np.ndarray | None = None  # model that generates the observed data
+    rho: np.ndarray | None = None          # variable-density workloads
+    rho_observed: np.ndarray | None = None
 
     @property
     def gridpoints(self):
@@ -160,6 +164,15 @@ def acoustic2d_2001x801(seed: int = 3, nshots: int = 64) -> Workload:
     return Workload("acoustic2d_2001x801", vp, (h, h), dt, 20, False, 50, shots, vp_observed=vobs)
 
 
+def acoustic_vd2d_2001x801(seed: int = 3, nshots: int = 64) -> Workload:
+    w = acoustic2d_2001x801(seed, nshots)
+    w.name = "acoustic_vd2d_2001x801"
+    w.rho = np.asfortranarray(310.0 * w.vp ** 0.25)
+    w.rho_observed = np.asfortranarray(310.0 * w.vp_observed ** 0.25)
+    w.dt = _dt(np.maximum(w.vp, w.vp_observed), w.h) * 6 / 7
+    return w
+
+
 def acoustic3d_400(seed: int = 5, n: int = 400, nshots_side: int = 4, patch: int = 40, nt: int = 2000) -> Workload:
     h = 10.0
     rng = np.random.default_rng(seed)
@@ -241,6 +254,7 @@ WORKLOADS = {
     "acoustic2d_201": acoustic2d_201,
     "acoustic2d_801": acoustic2d_801,
     "acoustic2d_2001x801": acoustic2d_2001x801,
+    "acoustic_vd2d_2001x801": acoustic_vd2d_2001x801,
     "acoustic3d_400": acoustic3d_400,
     "elastic2d_1200x600": elastic2d_1200x600,
 }

@@ -36,6 +36,18 @@ void elastic_forward_snapshots(sw_elastic* es, int nshots, const sw_elastic_shot
 sw_ctx* elastic_ctx(sw_elastic* es);
 sw_elastic* elastic_new();
 void elastic_delete(sw_elastic* es);
+void vd_init(sw_acoustic_vd* vd, sw_ctx* ctx, const sw_acoustic_params* p, int interp, int gradient,
+             const sw_grad_params* gp);
+void vd_set_material(sw_acoustic_vd* vd, const float* vp, const float* rho);
+void vd_forward(sw_acoustic_vd* vd, int nshots, const sw_acoustic_shot* shots, bool on_device);
+void vd_forward_snapshots(sw_acoustic_vd* vd, int nshots, const sw_acoustic_shot* shots, bool on_device, int snapevery,
+                          float* const* snapshots);
+void vd_gradient(sw_acoustic_vd* vd, int nshots, const sw_acoustic_shot* shots, bool on_device, double* g_vp,
+                 double* g_rho, double* misfit);
+void vd_set_tuning(sw_acoustic_vd* vd, int tz);
+sw_ctx* vd_ctx(sw_acoustic_vd* vd);
+sw_acoustic_vd* vd_new();
+void vd_delete(sw_acoustic_vd* vd);
 
 [[noreturn]] void fail(int code, const std::string& msg) { throw SwError{code, msg}; }
 
@@ -395,6 +407,79 @@ int sw_elastic_forward_snapshots(sw_elastic* es, int32_t nshots, const sw_elasti
     swgb::check_cuda(cudaSetDevice(ctx->device), "cudaSetDevice");
     swgb::elastic_forward_snapshots(es, nshots, shots, on_device != 0, snapevery, snapshots);
   });
+}
+
+int sw_acoustic_vd_create(sw_ctx* ctx, const sw_acoustic_params* params, int32_t interp_rho, int32_t gradient,
+                          const sw_grad_params* gparams, sw_acoustic_vd** out) {
+  if (!ctx || !out) return SW_ERR_ARG;
+  *out = nullptr;
+  sw_acoustic_vd* vd = nullptr;
+  const int rc = guarded(ctx, [&] {
+    swgb::check_cuda(cudaSetDevice(ctx->device), "cudaSetDevice");
+    vd = swgb::vd_new();
+    swgb::vd_init(vd, ctx, params, interp_rho, gradient, gparams);
+  });
+  if (rc != SW_OK) {
+    if (vd) swgb::vd_delete(vd);
+    return rc;
+  }
+  *out = vd;
+  return SW_OK;
+}
+
+int sw_acoustic_vd_destroy(sw_acoustic_vd* vd) {
+  if (!vd) return SW_ERR_ARG;
+  sw_ctx* ctx = swgb::vd_ctx(vd);
+  if (ctx) {
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+  }
+  swgb::vd_delete(vd);
+  return SW_OK;
+}
+
+int sw_acoustic_vd_set_material(sw_acoustic_vd* vd, const float* vp, const float* rho) {
+  if (!vd) return SW_ERR_ARG;
+  sw_ctx* ctx = swgb::vd_ctx(vd);
+  return guarded(ctx, [&] {
+    swgb::check_cuda(cudaSetDevice(ctx->device), "cudaSetDevice");
+    swgb::vd_set_material(vd, vp, rho);
+  });
+}
+
+int sw_acoustic_vd_forward(sw_acoustic_vd* vd, int32_t nshots, const sw_acoustic_shot* shots, int32_t on_device) {
+  if (!vd) return SW_ERR_ARG;
+  sw_ctx* ctx = swgb::vd_ctx(vd);
+  return guarded(ctx, [&] {
+    swgb::check_cuda(cudaSetDevice(ctx->device), "cudaSetDevice");
+    swgb::vd_forward(vd, nshots, shots, on_device != 0);
+  });
+}
+
+int sw_acoustic_vd_forward_snapshots(sw_acoustic_vd* vd, int32_t nshots, const sw_acoustic_shot* shots,
+                                     int32_t on_device, int32_t snapevery, float* const* snapshots) {
+  if (!vd) return SW_ERR_ARG;
+  sw_ctx* ctx = swgb::vd_ctx(vd);
+  return guarded(ctx, [&] {
+    swgb::check_cuda(cudaSetDevice(ctx->device), "cudaSetDevice");
+    swgb::vd_forward_snapshots(vd, nshots, shots, on_device != 0, snapevery, snapshots);
+  });
+}
+
+int sw_acoustic_vd_gradient(sw_acoustic_vd* vd, int32_t nshots, const sw_acoustic_shot* shots, int32_t on_device,
+                            double* grad_vp, double* grad_rho, double* misfit) {
+  if (!vd) return SW_ERR_ARG;
+  sw_ctx* ctx = swgb::vd_ctx(vd);
+  return guarded(ctx, [&] {
+    swgb::check_cuda(cudaSetDevice(ctx->device), "cudaSetDevice");
+    swgb::vd_gradient(vd, nshots, shots, on_device != 0, grad_vp, grad_rho, misfit);
+  });
+}
+
+int sw_acoustic_vd_set_tuning(sw_acoustic_vd* vd, int32_t tz) {
+  if (!vd) return SW_ERR_ARG;
+  sw_ctx* ctx = swgb::vd_ctx(vd);
+  return guarded(ctx, [&] { swgb::vd_set_tuning(vd, tz); });
 }
 
 }  // extern "C"
