@@ -24,9 +24,11 @@ def ctx():
     c.close()
 
 
-def _observed(case, shot, scale=1.04):
+def _observed(case, shot, scale=1.10):
     """Observed data from the oracle on a perturbed model, rounded to FP32 (the
-    precision the library takes them in), so both sides see the same data."""
+    precision the library takes them in), so both sides see the same data.  The
+    perturbation keeps the residuals well above the FP32 rounding of the
+    traces, which the misfit (a difference of nearby numbers) would amplify."""
     pert = VDCase(case.vp * scale, case.rho * (2.0 - scale), case.h, case.dt, case.halo, freetop=case.freetop,
                   interp=case.interp, shots=[shot])
     return oracle_forward(pert, shot).astype(np.float32).astype(np.float64)
@@ -102,7 +104,7 @@ def test_vd_gradient_matches_oracle(ctx, freetop, interp, K):
 def test_vd_gradient_windows_invcov_mute(ctx):
     case = small_case(nt=360)
     shot = case.shots[0]
-    obs = _observed(case, shot, 1.06)
+    obs = _observed(case, shot, 1.12)
     ic = np.linspace(0.5, 1.5, shot.nt)
     win = [(20, 150), (200, 330)]
     gref, mref, _ = oracle_gradient(case, shot, obs, check_freq=19, invcov=ic, windows=win, mute_src=6, mute_rec=3)
