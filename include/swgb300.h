@@ -147,6 +147,9 @@ typedef struct {
   const double* rec_pos;    /* (nrec, ndim) metres, muting only (host memory) */
   const float* invcov;      /* gradient: NULL, or the full inverse covariance (nt, nt) column-major
                                (L2Misfit.invcov as a dense matrix); takes precedence over invcov_diag */
+  int32_t misfit_kind;      /* gradient: 0 = L2Misfit, 1 = CCTSMisfit (src/inversion/misfits/CCTSMisfit.jl:17-61;
+                               windows and inverse covariances are then unused, nt <= 13000) */
+  double misfit_dt;         /* CCTSMisfit.dt (misfit_kind 1) */
 } sw_acoustic_shot;
 
 /* GradParameters. */

@@ -53,7 +53,7 @@ def load():
         lib.oracle_acoustic_forward.argtypes = [i, i, P, P, d, i, P, P, i, i, P, P, i, P, P, i]
         lib.oracle_acoustic_forward.restype = i
         lib.oracle_acoustic_gradient.argtypes = [i, i, P, P, d, i, P, P, i, i, P, P, i, P, P, P, i, i, P, i,
-                                                 i, i, P, P, P, P, P, i]
+                                                 i, i, P, P, P, P, P, i, i, d]
         lib.oracle_acoustic_gradient.restype = i
         lib.oracle_max_threads.restype = i
         lib.oracle_spread_positions.argtypes = [P, P, i, P, P, i, i, d, P, P, P, ctypes.c_long]
@@ -78,7 +78,7 @@ def load():
         lib.oracle_vd_forward.argtypes = [i, P, P, d, i, P, P, i, P, i, i, P, P, i, P, P, i, i, P]
         lib.oracle_vd_forward.restype = i
         lib.oracle_vd_gradient.argtypes = [i, P, P, d, i, P, P, i, P, i, i, P, P, i, P, P, P, i, i, P, i, i, i, P,
-                                           P, P, P, P, P, i]
+                                           P, P, P, P, P, i, i, d]
         lib.oracle_vd_gradient.restype = i
         _lib = lib
     return _lib
@@ -137,11 +137,12 @@ def acoustic_forward(vp, h, dt, halo, cpml, srctf, src_idx, rec_idx, *, f32=Fals
 
 def acoustic_gradient(vp, h, dt, halo, cpml, srctf, src_idx, rec_idx, observed, *, invcov=None,
                       windows=(), check_freq=1, mute_src=0, mute_rec=0, src_pos=None, rec_pos=None,
-                      f32=False, nthreads=0):
+                      f32=False, nthreads=0, ccts_dt=None):
     """swgradient_1shot! (CD) plus calcmisfit for one shot.
 
     Returns (grad (shape of vp), misfit, traces).  ``invcov`` may be None
-    (identity), a 1-D diagonal, or a dense (nt, nt) matrix.
+    (identity), a 1-D diagonal, or a dense (nt, nt) matrix.  ``ccts_dt``:
+    CCTSMisfit(ccts_dt) instead of the L2 misfit.
     """
     vp = np.asfortranarray(vp, dtype=np.float64)
     N, n, hh = _grid(vp, h)
@@ -171,7 +172,8 @@ def acoustic_gradient(vp, h, dt, halo, cpml, srctf, src_idx, rec_idx, observed, 
                                          nt, nsrc, _p(src_idx), _p(srctf), nrec, _p(rec_idx), _p(observed),
                                          _p(ic), kind, nwin, _p(win), int(check_freq), int(mute_src),
                                          int(mute_rec), _p(sp), _p(rp), _p(traces), _p(grad), _p(misfit),
-                                         int(nthreads or max_threads()))
+                                         int(nthreads or max_threads()), 0 if ccts_dt is None else 1,
+                                         float(ccts_dt or 0.0))
     if rc != 0:
         raise RuntimeError(f"oracle_acoustic_gradient failed ({rc})")
     return grad, float(misfit[0]), traces
@@ -409,10 +411,10 @@ def vd_forward(vp, rho, h, dt, halo, cpml, srctf, src_idx, rec_idx, *, interp=0,
 
 def vd_gradient(vp, rho, h, dt, halo, cpml, srctf, src_idx, rec_idx, observed, *, interp=0, invcov=None,
                 windows=(), check_freq=1, mute_src=0, mute_rec=0, src_pos=None, rec_pos=None, f32=False,
-                nthreads=0):
+                nthreads=0, ccts_dt=None):
     """swgradient_1shot! of the VD simulation plus calcmisfit for one shot.
 
-    Returns ({"vp": ..., "rho": ...}, misfit, traces).
+    Returns ({"vp": ..., "rho": ...}, misfit, traces).  ``ccts_dt``: CCTSMisfit(ccts_dt).
     """
     vp, rho, n, hh, srctf, src_idx, rec_idx, cpml = _vd_common(vp, rho, h, cpml, srctf, src_idx, rec_idx)
     nt, nsrc = srctf.shape
@@ -438,7 +440,8 @@ def vd_gradient(vp, rho, h, dt, halo, cpml, srctf, src_idx, rec_idx, observed, *
                                    _p(cpml), nt, nsrc, _p(src_idx), _p(srctf), nrec, _p(rec_idx), _p(observed),
                                    _p(ic), kind, nwin, _p(win), int(check_freq), int(mute_src), int(mute_rec),
                                    _p(sp), _p(rp), _p(traces), _p(gvp), _p(grho), _p(misfit),
-                                   int(nthreads or max_threads()))
+                                   int(nthreads or max_threads()), 0 if ccts_dt is None else 1,
+                                   float(ccts_dt or 0.0))
     if rc != 0:
         raise RuntimeError(f"oracle_vd_gradient failed ({rc})")
     return {"vp": gvp, "rho": grho}, float(misfit[0]), traces

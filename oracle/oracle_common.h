@@ -101,6 +101,35 @@ inline void back_interp(const double* m, int nx, int nz, const double* g, int gx
     }
 }
 
+// ---------------------------------------------------------------------------
+// CCTSMisfit for one trace, CCTSMisfit.jl:17-61 (scalar receivers).
+// xcorr(u, v) (DSP.jl: conv(u, reverse(v)), length 2 nt - 1) has at 1-based
+// index k the value sum_i u[i] v[i - (k - nt)]; the reference takes the first
+// k of the largest |xcorr(observed, synthetic)| and dtau = (k - (nt - 1)) dt.
+// Returns dtau^2 / 2 and writes dchi/du = dtau / N * ds/dt with ds/dt the
+// central difference (first sample (s[2] - 0) / 2dt, last sample 0) and N the
+// trapezoidal integral of (ds/dt)^2 over the times dt, 2 dt, ..., nt dt
+// (NumericalIntegration.integrate).
+// ---------------------------------------------------------------------------
+inline double ccts_trace(const double* obs, const double* syn, int nt, double dt, double* dchi) {
+  int kbest = 1;
+  double best = -1.0;
+  for (int k = 1; k <= 2 * nt - 1; ++k) {
+    const int L = k - nt;
+    double c = 0.0;
+    for (int i = std::max(1, 1 + L); i <= std::min(nt, nt + L); ++i) c += obs[i - 1] * syn[i - 1 - L];
+    if (std::fabs(c) > best) { best = std::fabs(c); kbest = k; }
+  }
+  const double dtau = (double)(kbest - (nt - 1)) * dt;
+  std::vector<double> ds(nt, 0.0);
+  for (int t = 2; t <= nt - 1; ++t) ds[t - 1] = (syn[t] - syn[t - 2]) / (2.0 * dt);
+  if (nt >= 2) ds[0] = (syn[1] - 0.0) / (2.0 * dt);
+  double norm = 0.0;
+  for (int t = 1; t <= nt - 1; ++t) norm += dt * (ds[t - 1] * ds[t - 1] + ds[t] * ds[t]) / 2.0;
+  for (int t = 0; t < nt; ++t) dchi[t] = (dtau / norm) * ds[t];
+  return dtau * dtau / 2.0;
+}
+
 template <typename T>
 using Snap = std::vector<std::vector<T>>;
 

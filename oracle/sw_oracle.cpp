@@ -288,7 +288,8 @@ int run_gradient(int N, const int* n, const double* h, double dt, int halo, cons
                  int nrec, const int* rec_idx, const double* observed, const double* invcov,
                  int invcov_kind, int nwin, const int* windows, int check_freq,
                  int mute_src, int mute_rec, const double* src_pos, const double* rec_pos,
-                 double* traces_out, double* grad_out, double* misfit_out, int nthreads) {
+                 double* traces_out, double* grad_out, double* misfit_out, int nthreads, int misfit_kind,
+                 double misfit_dt) {
   if (check_freq < 1 || check_freq >= nt) return 1;  // LinearCheckpointer assertion
   AcousticSim<T> sim(N, n, h, halo, nthreads);
   prepare_sim(sim, vp, dt, cpml);
@@ -365,6 +366,15 @@ int run_gradient(int N, const int* n, const double* h, double dt, int halo, cons
   double msf = 0;
   for (long q = 0; q < (long)nt * nrec; ++q) msf += res[q] * cres[q];
   *misfit_out = msf / 2;
+  if (misfit_kind == 1) {  // CCTSMisfit: dchi/du per trace instead
+    std::vector<double> syn(nt);
+    double m = 0.0;
+    for (int r = 0; r < nrec; ++r) {
+      for (int t = 0; t < nt; ++t) syn[t] = (double)tr[t + (long)r * nt];
+      m += oracle::ccts_trace(observed + (long)r * nt, syn.data(), nt, misfit_dt, cres.data() + (long)r * nt);
+    }
+    *misfit_out = m;
+  }
 
   // adjoint source = -dchi/du, prescaled by fact at the receivers (acoustic2D_xPU.jl:64-76)
   std::vector<T> adjsrc((long)nt * nrec);
@@ -466,15 +476,15 @@ int oracle_acoustic_gradient(int use_f32, int N, const int* n, const double* h, 
                              const double* invcov, int invcov_kind, int nwin, const int* windows,
                              int check_freq, int mute_src, int mute_rec, const double* src_pos,
                              const double* rec_pos, double* traces_out, double* grad_out,
-                             double* misfit_out, int nthreads) {
+                             double* misfit_out, int nthreads, int misfit_kind, double misfit_dt) {
   if (N != 2 && N != 3) return 1;
   if (use_f32)
     return run_gradient<float>(N, n, h, dt, halo, vp, cpml, nt, nsrc, src_idx, srctf, nrec, rec_idx, observed,
                                invcov, invcov_kind, nwin, windows, check_freq, mute_src, mute_rec, src_pos,
-                               rec_pos, traces_out, grad_out, misfit_out, nthreads);
+                               rec_pos, traces_out, grad_out, misfit_out, nthreads, misfit_kind, misfit_dt);
   return run_gradient<double>(N, n, h, dt, halo, vp, cpml, nt, nsrc, src_idx, srctf, nrec, rec_idx, observed,
                               invcov, invcov_kind, nwin, windows, check_freq, mute_src, mute_rec, src_pos,
-                              rec_pos, traces_out, grad_out, misfit_out, nthreads);
+                              rec_pos, traces_out, grad_out, misfit_out, nthreads, misfit_kind, misfit_dt);
 }
 
 }  // extern "C"

@@ -266,7 +266,7 @@ int run_gradient(const int* n, const double* h, double dt, int halo, const doubl
                  const double* cpml, const VDShot& sh, const double* observed, const double* invcov, int invcov_kind,
                  int nwin, const int* windows, int check_freq, int mute_src, int mute_rec, const double* src_pos,
                  const double* rec_pos, double* traces_out, double* g_vp, double* g_rho, double* misfit_out,
-                 int nthreads) {
+                 int nthreads, int misfit_kind, double misfit_dt) {
   const int nt = sh.nt, nx = n[0], nz = n[1];
   if (check_freq < 1 || check_freq >= nt) return 1;  // LinearCheckpointer assertion
   VDSim<T> sim(nx, nz, h, dt, halo, nthreads), adj(nx, nz, h, dt, halo, nthreads);
@@ -326,6 +326,15 @@ int run_gradient(const int* n, const double* h, double dt, int halo, const doubl
   double msf = 0;
   for (long q = 0; q < ntot; ++q) msf += res[q] * cres[q];
   *misfit_out = msf / 2;
+  if (misfit_kind == 1) {  // CCTSMisfit (CCTSMisfit.jl:17-61): dchi/du per trace instead
+    std::vector<double> syn(nt);
+    double m = 0.0;
+    for (int r = 0; r < sh.nrec; ++r) {
+      for (int t = 0; t < nt; ++t) syn[t] = (double)tr[t + (long)r * nt];
+      m += oracle::ccts_trace(observed + (long)r * nt, syn.data(), nt, misfit_dt, cres.data() + (long)r * nt);
+    }
+    *misfit_out = m;
+  }
   // adjoint source -C^-1 r, prescaled by fact_m0 at the receivers (acou_gradient.jl:146-150)
   std::vector<T> adjsrc(ntot);
   for (int r = 0; r < sh.nrec; ++r) {
@@ -437,23 +446,25 @@ int oracle_vd_forward(int use_f32, const int* n, const double* h, double dt, int
 }
 
 // swgradient_1shot! of the VD simulation plus calcmisfit for one shot.
-// invcov_kind: 0 identity, 1 diagonal (nt), 2 dense (nt, nt).
+// invcov_kind: 0 identity, 1 diagonal (nt), 2 dense (nt, nt).  misfit_kind 1:
+// CCTSMisfit with time step misfit_dt (windows and invcov then unused).
 int oracle_vd_gradient(int use_f32, const int* n, const double* h, double dt, int halo, const double* vp,
                        const double* rho, int method, const double* cpml, int nt, int nsrc, const int* src_idx,
                        const double* srctf, int nrec, const int* rec_idx, const double* observed,
                        const double* invcov, int invcov_kind, int nwin, const int* windows, int check_freq,
                        int mute_src, int mute_rec, const double* src_pos, const double* rec_pos, double* traces_out,
-                       double* g_vp, double* g_rho, double* misfit_out, int nthreads) {
+                       double* g_vp, double* g_rho, double* misfit_out, int nthreads, int misfit_kind,
+                       double misfit_dt) {
   if (n[0] < 4 || n[1] < 4) return 1;
   const VDShot sh = make_shot(nt, nsrc, src_idx, srctf, nrec, rec_idx);
   if (bad_indices(n, sh)) return 2;
   if (use_f32)
     return run_gradient<float>(n, h, dt, halo, vp, rho, method, cpml, sh, observed, invcov, invcov_kind, nwin, windows,
                                check_freq, mute_src, mute_rec, src_pos, rec_pos, traces_out, g_vp, g_rho, misfit_out,
-                               nthreads);
+                               nthreads, misfit_kind, misfit_dt);
   return run_gradient<double>(n, h, dt, halo, vp, rho, method, cpml, sh, observed, invcov, invcov_kind, nwin, windows,
                               check_freq, mute_src, mute_rec, src_pos, rec_pos, traces_out, g_vp, g_rho, misfit_out,
-                              nthreads);
+                              nthreads, misfit_kind, misfit_dt);
 }
 
 }  // extern "C"

@@ -7,7 +7,7 @@ import it through ``load_package()`` in ``__graft_entry__`` (or any
 importlib loader) under the module name ``seismicwaves_gb300``.
 """
 from . import _lib
-from .api import (AcousticCDCPMLWaveSimulation, CPMLBoundaryConditionParameters, GradParameters,
+from .api import (AcousticCDCPMLWaveSimulation, CCTSMisfit, CPMLBoundaryConditionParameters, GradParameters,
                   InputParametersAcoustic, L2Misfit, RunParameters, ScalarReceivers, ScalarShot, ScalarSources,
                   UniformFiniteDifferenceGrid, VpAcousticCDMaterialProperties, build_wavesim, courant_number, gaussderivstf,
                   gaussstf, nearest_grid_points, points_per_wavelength, rickerstf, scale_srctf,
@@ -18,7 +18,7 @@ from .elastic import (ArithmeticAverageInterpolation, ElasticIsoCPMLWaveSimulati
 from .vd import AcousticVDStaggeredCPMLWaveSimulation, VpRhoAcousticVDMaterialProperties
 
 __all__ = [
-    "AcousticCDCPMLWaveSimulation", "CPMLBoundaryConditionParameters", "GradParameters", "InputParametersAcoustic",
+    "AcousticCDCPMLWaveSimulation", "CCTSMisfit", "CPMLBoundaryConditionParameters", "GradParameters", "InputParametersAcoustic",
     "L2Misfit", "RunParameters", "ScalarReceivers", "ScalarShot", "ScalarSources", "UniformFiniteDifferenceGrid",
     "VpAcousticCDMaterialProperties", "build_wavesim", "courant_number", "nearest_grid_points",
     "points_per_wavelength", "scale_srctf", "gaussderivstf", "gaussstf", "rickerstf", "swforward",

@@ -43,7 +43,7 @@ class SwAcousticShot(ctypes.Structure):
     _fields_ = [("nt", i32), ("nsrc", i32), ("src_idx", vp_), ("srctf", vp_), ("nrec", i32),
                 ("rec_idx", vp_), ("traces", vp_), ("cpml", vp_), ("observed", vp_),
                 ("invcov_diag", vp_), ("nwin", i32), ("windows", vp_), ("src_pos", vp_), ("rec_pos", vp_),
-                ("invcov", vp_)]
+                ("invcov", vp_), ("misfit_kind", i32), ("misfit_dt", f64)]
 
 
 class SwGradParams(ctypes.Structure):

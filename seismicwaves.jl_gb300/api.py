@@ -6,7 +6,7 @@ v0.9.0); the Julia functions ending in ``!`` keep their behaviour (they fill
 
     InputParametersAcoustic, CPMLBoundaryConditionParameters, RunParameters,
     GradParameters, VpAcousticCDMaterialProperties, ScalarSources,
-    ScalarReceivers, ScalarShot, L2Misfit, rickerstf, build_wavesim,
+    ScalarReceivers, ScalarShot, L2Misfit, CCTSMisfit, rickerstf, build_wavesim,
     swforward (swforward!), swmisfit (swmisfit!), swgradient (swgradient!)
 
 Host logic kept from the reference: CFL and points-per-wavelength checks
@@ -197,6 +197,65 @@ class L2Misfit:
     def dchi_du(self, recs):
         """L2Misfit.jl:64-95: C^-1 r."""
         return self._apply_invcov(self._masked_residuals(recs.seismograms))
+
+
+class CCTSMisfit:
+    """src/inversion/misfits/CCTSMisfit.jl:1-15: cross-correlation time-shift misfit.
+
+    Per trace, dtau = (first index of max |xcorr(observed, synthetic)| - (nt - 1)) * dt
+    with DSP.jl's xcorr (conv(u, reverse(v)), 1-based index k holding
+    sum_i u[i] v[i - (k - nt)]); the misfit is sum dtau^2 / 2 and dchi/du =
+    dtau / N * ds/dt (CCTSMisfit.jl:17-80).  ``std`` is stored, as in the
+    reference, and not used.  The gradient evaluates it on the GPU (k_ccts);
+    these host versions serve swmisfit and checks.
+    """
+    kind = 1
+
+    def __init__(self, dt: float, std: float = 1.0, observed=None):
+        observed = np.zeros((0, 0)) if observed is None else np.asarray(observed)
+        if observed.ndim not in (2, 3):
+            raise ValueError("Observed data must be a 2D or 3D array!")
+        assert dt > 0, "Timestep size must be positive!"
+        assert std > 0, "Standard deviation must be positive!"
+        self.dt, self.std = float(dt), float(std)
+        self.observed = observed.copy()
+        self.windows = []
+        self.invcov = None
+
+    def invcov_diagonal(self):
+        return None
+
+    def invcov_dense(self):
+        return None
+
+    def _traces(self, seismograms):
+        s = np.asarray(seismograms, dtype=np.float64)
+        o = np.asarray(self.observed, dtype=np.float64)
+        nt = s.shape[0]
+        return s.reshape(nt, -1, order="F"), o.reshape(nt, -1, order="F"), s.shape
+
+    def _dtau(self, obs, syn):
+        # numpy's correlate(a, v, "full")[k0] = sum_n a[n + k0 - (nt - 1)] v[n] = DSP xcorr(a, v)[k0 + 1]
+        c = np.correlate(obs, syn, "full")
+        return (int(np.argmax(np.abs(c))) + 1 - (len(syn) - 1)) * self.dt
+
+    def calcmisfit(self, recs) -> float:
+        s, o, _ = self._traces(recs.seismograms)
+        return float(sum(self._dtau(o[:, r], s[:, r]) ** 2 / 2 for r in range(s.shape[1])))
+
+    def dchi_du(self, recs):
+        s, o, shape = self._traces(recs.seismograms)
+        nt, dt = s.shape[0], self.dt
+        ds = np.zeros_like(s)
+        ds[1:-1] = (s[2:] - s[:-2]) / (2 * dt)
+        ds[0] = (s[1] - 0) / (2 * dt)
+        out = np.zeros_like(s)
+        for r in range(s.shape[1]):
+            dtau = self._dtau(o[:, r], s[:, r])
+            y = ds[:, r] ** 2
+            norm = float(np.sum(dt * (y[:-1] + y[1:]) / 2))
+            out[:, r] = dtau / norm * ds[:, r]
+        return out.reshape(shape, order="F")
 
 
 @dataclass
@@ -427,6 +486,8 @@ class AcousticCDCPMLWaveSimulation:
                 assert obs.shape == (nt, posrecs.shape[0]), "observed data shape must be (nt, nrec)"
                 st.observed = obs.ctypes.data
                 arrs.append(obs)
+                if isinstance(m, CCTSMisfit):
+                    st.misfit_kind, st.misfit_dt = 1, m.dt
                 diag = m.invcov_diagonal()
                 if diag is not None:
                     diag = np.ascontiguousarray(diag, dtype=np.float32)

@@ -35,6 +35,7 @@
 
 #include "acoustic_kernels.cuh"
 #include "internal.h"
+#include "ccts.cuh"
 
 namespace swgb {
 
@@ -58,6 +59,7 @@ struct ShotDesc {
   const float* icd;          // dense inverse covariance (nt, nt) or nullptr
   float* resid;              // dense case: masked residuals (nt, nrec)
   const float* cres;         // dense case: C^-1 r (nt, nrec), from cuBLAS
+  int mkind;                 // 0 L2, 1 CCTS (k_ccts writes this shot's adjoint source)
 };
 
 // Boundary injection points.  The reference never updates the outermost grid
@@ -195,7 +197,7 @@ __global__ void k_misfit_adjsrc(const ShotDesc* __restrict__ desc, const long lo
                                 const float* __restrict__ fact, double* __restrict__ partial) {
   const int shot = blockIdx.y;
   const ShotDesc D = desc[shot];
-  const long long total = (long long)D.nt * D.nrec;
+  const long long total = D.mkind == 1 ? 0 : (long long)D.nt * D.nrec;  // CCTS shots: k_ccts
   double acc = 0.0;
   for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < total;
        q += (long long)gridDim.x * blockDim.x) {
@@ -386,6 +388,7 @@ struct sw_wavesim {
   DevMem zero;                         // zero state (one shot, stride 0)
   // tables
   DevMem d_desc, d_pts, d_ptr, d_ids, d_bslot, d_rec, d_tf, d_tr, d_obs, d_ic, d_mask, d_adj, d_cpml, d_partial, d_mis;
+  DevMem d_ccts, d_partial2;  // CCTS descriptors and per-trace misfit terms
   DevMem d_ring;  // boundary-injection rings (3 floats per point)
   DevMem d_icd, d_dres;  // dense inverse covariances; residuals and C^-1 r of those shots
   DevMem d_mute, d_mute_ptr;
@@ -592,6 +595,7 @@ void validate_shot(const sw_wavesim* ws, const sw_acoustic_shot& s, int k, bool 
         fail(SW_ERR_ARG, os.str());
       }
     }
+    validate_misfit_kind(s, k);
   }
 }
 
@@ -611,7 +615,7 @@ void build_tables(sw_wavesim* ws, const sw_acoustic_shot* shots, const std::vect
     tf_total += (long long)s.nt * s.nsrc;
     tr_total += (long long)s.nt * s.nrec;
     if (s.invcov_diag) ic_total += s.nt;
-    if (grad && s.invcov) {
+    if (grad && s.invcov && s.misfit_kind == 0) {
       icd_total += (long long)s.nt * s.nt;
       dres_total += (long long)s.nt * s.nrec;
     }
@@ -678,7 +682,8 @@ void build_tables(sw_wavesim* ws, const sw_acoustic_shot* shots, const std::vect
       }
     }
     D.tr = ws->d_tr.as<float>() + tr_o;
-    if (grad && s.invcov) {
+    D.mkind = grad ? s.misfit_kind : 0;
+    if (grad && s.invcov && s.misfit_kind == 0) {
       if (on_device) {
         D.icd = s.invcov;
       } else {
@@ -1461,7 +1466,30 @@ void acoustic_gradient(sw_wavesim* ws, int nshots, const sw_acoustic_shot* shots
     ensure(ws, ws->d_partial, (size_t)nblk * S * sizeof(double), "misfit partials");
     const bool accumulate = !first_group;
     bool any_dense = false;
-    for (const auto& h : group) any_dense = any_dense || shots[h.orig].invcov;
+    for (const auto& h : group) any_dense = any_dense || (shots[h.orig].invcov && shots[h.orig].misfit_kind == 0);
+    size_t ccts_smem = 0;
+    int ccts_rec = 0;
+    {
+      std::vector<int> kind(S), nt(S), nrec(S);
+      std::vector<double> mdt(S);
+      std::vector<const float*> tr(S), obs(S);
+      std::vector<float*> adj(S);
+      std::vector<const long long*> rl(S);
+      for (int k = 0; k < S; ++k) {
+        const sw_acoustic_shot& s = shots[group[k].orig];
+        kind[k] = s.misfit_kind;
+        mdt[k] = s.misfit_dt;
+        nt[k] = T.desc[k].nt;
+        nrec[k] = T.desc[k].nrec;
+        tr[k] = T.desc[k].tr;
+        obs[k] = T.desc[k].obs;
+        adj[k] = T.desc[k].adj;
+        rl[k] = ws->d_rec.as<long long>() + T.desc[k].rec_off;
+      }
+      ensure(ws, ws->d_ccts, (size_t)S * sizeof(CctsShot), "CCTS table");
+      ccts_rec = upload_ccts(ws->ctx, ws->d_ccts.as<CctsShot>(), kind, mdt, nt, nrec, tr, obs, adj, rl, &ccts_smem);
+      if (ccts_rec) ensure(ws, ws->d_partial2, (size_t)ccts_rec * S * sizeof(double), "CCTS partials");
+    }
     auto misfit_and_adjsrc = [&] {
       cudaEvent_t ev = nullptr;
       if (any_dense) {  // C^-1 r of the shots with a dense inverse covariance (cuBLAS)
@@ -1480,6 +1508,13 @@ void acoustic_gradient(sw_wavesim* ws, int nshots, const sw_acoustic_shot* shots
       ws->ctx->prof.begin(st, KK_OTHER, 0.0, &ev);
       k_misfit_sum<<<1, 256, 0, st>>>(ws->d_partial.as<double>(), nblk, S, mout, accumulate ? 1 : 0);
       check_cuda(cudaGetLastError(), "misfit sum launch");
+      if (ccts_rec) {
+        k_ccts<<<dim3(ccts_rec, S), CCTS_THREADS, ccts_smem, st>>>(ws->d_ccts.as<CctsShot>(), ws->fact.as<float>(),
+                                                                   ws->d_partial2.as<double>());
+        check_cuda(cudaGetLastError(), "CCTS misfit launch");
+        k_misfit_sum<<<1, 256, 0, st>>>(ws->d_partial2.as<double>(), ccts_rec, S, mout, 1);
+        check_cuda(cudaGetLastError(), "CCTS misfit sum launch");
+      }
       ws->ctx->prof.end(st, KK_OTHER, ev);
     };
     auto reduce = [&] {
@@ -1496,6 +1531,7 @@ void acoustic_gradient(sw_wavesim* ws, int nshots, const sw_acoustic_shot* shots
     if (!mute && !any_dense) {
       // the whole group -- forward, misfit, adjoint, shot sum -- as one graph
       std::vector<long long> key = group_key(ws, group, true);
+      for (const auto& h : group) key.push_back(shots[h.orig].misfit_kind);
       key.insert(key.end(), {accumulate ? 1 : 0, (long long)(uintptr_t)gout, (long long)(uintptr_t)mout});
       run_graph(ws, key, [&] {
         forward_group(ws, group, true);

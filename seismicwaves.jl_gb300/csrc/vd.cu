@@ -47,6 +47,7 @@
 #include <vector>
 
 #include "internal.h"
+#include "ccts.cuh"
 
 namespace swgb {
 namespace vd {
@@ -382,6 +383,7 @@ struct ShotDesc {
   const float* icd;             // dense inverse covariance (nt, nt) or null
   float* resid;                 // dense case: masked residuals
   const float* cres;            // dense case: C^-1 r
+  int mkind;                    // 0 L2, 1 CCTS (k_ccts writes this shot's adjoint source)
 };
 
 // inject_sources! then record_receivers! (the velocity update in between does
@@ -443,7 +445,7 @@ __global__ void k_vd_misfit(const ShotDesc* __restrict__ desc, const float* __re
                             double* __restrict__ partial) {
   const int shot = blockIdx.y;
   const ShotDesc D = desc[shot];
-  const long long total = (long long)D.nt * D.nrec;
+  const long long total = D.mkind == 1 ? 0 : (long long)D.nt * D.nrec;  // CCTS shots: k_ccts
   double acc = 0.0;
   for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < total; q += (long long)gridDim.x * blockDim.x) {
     const int t = (int)(q % D.nt);
@@ -625,7 +627,7 @@ struct sw_acoustic_vd {
   DevMem acc;                  // [cap][3][F]
   DevMem tot;                  // [groups][3][F] double
   DevMem d_desc, d_ll, d_int, d_flt, d_tf, d_tr, d_obs, d_ic, d_adj, d_cp, d_partial, d_balls, d_ball_ptr;
-  DevMem d_icd, d_dres, d_snap;
+  DevMem d_icd, d_dres, d_snap, d_ccts, d_partial2;
   int snapevery = 0;
   float* const* snap_out = nullptr;
   int tz = 8;
@@ -679,6 +681,7 @@ void validate_shot(const sw_acoustic_vd* vd, const sw_acoustic_shot& s, int k, b
       if (!(1 <= a && a <= b && b <= s.nt))
         fail(SW_ERR_ARG, "Windows indices must be between 1 and maximum number of timesteps!");
     }
+    validate_misfit_kind(s, k);
   }
 }
 
@@ -838,7 +841,7 @@ void build_tables(sw_acoustic_vd* vd, const sw_acoustic_shot* shots, const std::
   std::vector<long long> ic_off(S, -1);
   for (int k = 0; k < S; ++k) {
     const sw_acoustic_shot& s = shots[group[k].orig];
-    if (grad && s.invcov) {
+    if (grad && s.invcov && s.misfit_kind == 0) {
       icd_total += (long long)s.nt * s.nt;
       dres_total += (long long)s.nt * s.nrec;
     } else if (grad && s.invcov_diag) {
@@ -896,7 +899,8 @@ void build_tables(sw_acoustic_vd* vd, const sw_acoustic_shot* shots, const std::
       D.adj = vd->d_adj.as<float>() + tr_off[k];
       D.ic = ic_off[k] >= 0 ? vd->d_ic.as<float>() + ic_off[k] : nullptr;
       D.mask = o.has_mask ? FL + o.mask : nullptr;
-      if (s.invcov) {
+      D.mkind = s.misfit_kind;
+      if (s.invcov && s.misfit_kind == 0) {
         if (on_device) {
           D.icd = s.invcov;
         } else {
@@ -1360,6 +1364,34 @@ void vd_gradient(sw_acoustic_vd* vd, int nshots, const sw_acoustic_shot* shots, 
       check_cuda(cudaGetLastError(), "misfit launch");
       k_vd_misfit_sum<<<1, 256, 0, st>>>(vd->d_partial.as<double>(), nblk * S, mout, first_group ? 0 : 1);
       check_cuda(cudaGetLastError(), "misfit sum launch");
+      // CCTS shots: misfit and adjoint source from the cross-correlation time shift
+      std::vector<int> kind(S), ntv(S), nrec(S);
+      std::vector<double> mdt(S);
+      std::vector<const float*> tr(S), obs(S);
+      std::vector<float*> adj(S);
+      std::vector<const long long*> rl(S);
+      for (int k = 0; k < S; ++k) {
+        const sw_acoustic_shot& s = shots[group[k].orig];
+        kind[k] = s.misfit_kind;
+        mdt[k] = s.misfit_dt;
+        ntv[k] = desc[k].nt;
+        nrec[k] = desc[k].nrec;
+        tr[k] = desc[k].tr;
+        obs[k] = desc[k].obs;
+        adj[k] = desc[k].adj;
+        rl[k] = desc[k].rec_lin;
+      }
+      ensure(vd, vd->d_ccts, (size_t)S * sizeof(CctsShot), "CCTS table");
+      size_t smem = 0;
+      const int crec = upload_ccts(vd->ctx, vd->d_ccts.as<CctsShot>(), kind, mdt, ntv, nrec, tr, obs, adj, rl, &smem);
+      if (crec) {
+        ensure(vd, vd->d_partial2, (size_t)crec * S * sizeof(double), "CCTS partials");
+        k_ccts<<<dim3(crec, S), CCTS_THREADS, smem, st>>>(vd->d_ccts.as<CctsShot>(), vd->m0.as<float>(),
+                                                          vd->d_partial2.as<double>());
+        check_cuda(cudaGetLastError(), "CCTS misfit launch");
+        k_vd_misfit_sum<<<1, 256, 0, st>>>(vd->d_partial2.as<double>(), crec * S, mout, 1);
+        check_cuda(cudaGetLastError(), "CCTS misfit sum launch");
+      }
       vd->ctx->prof.end(st, KK_OTHER, ev);
     }
     // adjoint with recompute, fused correlation and window flushes

@@ -449,6 +449,8 @@ class ElasticIsoCPMLWaveSimulation:
     def run_gradient(self, shots, misfits):
         assert self.gradient, "The wavesim object was not built for gradient computations. (Was `gradient=true` specified?)"
         assert len(misfits) == len(shots)
+        if any(getattr(m, "kind", 0) == 1 for m in misfits):
+            raise NotImplementedError("the GB300 elastic gradient takes the L2 misfit (CCTSMisfit: acoustic paths)")
         self.init_shots(shots)
         structs, keep = self._shot_structs(shots, misfits)
         g = {k: np.zeros(self.grid.size, dtype=np.float64, order="F") for k in ("rho", "lambda", "mu")}

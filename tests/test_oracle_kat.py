@@ -146,3 +146,48 @@ def test_fp32_restatement_error_budget(oracle):
     a = oracle.acoustic_forward(vp, (h, h), dt, 20, cp, scal, si, ri)
     b = oracle.acoustic_forward(vp, (h, h), dt, 20, cp, scal, si, ri, f32=True)
     assert np.linalg.norm(a - b) / np.linalg.norm(a) < 1e-5
+
+
+# --------------------------------------------------------------------------- CCTS misfit
+def test_ccts_time_shift_known_answer(oracle):
+    """A wavelet delayed by L samples gives dtau = (L + 1) dt: the reference's
+    (argmax - (nt - 1)) indexing of DSP's 1-based xcorr (CCTSMisfit.jl:23).
+    The host mirror and the oracle agree on misfit and adjoint source."""
+    import __graft_entry__
+
+    sw = __graft_entry__.load_package()
+    nt, dt, f0 = 400, 1e-3, 25.0
+    t = np.arange(nt) * dt
+    syn = np.stack([ricker(t, 0.1, f0), 0.5 * ricker(t, 0.15, f0)], 1)
+    shifts = (7, -4)
+    obs = np.stack([np.roll(syn[:, r], s) for r, s in enumerate(shifts)], 1)
+    m = sw.CCTSMisfit(dt, observed=obs)
+    recs = sw.ScalarReceivers(np.zeros((2, 2)), nt)
+    recs.seismograms[...] = syn
+    want = sum(((s + 1) * dt) ** 2 / 2 for s in shifts)
+    assert m.calcmisfit(recs) == pytest.approx(want, rel=1e-12)
+    g = m.dchi_du(recs)
+    assert np.sign(g[np.argmax(np.abs(g[:, 0])), 0]) != 0 and g.shape == syn.shape
+
+
+def test_ccts_gradient_misfit_consistency(oracle):
+    """2D counterpart of the reference's CCTS gradient test
+    (test_gradient_acoustic_constant_density.jl:53-86): non-zero gradient and
+    the gradient run's misfit == CCTS misfit of a forward run (host mirror)."""
+    import __graft_entry__
+
+    sw = __graft_entry__.load_package()
+    c0, f0 = 2000.0, 10.0
+    n, h, nt = (101, 101), (10.0, 10.0), 600
+    dt = 0.99 * 10.0 / c0 / np.sqrt(2)
+    vp, srctf, possrc, posrec = _const_setup(n, h, c0, f0, nt, dt)
+    si, ri = _nearest(possrc, h), _nearest(posrec, h)
+    cp = oracle.cpml_blocks(vp, h, dt, 20, 1e-4, f0, False)
+    scal = _scaled(srctf, si, vp, h, dt)
+    observed = srctf.copy()
+    g, m, tr = oracle.acoustic_gradient(vp, h, dt, 20, cp, scal, si, ri, observed, check_freq=24, ccts_dt=dt)
+    assert np.any(g != 0) and m > 0
+    mis = sw.CCTSMisfit(dt, observed=observed)
+    recs = sw.ScalarReceivers(posrec, nt)
+    recs.seismograms[...] = tr
+    assert m == pytest.approx(mis.calcmisfit(recs), rel=1e-12)

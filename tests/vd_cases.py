@@ -80,12 +80,13 @@ def oracle_forward(case, shot, f32=False, snapevery=0):
 
 
 def oracle_gradient(case, shot, observed, *, check_freq=1, invcov=None, windows=(), mute_src=0, mute_rec=0,
-                    f32=False):
+                    f32=False, ccts_dt=None):
     import oracle
     return oracle.vd_gradient(case.vp, case.rho, (case.h, case.h), case.dt, case.halo, cpml(case, shot),
                               scaled_tf(case, shot), nearest(shot.src, case.h), nearest(shot.rec, case.h),
                               observed, interp=case.interp, invcov=invcov, windows=windows, check_freq=check_freq,
-                              mute_src=mute_src, mute_rec=mute_rec, src_pos=shot.src, rec_pos=shot.rec, f32=f32)
+                              mute_src=mute_src, mute_rec=mute_rec, src_pos=shot.src, rec_pos=shot.rec, f32=f32,
+                              ccts_dt=ccts_dt)
 
 
 class GpuVD:
@@ -116,7 +117,7 @@ class GpuVD:
             self.ctx.lib.sw_acoustic_vd_destroy(self.h)
             self.h = ctypes.c_void_p()
 
-    def _structs(self, shots, observed=None, invcov=None, windows=None):
+    def _structs(self, shots, observed=None, invcov=None, windows=None, ccts_dt=None):
         L = sw._lib
         keep, structs = [], (L.SwAcousticShot * len(shots))()
         for k, shot in enumerate(shots):
@@ -151,6 +152,8 @@ class GpuVD:
                 rpp = np.asfortranarray(shot.rec, dtype=np.float64)
                 st.src_pos, st.rec_pos = spp.ctypes.data, rpp.ctypes.data
                 arrs += [spp, rpp]
+                if ccts_dt is not None:
+                    st.misfit_kind, st.misfit_dt = 1, float(ccts_dt)
             keep.append((tr, arrs))
         return structs, keep
 
@@ -178,8 +181,8 @@ class GpuVD:
             out.append(snaps)
         return [k[0].astype(np.float64) for k in keep], out
 
-    def gradient(self, shots, observed, invcov=None, windows=None):
-        structs, keep = self._structs(shots, observed, invcov, windows)
+    def gradient(self, shots, observed, invcov=None, windows=None, ccts_dt=None):
+        structs, keep = self._structs(shots, observed, invcov, windows, ccts_dt)
         nx, nz = self.case.vp.shape
         g = {k: np.zeros((nx, nz), dtype=np.float64, order="F") for k in ("vp", "rho")}
         m = np.zeros(1)
