@@ -491,8 +491,12 @@ def measure_vd(a, name="acoustic_vd2d_2001x801", shots=0, nt_cap=0, steps=None, 
     ms_tot, launches, bytes_tot = prof[dom]
     achieved = bytes_tot / (ms_tot / 1e3) / 1e9 if ms_tot > 0 else None
     peak, peak_kind = _peak()
+    traffic_per_shot = _traffic_from_profiles("k_vd_v + k_vd_p<corr> adjoint", w.name) if dom == 1 else None
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-            "frac": achieved / peak if achieved else None, "traffic": None, "kernel": VD_KINDS[dom],
+            "frac": achieved / peak if achieved else None,
+            "traffic": traffic_per_shot * nshots if traffic_per_shot else None,
+            "algorithmic_bytes_per_launch": bytes_tot / max(launches, 1),
+            "avg_launch_us": ms_tot * 1e3 / max(launches, 1), "launches": launches, "kernel": VD_KINDS[dom],
             "peak_kind": peak_kind,
             "kernels": {VD_KINDS[k]: {"ms": prof[k][0], "launches": prof[k][1],
                                       "GB_per_s": (prof[k][2] / (prof[k][0] / 1e3) / 1e9) if prof[k][0] else None}
