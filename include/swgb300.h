@@ -200,8 +200,10 @@ int sw_acoustic_forward_snapshots(sw_wavesim* ws, int32_t nshots, const sw_acous
  * producer warp; + 4 keeps a second row of loads in flight in the forward
  * kernels of the 4-warp stencil; + 8 runs the grouped 2D adjoint (4+ shots)
  * with 5 resident blocks per SM instead of 4 (registers capped at 102);
- * + 16*k additionally prefetches the rows k rows ahead into L2 (k = 1..15).
- * Results do not depend on any of them. */
+ * + 16*k additionally prefetches the rows k rows ahead into L2 (k = 1..15);
+ * + 256 runs the 2D adjoint per shot with plain FP32 correlation sums that are
+ * flushed into an FP64 total every 32 steps (instead of Kahan-compensated sums).
+ * Results do not depend on any of them beyond rounding. */
 int sw_wavesim_set_tuning(sw_wavesim* ws, int32_t tz, int32_t variant);
 
 /* CUDA graphs (on by default): a batch's whole device-side time loop

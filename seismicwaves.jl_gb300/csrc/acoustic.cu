@@ -134,7 +134,7 @@ __global__ void k_adj_inject(const ShotDesc* __restrict__ desc, const long long*
                              const int* __restrict__ bslot, FieldArg lam, FieldArg lamd, FieldArg dcorr, FieldArg g,
                              FieldArg gc, int it, int nshots, int grp, int dbf16) {
   float* gp = g.p + (long long)blockIdx.x * g.s;
-  float* cp = gc.p + (long long)blockIdx.x * gc.s;
+  float* cp = gc.p ? gc.p + (long long)blockIdx.x * gc.s : nullptr;  // null: plain FP32 sums
   for (int j = 0; j < grp; ++j) {
     const int shot = blockIdx.x * grp + j;
     if (shot >= nshots) break;
@@ -170,10 +170,41 @@ __device__ void adj_inject_shot(const ShotDesc& D, const long long* __restrict__
       ld[lin] += add;
       corr = add;
     }
-    float gv = gp[lin], cv = cp[lin];
-    kahan_add(gv, cv, corr * dld1(dp, lin, dbf16));
-    gp[lin] = gv;
-    cp[lin] = cv;
+    if (cp) {
+      float gv = gp[lin], cv = cp[lin];
+      kahan_add(gv, cv, corr * dld1(dp, lin, dbf16));
+      gp[lin] = gv;
+      cp[lin] = cv;
+    } else {
+      gp[lin] += corr * dld1(dp, lin, dbf16);
+    }
+  }
+}
+
+// Plain FP32 correlation sums of the first S shots (MODE_ADJW) added into the
+// FP64 total and cleared; called every few adjoint steps so that no FP32 sum
+// runs over more than that many terms.
+__global__ void k_flush_grad(float* __restrict__ g, long long F, int S, double* __restrict__ tot) {
+  for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < F; c += (long long)gridDim.x * blockDim.x) {
+    double t = 0.0;
+    for (int k = 0; k < S; ++k) {
+      t += (double)g[(long long)k * F + c];
+      g[(long long)k * F + c] = 0.0f;
+    }
+    tot[c] += t;
+  }
+}
+
+// grad[c] (+)= 2/vp^3 * (1/dt^2) * total[c] (the MODE_ADJW counterpart of k_reduce_grad).
+__global__ void k_reduce_grad_tot(const double* __restrict__ tot, const float* __restrict__ vp, int n0, long long npts,
+                                  int P, double inv_dt2, double* __restrict__ out, int accumulate) {
+  for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < npts;
+       c += (long long)gridDim.x * blockDim.x) {
+    const long long rowi = c / n0;
+    const long long lin = rowi * P + (c - rowi * n0);
+    const double v = (double)vp[c];
+    const double val = (2.0 / (v * v * v)) * inv_dt2 * tot[lin];
+    out[c] = accumulate ? out[c] + val : val;
   }
 }
 
@@ -396,6 +427,9 @@ struct sw_wavesim {
   int variant = 0;  // 2D stencil: 0 = register-pipelined, 1 = TMA
   int pf = 0;       // 2D stencil: L2 prefetch distance in rows (0 = off)
   int grp = 1;      // shots per gradient accumulator in the adjoint (4: shot sum fused, 1: per shot)
+  bool adj_plain = false;  // 2D: per-shot adjoint with plain FP32 sums flushed to FP64 (MODE_ADJW)
+  bool adjw = false;       // the current gradient call uses MODE_ADJW
+  DevMem tot64;            // MODE_ADJW: FP64 gradient total (padded layout)
   // CUDA graphs of a group's whole time loop, keyed by what the captured launches depend on
   long long gen = 0;  // bumped whenever a device buffer the kernels see is (re)allocated
   bool use_graphs = true;
@@ -476,7 +510,8 @@ void run_graph(sw_wavesim* ws, std::vector<long long> key, Work&& work) {
 }
 
 std::vector<long long> group_key(const sw_wavesim* ws, const std::vector<HostShot>& group, bool grad) {
-  std::vector<long long> k = {grad ? 1 : 0, ws->grp, ws->variant, ws->tile_tz, ws->pf, (long long)group.size()};
+  std::vector<long long> k = {grad ? 1 : 0, ws->grp, ws->variant, ws->tile_tz, ws->pf, ws->adjw ? 1 : 0,
+                             (long long)group.size()};
   for (const auto& h : group) k.push_back(h.nt);
   return k;
 }
@@ -865,6 +900,7 @@ double stencil_bytes(const sw_wavesim* ws, int S, int mode, int n_dwrite, bool c
   double b = (16.0 * S + 4.0) * pts + 16.0 * strip * S;
   if (mode == MODE_FWD_D) b += 4.0 * pts * n_dwrite;
   if (mode == MODE_ADJ) b += ngroups < 0 ? 20.0 * pts * S : (4.0 * S + 16.0 * ngroups) * pts;
+  if (mode == MODE_ADJW) b += 12.0 * pts * S;  // R D, RMW the plain sum
   if (ckpt) b += 8.0 * pts * S + 8.0 * strip * S;
   return b;
 }
@@ -902,9 +938,17 @@ struct Launcher {
     check_vector_alignment(a);
     const long long blocks = (long long)a.nshots * c.tiles_x * c.tiles_y * c.tiles_z;
     cudaEvent_t ev = nullptr;
-    const int kind = MODE == MODE_ADJ ? KK_ADJOINT : (recompute ? KK_RECOMPUTE : KK_STENCIL);
+    const int kind = (MODE == MODE_ADJ || MODE == MODE_ADJW) ? KK_ADJOINT : (recompute ? KK_RECOMPUTE : KK_STENCIL);
     ws->ctx->prof.begin(st, kind, bytes, &ev);
-    if (ws->N == 2 && (ws->variant & 3) == 1) {
+    if constexpr (MODE == MODE_ADJW) {  // 2D register-pipelined stencil only
+      const int nw = block_warps(ws);
+      if (nw == 4)
+        k_ac2d_step<MODE, 4><<<(unsigned)blocks, 128, 0, st>>>(a);
+      else if (nw == 8)
+        k_ac2d_step<MODE, 8><<<(unsigned)blocks, 256, 0, st>>>(a);
+      else
+        k_ac2d_step<MODE, 16><<<(unsigned)blocks, 512, 0, st>>>(a);
+    } else if (ws->N == 2 && (ws->variant & 3) == 1) {
       enable_tma_smem<MODE>();
       k_ac2d_tma<MODE><<<(unsigned)blocks, 160, TmaLayout<MODE>::BYTES, st>>>(a);
     } else if (ws->N == 2) {
@@ -1148,6 +1192,7 @@ void adjoint_group(sw_wavesim* ws, const std::vector<HostShot>& group) {
   zero_state(ws, S, true);
   check_cuda(cudaMemsetAsync(ws->g.p, 0, (size_t)S * F * sizeof(float), st), "reset g");
   check_cuda(cudaMemsetAsync(ws->gc.p, 0, (size_t)S * F * sizeof(float), st), "reset gc");
+  if (ws->adjw) check_cuda(cudaMemsetAsync(ws->tot64.p, 0, (size_t)F * sizeof(double), st), "reset total");
   int apc = 0, apk = 0;
   for (int it = max_nt; it >= 1; --it) {
     const int Sa = active_count(group, it);
@@ -1218,8 +1263,10 @@ void adjoint_group(sw_wavesim* ws, const std::vector<HostShot>& group) {
     const long long dslot = K == 1 ? it - 1 : (it - 1) % K;
     a.dcorr = dslot_arg(ws, dslot);
     a.g = fa(ws->g, F);
-    a.gc = fa(ws->gc, F);
-    if (ws->grp == 4) {
+    a.gc = ws->adjw ? FieldArg{nullptr, 0} : fa(ws->gc, F);
+    if (ws->adjw) {
+      L.step<MODE_ADJW>(a, c, stencil_bytes(ws, Sa, MODE_ADJW, 0, false));
+    } else if (ws->grp == 4) {
       // 4 shots per block (one per warp) over 128-wide tiles; the correlation is
       // summed over the group before its single Kahan update
       StepArgs b = a;
@@ -1245,6 +1292,13 @@ void adjoint_group(sw_wavesim* ws, const std::vector<HostShot>& group) {
         ws->d_bslot.as<int>(), a.pnew, a.dout, a.dcorr, a.g, a.gc, it, Sa, ws->grp, a.dbf16);
     check_cuda(cudaGetLastError(), "adjoint inject launch");
     ws->ctx->prof.end(st, KK_SRCREC, ev);
+    if (ws->adjw && (it - 1) % 32 == 0) {  // at most 32 terms per FP32 sum
+      ws->ctx->prof.begin(st, KK_OTHER, 0.0, &ev);
+      const long long blocks = std::min<long long>((F + 255) / 256, 4096);
+      k_flush_grad<<<(unsigned)blocks, 256, 0, st>>>(ws->g.as<float>(), F, S, ws->tot64.as<double>());
+      check_cuda(cudaGetLastError(), "gradient flush launch");
+      ws->ctx->prof.end(st, KK_OTHER, ev);
+    }
     apc = 1 - apc;
     apk = 1 - apk;
   }
@@ -1454,13 +1508,15 @@ void acoustic_gradient(sw_wavesim* ws, int nshots, const sw_acoustic_shot* shots
     fail(SW_ERR_UNSUPPORTED, "BF16 snapshots are not available with the TMA stencil variant");
   // the shot sum is fused into the 2D adjoint for batches of 4 or more shots,
   // unless per-shot muting needs each shot's gradient
-  ws->grp = (!mute && ws->N == 2 && (ws->variant & 3) != 1 && nshots >= 4) ? 4 : 1;
+  ws->adjw = !mute && ws->N == 2 && (ws->variant & 3) != 1 && ws->adj_plain;
+  ws->grp = (!ws->adjw && !mute && ws->N == 2 && (ws->variant & 3) != 1 && nshots >= 4) ? 4 : 1;
   const int nblk = 64;
   bool first_group = true;
   for (const auto& group : plan_groups(ws, order, true)) {
     const int S = (int)group.size();
     const int max_nt = group.front().nt;
     ensure_state(ws, S, true, max_nt);
+    if (ws->adjw) ensure(ws, ws->tot64, (size_t)ws->F * sizeof(double), "gradient total");
     Tables T;
     build_tables(ws, shots, group, on_device, true, T);
     ensure(ws, ws->d_partial, (size_t)nblk * S * sizeof(double), "misfit partials");
@@ -1521,6 +1577,14 @@ void acoustic_gradient(sw_wavesim* ws, int nshots, const sw_acoustic_shot* shots
       cudaEvent_t ev = nullptr;
       ws->ctx->prof.begin(st, KK_OTHER, 0.0, &ev);
       const long long blocks = std::min<long long>((ws->npts + 255) / 256, 8192);
+      if (ws->adjw) {
+        k_reduce_grad_tot<<<(unsigned)blocks, 256, 0, st>>>(ws->tot64.as<double>(), ws->vp.as<float>(), ws->n[0],
+                                                            ws->npts, ws->P, 1.0 / (ws->prm.dt * ws->prm.dt), gout,
+                                                            accumulate ? 1 : 0);
+        check_cuda(cudaGetLastError(), "gradient reduction launch");
+        ws->ctx->prof.end(st, KK_OTHER, ev);
+        return;
+      }
       k_reduce_grad<<<(unsigned)blocks, 256, 0, st>>>(ws->g.as<float>(), ws->gc.as<float>(), ws->F,
                                                       (S + ws->grp - 1) / ws->grp,
                                                       ws->vp.as<float>(), ws->n[0], ws->npts, ws->P,
@@ -1601,7 +1665,8 @@ void acoustic_gradient(sw_wavesim* ws, int nshots, const sw_acoustic_shot* shots
 void wavesim_set_tuning(sw_wavesim* ws, int tz, int variant) {
   ws->tile_tz = tz;
   ws->variant = variant % 16;
-  ws->pf = variant / 16;
+  ws->pf = (variant / 16) % 16;
+  ws->adj_plain = (variant & 256) != 0;
 }
 void wavesim_use_graphs(sw_wavesim* ws, bool on) {
   ws->use_graphs = on;

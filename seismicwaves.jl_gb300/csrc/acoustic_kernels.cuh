@@ -40,7 +40,10 @@
 
 namespace swgb {
 
-enum StepMode { MODE_FWD = 0, MODE_FWD_D = 1, MODE_ADJ = 2 };
+// MODE_ADJW (2D only): the adjoint with plain FP32 correlation sums per shot
+// (no Kahan compensation), which the host flushes into FP64 totals every few
+// steps (k_flush_grad).
+enum StepMode { MODE_FWD = 0, MODE_FWD_D = 1, MODE_ADJ = 2, MODE_ADJW = 3 };
 
 struct StepArgs {
   int n0, n1, n2;  // grid points per axis (n2 = 1 in 2D; the depth axis is n1 in 2D, n2 in 3D)
@@ -198,7 +201,9 @@ __device__ __forceinline__ float* fptr(const FieldArg& f, int shot) {
 // which holds a second row of six arrays in registers, at 128.
 template <int MODE, int NW>
 struct Ac2dBounds {
-  static constexpr int MINB = MODE == MODE_ADJ ? (NW == 4 ? 4 : NW == 8 ? 2 : 1) : (NW == 4 ? 7 : NW == 8 ? 4 : 2);
+  static constexpr int MINB = MODE == MODE_ADJ    ? (NW == 4 ? 4 : NW == 8 ? 2 : 1)
+                              : MODE == MODE_ADJW ? (NW == 4 ? 6 : NW == 8 ? 3 : 1)
+                                                  : (NW == 4 ? 7 : NW == 8 ? 4 : 2);
 };
 
 template <int MODE, int NW, int DP = 1>
@@ -247,8 +252,9 @@ __global__ void __launch_bounds__(32 * NW, (Ac2dBounds<MODE, NW>::MINB - (DP - 1
   float* ckd = fptr(A.ck_d, shot);
   float* Dw = nullptr;
   if (MODE == MODE_FWD_D && shot >= A.d_first) Dw = dptr(A.Dout, shot, A.dbf16);
-  const float* dcr = MODE == MODE_ADJ ? dptr(A.dcorr, shot, A.dbf16) : nullptr;
-  float* gg = MODE == MODE_ADJ ? fptr(A.g, shot) : nullptr;
+  constexpr bool ADJ = MODE == MODE_ADJ || MODE == MODE_ADJW;
+  const float* dcr = ADJ ? dptr(A.dcorr, shot, A.dbf16) : nullptr;
+  float* gg = ADJ ? fptr(A.g, shot) : nullptr;
   float* gcp = MODE == MODE_ADJ ? fptr(A.gc, shot) : nullptr;
 
   // The loads of row z+1 (p of row z+2, d, fact and for the adjoint D, g, gc)
@@ -262,10 +268,10 @@ __global__ void __launch_bounds__(32 * NW, (Ac2dBounds<MODE, NW>::MINB - (DP - 1
     ld4(rp, pc + row + P + xa);
     ld4rw(o, di + row + xa);
     ld4(f, fa + row + xa);
-    if (MODE == MODE_ADJ) {
+    if (ADJ) {
       dld4(dv, dcr, row + xa, A.dbf16);
       ld4rw(g4, gg + row + xa);
-      ld4rw(c4, gcp + row + xa);
+      if (MODE == MODE_ADJ) ld4rw(c4, gcp + row + xa);
     }
   }
   // DP == 2 (forward kernels): a second row of loads in flight, issued one
@@ -288,10 +294,10 @@ __global__ void __launch_bounds__(32 * NW, (Ac2dBounds<MODE, NW>::MINB - (DP - 1
       const long long prow = row + (long long)A.pf * P + wx0;
       l2_prefetch(pc + prow + P, seg);
       l2_prefetch(di + prow, seg);
-      if (MODE == MODE_ADJ) {
+      if (ADJ) {
         if (!A.dbf16) l2_prefetch(dcr + prow, seg);
         l2_prefetch(gg + prow, seg);
-        l2_prefetch(gcp + prow, seg);
+        if (MODE == MODE_ADJ) l2_prefetch(gcp + prow, seg);
       }
     }
     float rpn[4], on[4], fn[4], dvn[4], g4n[4], c4n[4];
@@ -308,10 +314,10 @@ __global__ void __launch_bounds__(32 * NW, (Ac2dBounds<MODE, NW>::MINB - (DP - 1
       ld4(rpn, pc + nrow + P + xa);
       ld4rw(on, di + nrow + xa);
       ld4(fn, fa + nrow + xa);
-      if (MODE == MODE_ADJ) {
+      if (ADJ) {
         dld4(dvn, dcr, nrow + xa, A.dbf16);
         ld4rw(g4n, gg + nrow + xa);
-        ld4rw(c4n, gcp + nrow + xa);
+        if (MODE == MODE_ADJ) ld4rw(c4n, gcp + nrow + xa);
       }
     }
     float left = __shfl_up_sync(FULL, r0[3], 1);
@@ -360,6 +366,18 @@ __global__ void __launch_bounds__(32 * NW, (Ac2dBounds<MODE, NW>::MINB - (DP - 1
             if (x0 + e >= 1 && x0 + e <= nx - 2) { gg[row + x0 + e] = g4[e]; gcp[row + x0 + e] = c4[e]; }
         }
       }
+      if (MODE == MODE_ADJW) {
+#pragma unroll
+        for (int e = 0; e < 4; ++e)
+          if (x0 + e >= 1 && x0 + e <= nx - 2) g4[e] += outp[e] * dv[e];
+        if (vec_interior) {
+          st4(gg + row + x0, g4);
+        } else {
+#pragma unroll
+          for (int e = 0; e < 4; ++e)
+            if (x0 + e >= 1 && x0 + e <= nx - 2) gg[row + x0 + e] = g4[e];
+        }
+      }
       if (vec_interior) {
         st4(pn + row + x0, outp);
         st4(dn + row + x0, outd);
@@ -391,7 +409,8 @@ __global__ void __launch_bounds__(32 * NW, (Ac2dBounds<MODE, NW>::MINB - (DP - 1
         rp[e] = rpn[e];
         o[e] = on[e];
         f[e] = fn[e];
-        if (MODE == MODE_ADJ) { dv[e] = dvn[e]; g4[e] = g4n[e]; c4[e] = c4n[e]; }
+        if (ADJ) { dv[e] = dvn[e]; g4[e] = g4n[e]; }
+        if (MODE == MODE_ADJ) c4[e] = c4n[e];
       }
     }
   }

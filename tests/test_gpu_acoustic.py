@@ -321,10 +321,11 @@ def test_graph_replay_is_bitwise_identical(sw, oracle):
     on.close()
 
 
-@pytest.mark.parametrize("variant", [0, 8])
+@pytest.mark.parametrize("variant", [0, 8, 256])
 def test_gradient_grouped_adjoint_variants(sw, oracle, variant):
     """The grouped 2D adjoint (4+ shots, one Kahan update per group) with 4 or
-    5 resident blocks per SM matches the oracle's shot sum."""
+    5 resident blocks per SM, and the per-shot adjoint with plain FP32 sums
+    flushed into FP64 every 32 steps (variant 256), match the oracle's shot sum."""
     case, shot = _grad_case(sw, oracle, nt=300)
     run = GpuRun(sw, case, gradient=True, check_freq=10, variant=variant)
     g, msf, _ = run.gradient([shot] * 5)
