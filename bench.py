@@ -725,9 +725,14 @@ def run_gb300(a):
     # roofline of the dominant kernel (largest total time among the stencil kinds)
     nd = w.vp.ndim
     base = "k_ac2d_step" if nd == 2 else "k_ac3d_step"
-    adj = "k_ac2d_adj_grp" if (nd == 2 and nshots >= 4) else base + "<2>"
+    if nd == 2 and a.variant >= 0 and (a.variant & 256) and nshots >= 4:
+        adj, adj_what = "k_ac2d_adj_grp", "adjoint + correlation (4 shots per block, Kahan sums)"
+    elif nd == 2:
+        adj, adj_what = base + "<3>", "adjoint + correlation (plain FP32 sums, FP64 flush every 32 steps)"
+    else:
+        adj, adj_what = base + "<2>", "adjoint + correlation (Kahan sums)"
     kinds = {0: (f"{base}<0/1> forward", f"{base}<1>"), 4: (f"{base}<1> recompute (writes D)", f"{base}<1>"),
-             1: (f"{adj} adjoint + correlation", adj)}
+             1: (f"{adj} {adj_what}", adj)}
     dom = max(kinds, key=lambda k: prof[k][0])
     ms_tot, launches, bytes_tot = prof[dom]
     achieved = bytes_tot / (ms_tot / 1e3) / 1e9 if ms_tot > 0 else None

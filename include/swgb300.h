@@ -199,11 +199,12 @@ int sw_acoustic_forward_snapshots(sw_wavesim* ws, int32_t nshots, const sw_acous
  * 8 or 16 warps per block, 1 = TMA bulk copies through shared memory with a
  * producer warp; + 4 keeps a second row of loads in flight in the forward
  * kernels of the 4-warp stencil; + 8 runs the grouped 2D adjoint (4+ shots)
- * with 5 resident blocks per SM instead of 4 (registers capped at 102);
+ * with 5 resident blocks per SM instead of 4 (registers capped at 102; with + 256);
  * + 16*k additionally prefetches the rows k rows ahead into L2 (k = 1..15);
- * + 256 runs the 2D adjoint per shot with plain FP32 correlation sums that are
- * flushed into an FP64 total every 32 steps (instead of Kahan-compensated sums).
- * Results do not depend on any of them beyond rounding. */
+ * by default the 2D adjoint runs per shot with plain FP32 correlation sums
+ * flushed into an FP64 total every 32 steps; + 256 selects instead the grouped
+ * adjoint (4 shots per block, one Kahan-compensated FP32 sum per group; 4+
+ * shots).  Results do not depend on any of them beyond rounding. */
 int sw_wavesim_set_tuning(sw_wavesim* ws, int32_t tz, int32_t variant);
 
 /* CUDA graphs (on by default): a batch's whole device-side time loop

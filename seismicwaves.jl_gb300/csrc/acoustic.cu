@@ -427,7 +427,8 @@ struct sw_wavesim {
   int variant = 0;  // 2D stencil: 0 = register-pipelined, 1 = TMA
   int pf = 0;       // 2D stencil: L2 prefetch distance in rows (0 = off)
   int grp = 1;      // shots per gradient accumulator in the adjoint (4: shot sum fused, 1: per shot)
-  bool adj_plain = false;  // 2D: per-shot adjoint with plain FP32 sums flushed to FP64 (MODE_ADJW)
+  bool adj_plain = true;   // 2D: per-shot adjoint with plain FP32 sums flushed to FP64 (MODE_ADJW);
+                           // false: the grouped Kahan adjoint (k_ac2d_adj_grp) for 4+ shots
   bool adjw = false;       // the current gradient call uses MODE_ADJW
   DevMem tot64;            // MODE_ADJW: FP64 gradient total (padded layout)
   // CUDA graphs of a group's whole time loop, keyed by what the captured launches depend on
@@ -1666,7 +1667,7 @@ void wavesim_set_tuning(sw_wavesim* ws, int tz, int variant) {
   ws->tile_tz = tz;
   ws->variant = variant % 16;
   ws->pf = (variant / 16) % 16;
-  ws->adj_plain = (variant & 256) != 0;
+  ws->adj_plain = (variant & 256) == 0;
 }
 void wavesim_use_graphs(sw_wavesim* ws, bool on) {
   ws->use_graphs = on;

@@ -147,6 +147,7 @@ class GpuRun:
                 if shot.invcov is not None and np.ndim(shot.invcov) == 2:  # dense (nt, nt)
                     ic = np.asfortranarray(shot.invcov, dtype=np.float32)
                     st.invcov = ic.ctypes.data
+                    items.append(ic)  # keeps the buffer alive until the call returns
                 elif shot.invcov is not None:
                     ic = np.ascontiguousarray(shot.invcov, dtype=np.float32)
                     st.invcov_diag = ic.ctypes.data
