@@ -1496,6 +1496,22 @@ struct Run {
   const ShotDesc* ddesc;
   float sf_ref = 1.0f;  // the largest source scale of the group (the gradient's common scale)
   bool any_mt = true, any_force = true;  // source kinds present in the group (skip empty launches)
+  // blocks per shot of the source / adjoint-source / recording kernels: one
+  // thread per unique point (or receiver component) of the largest table
+  int gx_src = 1, gx_adj = 1, gx_rec = 1;
+  void size_grids(const std::vector<ShotDesc>& desc) {
+    int ns = 1, na = 1, nr = 1;
+    for (const auto& d : desc) {
+      for (int t = 0; t < 2; ++t) {
+        ns = std::max(ns, d.src[t].np);
+        na = std::max(na, d.adj[t].np);
+      }
+      nr = std::max(nr, 2 * d.nrec);
+    }
+    gx_src = (ns + 127) / 128;
+    gx_adj = (na + 127) / 128;
+    gx_rec = (nr + 255) / 256;
+  }
 
   Args args(bool adjoint) const {
     Args a{};
@@ -1528,7 +1544,7 @@ struct Run {
     DevMem* f = es->st;
     cudaEvent_t ev = nullptr;
     es->ctx->prof.begin(st, KK_SRCREC, 0.0, &ev);
-    k_el_inject_sigma<<<dim3(1, S), 128, 0, st>>>(ddesc, it, es->g.F, f[4].as<float>(), f[5].as<float>(),
+    k_el_inject_sigma<<<dim3(gx_src, S), 128, 0, st>>>(ddesc, it, es->g.F, f[4].as<float>(), f[5].as<float>(),
                                                   f[6].as<float>());
     check_cuda(cudaGetLastError(), "stress injection launch");
     es->ctx->prof.end(st, KK_SRCREC, ev);
@@ -1538,7 +1554,8 @@ struct Run {
     DevMem* f = adjoint ? es->ast : es->st;
     cudaEvent_t ev = nullptr;
     es->ctx->prof.begin(st, KK_SRCREC, 0.0, &ev);
-    k_el_inject_force<<<dim3(2, S), 128, 0, st>>>(ddesc, it, adjoint ? 1 : 0, scale, es->g.F, f[0].as<float>(),
+    k_el_inject_force<<<dim3(adjoint ? gx_adj : gx_src, S), 128, 0, st>>>(ddesc, it, adjoint ? 1 : 0, scale, es->g.F,
+                                                                         f[0].as<float>(),
                                                   f[1].as<float>(), f[2].as<float>(), f[3].as<float>(),
                                                   sD ? sD[0] : nullptr, sD ? sD[1] : nullptr, es->dtr_i.as<float>(),
                                                   es->dtr_j.as<float>());
@@ -1549,7 +1566,7 @@ struct Run {
     if (S <= 0) return;
     cudaEvent_t ev = nullptr;
     es->ctx->prof.begin(st, KK_SRCREC, 0.0, &ev);
-    k_el_record<<<dim3(2, S), 256, 0, st>>>(ddesc, it, es->g.F, es->st[0].as<float>(), es->st[1].as<float>());
+    k_el_record<<<dim3(gx_rec, S), 256, 0, st>>>(ddesc, it, es->g.F, es->st[0].as<float>(), es->st[1].as<float>());
     check_cuda(cudaGetLastError(), "record launch");
     es->ctx->prof.end(st, KK_SRCREC, ev);
   }
@@ -1823,6 +1840,7 @@ void elastic_forward(sw_elastic* es, int nshots, const sw_elastic_shot* shots, b
     build_tables(es, shots, group, on_device, false, desc);
     const float sf_ref = set_forward_scales(es, shots, group, desc);
     Run R{es, es->ctx->stream, es->d_desc.as<ShotDesc>(), sf_ref};
+    R.size_grids(desc);
     R.any_mt = R.any_force = false;
     for (const auto& h : group) (shots[h.orig].kind == 0 ? R.any_mt : R.any_force) = true;
     zero_state(es, S, false);
@@ -1899,6 +1917,7 @@ void elastic_gradient(sw_elastic* es, int nshots, const sw_elastic_shot* shots, 
     build_tables(es, shots, group, on_device, true, desc);
     const float sf_ref = set_forward_scales(es, shots, group, desc);
     Run R{es, st, es->d_desc.as<ShotDesc>(), sf_ref};
+    R.size_grids(desc);
     R.any_mt = R.any_force = false;
     for (const auto& h : group) (shots[h.orig].kind == 0 ? R.any_mt : R.any_force) = true;
     const long long F = g.F;
