@@ -783,7 +783,7 @@ def run_gb300(a):
 
 
 ELASTIC_KINDS = {0: "k_el_stress + k_el_disp forward", 4: "k_el_stress + k_el_disp recompute (writes slots)",
-                 1: "k_el_stress + k_el_disp adjoint", 5: "k_el_corr gradient correlation"}
+                 1: "k_el_stress + k_el_disp adjoint", 5: "k_el_corr4 gradient correlation"}
 
 
 def measure_elastic(a, name="elastic2d_1200x600", shots=0, nt_cap=0, steps=None, warmup=None, plain=True,

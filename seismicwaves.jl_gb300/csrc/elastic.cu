@@ -941,6 +941,123 @@ __global__ void __launch_bounds__(BX) k_el_corr(const CorrArgs A) {
   }
 }
 
+// Four x points per thread, 512 per block, one row per block (blockIdx.y):
+// the same sums as k_el_corr.  For every shot the thread loads float4s of the
+// rows it needs (ux rows j-1 .. j+2, uz rows j-2 .. j+1, forward and adjoint,
+// D of row j) and takes the x neighbours from the adjacent lanes (loaded at
+// the warp edges); the z re-reads of neighbouring rows hit L1/L2.
+__global__ void __launch_bounds__(BX) k_el_corr4(const CorrArgs A) {
+  const Geo g = A.g;
+  const int grp = blockIdx.z;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int wx0 = (blockIdx.x * 4 + warp) * 128;
+  const int j = blockIdx.y + 1;
+  if (wx0 >= g.nx || j > g.nz) return;  // warp uniform; no block-level synchronisation
+  const int i0 = wx0 + lane * 4 + 1;
+  const bool ldok = i0 <= g.nx + 2;
+  const int s0 = grp * A.gsize, s1 = min(s0 + A.gsize, A.nshots);
+  float* acc = A.acc + (long long)grp * 10 * g.F;
+  const int jlo = g.ft ? 1 : 2;
+  const bool on_uz = j <= g.nz - 1;
+  const bool fs1 = g.ft && j == 1, fs2 = g.ft && j == 2;
+  const int P = g.P;
+  const long long c = g.lin(i0, j);
+  float fsr[4] = {0.f, 0.f, 0.f, 0.f};  // -lambda / (lambda + 2 mu) on the free surface (row 1)
+  if (fs1 && ldok) {
+    const F4 L = ld4z(A.lam, c, true), M = ld4z(A.mu, c, true);
+#pragma unroll
+    for (int e = 0; e < 4; ++e) fsr[e] = (L.v[e] + 2.0f * M.v[e]) != 0.0f ? -L.v[e] / (L.v[e] + 2.0f * M.v[e]) : 0.0f;
+  }
+  float v[5][4];
+#pragma unroll
+  for (int q = 0; q < 5; ++q)
+#pragma unroll
+    for (int e = 0; e < 4; ++e) v[q][e] = 0.0f;
+  for (int s = s0; s < s1; ++s) {
+    const long long so = (long long)s * g.F;
+    const float cs = __ldg(A.cs + s);
+    float sx[2][4], sz[2][4], exz[2][4];  // [forward, adjoint]: exx, ezz, 2 exz at the 4 points
+    float rho_x[4], rho_z[4];
+#pragma unroll
+    for (int w = 0; w < 2; ++w) {
+      const float* ux = (w == 0 ? A.fux : A.aux) + so;
+      const float* uz = (w == 0 ? A.fuz : A.auz) + so;
+      // ux rows j-1 .. j+2, uz rows j-2 .. j+1
+      const F4 xm = ld4z(ux, c - P, ldok), x0 = ld4z(ux, c, ldok), xp = ld4z(ux, c + P, ldok),
+               xpp = ld4z(ux, c + 2 * P, ldok);
+      const F4 zmm = ld4z(uz, c - 2 * P, ldok), zm = ld4z(uz, c - P, ldok), z0 = ld4z(uz, c, ldok),
+               zp = ld4z(uz, c + P, ldok);
+      if (w == 1) {
+        const F4 DX = ld4z(A.Dx + so, c, ldok), DZ = ld4z(A.Dz + so, c, ldok);
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+          rho_x[e] = x0.v[e] * DX.v[e];
+          rho_z[e] = z0.v[e] * DZ.v[e];
+        }
+      }
+      // ux at i0-2 .. i0+4 and uz at i0-1 .. i0+5 of row j
+      float ua[7], za[7];
+      ua[0] = __shfl_up_sync(FULL, x0.v[2], 1);
+      ua[1] = __shfl_up_sync(FULL, x0.v[3], 1);
+      ua[6] = __shfl_down_sync(FULL, x0.v[0], 1);
+      za[0] = __shfl_up_sync(FULL, z0.v[3], 1);
+      za[5] = __shfl_down_sync(FULL, z0.v[0], 1);
+      za[6] = __shfl_down_sync(FULL, z0.v[1], 1);
+      if (lane == 0) {
+        ua[0] = ldz(ux, c - 2, ldok);
+        ua[1] = ldz(ux, c - 1, ldok);
+        za[0] = ldz(uz, c - 1, ldok);
+      }
+      if (lane == 31) {
+        ua[6] = ldz(ux, c + 4, ldok);
+        za[5] = ldz(uz, c + 4, ldok);
+        za[6] = ldz(uz, c + 5, ldok);
+      }
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        ua[2 + e] = x0.v[e];
+        za[1 + e] = z0.v[e];
+      }
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        const float exx = d4(ua[e], ua[e + 1], ua[e + 2], ua[e + 3], g.idx);
+        float ezz;
+        if (fs1) ezz = fsr[e] * exx;
+        else if (fs2) ezz = d4(zm.v[e], zm.v[e], z0.v[e], zp.v[e], g.idz);
+        else ezz = d4(zmm.v[e], zm.v[e], z0.v[e], zp.v[e], g.idz);
+        const float dzx = d4(za[e], za[e + 1], za[e + 2], za[e + 3], g.idx);
+        const float dxz = fs1 ? d4(xp.v[e], x0.v[e], xp.v[e], xpp.v[e], g.idz)
+                              : d4(xm.v[e], x0.v[e], xp.v[e], xpp.v[e], g.idz);
+        sx[w][e] = exx;
+        sz[w][e] = ezz;
+        exz[w][e] = dzx + dxz;
+      }
+    }
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+      v[0][e] += cs * rho_x[e];
+      v[1][e] += cs * rho_z[e];
+      v[2][e] += cs * ((sx[0][e] + sz[0][e]) * (sx[1][e] + sz[1][e]));
+      v[3][e] += cs * (sx[0][e] * sx[1][e] + sz[0][e] * sz[1][e]);
+      v[4][e] += cs * (exz[0][e] * exz[1][e]);
+    }
+  }
+  if (!ldok) return;
+#pragma unroll
+  for (int e = 0; e < 4; ++e) {
+    const int i = i0 + e;
+    const long long ce = c + e;
+    const bool on_ux = i <= g.nx - 1;
+    if (on_ux) kahan_add_el(acc + ce, acc + 5 * g.F + ce, fs1 ? 0.5f * v[0][e] : v[0][e]);
+    if (on_uz && i <= g.nx) kahan_add_el(acc + g.F + ce, acc + 6 * g.F + ce, v[1][e]);
+    if (i >= 2 && i <= g.nx - 1 && j >= jlo && on_uz) {
+      kahan_add_el(acc + 2 * g.F + ce, acc + 7 * g.F + ce, fs1 ? 0.5f * v[2][e] : v[2][e]);
+      kahan_add_el(acc + 3 * g.F + ce, acc + 8 * g.F + ce, fs1 ? v[3][e] : 2.0f * v[3][e]);
+    }
+    if (on_ux && on_uz) kahan_add_el(acc + 4 * g.F + ce, acc + 9 * g.F + ce, v[4][e]);
+  }
+}
+
 // One snapshot block per shot (blockIdx.y): ux, uz, sxx, szz, sxz unpadded and
 // scaled back from the shot's source scale, into stage + shot * B.
 __global__ void k_el_snapshot(Geo g, const ShotDesc* __restrict__ desc, const float* __restrict__ ux,
@@ -2049,7 +2166,12 @@ void elastic_gradient(sw_elastic* es, int nshots, const sw_elastic_shot* shots, 
         cudaEvent_t ev = nullptr;
         const double pts = (double)g.nx * g.nz;
         es->ctx->prof.begin(st, KK_CORR, pts * (A * 24.0 + ng * 80.0), &ev);
-        k_el_corr<<<grid, BX, 0, st>>>(c);
+        if (es->vec) {
+          const dim3 grid4((g.nx + 511) / 512, g.nz, ng);
+          k_el_corr4<<<grid4, BX, 0, st>>>(c);
+        } else {
+          k_el_corr<<<grid, BX, 0, st>>>(c);
+        }
         check_cuda(cudaGetLastError(), "correlation launch");
         es->ctx->prof.end(st, KK_CORR, ev);
       }
