@@ -356,7 +356,7 @@ __device__ __forceinline__ void st4v(float* p, long long c, const float (&v)[4])
 }
 
 template <int TZ>
-__global__ void __launch_bounds__(BX) k_el_stress4(const Args A) {
+__global__ void __launch_bounds__(BX, 6) k_el_stress4(const Args A) {
   const Geo g = A.g;
   const int s = blockIdx.z;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -485,7 +485,7 @@ __global__ void __launch_bounds__(BX) k_el_stress4(const Args A) {
 }
 
 template <int TZ>
-__global__ void __launch_bounds__(BX) k_el_disp4(const Args A) {
+__global__ void __launch_bounds__(BX, 5) k_el_disp4(const Args A) {
   const Geo g = A.g;
   const int s = blockIdx.z;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
