@@ -197,13 +197,15 @@ __device__ __forceinline__ float* fptr(const FieldArg& f, int shot) {
 // psi_0 / xi_0 layout: [z][q] (q fastest);  psi_1 / xi_1 layout: [q][P].
 // ---------------------------------------------------------------------------
 // Minimum resident blocks per SM for a block of NW warps: keeps the forward
-// kernels at <= 72 registers (4 warps) or <= 64 (8 and 16 warps); the adjoint,
-// which holds a second row of six arrays in registers, at 128.
+// kernels at <= 64 registers (8 blocks of 4 warps; measured 4.0 / 4.4 TB/s
+// forward / recompute against 3.8 / 4.3 at 7 blocks, a few bytes spilled);
+// the per-shot adjoint at <= 80 (6 blocks); the Kahan adjoint, which holds a
+// second row of six arrays in registers, at 128.
 template <int MODE, int NW>
 struct Ac2dBounds {
   static constexpr int MINB = MODE == MODE_ADJ    ? (NW == 4 ? 4 : NW == 8 ? 2 : 1)
                               : MODE == MODE_ADJW ? (NW == 4 ? 6 : NW == 8 ? 3 : 1)
-                                                  : (NW == 4 ? 7 : NW == 8 ? 4 : 2);
+                                                  : (NW == 4 ? 8 : NW == 8 ? 4 : 2);
 };
 
 template <int MODE, int NW, int DP = 1>
