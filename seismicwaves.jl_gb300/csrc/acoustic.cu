@@ -969,7 +969,10 @@ struct Launcher {
       else
         k_ac2d_step<MODE, 16><<<(unsigned)blocks, 512, 0, st>>>(a);
     } else {
-      k_ac3d_step<MODE><<<(unsigned)blocks, 128, 0, st>>>(a);
+      if constexpr (MODE == MODE_FWD)
+        k_ac3d_fwd<MODE_FWD><<<(unsigned)blocks, 128, 0, st>>>(a);
+      else
+        k_ac3d_step<MODE><<<(unsigned)blocks, 128, 0, st>>>(a);
     }
     check_cuda(cudaGetLastError(), "stencil launch");
     ws->ctx->prof.end(st, kind, ev);

@@ -615,17 +615,8 @@ __device__ __forceinline__ StripIO strip_io(const StepArgs& A, int d, int shot, 
   return s;
 }
 
-// Minimum resident blocks per SM of the 3D stencil: the gradient's forward /
-// recompute (D output) and adjoint steps run faster at 6 (<= 85 registers,
-// 23.3 against 22.0 Gpts/s on 16 shots of 400^3), the plain forward without a
-// bound (1.96 against 1.76 TB/s).
 template <int MODE>
-struct Ac3dBounds {
-  static constexpr int MINB = MODE == MODE_FWD ? 1 : 6;
-};
-
-template <int MODE>
-__global__ void __launch_bounds__(128, Ac3dBounds<MODE>::MINB) k_ac3d_step(const StepArgs A) {
+__device__ __forceinline__ void ac3d_body(const StepArgs& A) {
   constexpr unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int S = A.nshots;
@@ -784,6 +775,19 @@ __global__ void __launch_bounds__(128, Ac3dBounds<MODE>::MINB) k_ac3d_step(const
   }
 }
 
+
+// The gradient's forward / recompute (D output) and adjoint steps run faster
+// at 6 resident blocks per SM (<= 85 registers: 23.3 against 22.0 Gpts/s on
+// 16 shots of 400^3); the plain forward is fastest with the compiler's own
+// register choice (1.96 against 1.76 TB/s).
+template <int MODE>
+__global__ void __launch_bounds__(128, 6) k_ac3d_step(const StepArgs A) {
+  ac3d_body<MODE>(A);
+}
+template <int MODE>
+__global__ void __launch_bounds__(128) k_ac3d_fwd(const StepArgs A) {
+  ac3d_body<MODE>(A);
+}
 
 // ---------------------------------------------------------------------------
 // 2D, TMA pipeline with a dedicated producer warp.  Same arithmetic as
