@@ -162,8 +162,17 @@ constexpr unsigned FULL = 0xffffffffu;
 // neighbours of vx come from the adjacent lanes.  CORR (adjoint): also
 // acc[0] += -(p_new (pc - po) / dt), acc[1] += vx dpc/dx, acc[2] += vz dpc/dz
 // (pc rows j-1 .. j+2 in registers).
+// Resident blocks per SM: the correlating adjoint kernel runs faster at 7
+// (<= 72 registers; 5.06 against 4.92 TB/s for the adjoint step pair on 64
+// shots), the forward one is left at its own register count (55) by a bound
+// it already meets.
+template <bool CORR>
+struct VdPBounds {
+  static constexpr int MINB = CORR ? 7 : 8;
+};
+
 template <int TZ, bool CORR>
-__global__ void __launch_bounds__(BX) k_vd_p(const PArgs A) {
+__global__ void __launch_bounds__(BX, VdPBounds<CORR>::MINB) k_vd_p(const PArgs A) {
   const Geo g = A.g;
   const int s = blockIdx.z;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
