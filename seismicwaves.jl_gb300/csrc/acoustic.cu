@@ -182,16 +182,28 @@ __device__ void adj_inject_shot(const ShotDesc& D, const long long* __restrict__
 }
 
 // Plain FP32 correlation sums of the first S shots (MODE_ADJW) added into the
-// FP64 total and cleared; called every few adjoint steps so that no FP32 sum
-// runs over more than that many terms.
-__global__ void k_flush_grad(float* __restrict__ g, long long F, int S, double* __restrict__ tot) {
-  for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < F; c += (long long)gridDim.x * blockDim.x) {
-    double t = 0.0;
+// FP64 total; called every few adjoint steps so that no FP32 sum runs over
+// more than that many terms (the host clears the sums right after).  Four
+// consecutive points per thread; the shot loop only loads, so the loads of
+// several shots are in flight together.
+__global__ void k_flush_grad(const float* __restrict__ g, long long F, int S, double* __restrict__ tot) {
+  const long long F4 = F / 4;  // F is a multiple of 4 (padded pitch)
+  const float4* g4 = reinterpret_cast<const float4*>(g);
+  for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < F4; q += (long long)gridDim.x * blockDim.x) {
+    double t0 = 0.0, t1 = 0.0, t2 = 0.0, t3 = 0.0;
+#pragma unroll 8
     for (int k = 0; k < S; ++k) {
-      t += (double)g[(long long)k * F + c];
-      g[(long long)k * F + c] = 0.0f;
+      const float4 v = __ldg(g4 + (long long)k * F4 + q);
+      t0 += (double)v.x;
+      t1 += (double)v.y;
+      t2 += (double)v.z;
+      t3 += (double)v.w;
     }
-    tot[c] += t;
+    double* o = tot + 4 * q;
+    o[0] += t0;
+    o[1] += t1;
+    o[2] += t2;
+    o[3] += t3;
   }
 }
 
@@ -844,6 +856,8 @@ struct StepCtx {
 
 // Warps per block of the register-pipelined 2D stencil (variant 0: 4, 2: 8, 3: 16).
 int block_warps(const sw_wavesim* ws) { return (ws->variant & 3) == 2 ? 8 : (ws->variant & 3) == 3 ? 16 : 4; }
+// 3D: y rows (warps) per block, 4 or (variant 2) 8.
+int block_rows3d(const sw_wavesim* ws) { return (ws->variant & 3) == 2 ? 8 : 4; }
 
 StepCtx make_step_ctx(sw_wavesim* ws, int S) {
   StepCtx c{ws, 0, 0, 1, 0};
@@ -854,7 +868,8 @@ StepCtx make_step_ctx(sw_wavesim* ws, int S) {
     c.tiles_x = (int)((ws->P + w - 1) / w);
   } else {
     c.tiles_x = (int)((ws->P + 127) / 128);
-    c.tiles_y = (ws->n[1] - 2 + 3) / 4;
+    const int nw = block_rows3d(ws);
+    c.tiles_y = (ws->n[1] - 2 + nw - 1) / nw;
   }
   int TZ = ws->tile_tz;
   if (TZ <= 0) {
@@ -969,10 +984,14 @@ struct Launcher {
       else
         k_ac2d_step<MODE, 16><<<(unsigned)blocks, 512, 0, st>>>(a);
     } else {
-      if constexpr (MODE == MODE_FWD)
-        k_ac3d_fwd<MODE_FWD><<<(unsigned)blocks, 128, 0, st>>>(a);
-      else
-        k_ac3d_step<MODE><<<(unsigned)blocks, 128, 0, st>>>(a);
+      const int nw = block_rows3d(ws);
+      if constexpr (MODE == MODE_FWD) {
+        if (nw == 8) k_ac3d_fwd<MODE_FWD, 8><<<(unsigned)blocks, 256, 0, st>>>(a);
+        else k_ac3d_fwd<MODE_FWD><<<(unsigned)blocks, 128, 0, st>>>(a);
+      } else {
+        if (nw == 8) k_ac3d_step<MODE, 8><<<(unsigned)blocks, 256, 0, st>>>(a);
+        else k_ac3d_step<MODE><<<(unsigned)blocks, 128, 0, st>>>(a);
+      }
     }
     check_cuda(cudaGetLastError(), "stencil launch");
     ws->ctx->prof.end(st, kind, ev);
@@ -1298,9 +1317,10 @@ void adjoint_group(sw_wavesim* ws, const std::vector<HostShot>& group) {
     ws->ctx->prof.end(st, KK_SRCREC, ev);
     if (ws->adjw && (it - 1) % 32 == 0) {  // at most 32 terms per FP32 sum
       ws->ctx->prof.begin(st, KK_OTHER, 0.0, &ev);
-      const long long blocks = std::min<long long>((F + 255) / 256, 4096);
+      const long long blocks = std::min<long long>((F / 4 + 255) / 256, 8192);
       k_flush_grad<<<(unsigned)blocks, 256, 0, st>>>(ws->g.as<float>(), F, S, ws->tot64.as<double>());
       check_cuda(cudaGetLastError(), "gradient flush launch");
+      check_cuda(cudaMemsetAsync(ws->g.p, 0, (size_t)S * F * sizeof(float), st), "gradient sums clear");
       ws->ctx->prof.end(st, KK_OTHER, ev);
     }
     apc = 1 - apc;

@@ -615,7 +615,7 @@ __device__ __forceinline__ StripIO strip_io(const StepArgs& A, int d, int shot, 
   return s;
 }
 
-template <int MODE>
+template <int MODE, int NW>
 __device__ __forceinline__ void ac3d_body(const StepArgs& A) {
   constexpr unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -626,7 +626,7 @@ __device__ __forceinline__ void ac3d_body(const StepArgs& A) {
   tile /= A.tiles_x;
   const int tyi = tile % A.tiles_y, tzi = tile / A.tiles_y;
   const int nx = A.n0, ny = A.n1, nz = A.n2, P = A.P, H = A.halo;
-  const int y = 1 + tyi * 4 + warp;
+  const int y = 1 + tyi * NW + warp;  // one y row per warp, NW rows per block
   const int z_begin = 1 + tzi * A.TZ;
   const int z_end = min(z_begin + A.TZ, nz - 1);
   const int wx0 = txi * 128;
@@ -780,13 +780,13 @@ __device__ __forceinline__ void ac3d_body(const StepArgs& A) {
 // at 6 resident blocks per SM (<= 85 registers: 23.3 against 22.0 Gpts/s on
 // 16 shots of 400^3); the plain forward is fastest with the compiler's own
 // register choice (1.96 against 1.76 TB/s).
-template <int MODE>
-__global__ void __launch_bounds__(128, 6) k_ac3d_step(const StepArgs A) {
-  ac3d_body<MODE>(A);
+template <int MODE, int NW = 4>
+__global__ void __launch_bounds__(32 * NW, 24 / NW) k_ac3d_step(const StepArgs A) {
+  ac3d_body<MODE, NW>(A);
 }
-template <int MODE>
-__global__ void __launch_bounds__(128) k_ac3d_fwd(const StepArgs A) {
-  ac3d_body<MODE>(A);
+template <int MODE, int NW = 4>
+__global__ void __launch_bounds__(32 * NW) k_ac3d_fwd(const StepArgs A) {
+  ac3d_body<MODE, NW>(A);
 }
 
 // ---------------------------------------------------------------------------

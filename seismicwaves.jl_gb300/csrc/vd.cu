@@ -489,26 +489,31 @@ __global__ void k_vd_misfit_sum(const double* __restrict__ partial, int n, doubl
 }
 
 // End of a checkpoint window: the FP32 window sums of the first A shots are
-// added into the FP64 totals of their groups (gsize consecutive shots each)
-// and cleared.
-__global__ void k_vd_flush(Geo g, int A, int gsize, float* __restrict__ acc, double* __restrict__ tot) {
-  const long long npts = (long long)g.nx * g.nz;
-  for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < npts; q += (long long)gridDim.x * blockDim.x) {
-    const int i = (int)(q % g.nx) + 1, j = (int)(q / g.nx) + 1;
-    const long long c = g.lin(i, j);
+// added into the FP64 totals of their groups (gsize consecutive shots each);
+// the host clears the sums right after.  Four consecutive padded points per
+// thread (the padding holds zeros); the shot loop only loads, so the loads of
+// several shots are in flight together.
+__global__ void k_vd_flush(Geo g, int A, int gsize, const float* __restrict__ acc, double* __restrict__ tot) {
+  const long long F4 = g.F / 4;  // F is a multiple of 4
+  const float4* a4 = reinterpret_cast<const float4*>(acc);
+  for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < 3 * F4; q += (long long)gridDim.x * blockDim.x) {
+    const long long f = q / F4, r = q - f * F4;  // field, float4 index in the field
     for (int s0 = 0; s0 < A; s0 += gsize) {
-      double t[3] = {0.0, 0.0, 0.0};
-      for (int s = s0; s < min(s0 + gsize, A); ++s) {
-        float* a = acc + (long long)s * 3 * g.F;
-#pragma unroll
-        for (int f = 0; f < 3; ++f) {
-          t[f] += (double)a[f * g.F + c];
-          a[f * g.F + c] = 0.0f;
-        }
+      double t0 = 0.0, t1 = 0.0, t2 = 0.0, t3 = 0.0;
+      const int s1 = min(s0 + gsize, A);
+#pragma unroll 8
+      for (int s = s0; s < s1; ++s) {
+        const float4 v = __ldg(a4 + ((long long)s * 3 + f) * F4 + r);
+        t0 += (double)v.x;
+        t1 += (double)v.y;
+        t2 += (double)v.z;
+        t3 += (double)v.w;
       }
-      double* T = tot + (long long)(s0 / gsize) * 3 * g.F;
-#pragma unroll
-      for (int f = 0; f < 3; ++f) T[f * g.F + c] += t[f];
+      double* T = tot + ((long long)(s0 / gsize) * 3 + f) * g.F + 4 * r;
+      T[0] += t0;
+      T[1] += t1;
+      T[2] += t2;
+      T[3] += t3;
     }
   }
 }
@@ -1407,7 +1412,7 @@ void vd_gradient(sw_acoustic_vd* vd, int nshots, const sw_acoustic_shot* shots, 
     zero_state(vd, S, true);
     check_cuda(cudaMemsetAsync(vd->acc.p, 0, (size_t)S * 3 * F * sizeof(float), st), "window sums clear");
     check_cuda(cudaMemsetAsync(vd->tot.p, 0, (size_t)ngroups * 3 * F * sizeof(double), st), "totals clear");
-    const int fblocks = (int)std::min<long long>((np + 255) / 256, 4096);
+    const int fblocks = (int)std::min<long long>((3 * (F / 4) + 255) / 256, 8192);
     for (int m = M - 1; m >= 0; --m) {
       const int t0 = m * K + 1, t1 = std::min((m + 1) * K, ntmax);
       if (m < M - 1) {
@@ -1422,6 +1427,7 @@ void vd_gradient(sw_acoustic_vd* vd, int nshots, const sw_acoustic_shot* shots, 
         vd->ctx->prof.begin(st, KK_OTHER, 0.0, &ev);
         k_vd_flush<<<fblocks, 256, 0, st>>>(g, Aw, gsize, vd->acc.as<float>(), vd->tot.as<double>());
         check_cuda(cudaGetLastError(), "window flush launch");
+        check_cuda(cudaMemsetAsync(vd->acc.p, 0, (size_t)Aw * 3 * F * sizeof(float), st), "window sums clear");
         vd->ctx->prof.end(st, KK_OTHER, ev);
       }
     }

@@ -25,10 +25,12 @@ def ctx():
     c.close()
 
 
-def _observed(case, shot, scale=1.15):
+def _observed(case, shot, scale=1.3):
     """Observed data from the oracle on a perturbed model, rounded to FP32 (the
-    precision the library takes them in), so both sides see the same data."""
-    pert = ElCase(case.nx, case.nz, case.h, case.dt, case.halo, case.lam * scale, case.mu * 0.95, case.rho * 0.95,
+    precision the library takes them in), so both sides see the same data.  The
+    perturbation keeps the residuals well above the FP32 rounding of the
+    traces, which the misfit (a difference of nearby numbers) would amplify."""
+    pert = ElCase(case.nx, case.nz, case.h, case.dt, case.halo, case.lam * scale, case.mu * 0.88, case.rho * 0.92,
                   [shot], freetop=case.freetop, sinc=case.sinc, interp_rho=case.interp_rho, interp_mu=case.interp_mu)
     return oracle_forward(pert, shot).astype(np.float32).astype(np.float64)
 
@@ -95,7 +97,7 @@ def test_elastic_gradient_matches_oracle(ctx, kind, freetop, K):
 def test_elastic_gradient_windows_invcov_mute(ctx):
     case = small_case("force", nt=360)
     shot = case.shots[0]
-    obs = _observed(case, shot, 1.2)
+    obs = _observed(case, shot, 1.35)
     ic = np.linspace(0.5, 1.5, shot.nt)
     win = [(20, 150), (200, 330)]
     gref, mref, _ = oracle_gradient(case, shot, obs, check_freq=19, invcov=ic, windows=win, mute_src=6, mute_rec=3)
