@@ -194,27 +194,31 @@ def _case3d(n, h, halo, freetop, seed=1):
     return Case(vp=vp, h=(h, h, h), dt=stable_dt(vp, (h, h, h), 0.6), halo=halo, freetop=freetop)
 
 
+@pytest.mark.parametrize("variant", [0, 2])
 @pytest.mark.parametrize("halo,freetop", [(5, False), (6, True), (0, False)])
-def test_forward_3d_matches_oracle(sw, oracle, halo, freetop):
+def test_forward_3d_matches_oracle(sw, oracle, halo, freetop, variant):
     case = _case3d((37, 29, 33), 10.0, halo, freetop, seed=halo + 1)
     ex = _extent(case)
     rec = [[0.2 * ex[0], 0.3 * ex[1], 0.5 * ex[2]], [0.8 * ex[0], 0.6 * ex[1], 0.4 * ex[2]],
            [0.5 * ex[0], 0.5 * ex[1], 0.9 * ex[2]]]
     shot = make_shot(case.h, ex, 260, case.dt, 15.0, [[0.45 * ex[0], 0.55 * ex[1], 0.35 * ex[2]]], rec)
-    run = GpuRun(sw, case)
+    run = GpuRun(sw, case, variant=variant)
     tr = run.forward([shot])[0]
     run.close()
     assert rel_l2(tr, oracle_forward(oracle, sw, case, shot)) < TRACE_TOL
 
 
-def test_gradient_3d_matches_oracle(sw, oracle):
+@pytest.mark.parametrize("variant", [0, 2])
+def test_gradient_3d_matches_oracle(sw, oracle, variant):
+    """3D gradient with 4 (variant 0) or 8 (variant 2) y rows per block; the
+    y extent (30) leaves a partly filled last tile in both."""
     case = _case3d((34, 30, 32), 10.0, 5, False, seed=4)
     ex = _extent(case)
     rec = [[x, 0.5 * ex[1], 0.3 * ex[2]] for x in np.linspace(0.2 * ex[0], 0.8 * ex[0], 5)]
     shot = make_shot(case.h, ex, 200, case.dt, 15.0, [[0.5 * ex[0], 0.5 * ex[1], 0.6 * ex[2]]], rec)
     pert = Case(vp=np.asfortranarray(case.vp * 1.04), h=case.h, dt=case.dt, halo=case.halo, freetop=False)
     shot.observed = oracle_forward(oracle, sw, pert, shot)
-    run = GpuRun(sw, case, gradient=True, check_freq=13)
+    run = GpuRun(sw, case, gradient=True, check_freq=13, variant=variant)
     g, msf, _ = run.gradient([shot])
     run.close()
     gref, mref, _ = oracle_gradient(oracle, sw, case, shot, check_freq=13)
