@@ -759,7 +759,11 @@ def run_gb300(a):
                                            max(s.rec_pos.shape[0] for s in w.shots)],
                        "check_freq": w.check_freq, "halo": w.halo,
                        "cache": "inputs larger than L2 (each step streams tens of GB of wavefield state)",
-                       "precision": "fp32 wavefields and stencil, Kahan fp32 correlation, fp64 misfit and shot sum"
+                       "precision": "fp32 wavefields and stencil, "
+                                    + ("fp32 correlation sums flushed to fp64 every 32 steps"
+                                       if (nd == 2 and not (a.variant >= 0 and (a.variant & 256)))
+                                       else "Kahan fp32 correlation")
+                                    + ", fp64 misfit and shot sum"
                                     + (", bf16 recompute buffer" if a.bf16 >= 1 else "")
                                     + (", bf16 checkpoints" if a.bf16 >= 2 else ""),
                        "parallelism": f"replicas x{world}" if world > 1 else "1 GPU, all shots batched"},

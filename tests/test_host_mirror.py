@@ -53,3 +53,42 @@ def test_parameter_checks(sw):
         sw.ScalarSources(np.zeros((0, 2)), np.zeros((10, 0)), 5.0)
     assert sw.courant_number(np.full((3, 3), 2000.0), 1e-3, (5.0, 5.0)) == pytest.approx(2000 * 1e-3 * np.sqrt(0.08))
     assert sw.points_per_wavelength(np.full((3, 3), 1500.0), (10.0, 8.0), 8.0) == pytest.approx(1500 / 160)
+
+
+def test_vd_source_scaling_and_cfl(sw):
+    """possrcrec_scaletf of the VD simulation (tf * dt * vp^2 rho / prod(h),
+    acou_forward.jl:66-80) and its CFL number with the 7/6 factor (acou_models.jl:240-251)."""
+    import importlib
+    V = importlib.import_module(sw.__name__ + ".vd")
+    vp = np.asfortranarray(np.arange(1, 13, dtype=float).reshape(3, 4, order="F") * 100)
+    rho = np.asfortranarray(1000.0 + np.arange(12, dtype=float).reshape(3, 4, order="F"))
+    tf = np.ones((5, 2))
+    si = np.array([[2, 3], [1, 1]], dtype=np.int32)
+    out = V.scale_srctf_vd(tf, si, vp, rho, (2.0, 4.0), 1e-3)
+    assert out.dtype == np.float32
+    np.testing.assert_allclose(out[:, 0], 1e-3 / 8.0 * vp[1, 2] ** 2 * rho[1, 2], rtol=1e-6)
+    np.testing.assert_allclose(out[:, 1], 1e-3 / 8.0 * vp[0, 0] ** 2 * rho[0, 0], rtol=1e-6)
+    c = V.vd_courant_number(vp, 1e-3, (2.0, 4.0))
+    assert c == pytest.approx(1200.0 * 1e-3 * np.sqrt(1 / 4 + 1 / 16) * 7 / 6)
+    mp = sw.VpRhoAcousticVDMaterialProperties(vp, rho)
+    assert mp.interp_method.code == 0
+    assert sw.VpRhoAcousticVDMaterialProperties(vp, rho, sw.HarmonicAverageInterpolation()).interp_method.code == 1
+
+
+def test_vd_and_ccts_shot_consistency(sw):
+    """check_sim_consistency accepts scalar shots for VD material properties
+    and rejects vector receivers; CCTSMisfit keeps the reference's arguments."""
+    from seismicwaves_gb300 import api
+    vp = np.full((10, 8), 2000.0)
+    mp = sw.VpRhoAcousticVDMaterialProperties(vp, np.full((10, 8), 1800.0))
+    shot = sw.ScalarShot(srcs=sw.ScalarSources(np.array([[20.0, 20.0]]), np.ones((10, 1)), 10.0),
+                         recs=sw.ScalarReceivers(np.array([[30.0, 10.0]]), 10))
+    api._check_sim_consistency(mp, [shot])
+    bad = sw.ScalarShot(srcs=shot.srcs, recs=sw.VectorReceivers(np.array([[30.0, 10.0]]), 10))
+    with pytest.raises(TypeError):
+        api._check_sim_consistency(mp, [bad])
+    m = sw.CCTSMisfit(1e-3, std=2.0, observed=np.zeros((10, 1)))
+    assert m.kind == 1 and m.dt == 1e-3 and m.std == 2.0
+    assert m.invcov_diagonal() is None and m.invcov_dense() is None and m.windows == []
+    with pytest.raises(AssertionError):
+        sw.CCTSMisfit(0.0, observed=np.zeros((10, 1)))
