@@ -24,6 +24,12 @@
 // they are reached (no copy kernels).  Recovery events fall on it = mK for
 // every shot regardless of its nt, so shots with different record lengths
 // share one schedule; a shot takes part in step it only while it <= nt.
+//
+// Correlation sums.  In 2D the adjoint stencil adds lambda * D into a plain
+// FP32 sum per shot, which k_flush_grad adds into one FP64 total every 32
+// adjoint steps (no FP32 sum runs over more than 32 terms); 3D, muted runs
+// (which need each shot's own gradient) and the grouped 2D kernel of tuning
+// variant 256 keep Kahan-compensated FP32 sums instead.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
