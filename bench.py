@@ -56,6 +56,24 @@ def _args():
     return p.parse_args()
 
 
+def max_over_ranks(t: float, dist=None, device=None) -> float:
+    """The slowest rank's time (the job's time): all-reduce MAX over the process
+    group, or t itself when running alone."""
+    if dist is None or not dist.is_initialized() or dist.get_world_size() == 1:
+        return t
+    import torch
+
+    tt = torch.tensor([t], dtype=torch.float64, device=device)
+    dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+    return float(tt.item())
+
+
+def whole_job_rate(units_per_rank: float, steps: int, world: int, t: float) -> float:
+    """Whole-job throughput of `world` replicas that each process `units_per_rank`
+    per step for `steps` steps in (max-over-ranks) time t."""
+    return units_per_rank * steps * world / t
+
+
 def _dist():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -699,13 +717,10 @@ def run_gb300(a):
     t_prof = R.timed(lambda: R.gradient_device(allidx), 1)
     R.ctx.profile(False)
     prof = {k: R.ctx.profile_read(k) for k in range(5)}
-    if dist:
-        tt = torch.tensor([t_dev], device=R.dev)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_dev = float(tt.item())
+    t_dev = max_over_ranks(t_dev, dist, R.dev)
     barrier()
-    value = pts * a.steps * world / t_dev / 1e9
-    shots_per_s = nshots * a.steps * world / t_dev
+    value = whole_job_rate(pts, a.steps, world, t_dev) / 1e9
+    shots_per_s = whole_job_rate(nshots, a.steps, world, t_dev)
 
     # end to end through the C ABI with pinned host buffers (inputs up, gradient/traces down, every step)
     h2d, d2h = R.setup_host()
