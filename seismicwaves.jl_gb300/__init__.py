@@ -16,6 +16,7 @@ from .elastic import (ArithmeticAverageInterpolation, ElasticIsoCPMLWaveSimulati
                       ExternalForceShot, ExternalForceSources, HarmonicAverageInterpolation, InputParametersElastic,
                       MomentTensor2D, MomentTensorShot, MomentTensorSources, VectorReceivers, spread_positions)
 from .vd import AcousticVDStaggeredCPMLWaveSimulation, VpRhoAcousticVDMaterialProperties
+from .rrules import GRADIENT_SIGN, misfit_function, rrule_swmisfit
 
 __all__ = [
     "AcousticCDCPMLWaveSimulation", "CCTSMisfit", "CPMLBoundaryConditionParameters", "GradParameters", "InputParametersAcoustic",
@@ -26,4 +27,5 @@ __all__ = [
     "ElasticIsoMaterialProperties", "ExternalForceShot", "ExternalForceSources", "HarmonicAverageInterpolation",
     "InputParametersElastic", "MomentTensor2D", "MomentTensorShot", "MomentTensorSources", "VectorReceivers",
     "spread_positions", "AcousticVDStaggeredCPMLWaveSimulation", "VpRhoAcousticVDMaterialProperties",
+    "GRADIENT_SIGN", "misfit_function", "rrule_swmisfit",
 ]

@@ -191,3 +191,26 @@ def test_ccts_gradient_misfit_consistency(oracle):
     recs = sw.ScalarReceivers(posrec, nt)
     recs.seismograms[...] = tr
     assert m == pytest.approx(mis.calcmisfit(recs), rel=1e-12)
+
+
+def test_vp_gradient_finite_difference_sign(oracle, sw):
+    """The reference's constant-density gradient is -d(chi)/d(vp): <g, dv> against
+    the central difference of the misfit along a Gaussian dv agrees to 1 % with
+    the opposite sign (the reverse-mode rule of the backend relies on it)."""
+    from cases import Case, make_shot, oracle_forward, oracle_gradient, smooth_model, stable_dt
+    n, h = (90, 80), (5.0, 5.0)
+    vp = smooth_model(n, 1800.0, 3000.0, seed=3)
+    dt = stable_dt(vp, h)
+    shot = make_shot(h, None, 500, dt, 15.0, [[200.0, 200.0]], [[x, 120.0] for x in np.linspace(80, 360, 9)])
+    case = Case(vp, h, dt, 10, False, shots=[shot])
+    shot.observed = oracle_forward(oracle, sw, Case(np.asfortranarray(vp * 1.03), h, dt, 10, False), shot)
+    g, _, _ = oracle_gradient(oracle, sw, case, shot, check_freq=7)
+    x = np.arange(n[0])[:, None]
+    z = np.arange(n[1])[None, :]
+    dv = np.exp(-((x - 60) ** 2 + (z - 30) ** 2) / (2 * 6.0 ** 2))
+    eps = 2.0
+    ms = [oracle_gradient(oracle, sw, Case(np.asfortranarray(vp + s * eps * dv), h, dt, 10, False), shot,
+                          check_freq=7)[1] for s in (1, -1)]
+    fd = (ms[0] - ms[1]) / (2 * eps)
+    an = float(np.sum(g * dv))
+    assert abs(fd) > 0 and abs(an + fd) <= 0.01 * abs(fd)

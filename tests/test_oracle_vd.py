@@ -144,3 +144,22 @@ def test_vd_snapshots_match_forward_state():
         it = 40 * (k + 1)
         assert vx.shape == (59, 50) and vz.shape == (60, 49)
         np.testing.assert_array_equal(tr[it - 1], p[ri[:, 0], ri[:, 1]])
+
+
+def test_vd_rho_gradient_finite_difference():
+    """The rho gradient carries the same sign as vp's (-d(chi)/d(rho)); it agrees
+    with the central difference of the misfit to 1 %."""
+    case = small_case(nt=500, nx=90, nz=80, halo=10)
+    shot = case.shots[0]
+    pert = VDCase(case.vp * 1.03, case.rho * 0.97, case.h, case.dt, case.halo, shots=[shot])
+    obs = oracle_forward(pert, shot)
+    g, _, _ = oracle_gradient(case, shot, obs, check_freq=7)
+    x = np.arange(case.vp.shape[0])[:, None]
+    z = np.arange(case.vp.shape[1])[None, :]
+    dv = np.exp(-((x - 40) ** 2 + (z - 55) ** 2) / (2 * 6.0 ** 2))
+    eps = 2.0
+    ms = [oracle_gradient(VDCase(case.vp, np.asfortranarray(case.rho + s * eps * dv), case.h, case.dt, case.halo,
+                                 shots=[shot]), shot, obs, check_freq=7)[1] for s in (1, -1)]
+    fd = (ms[0] - ms[1]) / (2 * eps)
+    an = float(np.sum(g["rho"] * dv))
+    assert abs(fd) > 0 and abs(an + fd) <= 0.01 * abs(fd)
