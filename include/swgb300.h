@@ -204,7 +204,10 @@ int sw_acoustic_forward_snapshots(sw_wavesim* ws, int32_t nshots, const sw_acous
  * by default the 2D adjoint runs per shot with plain FP32 correlation sums
  * flushed into an FP64 total every 32 steps; + 256 selects instead the grouped
  * adjoint (4 shots per block, one Kahan-compensated FP32 sum per group; 4+
- * shots).  Results do not depend on any of them beyond rounding. */
+ * shots); + 512 stages the rows of the 4-warp stencil through a per-warp
+ * shared-memory ring filled by cp.async (three rows in flight per warp
+ * instead of one, no registers held by the copies).  Results do not depend
+ * on any of them beyond rounding. */
 int sw_wavesim_set_tuning(sw_wavesim* ws, int32_t tz, int32_t variant);
 
 /* CUDA graphs (on by default): a batch's whole device-side time loop

@@ -444,6 +444,7 @@ struct sw_wavesim {
   int tile_tz = 0;  // 0 = heuristic
   int variant = 0;  // 2D stencil: 0 = register-pipelined, 1 = TMA
   int pf = 0;       // 2D stencil: L2 prefetch distance in rows (0 = off)
+  bool cpa = false; // 2D stencil (4 warps): rows staged through shared memory by cp.async
   int grp = 1;      // shots per gradient accumulator in the adjoint (4: shot sum fused, 1: per shot)
   bool adj_plain = true;   // 2D: per-shot adjoint with plain FP32 sums flushed to FP64 (MODE_ADJW);
                            // false: the grouped Kahan adjoint (k_ac2d_adj_grp) for 4+ shots
@@ -530,6 +531,7 @@ void run_graph(sw_wavesim* ws, std::vector<long long> key, Work&& work) {
 
 std::vector<long long> group_key(const sw_wavesim* ws, const std::vector<HostShot>& group, bool grad) {
   std::vector<long long> k = {grad ? 1 : 0, ws->grp, ws->variant, ws->tile_tz, ws->pf, ws->adjw ? 1 : 0,
+                              ws->cpa ? 1 : 0,
                              (long long)group.size()};
   for (const auto& h : group) k.push_back(h.nt);
   return k;
@@ -952,6 +954,21 @@ void enable_tma_smem() {
   done_for_device = dev;
 }
 
+// The cp.async-staged stencil keeps its row ring in shared memory (24-36 KB
+// per block): ask for the largest shared-memory carveout so that the
+// occupancy of its launch bounds is reached.
+template <int MODE>
+void enable_cpa_carveout() {
+  static int done_for_device = -1;
+  int dev = 0;
+  check_cuda(cudaGetDevice(&dev), "cudaGetDevice");
+  if (done_for_device == dev) return;
+  check_cuda(cudaFuncSetAttribute(k_ac2d_cpa<MODE, 4>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                  (int)cudaSharedmemCarveoutMaxShared),
+             "shared memory carveout");
+  done_for_device = dev;
+}
+
 struct Launcher {
   sw_wavesim* ws;
   cudaStream_t st;
@@ -962,9 +979,12 @@ struct Launcher {
     cudaEvent_t ev = nullptr;
     const int kind = (MODE == MODE_ADJ || MODE == MODE_ADJW) ? KK_ADJOINT : (recompute ? KK_RECOMPUTE : KK_STENCIL);
     ws->ctx->prof.begin(st, kind, bytes, &ev);
-    if constexpr (MODE == MODE_ADJW) {  // 2D register-pipelined stencil only
+    if constexpr (MODE == MODE_ADJW) {  // 2D register-pipelined or cp.async-staged stencil only
       const int nw = block_warps(ws);
-      if (nw == 4)
+      if (nw == 4 && ws->cpa) {
+        enable_cpa_carveout<MODE>();
+        k_ac2d_cpa<MODE, 4><<<(unsigned)blocks, 128, 0, st>>>(a);
+      } else if (nw == 4)
         k_ac2d_step<MODE, 4><<<(unsigned)blocks, 128, 0, st>>>(a);
       else if (nw == 8)
         k_ac2d_step<MODE, 8><<<(unsigned)blocks, 256, 0, st>>>(a);
@@ -976,8 +996,13 @@ struct Launcher {
     } else if (ws->N == 2) {
       const int nw = block_warps(ws);
       bool launched = false;
+      if (nw == 4 && ws->cpa) {
+        enable_cpa_carveout<MODE>();
+        k_ac2d_cpa<MODE, 4><<<(unsigned)blocks, 128, 0, st>>>(a);
+        launched = true;
+      }
       if constexpr (MODE != MODE_ADJ) {
-        if (nw == 4 && (ws->variant & 4)) {
+        if (!launched && nw == 4 && (ws->variant & 4)) {
           k_ac2d_step<MODE, 4, 2><<<(unsigned)blocks, 128, 0, st>>>(a);
           launched = true;
         }
@@ -1697,6 +1722,7 @@ void wavesim_set_tuning(sw_wavesim* ws, int tz, int variant) {
   ws->variant = variant % 16;
   ws->pf = (variant / 16) % 16;
   ws->adj_plain = (variant & 256) == 0;
+  ws->cpa = (variant & 512) != 0;
 }
 void wavesim_use_graphs(sw_wavesim* ws, bool on) {
   ws->use_graphs = on;

@@ -196,6 +196,125 @@ __device__ __forceinline__ float* fptr(const FieldArg& f, int shot) {
 // side in x (512 x points); tile = 512 x points x TZ rows.
 // psi_0 / xi_0 layout: [z][q] (q fastest);  psi_1 / xi_1 layout: [q][P].
 // ---------------------------------------------------------------------------
+// One row of the 2D step at one thread's four x points: given p[n] of rows
+// z-1, z, z+1 (rm, r0, rp) with the x neighbours of row z (left, right),
+// d[n] and fact of row z, it advances the C-PML variables and writes p[n+1],
+// d[n+1] and the side outputs (D, checkpoint copies) and, in the adjoint
+// modes, the correlation term into the sums g4 (and compensations c4) of the
+// row, which it stores.  Shared by the register-pipelined and the
+// cp.async-staged kernels, which differ only in how rows reach registers.
+template <int MODE>
+struct Ac2dRow {
+  int nx, nz, P, H, x0, dbf16;
+  bool inb, xstrip, vec_interior;
+  float ihx, ihz, ih2x, ih2z;
+  StripIO sx, sz;
+  float *pn, *dn, *ckp, *ckd, *Dw, *gg, *gcp;
+
+  __device__ __forceinline__ void init(const StepArgs& A, int shot, int x0_) {
+    nx = A.n0; nz = A.n1; P = A.P; H = A.halo; x0 = x0_; dbf16 = A.dbf16;
+    ihx = A.ih[0]; ihz = A.ih[1]; ih2x = A.ih2[0]; ih2z = A.ih2[1];
+    inb = x0 < P;
+    const int na = 2 * H + 2, nh = 2 * H, L = 2 * na + 2 * nh;
+    const float* cp = A.cpml + (long long)shot * A.cpml_stride;
+    sx.psi_in = fptr(A.psi_in[0], shot);  sx.psi_out = fptr(A.psi_out[0], shot);
+    sx.xi_in = fptr(A.xi_in[0], shot);    sx.xi_out = fptr(A.xi_out[0], shot);
+    sx.ck_psi = fptr(A.ck_psi[0], shot);  sx.ck_xi = fptr(A.ck_xi[0], shot);
+    sx.a = cp; sx.ah = cp + na; sx.b = cp + na + nh; sx.bh = cp + 2 * na + nh;
+    sx.psi_step = 1; sx.xi_step = 1;
+    sz.psi_in = fptr(A.psi_in[1], shot);  sz.psi_out = fptr(A.psi_out[1], shot);
+    sz.xi_in = fptr(A.xi_in[1], shot);    sz.xi_out = fptr(A.xi_out[1], shot);
+    sz.ck_psi = fptr(A.ck_psi[1], shot);  sz.ck_xi = fptr(A.ck_xi[1], shot);
+    sz.a = cp + L; sz.ah = cp + L + na; sz.b = cp + L + na + nh; sz.bh = cp + L + 2 * na + nh;
+    sz.psi_step = P; sz.xi_step = P;
+    xstrip = inb && (x0 < H || x0 + 3 >= nx - H);
+    vec_interior = (x0 >= 1) && (x0 + 3 <= nx - 2);
+    pn = fptr(A.pnew, shot);
+    dn = fptr(A.dout, shot);
+    ckp = fptr(A.ck_p, shot);
+    ckd = fptr(A.ck_d, shot);
+    Dw = (MODE == MODE_FWD_D && shot >= A.d_first) ? dptr(A.Dout, shot, A.dbf16) : nullptr;
+    constexpr bool ADJ = MODE == MODE_ADJ || MODE == MODE_ADJW;
+    gg = ADJ ? fptr(A.g, shot) : nullptr;
+    gcp = MODE == MODE_ADJ ? fptr(A.gc, shot) : nullptr;
+  }
+
+  __device__ __forceinline__ void update(int z, const float (&rm)[4], const float (&r0)[4], const float (&rp)[4],
+                                         const float (&o)[4], const float (&f)[4], const float (&dv)[4],
+                                         float (&g4)[4], float (&c4)[4], float left, float right) {
+    const long long row = (long long)z * P;
+    const bool zstrip = (z < H) || (z >= nz - H);
+    sx.psi_base = (long long)z * (2 * H);
+    sx.xi_base = (long long)z * (2 * H + 2);
+    float outp[4], outd[4], outD[4];
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+      const float xm = e == 0 ? left : r0[e - 1];
+      const float xp = e == 3 ? right : r0[e + 1];
+      const float c = r0[e];
+      float tx = (xm - 2.f * c + xp) * ih2x;
+      float tz = (rm[e] - 2.f * c + rp[e]) * ih2z;
+      const int x = x0 + e;
+      const bool pin = inb && x >= 1 && x <= nx - 2;
+      if (xstrip && pin) tx = cpml_axis_term(tx, xm, c, xp, x, nx, H, ihx, sx);
+      if (zstrip && pin) {
+        sz.psi_base = x;
+        sz.xi_base = x;
+        tz = cpml_axis_term(tz, rm[e], c, rp[e], z, nz, H, ihz, sz);
+      }
+      const float lap = tx + tz;
+      outD[e] = f[e] * lap;
+      outd[e] = o[e] + outD[e];
+      outp[e] = c + outd[e];
+    }
+    if (!inb) return;
+    if (ckp) {
+      st4(ckp + row + x0, r0);
+      st4(ckd + row + x0, o);
+    }
+    if (MODE == MODE_ADJ) {
+#pragma unroll
+      for (int e = 0; e < 4; ++e)
+        if (x0 + e >= 1 && x0 + e <= nx - 2) kahan_add(g4[e], c4[e], outp[e] * dv[e]);
+      if (vec_interior) {
+        st4(gg + row + x0, g4);
+        st4(gcp + row + x0, c4);
+      } else {
+#pragma unroll
+        for (int e = 0; e < 4; ++e)
+          if (x0 + e >= 1 && x0 + e <= nx - 2) { gg[row + x0 + e] = g4[e]; gcp[row + x0 + e] = c4[e]; }
+      }
+    }
+    if (MODE == MODE_ADJW) {
+#pragma unroll
+      for (int e = 0; e < 4; ++e)
+        if (x0 + e >= 1 && x0 + e <= nx - 2) g4[e] += outp[e] * dv[e];
+      if (vec_interior) {
+        st4(gg + row + x0, g4);
+      } else {
+#pragma unroll
+        for (int e = 0; e < 4; ++e)
+          if (x0 + e >= 1 && x0 + e <= nx - 2) gg[row + x0 + e] = g4[e];
+      }
+    }
+    if (vec_interior) {
+      st4(pn + row + x0, outp);
+      st4(dn + row + x0, outd);
+      if (MODE == MODE_FWD_D && Dw) dst4(Dw, row + x0, outD, dbf16);
+    } else {
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        const int x = x0 + e;
+        if (x >= 1 && x <= nx - 2) {
+          pn[row + x] = outp[e];
+          dn[row + x] = outd[e];
+          if (MODE == MODE_FWD_D && Dw) dst1(Dw, row + x, outD[e], dbf16);
+        }
+      }
+    }
+  }
+};
+
 // Minimum resident blocks per SM for a block of NW warps: keeps the forward
 // kernels at <= 64 registers (8 blocks of 4 warps; measured 4.0 / 4.4 TB/s
 // forward / recompute against 3.8 / 4.3 at 7 blocks, a few bytes spilled);
@@ -219,7 +338,7 @@ __global__ void __launch_bounds__(32 * NW, (Ac2dBounds<MODE, NW>::MINB - (DP - 1
   const int txi = blockIdx.x % A.tiles_x;
   const int rest = blockIdx.x / A.tiles_x;
   const int shot = rest % S, tzi = rest / S;
-  const int nx = A.n0, nz = A.n1, P = A.P, H = A.halo;
+  const int nz = A.n1, P = A.P;
   const int z_begin = 1 + tzi * A.TZ;
   const int z_end = min(z_begin + A.TZ, nz - 1);
   const int wx0 = (txi * nwarps + warp) * 128;
@@ -229,35 +348,14 @@ __global__ void __launch_bounds__(32 * NW, (Ac2dBounds<MODE, NW>::MINB - (DP - 1
   const int xa = inb ? x0 : P - 4;
 
   const float* __restrict__ pc = fptr(A.pcur, shot);
-  float* __restrict__ pn = fptr(A.pnew, shot);
   const float* di = fptr(A.din, shot);
-  float* dn = fptr(A.dout, shot);
   const float* __restrict__ fa = A.fact;
-  const float* cp = A.cpml + (long long)shot * A.cpml_stride;
-  const int na = 2 * H + 2, nh = 2 * H, L = 2 * na + 2 * nh;
-
-  StripIO sx, sz;
-  sx.psi_in = fptr(A.psi_in[0], shot);  sx.psi_out = fptr(A.psi_out[0], shot);
-  sx.xi_in = fptr(A.xi_in[0], shot);    sx.xi_out = fptr(A.xi_out[0], shot);
-  sx.ck_psi = fptr(A.ck_psi[0], shot);  sx.ck_xi = fptr(A.ck_xi[0], shot);
-  sx.a = cp; sx.ah = cp + na; sx.b = cp + na + nh; sx.bh = cp + 2 * na + nh;
-  sx.psi_step = 1; sx.xi_step = 1;
-  sz.psi_in = fptr(A.psi_in[1], shot);  sz.psi_out = fptr(A.psi_out[1], shot);
-  sz.xi_in = fptr(A.xi_in[1], shot);    sz.xi_out = fptr(A.xi_out[1], shot);
-  sz.ck_psi = fptr(A.ck_psi[1], shot);  sz.ck_xi = fptr(A.ck_xi[1], shot);
-  sz.a = cp + L; sz.ah = cp + L + na; sz.b = cp + L + na + nh; sz.bh = cp + L + 2 * na + nh;
-  sz.psi_step = P; sz.xi_step = P;
-
-  const bool xstrip = inb && (x0 < H || x0 + 3 >= nx - H);
-  const bool vec_interior = (x0 >= 1) && (x0 + 3 <= nx - 2);
-  float* ckp = fptr(A.ck_p, shot);
-  float* ckd = fptr(A.ck_d, shot);
-  float* Dw = nullptr;
-  if (MODE == MODE_FWD_D && shot >= A.d_first) Dw = dptr(A.Dout, shot, A.dbf16);
+  Ac2dRow<MODE> R;
+  R.init(A, shot, x0);
   constexpr bool ADJ = MODE == MODE_ADJ || MODE == MODE_ADJW;
   const float* dcr = ADJ ? dptr(A.dcorr, shot, A.dbf16) : nullptr;
-  float* gg = ADJ ? fptr(A.g, shot) : nullptr;
-  float* gcp = MODE == MODE_ADJ ? fptr(A.gc, shot) : nullptr;
+  float* gg = R.gg;
+  float* gcp = R.gcp;
 
   // The loads of row z+1 (p of row z+2, d, fact and for the adjoint D, g, gc)
   // are issued before the stores of row z, so each warp keeps two rows of
@@ -326,76 +424,7 @@ __global__ void __launch_bounds__(32 * NW, (Ac2dBounds<MODE, NW>::MINB - (DP - 1
     float right = __shfl_down_sync(FULL, r0[0], 1);
     if (lane == 0) left = xa > 0 ? pc[row + xa - 1] : 0.f;
     if (lane == 31) right = xa + 4 < P ? pc[row + xa + 4] : 0.f;
-    const bool zstrip = (z < H) || (z >= nz - H);
-    sx.psi_base = (long long)z * nh;
-    sx.xi_base = (long long)z * na;
-    float outp[4], outd[4], outD[4];
-#pragma unroll
-    for (int e = 0; e < 4; ++e) {
-      const float xm = e == 0 ? left : r0[e - 1];
-      const float xp = e == 3 ? right : r0[e + 1];
-      const float c = r0[e];
-      float tx = (xm - 2.f * c + xp) * A.ih2[0];
-      float tz = (rm[e] - 2.f * c + rp[e]) * A.ih2[1];
-      const int x = x0 + e;
-      const bool pin = inb && x >= 1 && x <= nx - 2;
-      if (xstrip && pin) tx = cpml_axis_term(tx, xm, c, xp, x, nx, H, A.ih[0], sx);
-      if (zstrip && pin) {
-        sz.psi_base = x;
-        sz.xi_base = x;
-        tz = cpml_axis_term(tz, rm[e], c, rp[e], z, nz, H, A.ih[1], sz);
-      }
-      const float lap = tx + tz;
-      outD[e] = f[e] * lap;
-      outd[e] = o[e] + outD[e];
-      outp[e] = c + outd[e];
-    }
-    if (inb) {
-      if (ckp) {
-        st4(ckp + row + x0, r0);
-        st4(ckd + row + x0, o);
-      }
-      if (MODE == MODE_ADJ) {
-#pragma unroll
-        for (int e = 0; e < 4; ++e)
-          if (x0 + e >= 1 && x0 + e <= nx - 2) kahan_add(g4[e], c4[e], outp[e] * dv[e]);
-        if (vec_interior) {
-          st4(gg + row + x0, g4);
-          st4(gcp + row + x0, c4);
-        } else {
-#pragma unroll
-          for (int e = 0; e < 4; ++e)
-            if (x0 + e >= 1 && x0 + e <= nx - 2) { gg[row + x0 + e] = g4[e]; gcp[row + x0 + e] = c4[e]; }
-        }
-      }
-      if (MODE == MODE_ADJW) {
-#pragma unroll
-        for (int e = 0; e < 4; ++e)
-          if (x0 + e >= 1 && x0 + e <= nx - 2) g4[e] += outp[e] * dv[e];
-        if (vec_interior) {
-          st4(gg + row + x0, g4);
-        } else {
-#pragma unroll
-          for (int e = 0; e < 4; ++e)
-            if (x0 + e >= 1 && x0 + e <= nx - 2) gg[row + x0 + e] = g4[e];
-        }
-      }
-      if (vec_interior) {
-        st4(pn + row + x0, outp);
-        st4(dn + row + x0, outd);
-        if (MODE == MODE_FWD_D && Dw) dst4(Dw, row + x0, outD, A.dbf16);
-      } else {
-#pragma unroll
-        for (int e = 0; e < 4; ++e) {
-          const int x = x0 + e;
-          if (x >= 1 && x <= nx - 2) {
-            pn[row + x] = outp[e];
-            dn[row + x] = outd[e];
-            if (MODE == MODE_FWD_D && Dw) dst1(Dw, row + x, outD[e], A.dbf16);
-          }
-        }
-      }
-    }
+    R.update(z, rm, r0, rp, o, f, dv, g4, c4, left, right);
 #pragma unroll
     for (int e = 0; e < 4; ++e) {
       rm[e] = r0[e];
@@ -418,6 +447,145 @@ __global__ void __launch_bounds__(32 * NW, (Ac2dBounds<MODE, NW>::MINB - (DP - 1
   }
 }
 
+
+// ---------------------------------------------------------------------------
+// 2D step with the rows staged through shared memory by cp.async.
+//
+// The register-pipelined kernel holds one row of loads in flight per warp;
+// its bandwidth is that of the bytes in flight (about 1.9 us of loaded DRAM
+// latency per row), and a second register row costs more occupancy than it
+// brings.  Here every lane copies its own 16-byte pieces of the rows ahead
+// into a per-warp ring of S row bundles with cp.async (no registers held
+// while in flight) and later reads back only what it copied itself, so no
+// barrier is needed: cp.async.wait_group orders a lane's copies with its own
+// reads.  Bundle k holds p of row k+1 (with the x neighbours x0-1 of lane 0
+// and x0+4 of lane 31), d and fact of row k and, in the adjoint, D and the
+// sums g (gc) of row k; S-1 bundles are in flight while row z is computed.
+// Bundle z+S-1 reuses the slot of bundle z-1, whose values the row update of
+// iteration z-1 has already consumed.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void cpa16(void* smem, const void* g) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(s), "l"(g) : "memory");
+}
+__device__ __forceinline__ void cpa8(void* smem, const void* g) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(s), "l"(g) : "memory");
+}
+__device__ __forceinline__ void cpa4(void* smem, const void* g) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(s), "l"(g) : "memory");
+}
+__device__ __forceinline__ void cpa_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cpa_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+__device__ __forceinline__ void sld4(float (&v)[4], const float4& s) {
+  v[0] = s.x; v[1] = s.y; v[2] = s.z; v[3] = s.w;
+}
+
+// Row arrays per bundle (p, d, fact [, D, g [, gc]]) and bundles in the ring:
+// 24 KB of ring per 4-warp block for the forward kinds (8 blocks per SM),
+// 30 / 36 KB for the adjoints (6 / 4 blocks per SM).
+template <int MODE>
+struct CpaRing {
+  static constexpr int NA = MODE == MODE_ADJ ? 6 : MODE == MODE_ADJW ? 5 : 3;
+  static constexpr int S = (MODE == MODE_ADJ || MODE == MODE_ADJW) ? 3 : 4;
+};
+
+template <int MODE, int NW>
+__global__ void __launch_bounds__(32 * NW, Ac2dBounds<MODE, NW>::MINB) k_ac2d_cpa(const StepArgs A) {
+  constexpr unsigned FULL = 0xffffffffu;
+  constexpr int NA = CpaRing<MODE>::NA, S = CpaRing<MODE>::S;
+  constexpr bool ADJ = MODE == MODE_ADJ || MODE == MODE_ADJW;
+  __shared__ float4 ring[NW][S][NA][32];
+  __shared__ float halo[NW][S][2];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int txi = blockIdx.x % A.tiles_x;
+  const int rest = blockIdx.x / A.tiles_x;
+  const int shot = rest % A.nshots, tzi = rest / A.nshots;
+  const int nz = A.n1, P = A.P;
+  const int z_begin = 1 + tzi * A.TZ;
+  const int z_end = min(z_begin + A.TZ, nz - 1);
+  const int wx0 = (txi * NW + warp) * 128;
+  if (z_begin >= z_end || wx0 >= P) return;  // warp-uniform
+  const int x0 = wx0 + lane * 4;
+  const int xa = x0 < P ? x0 : P - 4;
+  const bool has_left = lane == 0 && xa > 0, has_right = lane == 31 && xa + 4 < P;
+
+  const float* __restrict__ pc = fptr(A.pcur, shot);
+  const float* di = fptr(A.din, shot);
+  const float* __restrict__ fa = A.fact;
+  Ac2dRow<MODE> R;
+  R.init(A, shot, x0);
+  const float* dcr = ADJ ? dptr(A.dcorr, shot, A.dbf16) : nullptr;
+
+  auto issue = [&](int k) {  // bundle k into slot k % S; an empty group past the band
+    if (k < z_end) {
+      const int sl = k % S;
+      const long long row = (long long)k * P;
+      cpa16(&ring[warp][sl][0][lane], pc + row + P + xa);
+      cpa16(&ring[warp][sl][1][lane], di + row + xa);
+      cpa16(&ring[warp][sl][2][lane], fa + row + xa);
+      if (has_left) cpa4(&halo[warp][sl][0], pc + row + P + xa - 1);
+      if (has_right) cpa4(&halo[warp][sl][1], pc + row + P + xa + 4);
+      if constexpr (ADJ) {
+        if (A.dbf16)
+          cpa8(&ring[warp][sl][3][lane], reinterpret_cast<const __nv_bfloat16*>(dcr) + row + xa);
+        else
+          cpa16(&ring[warp][sl][3][lane], dcr + row + xa);
+        cpa16(&ring[warp][sl][4][lane], R.gg + row + xa);
+        if constexpr (MODE == MODE_ADJ) cpa16(&ring[warp][sl][5][lane], R.gcp + row + xa);
+      }
+    }
+    cpa_commit();
+  };
+
+  float rm[4], r0[4];
+  ld4(rm, pc + (long long)(z_begin - 1) * P + xa);
+  ld4(r0, pc + (long long)z_begin * P + xa);
+  float hl = has_left ? pc[(long long)z_begin * P + xa - 1] : 0.f;
+  float hr = has_right ? pc[(long long)z_begin * P + xa + 4] : 0.f;
+#pragma unroll
+  for (int q = 0; q < S - 1; ++q) issue(z_begin + q);
+  for (int z = z_begin; z < z_end; ++z) {
+    cpa_wait<S - 2>();  // bundle z has landed (bundles z+1 .. z+S-2 may be in flight)
+    const int sl = z % S;
+    float rp[4], o[4], f[4], dv[4], g4[4], c4[4];
+    sld4(rp, ring[warp][sl][0][lane]);
+    sld4(o, ring[warp][sl][1][lane]);
+    sld4(f, ring[warp][sl][2][lane]);
+    const float nhl = has_left ? halo[warp][sl][0] : 0.f;
+    const float nhr = has_right ? halo[warp][sl][1] : 0.f;
+    if constexpr (ADJ) {
+      if (A.dbf16) {
+        const uint2 u = *reinterpret_cast<const uint2*>(&ring[warp][sl][3][lane]);
+        const float2 a = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&u.x));
+        const float2 b = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&u.y));
+        dv[0] = a.x; dv[1] = a.y; dv[2] = b.x; dv[3] = b.y;
+      } else {
+        sld4(dv, ring[warp][sl][3][lane]);
+      }
+      sld4(g4, ring[warp][sl][4][lane]);
+      if constexpr (MODE == MODE_ADJ) sld4(c4, ring[warp][sl][5][lane]);
+    }
+    float left = __shfl_up_sync(FULL, r0[3], 1);
+    float right = __shfl_down_sync(FULL, r0[0], 1);
+    if (lane == 0) left = hl;
+    if (lane == 31) right = hr;
+    R.update(z, rm, r0, rp, o, f, dv, g4, c4, left, right);
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+      rm[e] = r0[e];
+      r0[e] = rp[e];
+    }
+    hl = nhl;
+    hr = nhr;
+    issue(z + S - 1);
+  }
+  cpa_wait<0>();
+}
 
 // ---------------------------------------------------------------------------
 // 2D adjoint step for a group of 4 shots with the correlation summed over the

@@ -19,7 +19,7 @@ from . import _lib
 
 _cache: dict = {}
 
-CANDIDATES_2D = [(0, 4), (0, 8), (0, 16), (2, 8), (1, 32), (1, 64)]
+CANDIDATES_2D = [(0, 4), (0, 8), (0, 16), (2, 8), (512, 8), (1, 32), (1, 64)]
 CANDIDATES_3D = [(0, 8), (0, 16), (0, 32), (0, 64)]
 
 

@@ -290,11 +290,12 @@ def test_gradient_bf16_checkpoints_2d(sw, oracle, check_freq):
 
 @pytest.mark.parametrize("tz", [0, 7, 64])
 def test_2d_stencil_variants_match_oracle(sw, oracle, tz):
-    """The TMA-pipelined 2D stencil (variant 1) and the register-pipelined one
-    (variant 0) give the oracle's traces and gradient for any tile height."""
+    """The register-pipelined 2D stencil (variant 0), the TMA-pipelined one
+    (variant 1) and the cp.async-staged one (variant 512) give the oracle's
+    traces and gradient for any tile height."""
     case, shot = _grad_case(sw, oracle, nt=300, freetop=True, halo=12, seed=8)
     gref, mref, tref = oracle_gradient(oracle, sw, case, shot, check_freq=11)
-    for variant in (0, 1):
+    for variant in (0, 1, 512):
         run = GpuRun(sw, case, gradient=True, check_freq=11, variant=variant, tz=tz)
         g, msf, tr = run.gradient([shot])
         fw = run.forward([shot])[0]
@@ -325,11 +326,12 @@ def test_graph_replay_is_bitwise_identical(sw, oracle):
     on.close()
 
 
-@pytest.mark.parametrize("variant", [0, 8, 256])
+@pytest.mark.parametrize("variant", [0, 256, 264, 512, 768])
 def test_gradient_grouped_adjoint_variants(sw, oracle, variant):
-    """The grouped 2D adjoint (4+ shots, one Kahan update per group) with 4 or
-    5 resident blocks per SM, and the per-shot adjoint with plain FP32 sums
-    flushed into FP64 every 32 steps (variant 256), match the oracle's shot sum."""
+    """The per-shot 2D adjoint with plain FP32 sums flushed into FP64 every 32
+    steps (default), the grouped adjoint (256: 4+ shots, one Kahan update per
+    group) with 4 or 5 (264) resident blocks per SM, and both with the
+    cp.async-staged stencil (512, 768) match the oracle's shot sum."""
     case, shot = _grad_case(sw, oracle, nt=300)
     run = GpuRun(sw, case, gradient=True, check_freq=10, variant=variant)
     g, msf, _ = run.gradient([shot] * 5)
@@ -359,3 +361,27 @@ def test_gradient_dense_invcov(sw, oracle):
     print(f"dense invcov: misfit {abs(msf - mref) / abs(mref):.2e} gradient {rel_l2(g, gref):.2e}")
     assert abs(msf - mref) / abs(mref) < MISFIT_TOL
     assert rel_l2(g, gref) < GRAD_TOL
+
+
+def test_cpa_stencil_agrees_with_register_pipeline(sw, oracle):
+    """The cp.async-staged 2D kernels (variant 512) run the same row update as
+    the register-pipelined ones: forward traces, misfit and gradient of a
+    5-shot batch agree to rounding, with FP32 and with BF16 D buffers and
+    with muting (the per-shot Kahan adjoint)."""
+    case, shot = _grad_case(sw, oracle, nt=320, seed=6)
+    shots = [shot] * 5
+    for bf16, mute in ((0, 0), (1, 0), (0, 3)):
+        out = []
+        for variant in (0, 512):
+            run = GpuRun(sw, case, gradient=True, check_freq=9, variant=variant, bf16=bf16, mute_src=mute)
+            g, m, t = run.gradient(shots)
+            f = run.forward(shots)
+            run.close()
+            out.append((g, m, t, f))
+        (g0, m0, t0, f0), (g1, m1, t1, f1) = out
+        same = np.array_equal(g0, g1) and m0 == m1 and all(np.array_equal(a, b) for a, b in zip(f0, f1))
+        print(f"bf16={bf16} mute={mute}: bitwise equal {same}, gradient rel diff {rel_l2(g1, g0):.2e}")
+        assert abs(m1 - m0) <= 1e-7 * abs(m0)
+        assert rel_l2(g1, g0) < 1e-6
+        assert all(rel_l2(a, b) < 1e-7 for a, b in zip(t1, t0))
+        assert all(rel_l2(a, b) < 1e-7 for a, b in zip(f1, f0))
