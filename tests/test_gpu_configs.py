@@ -1,6 +1,10 @@
-"""Parity at the sizes of the benchmark configurations that the FP64 oracle
-finishes in seconds to a minute: the 201 x 201 forward and the 801 x 801
-forward + L2 misfit + adjoint gradient with checkpoint period 50."""
+"""Parity at the sizes of the benchmark configurations, against the FP64
+oracle where it finishes in seconds to a minute: the 201 x 201 forward, the
+801 x 801 forward + L2 misfit + adjoint gradient with checkpoint period 50,
+two shots of the 2001 x 801 batch (shortest and longest record) and one of
+its variable-density twin, two elastic shots on the full 1200 x 600 grid
+(records capped at 600 steps) and the 3D generator at 200^3; plus the whole
+64-shot 2001 x 801 batch through properties that hold at any size."""
 import numpy as np
 import pytest
 
@@ -44,3 +48,146 @@ def test_acoustic2d_801_gradient(sw, oracle):
     assert errs[0] < TRACE_TOL
     assert errs[1] < MISFIT_TOL
     assert errs[2] < GRAD_TOL
+
+
+def _shot(s, dt, nt=None):
+    nt = nt or s.nt
+    return Shot(src_pos=s.src_pos, rec_pos=s.rec_pos, tf=np.asfortranarray(s.stf(dt)[:nt]), f0=s.f0, nt=nt)
+
+
+def _gpu_observed(sw, case, vp_obs, shots):
+    run = GpuRun(sw, Case(vp=np.asfortranarray(vp_obs), h=case.h, dt=case.dt, halo=case.halo, freetop=case.freetop))
+    obs = run.forward(shots)
+    run.close()
+    for s, o in zip(shots, obs):
+        s.observed = np.asfortranarray(o, dtype=np.float64)
+
+
+def test_acoustic2d_2001x801_batch_matches_oracle(sw, oracle):
+    """The headline grid (2001 x 801, 20-point C-PML, K = 50) at full size: its
+    shortest (nt 2002) and longest (nt 3982) shots, with different receiver
+    counts, in one batched gradient call against the sum of the oracle's
+    per-shot FP64 gradients (each shot with its own nt).  Observed data: the
+    GPU forward of 1.05 vp, so that the misfit is a well-conditioned
+    comparison."""
+    from seismicwaves_gb300 import configs
+    w = configs.acoustic2d_2001x801()
+    sel = [min(w.shots, key=lambda s: s.nt), max(w.shots, key=lambda s: s.nt)]
+    shots = [_shot(s, w.dt) for s in sel]
+    case = Case(vp=w.vp, h=w.h, dt=w.dt, halo=w.halo, freetop=w.freetop)
+    _gpu_observed(sw, case, w.vp * 1.05, shots)
+    run = GpuRun(sw, case, gradient=True, check_freq=w.check_freq)
+    g, msf, tr = run.gradient(shots)
+    run.close()
+    gref, mref = 0.0, 0.0
+    for k, s in enumerate(shots):
+        gk, mk, tk = oracle_gradient(oracle, sw, case, s, check_freq=w.check_freq)
+        assert rel_l2(tr[k], tk) < TRACE_TOL, k
+        gref, mref = gref + gk, mref + mk
+    errs = (abs(msf - mref) / mref, rel_l2(g, gref))
+    print(f"acoustic2d_2001x801 (nt {[s.nt for s in shots]}): misfit {errs[0]:.3e}  gradient {errs[1]:.3e}")
+    assert errs[0] < MISFIT_TOL
+    assert errs[1] < GRAD_TOL
+
+
+def test_acoustic2d_2001x801_all_shots_consistency(sw):
+    """All 64 shots of the headline workload at full size, through properties
+    that hold at any size: the gradient call's misfit equals the misfit of a
+    forward call's traces (summed on the host in FP64), and the 64-shot
+    gradient equals the sum of two 32-shot calls (batch composition changes
+    only the FP32 rounding of the correlation sums)."""
+    from seismicwaves_gb300 import configs
+    w = configs.acoustic2d_2001x801()
+    shots = [_shot(s, w.dt) for s in w.shots]
+    case = Case(vp=w.vp, h=w.h, dt=w.dt, halo=w.halo, freetop=w.freetop)
+    _gpu_observed(sw, case, w.vp_observed, shots)
+    run = GpuRun(sw, case, gradient=True, check_freq=w.check_freq)
+    g, msf, _ = run.gradient(shots)
+    fw = run.forward(shots)
+    ga, ma, _ = run.gradient(shots[:32])
+    gb, mb, _ = run.gradient(shots[32:])
+    run.close()
+    mfw = sum(0.5 * float(np.sum((t - s.observed) ** 2)) for t, s in zip(fw, shots))
+    print(f"64 shots: misfit {msf:.6e} (forward {mfw:.6e}), split gradient rel diff {rel_l2(ga + gb, g):.2e}")
+    assert msf > 0 and abs(msf - mfw) <= 1e-6 * mfw
+    assert abs((ma + mb) - msf) <= 1e-9 * msf
+    assert rel_l2(ga + gb, g) < 1e-5
+
+
+def test_acoustic_vd2d_2001x801_shot_matches_oracle(sw, oracle):
+    """The variable-density headline grid at full size: its shortest shot's vp
+    and rho gradients against the FP64 oracle (observed: 1.05 vp, 0.97 rho)."""
+    from seismicwaves_gb300 import configs
+    from vd_cases import GpuVD, VDCase, VDShot, oracle_forward as vd_forward, oracle_gradient as vd_gradient
+    w = configs.acoustic_vd2d_2001x801()
+    s = min(w.shots, key=lambda s: s.nt)
+    shot = VDShot(s.src_pos, s.rec_pos, s.stf(w.dt), s.f0)
+    case = VDCase(w.vp, w.rho, w.h[0], w.dt, w.halo, shots=[shot])
+    ctx = sw._lib.Context(0)
+    obs_run = GpuVD(ctx, VDCase(np.asfortranarray(w.vp * 1.05), np.asfortranarray(w.rho * 0.97), w.h[0], w.dt,
+                                w.halo, shots=[shot]))
+    obs = obs_run.forward([shot])[0]
+    obs_run.close()
+    run = GpuVD(ctx, case, gradient=True, check_freq=w.check_freq)
+    g, msf, tr = run.gradient([shot], [obs])
+    run.close()
+    ctx.close()
+    gref, mref, tref = vd_gradient(case, shot, obs, check_freq=w.check_freq)
+    errs = (rel_l2(tr[0], tref), abs(msf - mref) / mref, rel_l2(g["vp"], gref["vp"]), rel_l2(g["rho"], gref["rho"]))
+    print(f"acoustic_vd2d_2001x801 (nt {shot.nt}): traces {errs[0]:.3e} misfit {errs[1]:.3e} "
+          f"vp {errs[2]:.3e} rho {errs[3]:.3e}")
+    assert errs[0] < TRACE_TOL and errs[1] < MISFIT_TOL
+    assert errs[2] < GRAD_TOL and errs[3] < GRAD_TOL
+
+
+def test_elastic2d_1200x600_batch_matches_oracle(sw):
+    """The elastic grid at full size (1200 x 600, 300 receivers per shot, sinc
+    spreading, K = 50) with records capped at 600 steps: its first and last
+    shots in one batched gradient call against the sum of the oracle's
+    lambda, mu and rho gradients (observed: the GPU forward of lambda 1.3x,
+    mu 0.88x, rho 0.92x)."""
+    from seismicwaves_gb300 import configs
+    from elastic_cases import ElCase, ElShot, GpuElastic, oracle_gradient as el_gradient
+    w = configs.elastic2d_1200x600()
+    nx, nz = w.lam.shape
+    shots = [ElShot("mt", s.src_pos, s.rec_pos, 600, s.f0, momtens=[w.momtens]) for s in (w.shots[0], w.shots[-1])]
+    case = ElCase(nx, nz, w.h[0], w.dt, w.halo, w.lam, w.mu, w.rho, shots)
+    pert = ElCase(nx, nz, w.h[0], w.dt, w.halo, w.lam * 1.3, w.mu * 0.88, w.rho * 0.92, shots)
+    ctx = sw._lib.Context(0)
+    obs_run = GpuElastic(ctx, pert)
+    obs = obs_run.forward(shots)
+    obs_run.close()
+    run = GpuElastic(ctx, case, gradient=True, check_freq=w.check_freq)
+    g, msf, tr = run.gradient(shots, obs)
+    run.close()
+    ctx.close()
+    gref, mref = {k: 0.0 for k in ("rho", "lambda", "mu")}, 0.0
+    for k, s in enumerate(shots):
+        gk, mk, tk = el_gradient(case, s, obs[k], check_freq=w.check_freq)
+        assert rel_l2(tr[k], tk) < TRACE_TOL, k
+        gref = {n: gref[n] + gk[n] for n in gref}
+        mref += mk
+    errs = {n: rel_l2(g[n], gref[n]) for n in gref}
+    print(f"elastic2d_1200x600: misfit {abs(msf - mref) / mref:.3e} gradients {errs}")
+    assert abs(msf - mref) / mref < MISFIT_TOL
+    assert all(e < GRAD_TOL for e in errs.values())
+
+
+def test_acoustic3d_generator_200_matches_oracle(sw, oracle):
+    """The 3D workload's generator (smooth random velocity, surface source,
+    40 x 40-style receiver patch) at 200^3, the size the FP64 oracle finishes
+    in seconds: one shot, 150 steps, K = 50, the BF16 recompute buffer of the
+    benchmark, against the oracle within the BF16 bar (1e-3)."""
+    from seismicwaves_gb300 import configs
+    w = configs.acoustic3d_400(n=200, nshots_side=1, patch=10, nt=150)
+    shots = [_shot(s, w.dt) for s in w.shots]
+    case = Case(vp=w.vp, h=w.h, dt=w.dt, halo=w.halo, freetop=w.freetop)
+    _gpu_observed(sw, case, w.vp_observed, shots)
+    run = GpuRun(sw, case, gradient=True, check_freq=50, bf16=1)
+    g, msf, tr = run.gradient(shots)
+    run.close()
+    gref, mref, tref = oracle_gradient(oracle, sw, case, shots[0], check_freq=50)
+    errs = (rel_l2(tr[0], tref), abs(msf - mref) / mref, rel_l2(g, gref))
+    print(f"acoustic3d 200^3: traces {errs[0]:.3e} misfit {errs[1]:.3e} gradient {errs[2]:.3e}")
+    assert errs[0] < TRACE_TOL and errs[1] < MISFIT_TOL
+    assert errs[2] < 1e-3
