@@ -316,10 +316,10 @@ struct Ac2dRow {
 };
 
 // Minimum resident blocks per SM for a block of NW warps: keeps the forward
-// kernels at <= 64 registers (8 blocks of 4 warps; measured 4.0 / 4.4 TB/s
-// forward / recompute against 3.8 / 4.3 at 7 blocks, a few bytes spilled);
-// the per-shot adjoint at <= 80 (6 blocks); the Kahan adjoint, which holds a
-// second row of six arrays in registers, at 128.
+// kernels at <= 64 registers (8 blocks of 4 warps, no spills; measured 4.1 /
+// 4.5 TB/s forward / recompute against 3.8 / 4.3 at 7 blocks); the per-shot
+// adjoint at <= 80 (6 blocks, 8 bytes spilled); the Kahan adjoint, which holds
+// a second row of six arrays in registers, at 128.
 template <int MODE, int NW>
 struct Ac2dBounds {
   static constexpr int MINB = MODE == MODE_ADJ    ? (NW == 4 ? 4 : NW == 8 ? 2 : 1)
