@@ -2,8 +2,9 @@
 
 For a given simulation and batch of shots, times a short batched forward
 (the first `steps` time steps of every shot) for each candidate of the 2D
-stencil implementation (register-pipelined with 4 or 8 warps per block, or
-the TMA pipeline) and band height, and installs the fastest with
+stencil implementation (register-pipelined with 4, 8 or 16 warps per block,
+rows staged through shared memory by cp.async, or the TMA pipeline) and band
+height, and installs the fastest with
 sw_wavesim_set_tuning.  Results are cached per (grid, halo, number of shots).
 The numerics do not depend on the choice (all candidates run the same
 arithmetic), so tuning never changes results.
