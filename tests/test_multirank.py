@@ -33,7 +33,7 @@ def _worker(rank, world, port, out):
 
 def test_max_over_ranks_and_whole_job_rate_gloo():
     world, port = 2, _free_port()
-    with mp.Manager() as m:
+    with mp.get_context("spawn").Manager() as m:  # no fork of this (threaded) process
         out = m.dict()
         mp.spawn(_worker, args=(world, port, out), nprocs=world, join=True)
         res = dict(out)
