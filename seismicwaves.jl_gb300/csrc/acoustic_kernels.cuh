@@ -451,10 +451,13 @@ __global__ void __launch_bounds__(32 * NW, (Ac2dBounds<MODE, NW>::MINB - (DP - 1
 // ---------------------------------------------------------------------------
 // 2D step with the rows staged through shared memory by cp.async.
 //
-// The register-pipelined kernel holds one row of loads in flight per warp;
-// its bandwidth is that of the bytes in flight (about 1.9 us of loaded DRAM
-// latency per row), and a second register row costs more occupancy than it
-// brings.  Here every lane copies its own 16-byte pieces of the rows ahead
+// The register-pipelined kernel holds one row of loads in flight per warp,
+// and a second register row costs more occupancy than it brings.  This
+// variant keeps S-1 rows in flight without registers; on GB300 it measured
+// slower all the same (64 shots of 2001 x 801: 3.75 / 4.23 / 4.71 TB/s
+// forward / recompute / adjoint against 4.15 / 4.56 / 4.79), so more loads
+// in flight are not what these kernels lack, and it stays a tuning variant
+// (512).  Every lane copies its own 16-byte pieces of the rows ahead
 // into a per-warp ring of S row bundles with cp.async (no registers held
 // while in flight) and later reads back only what it copied itself, so no
 // barrier is needed: cp.async.wait_group orders a lane's copies with its own
