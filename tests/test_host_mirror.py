@@ -92,3 +92,62 @@ def test_vd_and_ccts_shot_consistency(sw):
     assert m.invcov_diagonal() is None and m.invcov_dense() is None and m.windows == []
     with pytest.raises(AssertionError):
         sw.CCTSMisfit(0.0, observed=np.zeros((10, 1)))
+
+
+def test_elastic_host_checks(sw):
+    """The elastic mirror keeps the reference's argument checks
+    (src/models/elastic/ela_params.jl:27-31, src/shots/sources.jl:71-86,
+    src/shots/receivers.jl:89) and material defaults
+    (ela_material_properties.jl:9-22: arithmetic rho and mu, harmonic lambda)."""
+    E = __import__(sw.__name__ + ".elastic", fromlist=["elastic"])
+    bc = sw.CPMLBoundaryConditionParameters()
+    with pytest.raises(AssertionError, match="Dimensionality"):
+        E.InputParametersElastic(10, 1e-3, (4, 4, 4, 4), (1.0,) * 4, bc)
+    with pytest.raises(AssertionError, match="grid points must be positive"):
+        E.InputParametersElastic(10, 1e-3, (4, 0), (1.0, 1.0), bc)
+    with pytest.raises(AssertionError, match="grid spacings must be positive"):
+        E.InputParametersElastic(10, 1e-3, (4, 4), (1.0, 0.0), bc)
+    with pytest.raises(AssertionError, match="timesteps must be positive"):
+        E.InputParametersElastic(0, 1e-3, (4, 4), (1.0, 1.0), bc)
+    with pytest.raises(AssertionError, match="Timestep size must be positive"):
+        E.InputParametersElastic(10, 0.0, (4, 4), (1.0, 1.0), bc)
+    pos = np.array([[10.0, 10.0], [20.0, 10.0]])
+    with pytest.raises(AssertionError, match="at least one source"):
+        E.MomentTensorSources(np.zeros((0, 2)), np.zeros((5, 0)), [], 10.0)
+    with pytest.raises(AssertionError, match="do not match between positions and time-functions"):
+        E.MomentTensorSources(pos, np.zeros((5, 3)), [E.MomentTensor2D(1, 1, 0)] * 2, 10.0)
+    with pytest.raises(AssertionError, match="moment tensors must match"):
+        E.MomentTensorSources(pos, np.zeros((5, 2)), [E.MomentTensor2D(1, 1, 0)], 10.0)
+    with pytest.raises(AssertionError, match="components do not match"):
+        E.ExternalForceSources(pos, np.zeros((5, 3, 2)), 10.0)
+    with pytest.raises(AssertionError, match="at least one receiver"):
+        E.VectorReceivers(np.zeros((0, 2)), 5)
+    assert E.VectorReceivers(pos, 7).seismograms.shape == (7, 2, 2)
+    m = E.ElasticIsoMaterialProperties(np.ones((3, 3)), np.ones((3, 3)), np.ones((3, 3)))
+    assert (m.interp_method_ρ.code, m.interp_method_λ.code, m.interp_method_μ.code) == (0, 1, 0)
+
+
+def test_elastic_shot_consistency_and_build_routing(sw):
+    """check_sim_consistency (src/utils/checks.jl:2-41) for elastic shots, and
+    build_wavesim's argument errors, which come before any device work."""
+    from seismicwaves_gb300 import api
+    E = __import__(sw.__name__ + ".elastic", fromlist=["elastic"])
+    m = E.ElasticIsoMaterialProperties(np.ones((8, 8)), np.ones((8, 8)), np.ones((8, 8)))
+    pos = np.array([[10.0, 10.0]])
+    mt = E.MomentTensorShot(srcs=E.MomentTensorSources(pos, np.zeros((5, 1)), [E.MomentTensor2D(1, 1, 0)], 10.0),
+                            recs=E.VectorReceivers(pos, 5))
+    ef = E.ExternalForceShot(srcs=E.ExternalForceSources(pos, np.zeros((5, 2, 1)), 10.0),
+                             recs=E.VectorReceivers(pos, 5))
+    api._check_sim_consistency(m, [mt, mt])
+    api._check_sim_consistency(m, [ef])
+    with pytest.raises(TypeError):
+        api._check_sim_consistency(m, [mt, ef])
+    scalar = E.MomentTensorShot(srcs=mt.srcs, recs=sw.ScalarReceivers(pos, 5))
+    with pytest.raises(TypeError):
+        api._check_sim_consistency(m, [scalar])
+    params = sw.InputParametersAcoustic(10, 1e-3, (8, 8), (1.0, 1.0), sw.CPMLBoundaryConditionParameters())
+    vp = sw.VpAcousticCDMaterialProperties(np.full((8, 8), 2000.0))
+    with pytest.raises(ValueError, match="threadpersrc"):
+        sw.build_wavesim(params, vp, runparams=sw.RunParameters(parall="threadpersrc"))
+    with pytest.raises(AssertionError, match="gradient keyword"):
+        sw.build_wavesim(params, vp, runparams=sw.RunParameters(), gradparams=sw.GradParameters(), gradient=False)
