@@ -59,3 +59,37 @@ def test_profile_summaries_name_their_command():
         for c in cmds:
             assert "--clock-control none" in c, f"{f.name}: {c.strip()}"
         assert "bench.py" in txt, f.name
+
+
+def _run_bench(args, env_extra=None):
+    import json
+    import os
+    import subprocess
+    env = dict(os.environ, **(env_extra or {}))
+    r = subprocess.run([sys.executable, str(ROOT / "bench.py"), *args], capture_output=True, text=True, env=env,
+                       timeout=600, cwd=str(ROOT))
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
+    return [json.loads(ln) for ln in lines]
+
+
+def test_reference_arm_json_line():
+    """bench.py --impl reference (the oracle port on the host cores) prints one
+    JSON line with the contract's keys on a bounded sample."""
+    out = _run_bench(["--impl", "reference", "--workload", "acoustic2d_201", "--steps", "1", "--warmup", "0",
+                      "--cpu-sample-nt", "20"])
+    assert len(out) == 1
+    d = out[0]
+    for k in ("impl", "metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better",
+              "scaling", "vs_baseline", "dtype", "data", "config", "cpu_baseline", "e2e"):
+        assert k in d, k
+    assert d["impl"] == "reference" and d["value"] > 0 and d["unit"] == "Gpts/s"
+    assert d["cpu_baseline"]["kind"] == "port" and d["cpu_baseline"]["cores"] >= 1
+    assert d["e2e"]["h2d_bytes_per_step"] == 0 and d["e2e"]["value"] == d["value"]
+
+
+def test_reference_arm_other_ranks_do_no_work():
+    """Under torchrun only rank 0 runs the reference arm; the others exit 0 silently."""
+    out = _run_bench(["--impl", "reference", "--workload", "acoustic2d_201", "--steps", "1", "--warmup", "0",
+                      "--cpu-sample-nt", "20"], {"RANK": "1", "WORLD_SIZE": "2", "LOCAL_RANK": "1"})
+    assert out == []
