@@ -1,0 +1,80 @@
+"""The C ABI's struct layouts, three ways: include/swgb300.h as gcc lays it
+out (sizeof / offsetof from a probe compiled here), the ctypes mirror in
+seismicwaves.jl_gb300/_lib.py, and the Julia structs that INTEGRATION.md
+gives a maintainer (field names and order).  A field added to the header
+but not to a binding shifts every later field or the array stride."""
+import json
+import re
+import shutil
+import subprocess
+from pathlib import Path
+
+import pytest
+
+import __graft_entry__
+
+ROOT = Path(__file__).resolve().parents[1]
+BUILD = Path(__file__).resolve().parent / "_build"
+sw = __graft_entry__.load_package()
+L = sw._lib
+
+STRUCTS = {  # C typedef -> (ctypes class, Julia struct in INTEGRATION.md)
+    "sw_acoustic_params": (L.SwAcousticParams, "SwAcousticParams"),
+    "sw_acoustic_shot": (L.SwAcousticShot, "SwAcousticShot"),
+    "sw_grad_params": (L.SwGradParams, "SwGradParams"),
+    "sw_elastic_params": (L.SwElasticParams, "SwElasticParams"),
+    "sw_point_table": (L.SwPointTable, "SwPointTable"),
+    "sw_elastic_shot": (L.SwElasticShot, "SwElasticShot"),
+}
+
+
+@pytest.fixture(scope="module")
+def c_layout():
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    BUILD.mkdir(exist_ok=True)
+    lines = ["#include <stddef.h>", "#include <stdio.h>", '#include "swgb300.h"', "int main(void) {",
+             '  printf("{");']
+    first = True
+    for cname, (cls, _) in STRUCTS.items():
+        sep = "" if first else ","
+        first = False
+        lines.append(f'  printf("{sep}\\"{cname}\\": {{\\"size\\": %zu", sizeof({cname}));')
+        for fname, _ in cls._fields_:
+            lines.append(f'  printf(", \\"{fname}\\": %zu", offsetof({cname}, {fname}));')
+        lines.append('  printf("}");')
+    lines += ['  printf("}\\n");', "  return 0;", "}"]
+    src = BUILD / "layout_probe.c"
+    exe = BUILD / "layout_probe"
+    src.write_text("\n".join(lines) + "\n")
+    subprocess.run([cc, "-std=c11", "-I", str(ROOT / "include"), str(src), "-o", str(exe)], check=True)
+    return json.loads(subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout)
+
+
+@pytest.mark.parametrize("cname", list(STRUCTS))
+def test_ctypes_layout_matches_header(c_layout, cname):
+    cls, _ = STRUCTS[cname]
+    lay = c_layout[cname]
+    assert ctypes_sizeof(cls) == lay["size"], cname
+    for fname, _ in cls._fields_:
+        assert getattr(cls, fname).offset == lay[fname], f"{cname}.{fname}"
+
+
+def ctypes_sizeof(cls):
+    import ctypes
+    return ctypes.sizeof(cls)
+
+
+def _julia_fields(text, name):
+    m = re.search(rf"struct {name}\b(.*?)\bend\b", text, re.S)
+    assert m, name
+    body = re.sub(r"#[^\n]*", "", m.group(1))
+    return re.findall(r"([A-Za-z_]\w*)::", body)
+
+
+@pytest.mark.parametrize("cname", list(STRUCTS))
+def test_integration_julia_structs_match_header(cname):
+    cls, jname = STRUCTS[cname]
+    text = (ROOT / "INTEGRATION.md").read_text()
+    assert _julia_fields(text, jname) == [f for f, _ in cls._fields_], jname
