@@ -78,3 +78,52 @@ def test_integration_julia_structs_match_header(cname):
     cls, jname = STRUCTS[cname]
     text = (ROOT / "INTEGRATION.md").read_text()
     assert _julia_fields(text, jname) == [f for f, _ in cls._fields_], jname
+
+
+def _prototypes():
+    """name -> [parameter C types] for every function the header declares."""
+    text = (ROOT / "include" / "swgb300.h").read_text()
+    text = re.sub(r"/\*.*?\*/", " ", text, flags=re.S)
+    protos = {}
+    for m in re.finditer(r"\b(?:int|void|const char\s*\*|void\s*\*|int32_t)\s*\**\s*(sw_\w+)\s*\(([^;{]*?)\)\s*;",
+                         text, re.S):
+        params = [p.strip() for p in m.group(2).split(",") if p.strip() and p.strip() != "void"]
+        protos[m.group(1)] = params
+    return protos
+
+
+def _kind_c(p):
+    if "*" in p:
+        return "ptr"
+    if p.startswith("double"):
+        return "f64"
+    if p.startswith("int64_t"):
+        return "i64"
+    return "i32"  # int, int32_t
+
+
+def _kind_ctypes(t):
+    import ctypes
+    if t in (ctypes.c_double,):
+        return "f64"
+    if t in (ctypes.c_int64, ctypes.c_longlong):
+        return "i64"
+    if t in (ctypes.c_int32, ctypes.c_int):
+        return "i32"
+    return "ptr"  # c_void_p, POINTER(...), c_char_p
+
+
+def test_ctypes_signatures_match_header():
+    """Every exported function's ctypes argtypes agree with its prototype in
+    count and kind (32-bit integer, double, pointer)."""
+    protos = _prototypes()
+    lib = L.load()
+    assert set(L.EXPORTS) <= set(protos), sorted(set(L.EXPORTS) - set(protos))
+    checked = 0
+    for name in L.EXPORTS:
+        argtypes = getattr(lib, name).argtypes
+        if argtypes is None:
+            continue
+        assert [_kind_ctypes(t) for t in argtypes] == [_kind_c(p) for p in protos[name]], name
+        checked += 1
+    assert checked >= 20
