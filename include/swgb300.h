@@ -50,7 +50,7 @@
  *       update_matprop! -> precompute_fact! (acou_models.jl:283-300)
  *   sw_acoustic_vd_forward
  *       run_swforward! + swforward_1shot! (VD) + forward_onestep_CPML!
- *       (src/models/acoustic/acou_forward.jl:83-128,
+ *       (src/models/acoustic/acou_forward.jl:83-125,
  *       src/models/acoustic/backends/shared/acoustic2D_VD_xPU.jl:1-125)
  *   sw_acoustic_vd_gradient
  *       run_swgradient! + swgradient_1shot! (VD) with LinearCheckpointer, L2 misfit,

@@ -21,7 +21,7 @@
 //   material factors ................. src/models/acoustic/acou_models.jl:283-300 (fact_m0 = vp^2 rho dt,
 //                                      fact_m1_stag = interp(1/rho) dt)
 //   source scaling ................... src/models/acoustic/acou_forward.jl:66-80 (done by the caller)
-//   forward driver ................... acou_forward.jl:83-128
+//   forward driver ................... acou_forward.jl:83-125
 //   gradient driver .................. src/models/acoustic/acou_gradient.jl:97-202, checkpointer set-up
 //                                      acou_models.jl:402-414 (pcur buffered with width 1)
 //   back-interpolation ............... src/utils/interpolations.jl:1-47

@@ -73,7 +73,7 @@ class CPMLBoundaryConditionParameters:
 
 
 class InputParametersAcoustic:
-    """src/models/genparameters.jl:89-115."""
+    """src/models/acoustic/acou_params.jl:9-35."""
 
     def __init__(self, ntimesteps: int, dt: float, gridsize: Sequence[int], gridspacing: Sequence[float],
                  boundcond: CPMLBoundaryConditionParameters):
@@ -585,7 +585,7 @@ def _check_sim_consistency(matprop, shots):
 
 def build_wavesim(params, matprop, *, runparams: RunParameters, gradparams: GradParameters | None = None,
                   gradient: bool | None = None, device: int = 0, sincinterp: bool = True):
-    """src/apis/build.jl:18-95: AcousticCDCPMLWaveSimulation, AcousticVDStaggeredCPMLWaveSimulation or
+    """src/apis/build.jl:18-90: AcousticCDCPMLWaveSimulation, AcousticVDStaggeredCPMLWaveSimulation or
     ElasticIsoCPMLWaveSimulation."""
     from . import elastic as E
     if gradparams is None and gradient:

@@ -12,7 +12,7 @@
 //   correlate_gradient_m0!, correlate_gradient_m1!  correlate_gradient_xPU.jl:12-21,
 //                                                   acoustic2D_VD_xPU.jl:171-192
 //   precompute_fact! (fact_m0 = vp^2 rho dt, fact_m1 = interp(1/rho) dt)  src/models/acoustic/acou_models.jl:292-300
-//   swforward_1shot! / swgradient_1shot! (VD)  src/models/acoustic/acou_forward.jl:83-128,
+//   swforward_1shot! / swgradient_1shot! (VD)  src/models/acoustic/acou_forward.jl:83-125,
 //                                              src/models/acoustic/acou_gradient.jl:97-202
 //   back_interp  src/utils/interpolations.jl:15-47;  L2 misfit  src/inversion/misfits/L2Misfit.jl:24-77
 //

@@ -39,7 +39,7 @@ log = logging.getLogger("seismicwaves_gb300")
 
 
 class InputParametersElastic:
-    """src/models/elastic/ela_params.jl:1-35."""
+    """src/models/elastic/ela_params.jl:1-34."""
 
     def __init__(self, ntimesteps: int, dt: float, gridsize: Sequence[int], gridspacing: Sequence[float], boundcond):
         assert len(gridsize) <= 3, "Dimensionality must be less than or equal to 3!"
