@@ -725,8 +725,8 @@ def run_gb300(a):
     # end to end through the C ABI with pinned host buffers (inputs up, gradient/traces down, every step)
     h2d, d2h = R.setup_host()
     R.gradient_host()
-    t_e2e = R.timed(R.gradient_host, a.steps)
-    e2e = pts * a.steps * world / t_e2e / 1e9
+    t_e2e = max_over_ranks(R.timed(R.gradient_host, a.steps), dist, R.dev)
+    e2e = whole_job_rate(pts, a.steps, world, t_e2e) / 1e9
 
     # plain per-shot path: the same library, one shot per call
     plain = None

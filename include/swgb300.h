@@ -361,8 +361,10 @@ int sw_acoustic_vd_set_tuning(sw_acoustic_vd* vd, int32_t tz);
  * returns after it finished.  Every call reuses the same array and clears
  * what must start at zero itself; calls whose GPU work overlaps race on it.
  * The first call on a device looks the array up (cudaGetSymbolAddress, with
- * that device current), so make it before any stream capture.  Status codes
- * only (no context, no message). */
+ * that device current), so make it before any stream capture; the address is
+ * cached per device ordinal for the device's primary context, so do not call
+ * it after a cudaDeviceReset or under another context of that device.  Status
+ * codes only (no context, no message). */
 int sw_acoustic2d_forward_noalloc(const sw_acoustic_params* params, const float* vp, const sw_acoustic_shot* shot,
                                   void* stream);
 

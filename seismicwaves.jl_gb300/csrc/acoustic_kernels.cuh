@@ -14,8 +14,11 @@
 //    xi_out on the first step after a checkpoint restore);
 //  * optional side outputs: D = fact * lap (the second time difference the
 //    gradient correlates with), and a checkpoint copy of the state read;
-//  * the adjoint variant also accumulates the gradient correlation
-//    g += lambda * D with Kahan compensation (correlate_gradient_xPU.jl:1-10).
+//  * the adjoint variants also accumulate the gradient correlation
+//    g += lambda * D (correlate_gradient_xPU.jl:1-10): MODE_ADJW (the 2D
+//    default) into a plain FP32 sum per shot that the host flushes into an
+//    FP64 total every 32 steps, so no FP32 sum runs over more than 32 terms;
+//    MODE_ADJ (3D, muted runs) with Kahan compensation.
 //
 // Time stepping in increment form.  The reference advances
 //     p[n+1] = 2 p[n] - p[n-1] + fact * lap(p[n]);

@@ -17,7 +17,11 @@
 // (for example on two streams at once) race on the array; serialise them.
 // The first call on a device looks the array's device address up
 // (cudaGetSymbolAddress, with that device current) and caches it; make that
-// first call before any stream capture.
+// first call before any stream capture.  The cache is keyed by device ordinal
+// and assumes the device's primary context for the life of the process: a
+// caller that resets the device (cudaDeviceReset) or runs the call under
+// another context of the same device must not use this entry point after
+// that.
 #include <algorithm>
 #include <cstdint>
 #include <cstring>
@@ -233,8 +237,9 @@ int run(const sw_acoustic_params* p, const float* vp, const sw_acoustic_shot* s,
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   const int tiles_x = (P + 511) / 512;
-  int TZ = 64;
-  while (TZ > 8 && (long long)tiles_x * ((nz - 2 + TZ - 1) / TZ) < 8LL * sms) TZ /= 2;
+  // the batched path's rule for the register-pipelined stencil: 8-row bands,
+  // 4-row bands when 8-row ones would leave the GPU under-filled
+  const int TZ = (long long)tiles_x * ((nz - 2 + 7) / 8) < 4LL * sms ? 4 : 8;
   const int tiles_z = (nz - 2 + TZ - 1) / TZ;
 
   StepArgs a;

@@ -9,8 +9,9 @@ and the adjoint gradient; the pullback only scales the stored gradient.
 Sign.  ``swgradient`` returns the reference's gradients as they are.  Central
 differences of the misfit show that these are
 
-  * ``-dchi/dm`` on the acoustic paths: the adjoint source is ``-C^-1 r``
-    (L2Misfit.jl:24-77) and the chain rules ``2/vp^3`` (acou_gradient.jl:4-95)
+  * ``-dchi/dm`` on the acoustic paths: ``dchi/du = C^-1 r``
+    (L2Misfit.jl:64-77) is negated into the adjoint source
+    (``adjointsource = .-dchi_du``, acou_gradient.jl:48 and :142), and the chain rules ``2/vp^3`` (acou_gradient.jl:4-95)
     and ``-2/(vp^3 rho)``, ``-1/(vp^2 rho^2)`` (acou_gradient.jl:146-201) keep
     that sign -- the returned field is a descent direction;
   * ``+dchi/dm`` on the elastic path (ela_gradient.jl:4-187), whose correlation

@@ -1,8 +1,10 @@
 """The C ABI's struct layouts, three ways: include/swgb300.h as gcc lays it
 out (sizeof / offsetof from a probe compiled here), the ctypes mirror in
-seismicwaves.jl_gb300/_lib.py, and the Julia structs that INTEGRATION.md
-gives a maintainer (field names and order).  A field added to the header
-but not to a binding shifts every later field or the array stride."""
+seismicwaves.jl_gb300/_lib.py, and the Julia structs of the Julia binding
+(julia/SeismicWavesGB300/src/abi.jl: field names and order).  A field added
+to the header but not to a binding shifts every later field or the array
+stride.  Also: every library function the Julia binding calls is declared in
+the header."""
 import json
 import re
 import shutil
@@ -18,7 +20,8 @@ BUILD = Path(__file__).resolve().parent / "_build"
 sw = __graft_entry__.load_package()
 L = sw._lib
 
-STRUCTS = {  # C typedef -> (ctypes class, Julia struct in INTEGRATION.md)
+JULIA = ROOT / "julia" / "SeismicWavesGB300"
+STRUCTS = {  # C typedef -> (ctypes class, Julia struct of the Julia binding)
     "sw_acoustic_params": (L.SwAcousticParams, "SwAcousticParams"),
     "sw_acoustic_shot": (L.SwAcousticShot, "SwAcousticShot"),
     "sw_grad_params": (L.SwGradParams, "SwGradParams"),
@@ -74,10 +77,19 @@ def _julia_fields(text, name):
 
 
 @pytest.mark.parametrize("cname", list(STRUCTS))
-def test_integration_julia_structs_match_header(cname):
+def test_julia_binding_structs_match_header(cname):
     cls, jname = STRUCTS[cname]
-    text = (ROOT / "INTEGRATION.md").read_text()
+    text = (JULIA / "src" / "abi.jl").read_text()
     assert _julia_fields(text, jname) == [f for f, _ in cls._fields_], jname
+
+
+def test_julia_binding_calls_only_declared_functions():
+    called = set()
+    for f in sorted(JULIA.rglob("*.jl")):
+        called |= set(re.findall(r"ccall\(\(:(sw_\w+),", f.read_text()))
+    assert called, "no ccall found in the Julia binding"
+    missing = sorted(called - set(_prototypes()))
+    assert not missing, missing
 
 
 def _prototypes():

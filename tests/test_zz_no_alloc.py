@@ -31,18 +31,36 @@ def _params(L, case, n=None):
     return prm
 
 
-def test_noalloc_forward_matches_regular_entry_point(sw):
-    torch = pytest.importorskip("torch")
-    L = sw._lib
-    lib = L.load()
+def _noalloc_case(kind):
+    """Two layouts: damped grid with an interior source pair and a receiver on
+    the free surface; and halo = 0 (no memory variables) with a source on the
+    grid's outermost line, whose node keeps the 3-value ring in the shared
+    array -- the state most exposed to a previous call's leftovers."""
     vp = smooth_model((203, 157), 1600.0, 3200.0, seed=21)
-    case = Case(vp=vp, h=(6.0, 6.0), dt=stable_dt(vp, (6.0, 6.0)), halo=15, freetop=True)
+    if kind == "damped":
+        case = Case(vp=vp, h=(6.0, 6.0), dt=stable_dt(vp, (6.0, 6.0)), halo=15, freetop=True)
+    else:
+        case = Case(vp=vp, h=(6.0, 6.0), dt=stable_dt(vp, (6.0, 6.0)), halo=0, freetop=False)
     ex = [h * (n - 1) for n, h in zip(vp.shape, case.h)]
     recx = np.linspace(0.05 * ex[0], 0.95 * ex[0], 23)
     rec = np.stack([recx, np.full_like(recx, 0.08 * ex[1])], 1)
-    rec[0, 1] = 0.0  # one receiver on the free surface
-    shot = make_shot(case.h, ex, 700, case.dt, 12.0,
-                     [[0.4 * ex[0], 0.3 * ex[1]], [0.4 * ex[0], 0.3 * ex[1]], [0.6 * ex[0], 0.5 * ex[1]]], rec)
+    if kind == "damped":
+        rec[0, 1] = 0.0  # one receiver on the free surface
+        src = [[0.4 * ex[0], 0.3 * ex[1]], [0.4 * ex[0], 0.3 * ex[1]], [0.6 * ex[0], 0.5 * ex[1]]]
+    else:
+        src = [[0.0, 0.3 * ex[1]], [0.6 * ex[0], 0.5 * ex[1]]]  # first source on the line i = 1
+        rec[1] = [0.0, 0.3 * ex[1]]  # a receiver on that boundary node
+    shot = make_shot(case.h, ex, 700, case.dt, 12.0, src, rec)
+    return case, shot
+
+
+@pytest.mark.parametrize("kind", ["damped", "edge_source_no_halo"])
+def test_noalloc_forward_matches_regular_entry_point(sw, kind):
+    torch = pytest.importorskip("torch")
+    L = sw._lib
+    lib = L.load()
+    case, shot = _noalloc_case(kind)
+    vp = case.vp
     run = GpuRun(sw, case)
     ref = run.forward([shot])[0]
     run.close()
