@@ -53,6 +53,8 @@ def _args():
     p.add_argument("--forward-only", action="store_true", help="time the batched forward instead of the gradient")
     p.add_argument("--bf16", type=int, default=0, help="acoustic snapshot_bf16 (0 FP32, 1 BF16 recompute buffer, "
                                                       "2 also BF16 checkpoints)")
+    p.add_argument("--no-parity", action="store_true", help="skip the FP64-oracle error of the benchmark's shortest shot")
+    p.add_argument("--check-freq", type=int, default=0, help="override the checkpoint period (small profiling cases)")
     return p.parse_args()
 
 
@@ -81,7 +83,7 @@ def _dist():
     return rank, world, local
 
 
-def _workload(name, shots, nt_cap=0):
+def _workload(name, shots, nt_cap=0, check_freq=0):
     import __graft_entry__
 
     sw = __graft_entry__.load_package()
@@ -93,6 +95,8 @@ def _workload(name, shots, nt_cap=0):
     if nt_cap:
         for s in w.shots:
             s.nt = min(s.nt, nt_cap)
+    if check_freq:
+        w.check_freq = check_freq
     return sw, w
 
 
@@ -580,6 +584,44 @@ def _peak():
     return 6800.0, "fallback"
 
 
+def _traffic_ratio_from_profiles(kind, workload):
+    """DRAM bytes over algorithmic bytes of the `kind` stencil launches
+    (forward / recompute / adjoint) in an ncu capture summary under profiles/
+    (a smaller case of the same workload; the ratio carries over to the full
+    launch because both grow with the active points per launch)."""
+    for f in sorted((ROOT / "profiles").glob("*.md")):
+        txt = f.read_text()
+        if f"workload: {workload}" not in txt:
+            continue
+        for line in txt.splitlines():
+            if line.startswith(f"traffic_over_algorithmic[{kind}]:"):
+                try:
+                    return float(line.split(":", 1)[1].split()[0])
+                except ValueError:
+                    return None
+    return None
+
+
+def _one_step_model_bytes(w):
+    """Bytes one gradient must move with one time step per launch in FP32: per
+    interior point-step 16 (forward: R/W p, d) + 16 (K-1)/K (recompute) +
+    4 + 4 (write / read D) + 16 (adjoint) + 8 (correlation RMW); per strip cell
+    and axis 16 per pass (R/W psi, xi, three passes); checkpoints 2 fields x
+    4 B written and read every K steps; fact once per launch (negligible)."""
+    nd = w.vp.ndim
+    n = w.vp.shape
+    pts = float(np.prod([k - 2 for k in n]))
+    strip = 0.0
+    for d in range(nd):
+        wd = sum(1 for x in range(1, n[d] - 1) if x < w.halo or x >= n[d] - w.halo)
+        strip += wd * pts / (n[d] - 2)
+    K = w.check_freq
+    per_pt = 16 + 16 * (K - 1) / K + 8 + 16 + 8 + 16.0 / K
+    per_strip = 16 * (2 + (K - 1) / K)
+    steps = float(sum(s.nt for s in w.shots))
+    return steps * (pts * per_pt + strip * per_strip)
+
+
 def _traffic_from_profiles(kernel, workload):
     """DRAM bytes per launch and per shot of `kernel` from an ncu capture summary in profiles/."""
     for f in sorted((ROOT / "profiles").glob("*.md")):
@@ -597,6 +639,48 @@ def _traffic_from_profiles(kernel, workload):
 def _sample_nt(w, nt_sample):
     """CPU sample length: the requested steps, fewer on large grids (about 2e9 point-steps at most)."""
     return int(max(20, min(nt_sample, 2e9 // max(w.gridpoints, 1))))
+
+
+# Error bars of the FP32 path against the FP64 oracle (relative L2 of traces
+# and gradient, relative misfit).
+PARITY_BARS = {"traces_rel_l2": 1e-5, "misfit_rel": 1e-6, "gradient_rel_l2": 1e-5}
+
+
+def _parity_2d(R, sw, w):
+    """Error of one benchmark shot against the FP64 oracle, outside the timed
+    region: the shortest shot of the workload at its full record length, one
+    GPU gradient call (same device inputs as the benchmark, observed data of
+    the perturbed model) against the oracle's forward + misfit + adjoint
+    gradient with the same checkpoint period on the same inputs."""
+    import oracle
+
+    oracle.load()
+    idx = min(range(len(w.shots)), key=lambda i: w.shots[i].nt)
+    s = w.shots[idx]
+    R.gradient_device([idx])
+    R.torch.cuda.synchronize(R.dev)
+    si, ri, _, _ = R.host[idx]
+    nrec = ri.shape[0]
+    g = R.grad_d.cpu().numpy().reshape(w.vp.shape, order="F")
+    mis = float(R.mis_d.item())
+    tr = R.tr_d[idx].cpu().numpy().reshape(nrec, s.nt).T
+    obs = R.obs_d[idx].cpu().numpy().reshape(nrec, s.nt).T.astype(np.float64)
+    tf = sw.scale_srctf(s.stf(w.dt), si, w.vp, w.h, w.dt).astype(np.float64)
+    cp = oracle.cpml_blocks(w.vp, w.h, w.dt, w.halo, 1e-4, s.f0, w.freetop)
+    t0 = time.perf_counter()
+    gref, mref, tref = oracle.acoustic_gradient(w.vp, w.h, w.dt, w.halo, cp, tf, si, ri, obs,
+                                                check_freq=w.check_freq, nthreads=os.cpu_count() or 1)
+    t_oracle = time.perf_counter() - t0
+
+    def rel(a, b):
+        return float(np.linalg.norm(np.asarray(a, np.float64) - b) / max(np.linalg.norm(b), 1e-300))
+
+    errs = {"traces_rel_l2": rel(tr, tref), "misfit_rel": abs(mis - mref) / abs(mref),
+            "gradient_rel_l2": rel(g, gref)}
+    return {"shot": idx, "nt": s.nt, "receivers": nrec, **errs, "bars": PARITY_BARS,
+            "within_bars": {k: errs[k] <= PARITY_BARS[k] for k in errs},
+            "oracle": "FP64 C++ restatement of the reference's CD path (oracle/), same inputs",
+            "oracle_s": round(t_oracle, 2)}
 
 
 def _cpu_baseline(sw, w, nt_sample):
@@ -660,7 +744,7 @@ def run_gb300(a):
 
         torch.cuda.set_device(local)
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
-    sw, w = _workload(a.workload, a.shots, a.nt)
+    sw, w = _workload(a.workload, a.shots, a.nt, a.check_freq)
     R = GradientRun(sw, w, local, bf16=a.bf16)
     if a.tz or a.variant >= 0:
         R.ctx.check(R.lib.sw_wavesim_set_tuning(R.h, a.tz, max(a.variant, 0)), "sw_wavesim_set_tuning")
@@ -736,6 +820,9 @@ def run_gb300(a):
         plain = {"value": pts / t_plain / 1e9, "unit": UNIT, "shots_per_s": nshots / t_plain,
                  "ms_per_step": t_plain * 1e3, "what": "same kernels, one shot per call"}
 
+    parity = None
+    if rank == 0 and not a.no_parity and w.vp.ndim == 2:
+        parity = _parity_2d(R, sw, w)
     if rank != 0:
         return
     # roofline of the dominant kernel (largest total time among the stencil kinds)
@@ -747,16 +834,31 @@ def run_gb300(a):
         adj, adj_what = base + "<3>", "adjoint + correlation (plain FP32 sums, FP64 flush every 32 steps)"
     else:
         adj, adj_what = base + "<2>", "adjoint + correlation (Kahan sums)"
-    kinds = {0: (f"{base}<0/1> forward", f"{base}<1>"), 4: (f"{base}<1> recompute (writes D)", f"{base}<1>"),
-             1: (f"{adj} {adj_what}", adj)}
+    two = "k_ac2d_pair (two steps per launch) / " if nd == 2 else ""
+    kinds = {0: (f"{two}{base}<0/1> forward", f"{base}<1>", "forward"),
+             4: (f"{two}{base}<1> recompute (writes D)", f"{base}<1>", "recompute"),
+             1: (f"{two}{adj} {adj_what}", adj, "adjoint")}
     dom = max(kinds, key=lambda k: prof[k][0])
     ms_tot, launches, bytes_tot = prof[dom]
     achieved = bytes_tot / (ms_tot / 1e3) / 1e9 if ms_tot > 0 else None
     peak, peak_kind = _peak()
-    traffic_per_shot = _traffic_from_profiles(kinds[dom][1] + (" recompute" if dom == 4 else ""), w.name)
+    algo_per_launch = bytes_tot / max(launches, 1)
+    ratio = _traffic_ratio_from_profiles(kinds[dom][2], w.name)
+    # whole gradient: the stencil kinds' algorithmic bytes over the timed step,
+    # and the same step against the one-step-per-launch byte model of the path
+    step_s = t_dev / a.steps
+    kern_bytes = sum(prof[k][2] for k in kinds)
+    model_bytes = _one_step_model_bytes(w)
+    whole = {"kernel_bytes_per_step": kern_bytes, "frac": kern_bytes / step_s / 1e9 / peak,
+             "one_step_model_bytes_per_step": model_bytes,
+             "frac_vs_one_step_model": model_bytes / step_s / 1e9 / peak,
+             "what": "frac: the kernels' own algorithmic bytes per gradient / ms_per_step / peak; "
+                     "frac_vs_one_step_model: bytes a one-step-per-launch gradient must move (FP32 state, "
+                     "K-step recompute, D buffer, correlation; strips and checkpoints) / ms_per_step / peak"}
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
             "frac": achieved / peak if achieved else None,
-            "traffic": traffic_per_shot * nshots if traffic_per_shot else None,
+            "traffic": ratio * algo_per_launch if ratio else None,
+            "traffic_over_algorithmic": ratio,
             "kernel": kinds[dom][0], "peak_kind": peak_kind,
             "algorithmic_bytes_per_launch": bytes_tot / max(launches, 1),
             "avg_launch_us": ms_tot * 1e3 / max(launches, 1),
@@ -789,6 +891,8 @@ def run_gb300(a):
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "gpu_launches": total_launches,
             "roofline": roof,
+            "whole_gradient": whole,
+            "parity": parity,
             "tuning": tuned or {"tz": a.tz, "variant": a.variant},
             "launch": "CUDA graph per batch (captured in the warm-up, replayed in the timed steps)",
             "profiled_step_ms": t_prof * 1e3}

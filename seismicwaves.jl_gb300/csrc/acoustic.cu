@@ -85,14 +85,21 @@ __device__ __forceinline__ float ring_update(float* ring, int slot, int it, floa
 // shot.  Duplicated points are summed in source order by one thread, like the
 // reference's serial loop.  Interior points add the source to p[n+1] and to
 // the increment d[n+1] (and to D when the gradient keeps it).
+// With two steps per stencil launch (k_ac2d_pair) the first step's pressure
+// on the receiver rows is in the stash; it_stash > 0 records that step from it.
 __global__ void k_inject_record(const ShotDesc* __restrict__ desc, const long long* __restrict__ pts,
                                 const int* __restrict__ ptr, const int* __restrict__ ids,
                                 const int* __restrict__ bslot, const long long* __restrict__ rec_lin,
                                 FieldArg pnew, FieldArg dnew, FieldArg dfield, int d_first, int it, int record,
-                                int dbf16) {
+                                int dbf16, const int* __restrict__ rec_stash, FieldArg stash, int it_stash) {
   const int shot = blockIdx.x;
   const ShotDesc D = desc[shot];
   if (it > D.nt) return;
+  if (it_stash > 0) {
+    const float* sp = stash.p + (long long)shot * stash.s;
+    for (int r = threadIdx.x; r < D.nrec; r += blockDim.x)
+      D.tr[(long long)(it_stash - 1) + (long long)r * D.nt] = sp[rec_stash[D.rec_off + r]];
+  }
   float* pn = pnew.p + (long long)shot * pnew.s;
   float* dn = dnew.p + (long long)shot * dnew.s;
   float* dd = (dfield.p && shot >= d_first) ? dptr(dfield, shot, dbf16) : nullptr;
@@ -182,7 +189,7 @@ __device__ void adj_inject_shot(const ShotDesc& D, const long long* __restrict__
       gp[lin] = gv;
       cp[lin] = cv;
     } else {
-      gp[lin] += corr * dld1(dp, lin, dbf16);
+      gp[lin] = __fmaf_rn(corr, dld1(dp, lin, dbf16), gp[lin]);
     }
   }
 }
@@ -427,6 +434,17 @@ struct sw_wavesim {
   // capacity (shots) of the state buffers
   int cap = 0;
   DevMem pb[2], db, psi[2][3], xi[3];     // forward state: p ping-pong, increment d, psi ping-pong, xi
+  DevMem db2, xi2[3];                     // second d / xi buffers (two-step launches write state n+2 apart)
+  DevMem psim[3], xim[3];                 // memory variables between the two steps of a two-step launch
+  DevMem d_pair, d_recstash, d_stash;     // two-step launches: per-shot source / receiver-row table,
+                                          // receiver -> stash index, first-step pressure of receiver rows
+  bool pair_on = true;                    // 2D: two time steps per launch where possible
+  int pair_tz = 0;                        // rows per block of the two-step kernel (0 = heuristic)
+  int pair_occ = 0;                       // resident-block bound of the two-step kernel (0 = default, 1, 2)
+  bool pair_ok = false;                   // the current group's shots allow two-step launches
+  DevMem adb2, axi2[3];                   // second adjoint d / xi buffers (two-step adjoint launches)
+  DevMem d_amap;                          // [shot][k][P]: receiver point (CSR index) at x on receiver row k, or -1
+  bool pair_adj_ok = false;               // ... and two-step adjoint launches
   DevMem ab[2], adb, apsi[2][3], axi[3];  // adjoint state
   DevMem g, gc;
   DevMem dbuf;                         // D slots
@@ -531,8 +549,8 @@ void run_graph(sw_wavesim* ws, std::vector<long long> key, Work&& work) {
 
 std::vector<long long> group_key(const sw_wavesim* ws, const std::vector<HostShot>& group, bool grad) {
   std::vector<long long> k = {grad ? 1 : 0, ws->grp, ws->variant, ws->tile_tz, ws->pf, ws->adjw ? 1 : 0,
-                              ws->cpa ? 1 : 0,
-                             (long long)group.size()};
+                              ws->cpa ? 1 : 0, ws->pair_ok ? 1 : 0, ws->pair_adj_ok ? 1 : 0, ws->pair_tz,
+                              ws->pair_occ, (long long)group.size()};
   for (const auto& h : group) k.push_back(h.nt);
   return k;
 }
@@ -553,6 +571,11 @@ struct Tables {
   int nring = 0;
   std::vector<HostShot> order;  // sorted by nt descending
   int max_nt = 0;
+  std::vector<PairShot> pair;    // two-step launches: per shot sources and receiver rows
+  std::vector<int> recstash;     // per receiver: stash index k * P + x (k = its row's slot)
+  bool pair_ok = false;
+  std::vector<int> amap;         // adjoint: receiver point on each receiver row, per x
+  bool pair_adj_ok = false;
 };
 
 long long lin_of(const sw_wavesim* ws, const int* I) {  // 1-based -> padded linear
@@ -766,6 +789,71 @@ void build_tables(sw_wavesim* ws, const sw_acoustic_shot* shots, const std::vect
     tf_o += ntf;
     tr_o += ntr;
   }
+  // Two-step launches (2D): every shot's source points and receivers off the
+  // outermost grid lines (no boundary ring), at most PAIR_MAXSP unique source
+  // points and PAIR_MAXRR receiver rows per shot.
+  T.pair.assign(S, PairShot{});
+  T.recstash.assign(T.rec.size(), 0);
+  T.pair_ok = ws->N == 2 && ws->pair_on && (ws->variant & 3) == 0 && !ws->cpa;
+  for (int k = 0; k < S && T.pair_ok; ++k) {
+    const ShotDesc& D = T.desc[k];
+    PairShot& ps = T.pair[k];
+    ps.tf = D.tf;
+    ps.nt = D.nt;
+    ps.nsp = D.nsp;
+    if (D.nsp > PAIR_MAXSP) { T.pair_ok = false; break; }
+    for (int u = 0; u < D.nsp; ++u) {
+      const long long lin = T.pts[D.sp_off + u];
+      if (T.bslot[D.sp_off + u] >= 0) T.pair_ok = false;
+      ps.sx[u] = (int)(lin % ws->P);
+      ps.sz[u] = (int)(lin / ws->P);
+      ps.k0[u] = T.ptr[D.sp_ptr + u];
+      ps.k1[u] = T.ptr[D.sp_ptr + u + 1];
+    }
+    ps.nrr = 0;
+    for (int r = 0; r < D.nrec && T.pair_ok; ++r) {
+      const long long lin = T.rec[D.rec_off + r];
+      const int z = (int)(lin / ws->P), x = (int)(lin % ws->P);
+      if (z < 1 || z > ws->n[1] - 2) { T.pair_ok = false; break; }
+      int slot = -1;
+      for (int q = 0; q < ps.nrr; ++q)
+        if (ps.rrow[q] == z) slot = q;
+      if (slot < 0) {
+        if (ps.nrr == PAIR_MAXRR) { T.pair_ok = false; break; }
+        slot = ps.nrr++;
+        ps.rrow[slot] = z;
+      }
+      T.recstash[D.rec_off + r] = slot * ws->P + x;
+    }
+  }
+  // two-step adjoint launches: the receiver points (the adjoint sources) off
+  // the outermost grid lines too; per receiver row a map x -> point
+  T.pair_adj_ok = T.pair_ok && grad;
+  if (T.pair_adj_ok) {
+    T.amap.assign((size_t)S * PAIR_MAXRR * ws->P, -1);
+    for (int k = 0; k < S && T.pair_adj_ok; ++k) {
+      const ShotDesc& D = T.desc[k];
+      T.pair[k].adj = D.adj;
+      for (int u = 0; u < D.nrp; ++u) {
+        const long long lin = T.pts[D.rp_off + u];
+        const int z = (int)(lin / ws->P), x = (int)(lin % ws->P);
+        if (T.bslot[D.rp_off + u] >= 0) { T.pair_adj_ok = false; break; }
+        int slot = -1;
+        for (int q = 0; q < T.pair[k].nrr; ++q)
+          if (T.pair[k].rrow[q] == z) slot = q;
+        if (slot < 0) { T.pair_adj_ok = false; break; }
+        T.amap[((size_t)k * PAIR_MAXRR + slot) * ws->P + x] = (int)(D.rp_ptr + u);
+      }
+    }
+  }
+  if (T.pair_adj_ok) upload(ws, ws->d_amap, T.amap, "adjoint receiver map");
+  ws->pair_adj_ok = T.pair_adj_ok;
+  if (T.pair_ok) {
+    upload(ws, ws->d_pair, T.pair, "two-step shot table");
+    upload(ws, ws->d_recstash, T.recstash, "receiver stash table");
+    ensure(ws, ws->d_stash, (size_t)S * PAIR_MAXRR * ws->P * sizeof(float), "receiver-row stash");
+  }
+  ws->pair_ok = T.pair_ok;
   ensure(ws, ws->d_ring, (size_t)std::max(3 * T.nring, 4) * sizeof(float), "boundary rings");
   for (int k = 0; k < S; ++k) T.desc[k].ring = ws->d_ring.as<float>() + 3LL * ring_off[k];
   upload(ws, ws->d_desc, T.desc, "shot descriptors");
@@ -789,6 +877,14 @@ void ensure_state(sw_wavesim* ws, int S, bool grad, int max_nt) {
     for (int k = 0; k < 2; ++k)
       for (int d = 0; d < ws->N; ++d) dev_alloc(ws->psi[k][d], (size_t)S * ws->psz[d] * sizeof(float), "psi", st);
     for (int d = 0; d < ws->N; ++d) dev_alloc(ws->xi[d], (size_t)S * ws->xsz[d] * sizeof(float), "xi", st);
+    if (ws->N == 2) {  // two-step launches
+      dev_alloc(ws->db2, (size_t)S * F * sizeof(float), "pressure increment (second buffer)", st);
+      for (int d = 0; d < ws->N; ++d) {
+        dev_alloc(ws->xi2[d], (size_t)S * ws->xsz[d] * sizeof(float), "xi (second buffer)", st);
+        dev_alloc(ws->psim[d], (size_t)S * ws->psz[d] * sizeof(float), "psi between two steps", st);
+        dev_alloc(ws->xim[d], (size_t)S * ws->xsz[d] * sizeof(float), "xi between two steps", st);
+      }
+    }
     if (ws->gradient) {
       for (int b = 0; b < 2; ++b) dev_alloc(ws->ab[b], (size_t)S * F * sizeof(float), "adjoint field", st);
       dev_alloc(ws->adb, (size_t)S * F * sizeof(float), "adjoint increment", st);
@@ -797,6 +893,11 @@ void ensure_state(sw_wavesim* ws, int S, bool grad, int max_nt) {
       for (int d = 0; d < ws->N; ++d) dev_alloc(ws->axi[d], (size_t)S * ws->xsz[d] * sizeof(float), "adjoint xi", st);
       dev_alloc(ws->g, (size_t)S * F * sizeof(float), "gradient", st);
       dev_alloc(ws->gc, (size_t)S * F * sizeof(float), "gradient compensation", st);
+      if (ws->N == 2) {  // two-step adjoint launches
+        dev_alloc(ws->adb2, (size_t)S * F * sizeof(float), "adjoint increment (second buffer)", st);
+        for (int d = 0; d < ws->N; ++d)
+          dev_alloc(ws->axi2[d], (size_t)S * ws->xsz[d] * sizeof(float), "adjoint xi (second buffer)", st);
+      }
     }
     ws->cap = S;
     ws->d_slots = 0;
@@ -842,6 +943,8 @@ size_t per_shot_bytes(const sw_wavesim* ws, bool grad, int max_nt) {
   long long floats = 3 * ws->F + ws->strip_total;
   for (int d = 0; d < ws->N; ++d) floats += ws->psz[d];
   if (ws->gradient) floats = 2 * floats + 2 * ws->F;
+  if (ws->N == 2) floats += ws->F + 2 * ws->strip_total;  // second d / xi buffers, scratch strips
+  if (ws->N == 2 && ws->gradient) floats += ws->F + ws->strip_total;  // second adjoint d / xi buffers
   if (grad) {
     const int K = ws->gp.check_freq;
     const long long dsl = (K == 1 ? (long long)max_nt : K) * ws->F;
@@ -901,6 +1004,46 @@ StepCtx make_step_ctx(sw_wavesim* ws, int S) {
   c.TZ = TZ;
   c.tiles_z = (nint + TZ - 1) / TZ;
   return c;
+}
+
+// Two-step launches: warps of PAIR_OUT x points, 4 per block; bands of 32
+// rows (the band halo of the first step repeats 2 of every 34 rows), shorter
+// bands where 32-row ones would leave the GPU with less than two waves of
+// blocks (small batches), 4 rows at least.
+StepCtx make_pair_ctx(sw_wavesim* ws, int S) {
+  StepCtx c{ws, 0, 0, 1, 0};
+  const int warps = (ws->n[0] - 2) / PAIR_OUT + 1;
+  c.tiles_x = (warps + 3) / 4;
+  int TZ = ws->pair_tz;
+  if (TZ <= 0) {
+    const int sms = ws->ctx->num_sms > 0 ? ws->ctx->num_sms : 148;
+    TZ = 32;
+    while (TZ > 4 && (long long)S * c.tiles_x * ((ws->n[1] - 2 + TZ - 1) / TZ) < 2LL * 6 * sms) TZ /= 2;
+  }
+  c.TZ = TZ;
+  c.tiles_z = (ws->n[1] - 2 + c.TZ - 1) / c.TZ;
+  return c;
+}
+
+// Algorithmic bytes of one two-step launch: per interior point and shot R
+// p[n], d[n], W p[n+2], d[n+2] (16 B for both steps), fact once for the
+// launch, per strip cell and axis R psi/xi of step n and W those of step n+2;
+// the D slots of both steps; checkpoint copies of step n; adjoint: R D of
+// both steps and R/W the per-shot FP32 correlation sum once.
+double pair_bytes(const sw_wavesim* ws, int S, int n_dwrite, bool ckpt, bool adjoint = false) {
+  double pts = (double)(ws->n[0] - 2) * (ws->n[1] - 2);
+  double strip = 0.0;
+  const int H = ws->prm.halo;
+  for (int d = 0; d < 2; ++d) {
+    double w = 0.0;
+    for (int x = 1; x <= ws->n[d] - 2; ++x) w += (x < H || x >= ws->n[d] - H) ? 1.0 : 0.0;
+    strip += w * (double)(ws->n[1 - d] - 2);
+  }
+  const double dsz = (ws->gradient && ws->gp.snapshot_bf16 >= 1) ? 2.0 : 4.0;
+  double b = (16.0 * S + 4.0) * pts + 16.0 * strip * S + 2.0 * dsz * pts * n_dwrite;
+  if (ckpt) b += 8.0 * pts * S + 8.0 * strip * S;
+  if (adjoint) b += (2.0 * dsz + 8.0) * pts * S;
+  return b;
 }
 
 // Algorithmic bytes of one stencil launch (FP32 words): per interior point and
@@ -969,6 +1112,27 @@ void enable_cpa_carveout() {
   done_for_device = dev;
 }
 
+// The two-step kernels keep a row ring in shared memory (25 / 37 KB per
+// block): ask for the largest carveout so the occupancy of their launch
+// bounds is reached.
+template <int MODE, int MB>
+void enable_pair_carveout() {
+  static int done_for_device = -1;
+  int dev = 0;
+  check_cuda(cudaGetDevice(&dev), "cudaGetDevice");
+  if (done_for_device == dev) return;
+  check_cuda(cudaFuncSetAttribute(k_ac2d_pair<MODE, 4, MB>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                  (int)cudaSharedmemCarveoutMaxShared),
+             "shared memory carveout");
+  done_for_device = dev;
+}
+
+template <int MODE, int MB>
+void launch_pair(long long blocks, cudaStream_t st, const StepArgs& a, const PairArgs& b) {
+  enable_pair_carveout<MODE, MB>();
+  k_ac2d_pair<MODE, 4, MB><<<(unsigned)blocks, 128, 0, st>>>(a, b);
+}
+
 struct Launcher {
   sw_wavesim* ws;
   cudaStream_t st;
@@ -1025,6 +1189,36 @@ struct Launcher {
       }
     }
     check_cuda(cudaGetLastError(), "stencil launch");
+    ws->ctx->prof.end(st, kind, ev);
+  }
+  // two time steps in one launch (2D)
+  template <int MODE>
+  void pair(const StepArgs& a, const PairArgs& b, double bytes, bool recompute = false) {
+    check_vector_alignment(a);
+    if (reinterpret_cast<uintptr_t>(b.Dout2.p) % 16 != 0 || reinterpret_cast<uintptr_t>(b.dcorr2.p) % 16 != 0 ||
+        (b.stash.p && b.stash.s % 4 != 0))
+      fail(SW_ERR_CUDA, "internal error: misaligned field handed to the two-step stencil");
+    const long long blocks = (long long)a.nshots * a.tiles_x * a.tiles_y * a.tiles_z;
+    cudaEvent_t ev = nullptr;
+    const int kind = MODE == MODE_ADJW ? KK_ADJOINT : recompute ? KK_RECOMPUTE : KK_STENCIL;
+    ws->ctx->prof.begin(st, kind, bytes, &ev);
+    // resident blocks per SM: forward kinds 6 (default), 4 or 7; adjoint 5, 3 or 4
+    if constexpr (MODE == MODE_ADJW) {
+      if (ws->pair_occ == 1)
+        launch_pair<MODE, 3>(blocks, st, a, b);
+      else if (ws->pair_occ == 2)
+        launch_pair<MODE, 4>(blocks, st, a, b);
+      else
+        launch_pair<MODE, 5>(blocks, st, a, b);
+    } else {
+      if (ws->pair_occ == 1)
+        launch_pair<MODE, 4>(blocks, st, a, b);
+      else if (ws->pair_occ == 2)
+        launch_pair<MODE, 7>(blocks, st, a, b);
+      else
+        launch_pair<MODE, 6>(blocks, st, a, b);
+    }
+    check_cuda(cudaGetLastError(), "two-step stencil launch");
     ws->ctx->prof.end(st, kind, ev);
   }
 };
@@ -1084,6 +1278,13 @@ void zero_state(sw_wavesim* ws, int S, bool adjoint) {
   for (int d = 0; d < ws->N; ++d)
     check_cuda(cudaMemsetAsync((adjoint ? ws->axi : ws->xi)[d].p, 0, (size_t)S * ws->xsz[d] * sizeof(float), st),
                "reset xi");
+  DevMem& d2 = adjoint ? ws->adb2 : ws->db2;
+  if (d2.p) {
+    check_cuda(cudaMemsetAsync(d2.p, 0, (size_t)S * ws->F * sizeof(float), st), "reset d");
+    for (int d = 0; d < ws->N; ++d)
+      check_cuda(cudaMemsetAsync((adjoint ? ws->axi2 : ws->xi2)[d].p, 0, (size_t)S * ws->xsz[d] * sizeof(float), st),
+                 "reset xi");
+  }
   check_cuda(cudaMemsetAsync(ws->d_ring.p, 0, ws->d_ring.bytes, st), "reset rings");
 }
 
@@ -1103,14 +1304,16 @@ void download_traces(sw_wavesim* ws, const sw_acoustic_shot* shots, const std::v
 }
 
 void launch_inject(sw_wavesim* ws, int Sa, const FieldArg& pnew, const FieldArg& dnew, const FieldArg& Dw,
-                   int d_first, int it, int record) {
+                   int d_first, int it, int record, int it_stash = 0) {
   cudaStream_t st = ws->ctx->stream;
   cudaEvent_t ev = nullptr;
   ws->ctx->prof.begin(st, KK_SRCREC, 0.0, &ev);
+  const FieldArg stash{ws->d_stash.as<float>(), (long long)PAIR_MAXRR * ws->P};
   k_inject_record<<<Sa, 128, 0, st>>>(ws->d_desc.as<ShotDesc>(), ws->d_pts.as<long long>(), ws->d_ptr.as<int>(),
                                       ws->d_ids.as<int>(), ws->d_bslot.as<int>(), ws->d_rec.as<long long>(), pnew,
                                       dnew, Dw, d_first, it, record,
-                                      (ws->gradient && ws->gp.snapshot_bf16 >= 1) ? 1 : 0);
+                                      (ws->gradient && ws->gp.snapshot_bf16 >= 1) ? 1 : 0,
+                                      ws->d_recstash.as<int>(), stash, it_stash);
   check_cuda(cudaGetLastError(), "inject/record launch");
   ws->ctx->prof.end(st, KK_SRCREC, ev);
 }
@@ -1147,8 +1350,58 @@ void unpack_checkpoint(sw_wavesim* ws, int S, int slot) {
   ws->ctx->prof.end(st, KK_OTHER, ev);
 }
 
+// Forward state buffers.  A launch reads state (p, d, psi, xi) from buffers
+// (p, d, k, x) and writes the other p and psi buffers; a two-step launch also
+// writes the other d and xi buffers (its repeated first steps at band and
+// warp edges read d and xi of points other warps update), a one-step launch
+// updates d and xi in place.  The adjoint state uses the same scheme.
+struct FwdState {
+  int p = 0, d = 0, k = 0, x = 0;
+};
+
+void set_io(sw_wavesim* ws, StepArgs& a, FwdState& s, bool two, bool adjoint) {
+  const long long F = ws->F;
+  const int dn = two ? 1 - s.d : s.d, xn = two ? 1 - s.x : s.x;
+  DevMem* pb = adjoint ? ws->ab : ws->pb;
+  DevMem* db[2] = {adjoint ? &ws->adb : &ws->db, adjoint ? &ws->adb2 : &ws->db2};
+  a.pcur = fa(pb[s.p], F);
+  a.pnew = fa(pb[1 - s.p], F);
+  a.din = fa(*db[s.d], F);
+  a.dout = fa(*db[dn], F);
+  for (int d = 0; d < ws->N; ++d) {
+    DevMem* xb[2] = {adjoint ? &ws->axi[d] : &ws->xi[d], adjoint ? &ws->axi2[d] : &ws->xi2[d]};
+    DevMem(*ps)[3] = adjoint ? ws->apsi : ws->psi;
+    a.psi_in[d] = fa(ps[s.k][d], ws->psz[d]);
+    a.psi_out[d] = fa(ps[1 - s.k][d], ws->psz[d]);
+    a.xi_in[d] = fa(*xb[s.x], ws->xsz[d]);
+    a.xi_out[d] = fa(*xb[xn], ws->xsz[d]);
+  }
+  s.p = 1 - s.p;
+  s.k = 1 - s.k;
+  s.d = dn;
+  s.x = xn;
+  // the second d / xi buffers exist for 2D simulations only
+  bool ok = a.din.p && a.dout.p;
+  for (int d = 0; d < ws->N; ++d) ok = ok && a.xi_in[d].p && a.xi_out[d].p;
+  if (!ok) fail(SW_ERR_CUDA, "internal error: state buffer missing for this launch");
+}
+
+PairArgs pair_args(sw_wavesim* ws, int it1) {
+  PairArgs b;
+  std::memset(&b, 0, sizeof(b));
+  for (int d = 0; d < 2; ++d) {
+    b.psi_mid[d] = fa(ws->psim[d], ws->psz[d]);
+    b.xi_mid[d] = fa(ws->xim[d], ws->xsz[d]);
+  }
+  b.shots = ws->d_pair.as<PairShot>();
+  b.ids = ws->d_ids.as<int>();
+  b.it1 = it1;
+  return b;
+}
+
 // Forward of one group: all shots step together.  Gradient mode (grad = true)
-// also writes checkpoints and the top-segment D.
+// also writes checkpoints and the top-segment D.  Consecutive steps run as one
+// two-step launch where nothing happens between them (see k_ac2d_pair).
 void forward_group(sw_wavesim* ws, const std::vector<HostShot>& group, bool grad) {
   const int S = (int)group.size();
   cudaStream_t st = ws->ctx->stream;
@@ -1158,25 +1411,31 @@ void forward_group(sw_wavesim* ws, const std::vector<HostShot>& group, bool grad
   const long long F = ws->F;
   const bool bf16 = grad && ws->gp.snapshot_bf16 >= 2;
   const long long slot = bf16 ? ws->strip_total : 2 * F + ws->strip_total;
-  int pc = 0, pk = 0;
+  FwdState sta;
   Launcher L{ws, st};
-  for (int it = 1; it <= max_nt; ++it) {
-    int ck_slot = -1;
+  // D(it-1) is kept at step it by shots >= d_first: every shot when K == 1,
+  // else the shots whose top segment (after their last checkpoint) holds it-1
+  auto d_first_of = [&](int it, int Sa) {
+    if (K == 1) return 0;
+    for (int k = 0; k < Sa; ++k)
+      if (it - 1 >= group[k].nt / K * K) return k;
+    return Sa;
+  };
+  auto dslot_of = [&](int it) -> long long { return K == 1 ? it - 1 : (it - 1) % K; };
+  const bool snap = !grad && ws->snapevery > 0;
+  for (int it = 1; it <= max_nt;) {
     const int Sa = active_count(group, it);
-    const StepCtx c = make_step_ctx(ws, Sa);
+    const int d_first = grad ? d_first_of(it, Sa) : Sa;
+    // two steps (it, it+1) when state `it` needs no checkpoint or snapshot and
+    // the active shots and D writers stay the same
+    bool two = ws->pair_ok && it + 1 <= max_nt && active_count(group, it + 1) == Sa &&
+               !(snap && it % ws->snapevery == 0);
+    if (two && grad) two = !(K > 1 && it % K == 0) && d_first_of(it + 1, Sa) == d_first;
+    const StepCtx c = two ? make_pair_ctx(ws, Sa) : make_step_ctx(ws, Sa);
     StepArgs a = base_args(ws, c, Sa);
-    a.pcur = fa(ws->pb[pc], F);
-    a.pnew = fa(ws->pb[1 - pc], F);
-    a.din = fa(ws->db, F);
-    a.dout = a.din;
-    for (int d = 0; d < ws->N; ++d) {
-      a.psi_in[d] = fa(ws->psi[pk][d], ws->psz[d]);
-      a.psi_out[d] = fa(ws->psi[1 - pk][d], ws->psz[d]);
-      a.xi_in[d] = fa(ws->xi[d], ws->xsz[d]);
-      a.xi_out[d] = a.xi_in[d];
-    }
+    set_io(ws, a, sta, two, false);
+    int ck_slot = -1;
     bool ckpt = false;
-    int d_first = Sa;
     if (grad) {
       // checkpoint m = (it-1)/K holds the state (p, d, psi, xi) after step mK
       if (K > 1 && (it - 1) % K == 0 && (it - 1) / K >= 1) {
@@ -1197,40 +1456,42 @@ void forward_group(sw_wavesim* ws, const std::vector<HostShot>& group, bool grad
         for (int d = 0; d < ws->N; ++d) { a.ck_xi[d] = FieldArg{base + off, sstride}; off += ws->xsz[d]; }
         ckpt = true;
       }
-      // D(it-1) is kept for shots whose top segment contains it-1 (every step when K == 1)
-      long long dslot;
-      if (K == 1) {
-        d_first = 0;
-        dslot = it - 1;
-      } else {
-        for (int k = 0; k < Sa; ++k)
-          if (it - 1 >= group[k].nt / K * K) { d_first = k; break; }
-        dslot = (it - 1) % K;
-      }
-      a.Dout = dslot_arg(ws, dslot);
+      a.Dout = dslot_arg(ws, dslot_of(it));
       a.d_first = d_first;
     }
     const int n_dwrite = grad ? Sa - d_first : 0;
-    const double bytes = stencil_bytes(ws, Sa, grad ? MODE_FWD_D : MODE_FWD, n_dwrite, ckpt);
-    if (grad)
-      L.step<MODE_FWD_D>(a, c, bytes);
-    else
-      L.step<MODE_FWD>(a, c, bytes);
-    launch_inject(ws, Sa, a.pnew, a.dout, grad ? a.Dout : FieldArg{nullptr, 0}, d_first, it, 1);
+    if (two) {
+      PairArgs b = pair_args(ws, it);
+      b.Dout2 = grad ? dslot_arg(ws, dslot_of(it + 1)) : FieldArg{nullptr, 0};
+      b.stash = FieldArg{ws->d_stash.as<float>(), (long long)PAIR_MAXRR * ws->P};
+      const double bytes = pair_bytes(ws, Sa, n_dwrite, ckpt);
+      if (grad)
+        L.pair<MODE_FWD_D>(a, b, bytes);
+      else
+        L.pair<MODE_FWD>(a, b, bytes);
+      launch_inject(ws, Sa, a.pnew, a.dout, grad ? b.Dout2 : FieldArg{nullptr, 0}, d_first, it + 1, 1, it);
+    } else {
+      const double bytes = stencil_bytes(ws, Sa, grad ? MODE_FWD_D : MODE_FWD, n_dwrite, ckpt);
+      if (grad)
+        L.step<MODE_FWD_D>(a, c, bytes);
+      else
+        L.step<MODE_FWD>(a, c, bytes);
+      launch_inject(ws, Sa, a.pnew, a.dout, grad ? a.Dout : FieldArg{nullptr, 0}, d_first, it, 1);
+    }
     if (ck_slot >= 0) pack_checkpoint(ws, Sa, ck_slot);
-    if (!grad && ws->snapevery > 0 && it % ws->snapevery == 0) {
+    const int it_end = two ? it + 1 : it;
+    if (snap && it_end % ws->snapevery == 0) {
       // savesnapshot!("pcur" => p[it]): unpadded copy into the caller's buffer of each active shot
       const long long rows = (long long)ws->n[1] * (ws->N == 3 ? ws->n[2] : 1);
       for (int k = 0; k < Sa; ++k) {
-        float* dst = ws->snap_out[group[k].orig] + (long long)(it / ws->snapevery - 1) * ws->npts;
+        float* dst = ws->snap_out[group[k].orig] + (long long)(it_end / ws->snapevery - 1) * ws->npts;
         check_cuda(cudaMemcpy2DAsync(dst, (size_t)ws->n[0] * sizeof(float), a.pnew.p + (long long)k * a.pnew.s,
                                      (size_t)ws->P * sizeof(float), (size_t)ws->n[0] * sizeof(float), (size_t)rows,
                                      cudaMemcpyDefault, st),
                    "snapshot copy");
       }
     }
-    pc = 1 - pc;
-    pk = 1 - pk;
+    it = it_end + 1;
   }
 }
 
@@ -1247,8 +1508,8 @@ void adjoint_group(sw_wavesim* ws, const std::vector<HostShot>& group) {
   check_cuda(cudaMemsetAsync(ws->g.p, 0, (size_t)S * F * sizeof(float), st), "reset g");
   check_cuda(cudaMemsetAsync(ws->gc.p, 0, (size_t)S * F * sizeof(float), st), "reset gc");
   if (ws->adjw) check_cuda(cudaMemsetAsync(ws->tot64.p, 0, (size_t)F * sizeof(double), st), "reset total");
-  int apc = 0, apk = 0;
-  for (int it = max_nt; it >= 1; --it) {
+  FwdState ast;  // adjoint state buffers (p = lambda, d, psi, xi), as the forward's
+  for (int it = max_nt; it >= 1;) {
     const int Sa = active_count(group, it);
     if (K > 1 && it % K == 0) {
       // recover segment m: forward steps (m-1)K+1 .. mK from the checkpoint at (m-1)K
@@ -1273,52 +1534,59 @@ void adjoint_group(sw_wavesim* ws, const std::vector<HostShot>& group) {
       }
       for (int d = 0; d < ws->N; ++d) { ck_psi[d] = FieldArg{cbase + off, cstride}; off += ws->psz[d]; }
       for (int d = 0; d < ws->N; ++d) { ck_xi[d] = FieldArg{cbase + off, cstride}; off += ws->xsz[d]; }
-      int pc = 0, pk = 0;
-      for (int t = (m - 1) * K + 1; t <= m * K; ++t) {
+      // the first launch reads the checkpoint and writes p / psi buffers 0 and
+      // d / xi buffer 0 (one step, in place) or 1 (two steps; 2D only)
+      FwdState rs{1, 0, 1, 0};
+      const StepCtx cp2 = make_pair_ctx(ws, Sa);
+      for (int t = (m - 1) * K + 1; t <= m * K;) {
         const bool first = t == (m - 1) * K + 1;
-        StepArgs a = base_args(ws, c, Sa);
-        a.pcur = first ? ck_p : fa(ws->pb[pc], F);
-        a.pnew = fa(ws->pb[first ? 0 : 1 - pc], F);
-        a.din = first ? ck_d : fa(ws->db, F);
-        a.dout = fa(ws->db, F);
-        for (int d = 0; d < ws->N; ++d) {
-          a.psi_in[d] = first ? ck_psi[d] : fa(ws->psi[pk][d], ws->psz[d]);
-          a.psi_out[d] = fa(ws->psi[first ? 0 : 1 - pk][d], ws->psz[d]);
-          a.xi_in[d] = first ? ck_xi[d] : fa(ws->xi[d], ws->xsz[d]);
-          a.xi_out[d] = fa(ws->xi[d], ws->xsz[d]);
-        }
-        const long long dslot = (t - 1) % K;
-        a.Dout = dslot_arg(ws, dslot);
-        a.d_first = 0;
-        L.step<MODE_FWD_D>(a, c, stencil_bytes(ws, Sa, MODE_FWD_D, Sa, false), true);
-        launch_inject(ws, Sa, a.pnew, a.dout, a.Dout, 0, t, 0);
+        const bool two = ws->pair_ok && t + 1 <= m * K;
+        StepArgs a = base_args(ws, two ? cp2 : c, Sa);
+        set_io(ws, a, rs, two, false);
         if (first) {
-          pc = 0;
-          pk = 0;
+          a.pcur = ck_p;
+          a.din = ck_d;
+          for (int d = 0; d < ws->N; ++d) {
+            a.psi_in[d] = ck_psi[d];
+            a.xi_in[d] = ck_xi[d];
+          }
+        }
+        a.Dout = dslot_arg(ws, (t - 1) % K);
+        a.d_first = 0;
+        if (two) {
+          PairArgs b = pair_args(ws, t);
+          b.Dout2 = dslot_arg(ws, t % K);
+          L.pair<MODE_FWD_D>(a, b, pair_bytes(ws, Sa, Sa, false), true);
+          launch_inject(ws, Sa, a.pnew, a.dout, b.Dout2, 0, t + 1, 0);
+          t += 2;
         } else {
-          pc = 1 - pc;
-          pk = 1 - pk;
+          L.step<MODE_FWD_D>(a, c, stencil_bytes(ws, Sa, MODE_FWD_D, Sa, false), true);
+          launch_inject(ws, Sa, a.pnew, a.dout, a.Dout, 0, t, 0);
+          t += 1;
         }
       }
     }
-    // adjoint step it with the fused correlation against D(it-1)
-    const StepCtx c = make_step_ctx(ws, Sa);
+    // adjoint step it with the fused correlation against D(it-1); two steps
+    // (it, it-1) in one launch when no recompute and no flush of the FP32 sums
+    // falls between them and the active shots stay the same
+    const bool two = ws->pair_adj_ok && ws->adjw && it - 1 >= 1 && active_count(group, it - 1) == Sa &&
+                     !(K > 1 && (it - 1) % K == 0) && (it - 1) % 32 != 0;
+    const StepCtx c = two ? make_pair_ctx(ws, Sa) : make_step_ctx(ws, Sa);
     StepArgs a = base_args(ws, c, Sa);
-    a.pcur = fa(ws->ab[apc], F);
-    a.pnew = fa(ws->ab[1 - apc], F);
-    a.din = fa(ws->adb, F);
-    a.dout = a.din;
-    for (int d = 0; d < ws->N; ++d) {
-      a.psi_in[d] = fa(ws->apsi[apk][d], ws->psz[d]);
-      a.psi_out[d] = fa(ws->apsi[1 - apk][d], ws->psz[d]);
-      a.xi_in[d] = fa(ws->axi[d], ws->xsz[d]);
-      a.xi_out[d] = a.xi_in[d];
-    }
+    set_io(ws, a, ast, two, true);
     const long long dslot = K == 1 ? it - 1 : (it - 1) % K;
     a.dcorr = dslot_arg(ws, dslot);
     a.g = fa(ws->g, F);
     a.gc = ws->adjw ? FieldArg{nullptr, 0} : fa(ws->gc, F);
-    if (ws->adjw) {
+    FieldArg dcorr_last = a.dcorr;  // the D of the step whose injection follows
+    if (two) {
+      PairArgs b = pair_args(ws, it);
+      b.dcorr2 = dslot_arg(ws, K == 1 ? it - 2 : (it - 2) % K);
+      b.ptr = ws->d_ptr.as<int>();
+      b.amap = ws->d_amap.as<int>();
+      L.pair<MODE_ADJW>(a, b, pair_bytes(ws, Sa, 0, false, true));
+      dcorr_last = b.dcorr2;
+    } else if (ws->adjw) {
       L.step<MODE_ADJW>(a, c, stencil_bytes(ws, Sa, MODE_ADJW, 0, false));
     } else if (ws->grp == 4) {
       // 4 shots per block (one per warp) over 128-wide tiles; the correlation is
@@ -1339,14 +1607,15 @@ void adjoint_group(sw_wavesim* ws, const std::vector<HostShot>& group) {
     } else {
       L.step<MODE_ADJ>(a, c, stencil_bytes(ws, Sa, MODE_ADJ, 0, false));
     }
+    const int it_last = two ? it - 1 : it;  // the step whose adjoint sources are injected now
     cudaEvent_t ev = nullptr;
     ws->ctx->prof.begin(st, KK_SRCREC, 0.0, &ev);
     k_adj_inject<<<(Sa + ws->grp - 1) / ws->grp, 128, 0, st>>>(
         ws->d_desc.as<ShotDesc>(), ws->d_pts.as<long long>(), ws->d_ptr.as<int>(), ws->d_ids.as<int>(),
-        ws->d_bslot.as<int>(), a.pnew, a.dout, a.dcorr, a.g, a.gc, it, Sa, ws->grp, a.dbf16);
+        ws->d_bslot.as<int>(), a.pnew, a.dout, dcorr_last, a.g, a.gc, it_last, Sa, ws->grp, a.dbf16);
     check_cuda(cudaGetLastError(), "adjoint inject launch");
     ws->ctx->prof.end(st, KK_SRCREC, ev);
-    if (ws->adjw && (it - 1) % 32 == 0) {  // at most 32 terms per FP32 sum
+    if (ws->adjw && (it_last - 1) % 32 == 0) {  // at most 32 terms per FP32 sum
       ws->ctx->prof.begin(st, KK_OTHER, 0.0, &ev);
       const long long blocks = std::min<long long>((F / 4 + 255) / 256, 8192);
       k_flush_grad<<<(unsigned)blocks, 256, 0, st>>>(ws->g.as<float>(), F, S, ws->tot64.as<double>());
@@ -1354,8 +1623,7 @@ void adjoint_group(sw_wavesim* ws, const std::vector<HostShot>& group) {
       check_cuda(cudaMemsetAsync(ws->g.p, 0, (size_t)S * F * sizeof(float), st), "gradient sums clear");
       ws->ctx->prof.end(st, KK_OTHER, ev);
     }
-    apc = 1 - apc;
-    apk = 1 - apk;
+    it = it_last - 1;
   }
 }
 
@@ -1723,6 +1991,10 @@ void wavesim_set_tuning(sw_wavesim* ws, int tz, int variant) {
   ws->pf = (variant / 16) % 16;
   ws->adj_plain = (variant & 256) == 0;
   ws->cpa = (variant & 512) != 0;
+  ws->pair_on = (variant & 1024) == 0;
+  static const int pair_tz[8] = {0, 8, 16, 32, 64, 128, 4, 0};
+  ws->pair_tz = pair_tz[(variant >> 11) & 7];
+  ws->pair_occ = (variant >> 14) & 3;
 }
 void wavesim_use_graphs(sw_wavesim* ws, bool on) {
   ws->use_graphs = on;

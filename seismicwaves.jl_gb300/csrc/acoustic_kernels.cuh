@@ -144,6 +144,18 @@ __device__ __forceinline__ void kahan_add(float& g, float& c, float y) {
   g = t;
 }
 
+// Rounded FP32 operations that the compiler may not contract into FMAs: the
+// stencil arithmetic below is spelled out with them so that every kernel
+// that advances a point (one step per launch or two) rounds identically,
+// whatever the surrounding code lets the compiler fuse.
+__device__ __forceinline__ float radd(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float rsub(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ float rmul(float a, float b) { return __fmul_rn(a, b); }
+// (l - 2c + r) * ih2: the second difference along one axis
+__device__ __forceinline__ float d2term(float l, float c, float r, float ih2) {
+  return rmul(radd(radd(l, rmul(-2.f, c)), r), ih2);
+}
+
 // C-PML term of one axis at point x (0-based) along an axis of n points.
 // Without damping the term is d2 (the plain second derivative).  In a strip
 // the two half-node memory variables psi around x are advanced (psi_out), the
@@ -166,22 +178,22 @@ __device__ __forceinline__ float cpml_axis_term(float d2, float pl, float p0, fl
   const long long ir = s.psi_base + (long long)qr * s.psi_step;
   const float oldl = s.psi_in[il];
   const float oldr = s.psi_in[ir];
-  const float newl = s.bh[ql] * oldl + s.ah[ql] * ((p0 - pl) * ih);
-  const float newr = s.bh[qr] * oldr + s.ah[qr] * ((pr - p0) * ih);
+  const float newl = radd(rmul(s.bh[ql], oldl), rmul(s.ah[ql], rmul(rsub(p0, pl), ih)));
+  const float newr = radd(rmul(s.bh[qr], oldr), rmul(s.ah[qr], rmul(rsub(pr, p0), ih)));
   s.psi_out[ir] = newr;
   if (s.ck_psi) s.ck_psi[ir] = oldr;
   if (first) {
     s.psi_out[il] = newl;
     if (s.ck_psi) s.ck_psi[il] = oldl;
   }
-  const float dpsi = (newr - newl) * ih;
+  const float dpsi = rmul(rsub(newr, newl), ih);
   const long long iq = s.xi_base + (long long)qr * s.xi_step;
   const float xo = s.xi_in[iq];
   if (s.ck_xi) s.ck_xi[iq] = xo;
-  const float t = d2 + dpsi;
-  const float xn = s.b[qr] * xo + s.a[qr] * t;
+  const float t = radd(d2, dpsi);
+  const float xn = radd(rmul(s.b[qr], xo), rmul(s.a[qr], t));
   s.xi_out[iq] = xn;
-  return t + xn;
+  return radd(t, xn);
 }
 
 // TMA prefetch of a contiguous global range into L2 (no registers, no
@@ -255,8 +267,8 @@ struct Ac2dRow {
       const float xm = e == 0 ? left : r0[e - 1];
       const float xp = e == 3 ? right : r0[e + 1];
       const float c = r0[e];
-      float tx = (xm - 2.f * c + xp) * ih2x;
-      float tz = (rm[e] - 2.f * c + rp[e]) * ih2z;
+      float tx = d2term(xm, c, xp, ih2x);
+      float tz = d2term(rm[e], c, rp[e], ih2z);
       const int x = x0 + e;
       const bool pin = inb && x >= 1 && x <= nx - 2;
       if (xstrip && pin) tx = cpml_axis_term(tx, xm, c, xp, x, nx, H, ihx, sx);
@@ -265,10 +277,10 @@ struct Ac2dRow {
         sz.xi_base = x;
         tz = cpml_axis_term(tz, rm[e], c, rp[e], z, nz, H, ihz, sz);
       }
-      const float lap = tx + tz;
-      outD[e] = f[e] * lap;
-      outd[e] = o[e] + outD[e];
-      outp[e] = c + outd[e];
+      const float lap = radd(tx, tz);
+      outD[e] = rmul(f[e], lap);
+      outd[e] = radd(o[e], outD[e]);
+      outp[e] = radd(c, outd[e]);
     }
     if (!inb) return;
     if (ckp) {
@@ -291,7 +303,7 @@ struct Ac2dRow {
     if (MODE == MODE_ADJW) {
 #pragma unroll
       for (int e = 0; e < 4; ++e)
-        if (x0 + e >= 1 && x0 + e <= nx - 2) g4[e] += outp[e] * dv[e];
+        if (x0 + e >= 1 && x0 + e <= nx - 2) g4[e] = __fmaf_rn(outp[e], dv[e], g4[e]);
       if (vec_interior) {
         st4(gg + row + x0, g4);
       } else {
@@ -452,24 +464,67 @@ __global__ void __launch_bounds__(32 * NW, (Ac2dBounds<MODE, NW>::MINB - (DP - 1
 
 
 // ---------------------------------------------------------------------------
-// 2D step with the rows staged through shared memory by cp.async.
+// 2D, two time steps per pass (temporal blocking) for the forward kinds and
+// the adjoint.
 //
-// The register-pipelined kernel holds one row of loads in flight per warp,
-// and a second register row costs more occupancy than it brings.  This
-// variant keeps S-1 rows in flight without registers; on GB300 it measured
-// slower all the same (64 shots of 2001 x 801: 3.75 / 4.23 / 4.71 TB/s
-// forward / recompute / adjoint against 4.15 / 4.56 / 4.79), so more loads
-// in flight are not what these kernels lack, and it stays a tuning variant
-// (512).  Every lane copies its own 16-byte pieces of the rows ahead
-// into a per-warp ring of S row bundles with cp.async (no registers held
-// while in flight) and later reads back only what it copied itself, so no
-// barrier is needed: cp.async.wait_group orders a lane's copies with its own
-// reads.  Bundle k holds p of row k+1 (with the x neighbours x0-1 of lane 0
-// and x0+4 of lane 31), d and fact of row k and, in the adjoint, D and the
-// sums g (gc) of row k; S-1 bundles are in flight while row z is computed.
-// Bundle z+S-1 reuses the slot of bundle z-1, whose values the row update of
-// iteration z-1 has already consumed.
+// The one-step kernels move 16 bytes per point and step (read p and d, write
+// them back); here one launch advances the state from step n to n+2 and moves
+// the same 16 bytes once.  A warp covers 128 x points (4 per lane) and
+// advances the first step on all of them, the second only on lanes 1..30
+// (120 points): the first step of lanes 0 and 31 supplies the x neighbours of
+// the second.  Along z the march runs the first step one row ahead of the
+// second (rows zb-1 .. ze of the first step for rows zb .. ze-1 of the second),
+// so a band's first and last rows come from the first step of its own halo.
+// Every point the first step touches is computed by the same arithmetic
+// wherever it is computed (neighbouring warps and bands repeat it), so the
+// copies agree bit for bit; the two steps round exactly as two launches of the
+// one-step kernel do (same rounded operations, see d2term / cpml_axis_term).
+//
+// State is double-buffered throughout (p, d, psi, xi read from one buffer,
+// written to the other): a neighbour's repeated first step reads d and xi of
+// points this warp owns.  The memory variables after the first step go to
+// scratch strips (psi_mid, xi_mid); the second step reads them back from the
+// same warp's earlier writes.  What lies between the two steps is done here:
+// the sources of the first step are injected (same summation order as
+// k_inject_record), and the pressure of receiver rows after the first step is
+// kept in a small per-shot stash that the recording kernel reads.  The host
+// pairs steps only where nothing else lies between them (no checkpoint state,
+// snapshot or change of the active shots), and only for shots whose sources
+// and receivers sit off the outermost grid lines.
+//
+// MODE_ADJW: two adjoint steps (it1 and it1 - 1) with the correlation of
+// both: the first step's adjoint sources at the receivers are injected here
+// (summed like k_adj_inject), and the per-shot FP32 sum g of a row is read
+// once, takes lambda * D of the first step (with its injected share) and of
+// the second, and is written once.  The injection of the second step is left
+// to k_adj_inject, as after a one-step launch.
 // ---------------------------------------------------------------------------
+constexpr int PAIR_MAXSP = 4;  // unique source points per shot
+constexpr int PAIR_MAXRR = 4;  // distinct receiver rows per shot
+constexpr int PAIR_OUT = 120;  // x points a warp advances by both steps
+
+struct PairShot {
+  const float* tf;   // (nt, nsrc) scaled source time functions
+  const float* adj;  // adjoint: (nt, nrec) prescaled adjoint sources
+  int nt, nsp, nrr, pad;
+  int sx[PAIR_MAXSP], sz[PAIR_MAXSP];  // unique source points (0-based)
+  int k0[PAIR_MAXSP], k1[PAIR_MAXSP];  // their source ids: ids[k0 .. k1)
+  int rrow[PAIR_MAXRR];                // receiver rows (0-based z), stash slot = index
+};
+
+struct PairArgs {
+  FieldArg psi_mid[2], xi_mid[2];  // memory variables after the first step (scratch)
+  FieldArg Dout2;                  // MODE_FWD_D: D of the second step (shots >= A.d_first)
+  FieldArg stash;                  // [shot][k][P]: p after the first step on receiver row k (p == nullptr: none)
+  FieldArg dcorr2;                 // MODE_ADJW: D the second step correlates with (A.dcorr: the first)
+  const PairShot* shots;
+  const int* ids;                  // source / receiver ids of the CSR ranges
+  const int* ptr;                  // MODE_ADJW: CSR ranges of the unique receiver points
+  const int* amap;                 // MODE_ADJW: [shot][k][P] CSR index of the receiver point at x on row k, or -1
+  int it1;                         // 1-based index of the first step (the adjoint counts down: it1, it1 - 1)
+};
+
+// cp.async helpers (per-lane 4/8/16-byte copies into shared memory)
 __device__ __forceinline__ void cpa16(void* smem, const void* g) {
   const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(s), "l"(g) : "memory");
@@ -491,6 +546,354 @@ __device__ __forceinline__ void sld4(float (&v)[4], const float4& s) {
   v[0] = s.x; v[1] = s.y; v[2] = s.z; v[3] = s.w;
 }
 
+// One row of four points advanced by one step (the arithmetic of
+// Ac2dRow::update).  Points that are not advanced (act false, boundary nodes,
+// padding) keep p and d; their D is 0.  mk(d) builds the C-PML strip
+// descriptor of axis d only where a strip is met.
+template <typename MK>
+__device__ __forceinline__ void pair_row(const float (&rm)[4], const float (&r0)[4], const float (&rp)[4],
+                                         float left, float right, const float (&o)[4], const float (&f)[4], int x0,
+                                         int z, bool act, bool xstrip, const StepArgs& A, MK&& mk, float (&outp)[4],
+                                         float (&outd)[4], float (&outD)[4]) {
+  const int nx = A.n0, nz = A.n1, H = A.halo;
+  const bool zin = z >= 1 && z <= nz - 2;
+  const bool zstrip = z < H || z >= nz - H;
+#pragma unroll
+  for (int e = 0; e < 4; ++e) {
+    const float xm = e == 0 ? left : r0[e - 1];
+    const float xp = e == 3 ? right : r0[e + 1];
+    const float c = r0[e];
+    const int x = x0 + e;
+    const bool pin = act && zin && x >= 1 && x <= nx - 2;
+    float tx = d2term(xm, c, xp, A.ih2[0]);
+    float tz = d2term(rm[e], c, rp[e], A.ih2[1]);
+    if (xstrip && pin) {
+      StripIO s = mk(0);
+      s.psi_base = (long long)z * (2 * H);
+      s.xi_base = (long long)z * (2 * H + 2);
+      tx = cpml_axis_term(tx, xm, c, xp, x, nx, H, A.ih[0], s);
+    }
+    if (zstrip && pin) {
+      StripIO s = mk(1);
+      s.psi_base = x;
+      s.xi_base = x;
+      tz = cpml_axis_term(tz, rm[e], c, rp[e], z, nz, H, A.ih[1], s);
+    }
+    const float lap = radd(tx, tz);
+    const float D = rmul(f[e], lap);
+    const float dd = radd(o[e], D);
+    outD[e] = pin ? D : 0.f;
+    outd[e] = pin ? dd : o[e];
+    outp[e] = pin ? radd(c, dd) : c;
+  }
+}
+
+// Stores four points of a row, interior x only (boundary nodes are never written).
+__device__ __forceinline__ void pair_store(float* dst, long long row, int x0, int nx, bool vec, const float (&v)[4]) {
+  if (vec) {
+    st4(dst + row + x0, v);
+  } else {
+#pragma unroll
+    for (int e = 0; e < 4; ++e)
+      if (x0 + e >= 1 && x0 + e <= nx - 2) dst[row + x0 + e] = v[e];
+  }
+}
+__device__ __forceinline__ void pair_dstore(float* dst, long long row, int x0, int nx, bool vec, const float (&v)[4],
+                                            int bf) {
+  if (vec) {
+    dst4(dst, row + x0, v, bf);
+  } else {
+#pragma unroll
+    for (int e = 0; e < 4; ++e)
+      if (x0 + e >= 1 && x0 + e <= nx - 2) dst1(dst, row + x0 + e, v[e], bf);
+  }
+}
+
+// Rows reach the warp through a per-warp shared-memory ring filled by
+// cp.async: every lane copies its own 16-byte pieces of the rows PairRing::S-1
+// iterations ahead (no registers held while they are in flight) and reads
+// back only what it copied, so no barrier is needed; lanes 0 and 31 also copy
+// the x neighbour beyond the warp.  Bundle j (iteration y = zb-1+j) holds p of
+// row y+1, d and fact of row y and, in the adjoint, D of the first step and
+// the sum g of row y and D of the second step of row y-1.
+template <int MODE>
+struct PairRing {
+  static constexpr int NA = MODE == MODE_ADJW ? 6 : 3;  // arrays per bundle
+  static constexpr int S = MODE == MODE_ADJW ? 3 : 4;   // bundles in the ring
+};
+
+// MB: resident blocks per SM the registers are bounded for (forward kinds:
+// 6 blocks at <= 80 registers without spills; adjoint: 5 at <= 96).
+template <int MODE, int NW, int MB>
+__global__ void __launch_bounds__(32 * NW, MB) k_ac2d_pair(const StepArgs A, const PairArgs B) {
+  constexpr bool ADJ = MODE == MODE_ADJW;
+  constexpr unsigned FULL = 0xffffffffu;
+  constexpr int NA = PairRing<MODE>::NA, SR = PairRing<MODE>::S;
+  __shared__ float4 ring[NW][SR][NA][32];
+  __shared__ float hal[NW][SR][2];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int S = A.nshots;
+  // block order as k_ac2d_step: x tiles fastest, then shots, then row bands
+  const int txi = blockIdx.x % A.tiles_x;
+  const int rest = blockIdx.x / A.tiles_x;
+  const int shot = rest % S, tzi = rest / S;
+  const int nx = A.n0, nz = A.n1, P = A.P, H = A.halo;
+  const int zb = 1 + tzi * A.TZ;
+  const int ze = min(zb + A.TZ, nz - 1);
+  const int ox0 = (txi * NW + warp) * PAIR_OUT;  // first x point this warp advances by both steps
+  if (zb >= ze || ox0 > nx - 2) return;          // warp-uniform
+  const int x0 = ox0 - 4 + 4 * lane;
+  const bool inb = x0 >= 0 && x0 < P;
+  const int xa = min(max(x0, 0), P - 4);
+  const bool own = inb && lane >= 1 && lane <= 30;
+  const bool vec = x0 >= 1 && x0 + 3 <= nx - 2;
+  const bool xstrip = inb && (x0 < H || x0 + 3 >= nx - H);
+
+  const float* __restrict__ pc = fptr(A.pcur, shot);
+  const float* __restrict__ di = fptr(A.din, shot);
+  const float* __restrict__ fa = A.fact;
+  float* pn = fptr(A.pnew, shot);
+  float* dn = fptr(A.dout, shot);
+  float* ckp = fptr(A.ck_p, shot);
+  float* ckd = fptr(A.ck_d, shot);
+  const bool dw = MODE == MODE_FWD_D && shot >= A.d_first;
+  float* Dw1 = dw ? dptr(A.Dout, shot, A.dbf16) : nullptr;
+  float* Dw2 = dw ? dptr(B.Dout2, shot, A.dbf16) : nullptr;
+  float* stash = B.stash.p ? B.stash.p + (long long)shot * B.stash.s : nullptr;
+  const PairShot* T = B.shots + shot;
+  const int nsp = ADJ ? 0 : T->nsp, nrr = (stash || ADJ) ? T->nrr : 0;
+  const float* dc1 = ADJ ? dptr(A.dcorr, shot, A.dbf16) : nullptr;
+  const float* dc2 = ADJ ? dptr(B.dcorr2, shot, A.dbf16) : nullptr;
+  float* gg = ADJ ? fptr(A.g, shot) : nullptr;
+  const int* am = ADJ ? B.amap + (long long)shot * PAIR_MAXRR * P : nullptr;
+
+  const int na = 2 * H + 2, nh = 2 * H, L = 2 * na + 2 * nh;
+  const float* cpb = A.cpml + (long long)shot * A.cpml_stride;
+  // first step: psi, xi of step n -> scratch, with the checkpoint copies of step n
+  auto mk1 = [&](int d) {
+    StripIO s;
+    const float* c = cpb + d * L;
+    s.a = c; s.ah = c + na; s.b = c + na + nh; s.bh = c + 2 * na + nh;
+    s.psi_in = fptr(A.psi_in[d], shot); s.psi_out = fptr(B.psi_mid[d], shot); s.ck_psi = fptr(A.ck_psi[d], shot);
+    s.xi_in = fptr(A.xi_in[d], shot);   s.xi_out = fptr(B.xi_mid[d], shot);   s.ck_xi = fptr(A.ck_xi[d], shot);
+    s.psi_step = d == 0 ? 1 : P;
+    s.xi_step = s.psi_step;
+    return s;
+  };
+  // second step: scratch -> psi, xi of step n+2
+  auto mk2 = [&](int d) {
+    StripIO s;
+    const float* c = cpb + d * L;
+    s.a = c; s.ah = c + na; s.b = c + na + nh; s.bh = c + 2 * na + nh;
+    s.psi_in = fptr(B.psi_mid[d], shot); s.psi_out = fptr(A.psi_out[d], shot); s.ck_psi = nullptr;
+    s.xi_in = fptr(B.xi_mid[d], shot);   s.xi_out = fptr(A.xi_out[d], shot);   s.ck_xi = nullptr;
+    s.psi_step = d == 0 ? 1 : P;
+    s.xi_step = s.psi_step;
+    return s;
+  };
+
+  auto issue = [&](int j) {  // bundle j into slot j % SR; an empty group past the band
+    const int yj = zb - 1 + j;
+    if (yj <= ze) {
+      const int sl = j % SR;
+      const long long rj = (long long)yj * P;
+      const bool nxt = yj + 1 <= nz - 1;
+      if (inb) {
+        if (nxt) cpa16(&ring[warp][sl][0][lane], pc + rj + P + x0);
+        cpa16(&ring[warp][sl][1][lane], di + rj + x0);
+        cpa16(&ring[warp][sl][2][lane], fa + rj + x0);
+      }
+      if constexpr (ADJ) {
+        if (own && yj >= zb && yj < ze) {
+          if (A.dbf16)
+            cpa8(&ring[warp][sl][3][lane], reinterpret_cast<const __nv_bfloat16*>(dc1) + rj + x0);
+          else
+            cpa16(&ring[warp][sl][3][lane], dc1 + rj + x0);
+          cpa16(&ring[warp][sl][4][lane], gg + rj + x0);
+        }
+        if (own && yj >= zb + 1) {
+          if (A.dbf16)
+            cpa8(&ring[warp][sl][5][lane], reinterpret_cast<const __nv_bfloat16*>(dc2) + rj - P + x0);
+          else
+            cpa16(&ring[warp][sl][5][lane], dc2 + rj - P + x0);
+        }
+      }
+      if (nxt && lane == 0 && x0 >= 1) cpa4(&hal[warp][sl][0], pc + rj + P + x0 - 1);
+      if (nxt && lane == 31 && x0 + 4 < P) cpa4(&hal[warp][sl][1], pc + rj + P + x0 + 4);
+    }
+    cpa_commit();
+  };
+  auto bundle_d = [&](float (&v)[4], const float4& slot) {  // D slot of a bundle, FP32 or BF16
+    if (A.dbf16) {
+      const uint2 u = *reinterpret_cast<const uint2*>(&slot);
+      const float2 lo = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&u.x));
+      const float2 hi = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&u.y));
+      v[0] = lo.x; v[1] = lo.y; v[2] = hi.x; v[3] = hi.y;
+    } else {
+      sld4(v, slot);
+    }
+  };
+
+  // p of step n at rows y-1, y, y+1 (rm, r0, rp) with the x neighbours of row
+  // y beyond the warp (hl, hr), d and fact of row y; p of step n+1 at rows
+  // y-2, y-1 (qm, q0), d of step n+1 and fact of row y-1
+  float rm[4] = {0.f, 0.f, 0.f, 0.f}, r0[4], rp[4], o[4], f[4];
+  float qm[4] = {0.f, 0.f, 0.f, 0.f}, q0[4] = {0.f, 0.f, 0.f, 0.f}, dq[4] = {0.f, 0.f, 0.f, 0.f},
+        fq[4] = {0.f, 0.f, 0.f, 0.f};
+  float g1[4] = {0.f, 0.f, 0.f, 0.f};  // adjoint: the sum g of row y-1 after its first step's correlation
+  int y = zb - 1;
+  if (y >= 1) ld4(rm, pc + (long long)(y - 1) * P + xa);
+  ld4(r0, pc + (long long)y * P + xa);
+  float hl = (lane == 0 && x0 >= 1) ? pc[(long long)y * P + x0 - 1] : 0.f;
+  float hr = (lane == 31 && x0 + 4 < P) ? pc[(long long)y * P + x0 + 4] : 0.f;
+#pragma unroll
+  for (int q = 0; q < SR - 1; ++q) issue(q);
+  for (int j = 0; y <= ze; ++y, ++j) {
+    const long long row = (long long)y * P;
+    cpa_wait<SR - 2>();  // bundle j has landed (bundles j+1 .. j+SR-2 may be in flight)
+    __syncwarp();        // and the scratch strips written by the lanes' first step of the previous row
+    const int sl = j % SR;
+    sld4(rp, ring[warp][sl][0][lane]);
+    sld4(o, ring[warp][sl][1][lane]);
+    sld4(f, ring[warp][sl][2][lane]);
+    const float nhl = hal[warp][sl][0], nhr = hal[warp][sl][1];
+    // adjoint: D of both steps and the sum g, for the rows they are used on;
+    // gn: the sum of row y after the first step (g1 holds row y-1's)
+    const bool orow = y >= zb && y < ze;
+    float dv1[4] = {0.f, 0.f, 0.f, 0.f}, dv2[4] = {0.f, 0.f, 0.f, 0.f}, gv[4] = {0.f, 0.f, 0.f, 0.f};
+    float gn[4] = {0.f, 0.f, 0.f, 0.f};
+    if constexpr (ADJ) {
+      if (own && orow) {
+        bundle_d(dv1, ring[warp][sl][3][lane]);
+        sld4(gv, ring[warp][sl][4][lane]);
+      }
+      if (own && y >= zb + 1) bundle_d(dv2, ring[warp][sl][5][lane]);
+    }
+    // first step, row y
+    float left = __shfl_up_sync(FULL, r0[3], 1);
+    float right = __shfl_down_sync(FULL, r0[0], 1);
+    if (lane == 0) left = hl;
+    if (lane == 31) right = hr;
+    float p1[4], d1[4], D1[4];
+    pair_row(rm, r0, rp, left, right, o, f, x0, y, inb, xstrip, A, mk1, p1, d1, D1);
+    if constexpr (ADJ) {
+      // correlation of the first step on the band's rows (before its
+      // injection, as the one-step kernel), then the first step's adjoint
+      // sources at the receivers with their share lambda_add * D
+      const bool cor = own && orow;
+      if (cor) {
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+          gn[e] = gv[e];
+          if (x0 + e >= 1 && x0 + e <= nx - 2) gn[e] = __fmaf_rn(p1[e], dv1[e], gn[e]);
+        }
+      }
+      for (int k = 0; k < nrr; ++k) {
+        if (T->rrow[k] != y || !inb) continue;
+        const int4 m = *reinterpret_cast<const int4*>(am + (long long)k * P + x0);
+        const int mm[4] = {m.x, m.y, m.z, m.w};
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+          if (mm[e] < 0) continue;
+          float acc = p1[e], add = 0.f;
+          for (int jj = B.ptr[mm[e]]; jj < B.ptr[mm[e] + 1]; ++jj) {
+            const float v = T->adj[(long long)(B.it1 - 1) + (long long)B.ids[jj] * T->nt];
+            acc = radd(acc, v);
+            add = radd(add, v);
+          }
+          p1[e] = acc;
+          d1[e] = radd(d1[e], add);
+          if (cor) gn[e] = __fmaf_rn(add, dv1[e], gn[e]);
+        }
+      }
+    }
+    for (int s = 0; s < nsp; ++s) {  // sources of the first step
+      if (T->sz[s] != y) continue;
+      const int dx = T->sx[s] - x0;
+      if (dx < 0 || dx > 3 || !inb) continue;
+      const int k0 = T->k0[s], k1 = T->k1[s];
+#pragma unroll
+      for (int e = 0; e < 4; ++e)
+        if (e == dx) {
+          float acc = p1[e], add = 0.f;
+          for (int k = k0; k < k1; ++k) {
+            const float v = T->tf[(long long)(B.it1 - 1) + (long long)B.ids[k] * T->nt];
+            acc = radd(acc, v);
+            add = radd(add, v);
+          }
+          p1[e] = acc;
+          d1[e] = radd(d1[e], add);
+          // k_inject_record adds to the stored D: with BF16 slots the stencil's
+          // D is rounded to BF16 before the source is added
+          const float Ds = A.dbf16 ? __bfloat162float(__float2bfloat16_rn(D1[e])) : D1[e];
+          D1[e] = radd(Ds, add);
+        }
+    }
+    if (own && orow) {  // outputs of the first step on the band's own rows
+      if (ckp) {
+        st4(ckp + row + x0, r0);
+        st4(ckd + row + x0, o);
+      }
+      if (Dw1) pair_dstore(Dw1, row, x0, nx, vec, D1, A.dbf16);
+      if (stash)
+        for (int k = 0; k < nrr; ++k)
+          if (T->rrow[k] == y) st4(stash + (long long)k * P + x0, p1);
+    }
+    // second step, row y-1
+    if (y >= zb + 1) {
+      const long long zrow = row - P;
+      const float l2 = __shfl_up_sync(FULL, q0[3], 1);
+      const float r2 = __shfl_down_sync(FULL, q0[0], 1);
+      float p2[4], d2[4], D2[4];
+      pair_row(qm, q0, p1, l2, r2, dq, fq, x0, y - 1, own, xstrip, A, mk2, p2, d2, D2);
+      if (own) {
+        pair_store(pn, zrow, x0, nx, vec, p2);
+        pair_store(dn, zrow, x0, nx, vec, d2);
+        if (Dw2) pair_dstore(Dw2, zrow, x0, nx, vec, D2, A.dbf16);
+        if constexpr (ADJ) {  // correlation of the second step, then the row's sum goes back once
+#pragma unroll
+          for (int e = 0; e < 4; ++e)
+            if (x0 + e >= 1 && x0 + e <= nx - 2) g1[e] = __fmaf_rn(p2[e], dv2[e], g1[e]);
+          pair_store(gg, zrow, x0, nx, vec, g1);
+        }
+      }
+    }
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+      if constexpr (ADJ) g1[e] = gn[e];
+      qm[e] = q0[e];
+      q0[e] = p1[e];
+      dq[e] = d1[e];
+      fq[e] = f[e];
+      rm[e] = r0[e];
+      r0[e] = rp[e];
+    }
+    hl = nhl;
+    hr = nhr;
+    issue(j + SR - 1);  // into the slot of bundle j-1, consumed in the previous iteration
+  }
+  cpa_wait<0>();
+}
+
+// ---------------------------------------------------------------------------
+// 2D step with the rows staged through shared memory by cp.async.
+//
+// The register-pipelined kernel holds one row of loads in flight per warp,
+// and a second register row costs more occupancy than it brings.  This
+// variant keeps S-1 rows in flight without registers; on GB300 it measured
+// slower all the same (64 shots of 2001 x 801: 3.75 / 4.23 / 4.71 TB/s
+// forward / recompute / adjoint against 4.15 / 4.56 / 4.79), so more loads
+// in flight are not what these kernels lack, and it stays a tuning variant
+// (512).  Every lane copies its own 16-byte pieces of the rows ahead
+// into a per-warp ring of S row bundles with cp.async (no registers held
+// while in flight) and later reads back only what it copied itself, so no
+// barrier is needed: cp.async.wait_group orders a lane's copies with its own
+// reads.  Bundle k holds p of row k+1 (with the x neighbours x0-1 of lane 0
+// and x0+4 of lane 31), d and fact of row k and, in the adjoint, D and the
+// sums g (gc) of row k; S-1 bundles are in flight while row z is computed.
+// Bundle z+S-1 reuses the slot of bundle z-1, whose values the row update of
+// iteration z-1 has already consumed.
+// ---------------------------------------------------------------------------
 // Row arrays per bundle (p, d, fact [, D, g [, gc]]) and bundles in the ring:
 // 24 KB of ring per 4-warp block for the forward kinds (8 blocks per SM),
 // 30 / 36 KB for the adjoints (6 / 4 blocks per SM).
