@@ -131,8 +131,8 @@ class ScalarShot:
 class L2Misfit:
     """src/inversion/misfits/L2Misfit.jl:2-20.
 
-    ``invcov`` may be None (identity), a vector (its diagonal) or a square
-    matrix (applied on the GPU by a cuBLAS product when it has off-diagonal
+    matrix (applied on the GPU by the library's own tiled FP32 product when it has
+    off-diagonal terms).
     terms).
     """
 

@@ -17,7 +17,7 @@ INCLUDE = HERE.parent / "include"
 BUILD = HERE / "_build"
 LIB = HERE / "libswgb300.so"
 
-SOURCES = ["api.cu", "acoustic.cu", "elastic.cu", "vd.cu", "cpml.cpp", "noalloc.cu"]
+SOURCES = ["api.cu", "acoustic.cu", "elastic.cu", "vd.cu", "cpml.cpp", "noalloc.cu", "dense.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -47,7 +47,7 @@ def build(force: bool = False, verbose: bool = False) -> Path:
     with cf.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
         objs = list(ex.map(lambda s: _compile(s, verbose), SOURCES))
     tmp = LIB.with_suffix(f".{os.getpid()}.tmp")
-    subprocess.run([_nvcc(), *ARCH, "-shared", "-o", str(tmp), *map(str, objs), "-lcublas", "-lcudart"], check=True)
+    subprocess.run([_nvcc(), *ARCH, "-shared", "-o", str(tmp), *map(str, objs), "-lcudart"], check=True)
     os.replace(tmp, LIB)
     return LIB
 

@@ -64,7 +64,7 @@ struct ShotDesc {
   float* ring;               // 3 values per boundary injection point (see k_inject_record)
   const float* icd;          // dense inverse covariance (nt, nt) or nullptr
   float* resid;              // dense case: masked residuals (nt, nrec)
-  const float* cres;         // dense case: C^-1 r (nt, nrec), from cuBLAS
+  const float* cres;         // dense case: C^-1 r (nt, nrec), from the dense product (dense.cu)
   int mkind;                 // 0 L2, 1 CCTS (k_ccts writes this shot's adjoint source)
 };
 
@@ -234,7 +234,7 @@ __global__ void k_reduce_grad_tot(const double* __restrict__ tot, const float* _
 }
 
 // Masked residuals of the shots with a dense inverse covariance (the input of
-// the cuBLAS product C^-1 r).  gridDim = (blocks per shot, shots).
+// the dense product C^-1 r).  gridDim = (blocks per shot, shots).
 __global__ void k_residual_dense(const ShotDesc* __restrict__ desc) {
   const ShotDesc& D = desc[blockIdx.y];
   if (!D.icd) return;
@@ -1871,7 +1871,7 @@ void acoustic_gradient(sw_wavesim* ws, int nshots, const sw_acoustic_shot* shots
     }
     auto misfit_and_adjsrc = [&] {
       cudaEvent_t ev = nullptr;
-      if (any_dense) {  // C^-1 r of the shots with a dense inverse covariance (cuBLAS)
+      if (any_dense) {  // C^-1 r of the shots with a dense inverse covariance (dense.cu)
         k_residual_dense<<<dim3(nblk, S), 256, 0, st>>>(ws->d_desc.as<ShotDesc>());
         check_cuda(cudaGetLastError(), "residual launch");
         for (int k = 0; k < S; ++k)
@@ -1915,10 +1915,13 @@ void acoustic_gradient(sw_wavesim* ws, int nshots, const sw_acoustic_shot* shots
       check_cuda(cudaGetLastError(), "gradient reduction launch");
       ws->ctx->prof.end(st, KK_OTHER, ev);
     };
-    if (!mute && !any_dense) {
-      // the whole group -- forward, misfit, adjoint, shot sum -- as one graph
+    if (!mute) {
+      // the whole group -- forward, misfit (with the dense C^-1 products),
+      // adjoint, shot sum -- as one graph
       std::vector<long long> key = group_key(ws, group, true);
       for (const auto& h : group) key.push_back(shots[h.orig].misfit_kind);
+      for (int k = 0; k < S; ++k)  // the dense products' operands are launch arguments
+        if (T.desc[k].icd) key.insert(key.end(), {k, T.desc[k].nrec, (long long)(uintptr_t)T.desc[k].icd});
       key.insert(key.end(), {accumulate ? 1 : 0, (long long)(uintptr_t)gout, (long long)(uintptr_t)mout});
       run_graph(ws, key, [&] {
         forward_group(ws, group, true);

@@ -7,7 +7,6 @@
 #include <new>
 #include <string>
 
-#include <cublas_v2.h>
 
 #include "internal.h"
 
@@ -50,21 +49,6 @@ sw_acoustic_vd* vd_new();
 void vd_delete(sw_acoustic_vd* vd);
 
 [[noreturn]] void fail(int code, const std::string& msg) { throw SwError{code, msg}; }
-
-void dense_invcov(sw_ctx* ctx, int nt, int ncols, const float* C, const float* R, float* CR) {
-  if (!ctx->cublas) {
-    cublasHandle_t h = nullptr;
-    if (cublasCreate(&h) != CUBLAS_STATUS_SUCCESS) fail(SW_ERR_CUDA, "cublasCreate failed");
-    ctx->cublas = h;
-    cublasSetMathMode(h, CUBLAS_DEFAULT_MATH);  // FP32 arithmetic, no TF32
-  }
-  cublasHandle_t h = static_cast<cublasHandle_t>(ctx->cublas);
-  if (cublasSetStream(h, ctx->stream) != CUBLAS_STATUS_SUCCESS) fail(SW_ERR_CUDA, "cublasSetStream failed");
-  const float one = 1.0f, zero = 0.0f;
-  if (cublasSgemm(h, CUBLAS_OP_N, CUBLAS_OP_N, nt, ncols, nt, &one, C, nt, R, nt, &zero, CR, nt) !=
-      CUBLAS_STATUS_SUCCESS)
-    fail(SW_ERR_CUDA, "cublasSgemm (dense inverse covariance) failed");
-}
 
 void check_cuda(cudaError_t e, const char* what) {
   if (e == cudaSuccess) return;
@@ -208,7 +192,6 @@ int sw_ctx_destroy(sw_ctx* ctx) {
   if (!ctx) return SW_ERR_ARG;
   cudaSetDevice(ctx->device);
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
-  if (ctx->cublas) cublasDestroy(static_cast<cublasHandle_t>(ctx->cublas));
   if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
   return SW_OK;

@@ -676,7 +676,7 @@ struct ShotDesc {
   float* adjsrc;             // adjoint source (nt, 2, nrec)
   const float* icd;          // dense inverse covariance (nt, nt) or null
   float* resid;              // dense case: masked residuals (nt, 2 nrec)
-  const float* cres;         // dense case: C^-1 r (nt, 2 nrec), from cuBLAS
+  const float* cres;         // dense case: C^-1 r (nt, 2 nrec), from the dense product (dense.cu)
 };
 
 // sigma_xx += Mxx w tf, sigma_zz += Mzz w tf (table 0), sigma_xz += Mxz w tf (table 1)
@@ -713,10 +713,12 @@ __global__ void k_el_inject_sigma(const ShotDesc* __restrict__ desc, int it, lon
 }
 
 // u += w tf / rho dt^2 on the ux (table 0) and uz (table 1) grids; adjoint = 1
-// uses the receivers' tables and the adjoint source scaled by adj_scale (the
-// forward sources use the shot's own scale).  With D slots, D(it) gets the
+// uses the receivers' tables and the adjoint source scaled by *adj_scale (a
+// device value, set by k_el_adj_scale; the forward sources use the shot's
+// own scale).  With D slots, D(it) gets the
 // same increment (it is part of the second time difference).
-__global__ void k_el_inject_force(const ShotDesc* __restrict__ desc, int it, int adjoint, float adj_scale, long long F,
+__global__ void k_el_inject_force(const ShotDesc* __restrict__ desc, int it, int adjoint,
+                                  const float* __restrict__ adj_scale, long long F,
                                   float* ux, float* uz, float* dux, float* duz, float* Dx, float* Dz,
                                   const float* __restrict__ dtr_i, const float* __restrict__ dtr_j) {
   const int s = blockIdx.y;
@@ -725,7 +727,7 @@ __global__ void k_el_inject_force(const ShotDesc* __restrict__ desc, int it, int
   if (!adjoint && D.kind != 1) return;
   const long long so = (long long)s * F;
   const float* tf = adjoint ? D.adjsrc : D.tf;
-  const float scale = adjoint ? adj_scale : D.sf;
+  const float scale = adjoint ? *adj_scale : D.sf;
   for (int t = 0; t < 2; ++t) {
     const Inj J = adjoint ? D.adj[t] : D.src[t];
     float* u = t == 0 ? ux : uz;
@@ -762,6 +764,20 @@ __global__ void k_el_record(const ShotDesc* __restrict__ desc, int it, long long
     for (int e = D.rptr[t][r]; e < D.rptr[t][r + 1]; ++e) acc += D.rcoef[t][e] * u[D.rlin[t][e]];
     D.tr[(long long)(it - 1) + (long long)D.nt * (t + 2LL * r)] = acc * inv_scale;
   }
+}
+
+// The power of two 2^e with 2^e * max|C^-1 r| close to 2^20 (1 for a zero or
+// non-finite maximum), the adjoint source's scale, written to scales[1] on
+// the device, so that no host round trip sits between the misfit and the
+// adjoint (the gradient's time loop can run as one CUDA graph).
+__global__ void k_el_adj_scale(const unsigned int* __restrict__ amax, float* __restrict__ scales) {
+  const float v = __uint_as_float(*amax);
+  float sc = 1.0f;
+  if (v > 0.0f && isfinite(v)) {
+    const int e = 20 - (int)lround(log2((double)v));
+    sc = ldexpf(1.0f, max(-100, min(100, e)));
+  }
+  scales[1] = sc;
 }
 
 // Residuals, windows, C^-1 r, misfit partials (FP64), adjoint source -C^-1 r
@@ -1097,13 +1113,16 @@ __device__ __forceinline__ double acc_val(const float* acc, int q, long long F, 
 // Final gradients (FP64, (nx, nz) column-major), summed over the groups:
 // lambda; mu + back_interp(mu_ihalf_jhalf); back_interp(rho_ihalf) +
 // back_interp(rho_jhalf) (times 1/dt^2); each group's sum muted around its
-// shot's positions; times inv_scale.
+// shot's positions; times 1 / (scales[0] scales[1]) (the forward and adjoint
+// source scales).
 __global__ void k_el_reduce(Geo g, int ngroups, const float* __restrict__ acc, const double* __restrict__ rho,
-                            const double* __restrict__ mu, int irho, int imu, double inv_dt2, double inv_scale,
+                            const double* __restrict__ mu, int irho, int imu, double inv_dt2,
+                            const float* __restrict__ scales,
                             const MuteBall* __restrict__ balls, const int* __restrict__ ball_ptr,
                             double* __restrict__ grho, double* __restrict__ glam, double* __restrict__ gmu,
                             int accumulate) {
   const long long npts = (long long)g.nx * g.nz;
+  const double inv_scale = 1.0 / ((double)scales[0] * (double)scales[1]);
   for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < npts;
        q += (long long)gridDim.x * blockDim.x) {
     const int i = (int)(q % g.nx) + 1, j = (int)(q / g.nx) + 1;
@@ -1218,6 +1237,19 @@ struct sw_elastic {
   float* const* snap_out = nullptr;  // per caller shot: nt/snapevery blocks [ux, uz, sxx, szz, sxz]
   int tz = 8;  // rows per block of the stencil kernels (8, 16 or 32; 8 measured fastest)
   bool vec = true;  // four x points per thread (k_el_*4) instead of one
+  DevMem d_scales;        // [0] the forward sources' common scale, [1] the adjoint source's scale
+  DevMem d_gout, d_mout;  // gradient / misfit of the host-buffer path (stable addresses for the graphs)
+  // CUDA graphs of a group's whole gradient (forward, misfit, adjoint,
+  // reduction), keyed by what the captured launches depend on
+  long long gen = 0;  // bumped whenever a device buffer the kernels see is (re)allocated
+  std::map<std::vector<long long>, cudaGraphExec_t> graphs;
+  std::map<std::vector<long long>, int> graph_uses;
+  void drop_graphs() {
+    for (auto& kv : graphs) cudaGraphExecDestroy(kv.second);
+    graphs.clear();
+    graph_uses.clear();
+  }
+  ~sw_elastic() { drop_graphs(); }
 };
 
 namespace {
@@ -1227,6 +1259,50 @@ inline long long round_up(long long v, long long m) { return (v + m - 1) / m * m
 void ensure(sw_elastic* es, DevMem& m, size_t bytes, const char* what) {
   if (m.bytes >= bytes && m.p) return;
   dev_alloc(m, bytes, what, es->ctx->stream);
+  ++es->gen;
+}
+
+// Runs `work` (the device work of one group's gradient: launches, memsets and
+// device copies, no host synchronisation, no allocation) through a CUDA
+// graph: captured on the second call with `key`, replayed afterwards (at most
+// 32 graphs per simulation); directly while profiling or when the caller's
+// stream is itself being captured (the launches then join the caller's graph).
+template <typename Work>
+void el_run_graph(sw_elastic* es, std::vector<long long> key, Work&& work) {
+  cudaStream_t st = es->ctx->stream;
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  check_cuda(cudaStreamIsCapturing(st, &cs), "cudaStreamIsCapturing");
+  if (es->ctx->prof.on || cs != cudaStreamCaptureStatusNone) {
+    work();
+    return;
+  }
+  key.push_back(es->gen);
+  auto it = es->graphs.find(key);
+  if (it == es->graphs.end()) {
+    if (es->graph_uses.size() > 4096) es->graph_uses.clear();
+    if (++es->graph_uses[key] < 2 || es->graphs.size() >= 32) {
+      work();
+      return;
+    }
+    check_cuda(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal), "begin stream capture");
+    try {
+      work();
+    } catch (...) {
+      cudaGraph_t g = nullptr;
+      cudaStreamEndCapture(st, &g);
+      if (g) cudaGraphDestroy(g);
+      cudaGetLastError();
+      throw;
+    }
+    cudaGraph_t g = nullptr;
+    check_cuda(cudaStreamEndCapture(st, &g), "end stream capture");
+    cudaGraphExec_t ex = nullptr;
+    const cudaError_t e = cudaGraphInstantiate(&ex, g, 0);
+    cudaGraphDestroy(g);
+    check_cuda(e, "graph instantiate");
+    it = es->graphs.emplace(key, ex).first;
+  }
+  check_cuda(cudaGraphLaunch(it->second, st), "graph launch");
 }
 
 template <typename T>
@@ -1344,18 +1420,19 @@ void ensure_state(sw_elastic* es, int S, bool grad, int max_nt, int ngroups) {
     es->cap = S;
     es->cap_slots = 0;
     es->cap_ck = 0;
+    ++es->gen;
   }
   if (grad) {
     const int K = es->gp.check_freq;
     const int M = (max_nt + K - 1) / K;
     const size_t slot_b = (size_t)K * 4 * es->cap * F * sizeof(float);
-    if (es->slots.bytes < slot_b) dev_alloc(es->slots, slot_b, "gradient slots", es->ctx->stream);
+    if (es->slots.bytes < slot_b) { dev_alloc(es->slots, slot_b, "gradient slots", es->ctx->stream); ++es->gen; }
     // per checkpoint: u, du (4 fields) and the 8 memory-variable strips of every shot
     const size_t ck_b = (size_t)std::max(M - 1, 1) * (4 * (size_t)es->cap * F + 4 * (size_t)es->cap * (es->xs + es->zs)) *
                         sizeof(float);
-    if (es->ck.bytes < ck_b) dev_alloc(es->ck, ck_b, "checkpoints", es->ctx->stream);
+    if (es->ck.bytes < ck_b) { dev_alloc(es->ck, ck_b, "checkpoints", es->ctx->stream); ++es->gen; }
     const size_t acc_b = (size_t)ngroups * 10 * F * sizeof(float);
-    if (es->acc.bytes < acc_b) dev_alloc(es->acc, acc_b, "gradient accumulators", es->ctx->stream);
+    if (es->acc.bytes < acc_b) { dev_alloc(es->acc, acc_b, "gradient accumulators", es->ctx->stream); ++es->gen; }
   }
 }
 
@@ -1666,12 +1743,13 @@ struct Run {
     check_cuda(cudaGetLastError(), "stress injection launch");
     es->ctx->prof.end(st, KK_SRCREC, ev);
   }
-  void inject_force(int S, int it, bool adjoint, float scale, float* sD[2]) {
+  void inject_force(int S, int it, bool adjoint, const float* adj_scale, float* sD[2]) {
     if (S <= 0) return;
     DevMem* f = adjoint ? es->ast : es->st;
     cudaEvent_t ev = nullptr;
     es->ctx->prof.begin(st, KK_SRCREC, 0.0, &ev);
-    k_el_inject_force<<<dim3(adjoint ? gx_adj : gx_src, S), 128, 0, st>>>(ddesc, it, adjoint ? 1 : 0, scale, es->g.F,
+    k_el_inject_force<<<dim3(adjoint ? gx_adj : gx_src, S), 128, 0, st>>>(ddesc, it, adjoint ? 1 : 0, adj_scale,
+                                                                         es->g.F,
                                                                          f[0].as<float>(),
                                                   f[1].as<float>(), f[2].as<float>(), f[3].as<float>(),
                                                   sD ? sD[0] : nullptr, sD ? sD[1] : nullptr, es->dtr_i.as<float>(),
@@ -1734,11 +1812,11 @@ void full_step(Run& R, int S, int it, bool record, int kind, float* sU[2], float
   es->ctx->prof.begin(R.st, kind, R.step_bytes(S, sU != nullptr), &ev);
   launch_stencil(es, R.st, a, S, false);
   es->ctx->prof.end(R.st, kind, ev);
-  if (R.any_force) R.inject_force(S, it, false, 1.0f, sD);
+  if (R.any_force) R.inject_force(S, it, false, nullptr, sD);
   if (record) R.record(S, it);
 }
 
-void adjoint_step(Run& R, int S, int it, float sa) {
+void adjoint_step(Run& R, int S, int it) {
   if (S <= 0) return;
   sw_elastic* es = R.es;
   Args a = R.args(true);
@@ -1747,7 +1825,7 @@ void adjoint_step(Run& R, int S, int it, float sa) {
   launch_stencil(es, R.st, a, S, true);
   launch_stencil(es, R.st, a, S, false);
   es->ctx->prof.end(R.st, KK_ADJOINT, ev);
-  R.inject_force(S, it, true, sa, nullptr);
+  R.inject_force(S, it, true, es->d_scales.as<float>() + 1, nullptr);
 }
 
 // savesnapshot!("ucur" => ..., "σ" => ...) of ela_forward.jl:74-78 for the active shots:
@@ -2011,16 +2089,15 @@ void elastic_gradient(sw_elastic* es, int nshots, const sw_elastic_shot* shots, 
   const Geo& g = es->g;
   const long long np = (long long)g.nx * g.nz;
   const int K = es->gp.check_freq;
-  DevMem dout, dmis;
   double* out[3] = {g_rho, g_lam, g_mu};
   double* mout = misfit;
   if (!on_device) {
-    dev_alloc(dout, (size_t)3 * np * sizeof(double), "gradient output", st);
-    for (int q = 0; q < 3; ++q) out[q] = dout.as<double>() + q * np;
+    ensure(es, es->d_gout, (size_t)3 * np * sizeof(double), "gradient output");
+    for (int q = 0; q < 3; ++q) out[q] = es->d_gout.as<double>() + q * np;
   }
   if (!on_device || !mout) {
-    dev_alloc(dmis, sizeof(double), "misfit output", st);
-    mout = dmis.as<double>();
+    ensure(es, es->d_mout, sizeof(double), "misfit output");
+    mout = es->d_mout.as<double>();
   }
   const std::vector<HostShot> order = sorted_order(nshots, shots);
   bool first_group = true;
@@ -2085,97 +2162,6 @@ void elastic_gradient(sw_elastic* es, int nshots, const sw_elastic_shot* shots, 
                    "checkpoint load");
       }
     };
-    // forward with checkpoints; the last window writes its slots directly
-    zero_state(es, S, false);
-    const int last_start = (M - 1) * K;
-    for (int it = 1; it <= ntmax; ++it) {
-      const int A = active_count(group, it);
-      if (it > last_start) {
-        float* sU[2];
-        float* sD[2];
-        slot_ptrs(it - last_start - 1, sU, sD);
-        full_step(R, A, it, true, KK_STENCIL, sU, sD);
-      } else {
-        full_step(R, A, it, true, KK_STENCIL, nullptr, nullptr);
-      }
-      if (it % K == 0 && it / K <= M - 1) save_ck(it / K);
-    }
-    download_traces(es, shots, group, desc, on_device);
-    // misfit and adjoint source
-    const int nblk = 64;
-    ensure(es, es->d_partial, (size_t)nblk * S * sizeof(double), "misfit partials");
-    ensure(es, es->d_amax, 16, "max reduction");
-    check_cuda(cudaMemsetAsync(es->d_amax.p, 0, sizeof(unsigned), st), "max clear");
-    {
-      cudaEvent_t ev = nullptr;
-      bool any_dense = false;
-      for (const auto& d : desc) any_dense = any_dense || d.icd;
-      if (any_dense) {  // C^-1 r of the shots with a dense inverse covariance (cuBLAS), per component
-        k_el_residual_dense<<<dim3(nblk, S), 256, 0, st>>>(R.ddesc);
-        check_cuda(cudaGetLastError(), "residual launch");
-        for (const auto& d : desc)
-          if (d.icd) dense_invcov(es->ctx, d.nt, 2 * d.nrec, d.icd, d.resid, const_cast<float*>(d.cres));
-      }
-      es->ctx->prof.begin(st, KK_OTHER, 0.0, &ev);
-      k_el_misfit<<<dim3(nblk, S), 256, 0, st>>>(R.ddesc, es->d_partial.as<double>(), es->d_amax.as<unsigned>());
-      check_cuda(cudaGetLastError(), "misfit launch");
-      k_el_misfit_sum<<<1, 256, 0, st>>>(es->d_partial.as<double>(), nblk * S, mout, first_group ? 0 : 1);
-      check_cuda(cudaGetLastError(), "misfit sum launch");
-      es->ctx->prof.end(st, KK_OTHER, ev);
-    }
-    unsigned bits = 0;
-    check_cuda(cudaMemcpyAsync(&bits, es->d_amax.p, sizeof(unsigned), cudaMemcpyDeviceToHost, st), "max download");
-    check_cuda(cudaStreamSynchronize(st), "misfit");
-    float amax;
-    std::memcpy(&amax, &bits, sizeof(float));
-    const float sa = pow2_scale(amax);
-    // adjoint with recompute and correlation
-    zero_state(es, S, true);
-    check_cuda(cudaMemsetAsync(es->acc.p, 0, (size_t)ngroups * 10 * F * sizeof(float), st), "accumulators clear");
-    Args ca = R.args(true);
-    for (int m = M - 1; m >= 0; --m) {
-      const int t0 = m * K + 1, t1 = std::min((m + 1) * K, ntmax);
-      if (m < M - 1) {
-        load_ck(m);
-        for (int t = t0; t <= t1; ++t) {
-          float* sU[2];
-          float* sD[2];
-          slot_ptrs(t - t0, sU, sD);
-          full_step(R, active_count(group, t), t, false, KK_RECOMPUTE, sU, sD);
-        }
-      }
-      for (int it = t1; it >= t0; --it) {
-        const int A = active_count(group, it);
-        if (A <= 0) continue;
-        adjoint_step(R, A, it, sa);
-        float* sU[2];
-        float* sD[2];
-        slot_ptrs(it - t0, sU, sD);
-        CorrArgs c{};
-        c.g = g;
-        c.nshots = A;
-        c.gsize = gsize;
-        c.cs = es->d_cs.as<float>();
-        c.aux = ca.ux; c.auz = ca.uz;
-        c.fux = sU[0]; c.fuz = sU[1];
-        c.Dx = sD[0]; c.Dz = sD[1];
-        c.lam = es->lam.as<float>(); c.mu = es->mu.as<float>();
-        c.acc = es->acc.as<float>();
-        const int ng = (A + gsize - 1) / gsize;
-        const dim3 grid((g.nx + BX - 1) / BX, (g.nz + CTZ - 1) / CTZ, ng);
-        cudaEvent_t ev = nullptr;
-        const double pts = (double)g.nx * g.nz;
-        es->ctx->prof.begin(st, KK_CORR, pts * (A * 24.0 + ng * 80.0), &ev);
-        if (es->vec) {
-          const dim3 grid4((g.nx + 511) / 512, g.nz, ng);
-          k_el_corr4<<<grid4, BX, 0, st>>>(c);
-        } else {
-          k_el_corr<<<grid, BX, 0, st>>>(c);
-        }
-        check_cuda(cudaGetLastError(), "correlation launch");
-        es->ctx->prof.end(st, KK_CORR, ev);
-      }
-    }
     // mute balls per group (= per shot when muting)
     std::vector<MuteBall> balls;
     std::vector<int> bptr(1, 0);
@@ -2206,23 +2192,127 @@ void elastic_gradient(sw_elastic* es, int nshots, const sw_elastic_shot* shots, 
       upload(es, es->d_balls, balls, "mute balls");
       upload(es, es->d_ball_ptr, bptr, "mute balls");
     }
+    // the group's device work -- forward, misfit (with the dense C^-1
+    // products), adjoint scale, adjoint with recompute and correlation,
+    // reduction -- as one CUDA graph
+    const int nblk = 64;
+    ensure(es, es->d_partial, (size_t)nblk * S * sizeof(double), "misfit partials");
+    ensure(es, es->d_amax, 16, "max reduction");
     {
-      Geo gh = g;
-      gh.idx = (float)es->prm.h[0];  // the reduction uses the spacings
-      gh.idz = (float)es->prm.h[1];
-      cudaEvent_t ev = nullptr;
-      es->ctx->prof.begin(st, KK_OTHER, 0.0, &ev);
-      const int blocks = (int)std::min<long long>((np + 255) / 256, 8192);
-      const double inv_scale = 1.0 / ((double)R.sf_ref * (double)sa);
-      k_el_reduce<<<blocks, 256, 0, st>>>(gh, ngroups, es->acc.as<float>(), es->rho_d.as<double>(), es->mu_d.as<double>(),
-                                          es->prm.interp_rho, es->prm.interp_mu,
-                                          1.0 / (es->prm.dt * es->prm.dt), inv_scale,
-                                          mute ? es->d_balls.as<MuteBall>() : nullptr,
-                                          mute ? es->d_ball_ptr.as<int>() : nullptr, out[0], out[1], out[2],
-                                          first_group ? 0 : 1);
-      check_cuda(cudaGetLastError(), "gradient reduction launch");
-      es->ctx->prof.end(st, KK_OTHER, ev);
+      const std::vector<float> sc = {sf_ref, 1.0f};
+      upload(es, es->d_scales, sc, "source scales");
     }
+    std::vector<long long> key = {S, ntmax, es->tz, es->vec ? 1 : 0, first_group ? 1 : 0, mute ? 1 : 0,
+                                  R.gx_src, R.gx_adj, R.gx_rec, (long long)(uintptr_t)out[0],
+                                  (long long)(uintptr_t)out[1], (long long)(uintptr_t)out[2],
+                                  (long long)(uintptr_t)mout};
+    for (const auto& h : group) key.push_back(h.nt);
+    for (const auto& h : group) key.push_back(shots[h.orig].kind);
+    for (int k = 0; k < S; ++k)  // the dense products' operands are launch arguments
+      if (desc[k].icd) key.insert(key.end(), {k, desc[k].nrec, (long long)(uintptr_t)desc[k].icd});
+    auto body = [&] {
+      // forward with checkpoints; the last window writes its slots directly
+      zero_state(es, S, false);
+      const int last_start = (M - 1) * K;
+      for (int it = 1; it <= ntmax; ++it) {
+        const int A = active_count(group, it);
+        if (it > last_start) {
+          float* sU[2];
+          float* sD[2];
+          slot_ptrs(it - last_start - 1, sU, sD);
+          full_step(R, A, it, true, KK_STENCIL, sU, sD);
+        } else {
+          full_step(R, A, it, true, KK_STENCIL, nullptr, nullptr);
+        }
+        if (it % K == 0 && it / K <= M - 1) save_ck(it / K);
+      }
+      // misfit and adjoint source
+      check_cuda(cudaMemsetAsync(es->d_amax.p, 0, sizeof(unsigned), st), "max clear");
+      {
+        cudaEvent_t ev = nullptr;
+        bool any_dense = false;
+        for (const auto& d : desc) any_dense = any_dense || d.icd;
+        if (any_dense) {  // C^-1 r of the shots with a dense inverse covariance (dense.cu), per component
+          k_el_residual_dense<<<dim3(nblk, S), 256, 0, st>>>(R.ddesc);
+          check_cuda(cudaGetLastError(), "residual launch");
+          for (const auto& d : desc)
+            if (d.icd) dense_invcov(es->ctx, d.nt, 2 * d.nrec, d.icd, d.resid, const_cast<float*>(d.cres));
+        }
+        es->ctx->prof.begin(st, KK_OTHER, 0.0, &ev);
+        k_el_misfit<<<dim3(nblk, S), 256, 0, st>>>(R.ddesc, es->d_partial.as<double>(), es->d_amax.as<unsigned>());
+        check_cuda(cudaGetLastError(), "misfit launch");
+        k_el_misfit_sum<<<1, 256, 0, st>>>(es->d_partial.as<double>(), nblk * S, mout, first_group ? 0 : 1);
+        check_cuda(cudaGetLastError(), "misfit sum launch");
+        es->ctx->prof.end(st, KK_OTHER, ev);
+      }
+      k_el_adj_scale<<<1, 1, 0, st>>>(es->d_amax.as<unsigned>(), es->d_scales.as<float>());
+      check_cuda(cudaGetLastError(), "adjoint scale launch");
+      // adjoint with recompute and correlation
+      zero_state(es, S, true);
+      check_cuda(cudaMemsetAsync(es->acc.p, 0, (size_t)ngroups * 10 * F * sizeof(float), st), "accumulators clear");
+      Args ca = R.args(true);
+      for (int m = M - 1; m >= 0; --m) {
+        const int t0 = m * K + 1, t1 = std::min((m + 1) * K, ntmax);
+        if (m < M - 1) {
+          load_ck(m);
+          for (int t = t0; t <= t1; ++t) {
+            float* sU[2];
+            float* sD[2];
+            slot_ptrs(t - t0, sU, sD);
+            full_step(R, active_count(group, t), t, false, KK_RECOMPUTE, sU, sD);
+          }
+        }
+        for (int it = t1; it >= t0; --it) {
+          const int A = active_count(group, it);
+          if (A <= 0) continue;
+          adjoint_step(R, A, it);
+          float* sU[2];
+          float* sD[2];
+          slot_ptrs(it - t0, sU, sD);
+          CorrArgs c{};
+          c.g = g;
+          c.nshots = A;
+          c.gsize = gsize;
+          c.cs = es->d_cs.as<float>();
+          c.aux = ca.ux; c.auz = ca.uz;
+          c.fux = sU[0]; c.fuz = sU[1];
+          c.Dx = sD[0]; c.Dz = sD[1];
+          c.lam = es->lam.as<float>(); c.mu = es->mu.as<float>();
+          c.acc = es->acc.as<float>();
+          const int ng = (A + gsize - 1) / gsize;
+          const dim3 grid((g.nx + BX - 1) / BX, (g.nz + CTZ - 1) / CTZ, ng);
+          cudaEvent_t ev = nullptr;
+          const double pts = (double)g.nx * g.nz;
+          es->ctx->prof.begin(st, KK_CORR, pts * (A * 24.0 + ng * 80.0), &ev);
+          if (es->vec) {
+            const dim3 grid4((g.nx + 511) / 512, g.nz, ng);
+            k_el_corr4<<<grid4, BX, 0, st>>>(c);
+          } else {
+            k_el_corr<<<grid, BX, 0, st>>>(c);
+          }
+          check_cuda(cudaGetLastError(), "correlation launch");
+          es->ctx->prof.end(st, KK_CORR, ev);
+        }
+      }
+      {
+        Geo gh = g;
+        gh.idx = (float)es->prm.h[0];  // the reduction uses the spacings
+        gh.idz = (float)es->prm.h[1];
+        cudaEvent_t ev = nullptr;
+        es->ctx->prof.begin(st, KK_OTHER, 0.0, &ev);
+        const int blocks = (int)std::min<long long>((np + 255) / 256, 8192);
+        k_el_reduce<<<blocks, 256, 0, st>>>(gh, ngroups, es->acc.as<float>(), es->rho_d.as<double>(), es->mu_d.as<double>(),
+                                            es->prm.interp_rho, es->prm.interp_mu,
+                                            1.0 / (es->prm.dt * es->prm.dt), es->d_scales.as<float>(),
+                                            mute ? es->d_balls.as<MuteBall>() : nullptr,
+                                            mute ? es->d_ball_ptr.as<int>() : nullptr, out[0], out[1], out[2],
+                                            first_group ? 0 : 1);
+        check_cuda(cudaGetLastError(), "gradient reduction launch");
+        es->ctx->prof.end(st, KK_OTHER, ev);
+      }
+    };
+    el_run_graph(es, key, body);
+    download_traces(es, shots, group, desc, on_device);
     check_cuda(cudaStreamSynchronize(st), "elastic gradient group");
     first_group = false;
   }

@@ -78,13 +78,13 @@ struct sw_ctx {
   std::string last_error;
   swgb::Profiler prof;
   swgb::DevMem err;  // int flag raised by kernels whose bounded waits gave up
-  void* cublas = nullptr;  // cuBLAS handle, created on first use (dense inverse covariances)
 };
 
 namespace swgb {
 
-// CR = C * R on the context's stream (cuBLAS SGEMM, FP32 arithmetic): C is a
-// dense (nt, nt) inverse covariance, R the (nt, ncols) residuals of one shot.
+// CR = C * R on the context's stream (the library's own tiled FP32 GEMM,
+// dense.cu): C is a dense (nt, nt) inverse covariance, R the (nt, ncols)
+// residuals of one shot.
 void dense_invcov(sw_ctx* ctx, int nt, int ncols, const float* C, const float* R, float* CR);
 
 // Host-side C-PML coefficients (double precision), one axis.
