@@ -131,9 +131,9 @@ class ScalarShot:
 class L2Misfit:
     """src/inversion/misfits/L2Misfit.jl:2-20.
 
-    matrix (applied on the GPU by the library's own tiled FP32 product when it has
-    off-diagonal terms).
-    terms).
+    ``invcov`` may be None (identity), a vector (its diagonal) or a square
+    matrix (applied on the GPU by the library's own tiled FP32 product when it
+    has off-diagonal terms).
     """
 
     def __init__(self, observed=None, invcov=None, windows: Sequence[tuple[int, int]] = ()):
