@@ -55,6 +55,8 @@ def _args():
                                                       "2 also BF16 checkpoints)")
     p.add_argument("--no-parity", action="store_true", help="skip the FP64-oracle error of the benchmark's shortest shot")
     p.add_argument("--check-freq", type=int, default=0, help="override the checkpoint period (small profiling cases)")
+    p.add_argument("--no-extras", action="store_true",
+                   help="skip the full-length 3D and elastic gradients that the default run times after the headline")
     return p.parse_args()
 
 
@@ -734,6 +736,60 @@ def run_reference(a):
     print(json.dumps(line), flush=True)
 
 
+def _extra_acoustic3d(a, device):
+    """The 3D workload at full size and length (16 shots of 400^3, nt 2000,
+    K = 100, BF16 recompute buffer): one warm-up gradient, one timed; Gpts/s,
+    shots/s and the stencil kinds' bandwidth."""
+    import torch
+
+    sw, w = _workload("acoustic3d_400", 0, 0)
+    R = GradientRun(sw, w, device, bf16=1)
+    R.make_observed()
+    idx = list(range(len(w.shots)))
+    R.gradient_device(idx)
+    torch.cuda.synchronize(R.dev)
+    clocks = ClockSampler(device)
+    clocks.start()
+    t = R.timed(lambda: R.gradient_device(idx), 1)
+    clk = clocks.stop()
+    R.ctx.profile(True)
+    R.timed(lambda: R.gradient_device(idx), 1)
+    R.ctx.profile(False)
+    prof = {k: R.ctx.profile_read(k) for k in (0, 1, 4)}
+    pts = float(w.point_steps())
+    peak, _ = _peak()
+    names = {0: "k_ac3d_step<1> forward", 4: "k_ac3d_step<1> recompute", 1: "k_ac3d_step<2> adjoint + correlation"}
+    kern = {names[k]: {"ms": prof[k][0], "GB_per_s": prof[k][2] / (prof[k][0] / 1e3) / 1e9 if prof[k][0] else None,
+                       "frac": prof[k][2] / (prof[k][0] / 1e3) / 1e9 / peak if prof[k][0] else None}
+            for k in prof}
+    out = {"workload": w.name, "grid": list(w.vp.shape), "shots": len(w.shots), "nt": max(s.nt for s in w.shots),
+           "check_freq": w.check_freq, "buffer": "bf16 recompute buffer", "value": pts / t / 1e9, "unit": UNIT,
+           "ms_per_step": t * 1e3, "shots_per_s": len(w.shots) / t, "steps": 1, "warmup": 1, "kernels": kern,
+           "clocks": clk}
+    R.lib.sw_wavesim_destroy(R.h)
+    return out
+
+
+def _extras(a, device):
+    """Full-length gradients of the 3D and elastic workloads, timed after the
+    headline (its device memory released first)."""
+    import gc
+
+    import torch
+
+    out = {}
+    gc.collect()
+    torch.cuda.empty_cache()
+    e = measure_elastic(a, "elastic2d_1200x600", steps=1, warmup=2, plain=False, cpu=False, device=device)
+    out["elastic2d_1200x600"] = {k: e[k] for k in ("value", "unit", "ms_per_step", "shots_per_s", "steps", "warmup",
+                                                    "config", "clocks")}
+    out["elastic2d_1200x600"]["roofline"] = {k: e["roofline"][k] for k in ("kernel", "achieved", "frac", "kernels")}
+    gc.collect()
+    torch.cuda.empty_cache()
+    out["acoustic3d_400"] = _extra_acoustic3d(a, device)
+    return out
+
+
 def run_gb300(a):
     import torch
 
@@ -902,6 +958,10 @@ def run_gb300(a):
         oracle.load()
         v, threads, sample, _ = _cpu_baseline(sw, w, a.cpu_sample_nt)
         line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample}
+    if not a.no_extras and world == 1 and a.workload == "acoustic2d_2001x801" and not (a.shots or a.nt):
+        R.lib.sw_wavesim_destroy(R.h)
+        del R
+        line["extras"] = _extras(a, local)
     print(json.dumps(line), flush=True)
 
 
