@@ -890,7 +890,7 @@ def run_gb300(a):
         adj, adj_what = base + "<3>", "adjoint + correlation (plain FP32 sums, FP64 flush every 32 steps)"
     else:
         adj, adj_what = base + "<2>", "adjoint + correlation (Kahan sums)"
-    two = "k_ac2d_pair (two steps per launch) / " if nd == 2 else ""
+    two = "k_ac2d_pair (two steps per launch) / " if (nd == 2 and a.variant >= 0 and a.variant & 1024) else ""
     kinds = {0: (f"{two}{base}<0/1> forward", f"{base}<1>", "forward"),
              4: (f"{two}{base}<1> recompute (writes D)", f"{base}<1>", "recompute"),
              1: (f"{two}{adj} {adj_what}", adj, "adjoint")}

@@ -206,14 +206,14 @@ int sw_acoustic_forward_snapshots(sw_wavesim* ws, int32_t nshots, const sw_acous
  * adjoint (4 shots per block, one Kahan-compensated FP32 sum per group; 4+
  * shots); + 512 stages the rows of the 4-warp stencil through a per-warp
  * shared-memory ring filled by cp.async (three rows in flight per warp
- * instead of one, no registers held by the copies).  By default the 2D
+ * instead of one, no registers held by the copies).  + 1024 makes the 2D
  * forward kinds (forward, recompute) and the adjoint advance two time steps
- * per launch wherever nothing happens between the steps (same rounding as two
- * one-step launches); + 1024 turns that off, bits 11-13 pick the rows per
- * block of the two-step kernel (0 = heuristic: 32, fewer for small batches;
- * 1 = 8, 2 = 16, 3 = 32, 4 = 64, 5 = 128, 6 = 4) and bits 14-15 its
- * resident-block bound (0 = 6 forward / 5 adjoint blocks per SM, 1 = 4 / 3,
- * 2 = 7 / 4).  Results do not depend on any of them beyond rounding. */
+ * per launch wherever nothing happens between the steps (temporal blocking,
+ * the same rounding as two one-step launches); bits 11-13 pick the rows per
+ * block of that kernel (0 = heuristic: 32, fewer for small batches; 1 = 8,
+ * 2 = 16, 3 = 32, 4 = 64, 5 = 128, 6 = 4) and bits 14-15 its resident-block
+ * bound (0 = 6 forward / 5 adjoint blocks per SM, 1 = 4 / 3, 2 = 7 / 4).
+ * Results do not depend on any of them beyond rounding. */
 int sw_wavesim_set_tuning(sw_wavesim* ws, int32_t tz, int32_t variant);
 
 /* CUDA graphs (on by default): a batch's whole device-side time loop

@@ -438,7 +438,7 @@ struct sw_wavesim {
   DevMem psim[3], xim[3];                 // memory variables between the two steps of a two-step launch
   DevMem d_pair, d_recstash, d_stash;     // two-step launches: per-shot source / receiver-row table,
                                           // receiver -> stash index, first-step pressure of receiver rows
-  bool pair_on = true;                    // 2D: two time steps per launch where possible
+  bool pair_on = false;                   // 2D: two time steps per launch where possible (tuning variant)
   int pair_tz = 0;                        // rows per block of the two-step kernel (0 = heuristic)
   int pair_occ = 0;                       // resident-block bound of the two-step kernel (0 = default, 1, 2)
   bool pair_ok = false;                   // the current group's shots allow two-step launches
@@ -1994,7 +1994,7 @@ void wavesim_set_tuning(sw_wavesim* ws, int tz, int variant) {
   ws->pf = (variant / 16) % 16;
   ws->adj_plain = (variant & 256) == 0;
   ws->cpa = (variant & 512) != 0;
-  ws->pair_on = (variant & 1024) == 0;
+  ws->pair_on = (variant & 1024) != 0;
   static const int pair_tz[8] = {0, 8, 16, 32, 64, 128, 4, 0};
   ws->pair_tz = pair_tz[(variant >> 11) & 7];
   ws->pair_occ = (variant >> 14) & 3;

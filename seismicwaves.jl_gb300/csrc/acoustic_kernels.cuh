@@ -156,6 +156,31 @@ __device__ __forceinline__ float d2term(float l, float c, float r, float ih2) {
   return rmul(radd(radd(l, rmul(-2.f, c)), r), ih2);
 }
 
+// One row of four interior points outside the damping strips advanced by one
+// step: the arithmetic every stencil uses at such points (the general paths
+// below add the C-PML terms and the boundary handling), straight-line for the
+// warps whose whole row segment qualifies.
+__device__ __forceinline__ void row4_interior(const float (&rm)[4], const float (&r0)[4], const float (&rp)[4],
+                                              float left, float right, const float (&o)[4], const float (&f)[4],
+                                              float ih2x, float ih2z, float (&outp)[4], float (&outd)[4],
+                                              float (&outD)[4]) {
+#pragma unroll
+  for (int e = 0; e < 4; ++e) {
+    const float xm = e == 0 ? left : r0[e - 1];
+    const float xp = e == 3 ? right : r0[e + 1];
+    const float c = r0[e];
+    const float lap = radd(d2term(xm, c, xp, ih2x), d2term(rm[e], c, rp[e], ih2z));
+    outD[e] = rmul(f[e], lap);
+    outd[e] = radd(o[e], outD[e]);
+    outp[e] = radd(c, outd[e]);
+  }
+}
+
+// Points x (or rows z) in [lo, hi] are interior and outside the damping
+// strips of an axis of n points with halo cells.
+__device__ __forceinline__ int plain_lo(int H) { return H > 1 ? H : 1; }
+__device__ __forceinline__ int plain_hi(int n, int H) { return (n - 1 - H) < (n - 2) ? (n - 1 - H) : (n - 2); }
+
 // C-PML term of one axis at point x (0-based) along an axis of n points.
 // Without damping the term is d2 (the plain second derivative).  In a strip
 // the two half-node memory variables psi around x are advanced (psi_out), the
@@ -221,7 +246,7 @@ __device__ __forceinline__ float* fptr(const FieldArg& f, int shot) {
 template <int MODE>
 struct Ac2dRow {
   int nx, nz, P, H, x0, dbf16;
-  bool inb, xstrip, vec_interior;
+  bool inb, xstrip, vec_interior, fastx;
   float ihx, ihz, ih2x, ih2z;
   StripIO sx, sz;
   float *pn, *dn, *ckp, *ckd, *Dw, *gg, *gcp;
@@ -244,6 +269,9 @@ struct Ac2dRow {
     sz.psi_step = P; sz.xi_step = P;
     xstrip = inb && (x0 < H || x0 + 3 >= nx - H);
     vec_interior = (x0 >= 1) && (x0 + 3 <= nx - 2);
+    // the warp's 128 points all interior and outside the x strips (warp-uniform)
+    const int wx = x0 - 4 * (int)(threadIdx.x & 31);
+    fastx = wx >= plain_lo(H) && wx + 127 <= plain_hi(nx, H);
     pn = fptr(A.pnew, shot);
     dn = fptr(A.dout, shot);
     ckp = fptr(A.ck_p, shot);
@@ -262,25 +290,29 @@ struct Ac2dRow {
     sx.psi_base = (long long)z * (2 * H);
     sx.xi_base = (long long)z * (2 * H + 2);
     float outp[4], outd[4], outD[4];
+    if (fastx && z >= plain_lo(H) && z <= plain_hi(nz, H)) {
+      row4_interior(rm, r0, rp, left, right, o, f, ih2x, ih2z, outp, outd, outD);
+    } else {
 #pragma unroll
-    for (int e = 0; e < 4; ++e) {
-      const float xm = e == 0 ? left : r0[e - 1];
-      const float xp = e == 3 ? right : r0[e + 1];
-      const float c = r0[e];
-      float tx = d2term(xm, c, xp, ih2x);
-      float tz = d2term(rm[e], c, rp[e], ih2z);
-      const int x = x0 + e;
-      const bool pin = inb && x >= 1 && x <= nx - 2;
-      if (xstrip && pin) tx = cpml_axis_term(tx, xm, c, xp, x, nx, H, ihx, sx);
-      if (zstrip && pin) {
-        sz.psi_base = x;
-        sz.xi_base = x;
-        tz = cpml_axis_term(tz, rm[e], c, rp[e], z, nz, H, ihz, sz);
+      for (int e = 0; e < 4; ++e) {
+        const float xm = e == 0 ? left : r0[e - 1];
+        const float xp = e == 3 ? right : r0[e + 1];
+        const float c = r0[e];
+        float tx = d2term(xm, c, xp, ih2x);
+        float tz = d2term(rm[e], c, rp[e], ih2z);
+        const int x = x0 + e;
+        const bool pin = inb && x >= 1 && x <= nx - 2;
+        if (xstrip && pin) tx = cpml_axis_term(tx, xm, c, xp, x, nx, H, ihx, sx);
+        if (zstrip && pin) {
+          sz.psi_base = x;
+          sz.xi_base = x;
+          tz = cpml_axis_term(tz, rm[e], c, rp[e], z, nz, H, ihz, sz);
+        }
+        const float lap = radd(tx, tz);
+        outD[e] = rmul(f[e], lap);
+        outd[e] = radd(o[e], outD[e]);
+        outp[e] = radd(c, outd[e]);
       }
-      const float lap = radd(tx, tz);
-      outD[e] = rmul(f[e], lap);
-      outd[e] = radd(o[e], outD[e]);
-      outp[e] = radd(c, outd[e]);
     }
     if (!inb) return;
     if (ckp) {
@@ -553,8 +585,12 @@ __device__ __forceinline__ void sld4(float (&v)[4], const float4& s) {
 template <typename MK>
 __device__ __forceinline__ void pair_row(const float (&rm)[4], const float (&r0)[4], const float (&rp)[4],
                                          float left, float right, const float (&o)[4], const float (&f)[4], int x0,
-                                         int z, bool act, bool xstrip, const StepArgs& A, MK&& mk, float (&outp)[4],
-                                         float (&outd)[4], float (&outD)[4]) {
+                                         int z, bool act, bool xstrip, bool fast, const StepArgs& A, MK&& mk,
+                                         float (&outp)[4], float (&outd)[4], float (&outD)[4]) {
+  if (fast) {  // warp-uniform: every point of the row segment interior and outside the strips
+    row4_interior(rm, r0, rp, left, right, o, f, A.ih2[0], A.ih2[1], outp, outd, outD);
+    return;
+  }
   const int nx = A.n0, nz = A.n1, H = A.halo;
   const bool zin = z >= 1 && z <= nz - 2;
   const bool zstrip = z < H || z >= nz - H;
@@ -648,6 +684,9 @@ __global__ void __launch_bounds__(32 * NW, MB) k_ac2d_pair(const StepArgs A, con
   const bool own = inb && lane >= 1 && lane <= 30;
   const bool vec = x0 >= 1 && x0 + 3 <= nx - 2;
   const bool xstrip = inb && (x0 < H || x0 + 3 >= nx - H);
+  // the warp's 128 points (both steps) interior and outside the x strips
+  const bool fastx = ox0 - 4 >= plain_lo(H) && ox0 + 123 <= plain_hi(nx, H);
+  const int zlo = plain_lo(H), zhi = plain_hi(nz, H);
 
   const float* __restrict__ pc = fptr(A.pcur, shot);
   const float* __restrict__ di = fptr(A.din, shot);
@@ -775,7 +814,7 @@ __global__ void __launch_bounds__(32 * NW, MB) k_ac2d_pair(const StepArgs A, con
     if (lane == 0) left = hl;
     if (lane == 31) right = hr;
     float p1[4], d1[4], D1[4];
-    pair_row(rm, r0, rp, left, right, o, f, x0, y, inb, xstrip, A, mk1, p1, d1, D1);
+    pair_row(rm, r0, rp, left, right, o, f, x0, y, inb, xstrip, fastx && y >= zlo && y <= zhi, A, mk1, p1, d1, D1);
     if constexpr (ADJ) {
       // correlation of the first step on the band's rows (before its
       // injection, as the one-step kernel), then the first step's adjoint
@@ -845,7 +884,8 @@ __global__ void __launch_bounds__(32 * NW, MB) k_ac2d_pair(const StepArgs A, con
       const float l2 = __shfl_up_sync(FULL, q0[3], 1);
       const float r2 = __shfl_down_sync(FULL, q0[0], 1);
       float p2[4], d2[4], D2[4];
-      pair_row(qm, q0, p1, l2, r2, dq, fq, x0, y - 1, own, xstrip, A, mk2, p2, d2, D2);
+      pair_row(qm, q0, p1, l2, r2, dq, fq, x0, y - 1, own, xstrip, fastx && y - 1 >= zlo && y - 1 <= zhi, A, mk2,
+               p2, d2, D2);
       if (own) {
         pair_store(pn, zrow, x0, nx, vec, p2);
         pair_store(dn, zrow, x0, nx, vec, d2);
@@ -1192,7 +1232,7 @@ __device__ __forceinline__ StripIO strip_io(const StepArgs& A, int d, int shot, 
   return s;
 }
 
-template <int MODE, int NW>
+template <int MODE, int NW, bool FAST = false>
 __device__ __forceinline__ void ac3d_body(const StepArgs& A) {
   constexpr unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -1222,6 +1262,8 @@ __device__ __forceinline__ void ac3d_body(const StepArgs& A) {
 
   const bool xstrip = inb && (x0 < H || x0 + 3 >= nx - H);
   const bool ystrip = (y < H) || (y >= ny - H);
+  // the warp's 128 x points and its y row interior and outside the strips
+  const bool fastxy = wx0 >= plain_lo(H) && wx0 + 127 <= plain_hi(nx, H) && y >= plain_lo(H) && y <= plain_hi(ny, H);
   const bool vec_interior = (x0 >= 1) && (x0 + 3 <= nx - 2);
   float* ckp = fptr(A.ck_p, shot);
   float* ckd = fptr(A.ck_d, shot);
@@ -1266,14 +1308,28 @@ __device__ __forceinline__ void ac3d_body(const StepArgs& A) {
     if (lane == 31) right = xa + 4 < P ? pc[idx + 4] : 0.f;
     const bool zstrip = (z < H) || (z >= nz - H);
     float outp[4], outd[4], outD[4];
+    if (FAST && fastxy && z >= plain_lo(H) && z <= plain_hi(nz, H)) {
+      // warp-uniform: every point interior and outside the strips
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        const float xm = e == 0 ? left : r0[e - 1];
+        const float xp = e == 3 ? right : r0[e + 1];
+        const float c = r0[e];
+        const float lap = radd(radd(d2term(xm, c, xp, A.ih2[0]), d2term(ym[e], c, yp[e], A.ih2[1])),
+                               d2term(rm[e], c, rp[e], A.ih2[2]));
+        outD[e] = rmul(f[e], lap);
+        outd[e] = radd(o[e], outD[e]);
+        outp[e] = radd(c, outd[e]);
+      }
+    } else {
 #pragma unroll
     for (int e = 0; e < 4; ++e) {
       const float xm = e == 0 ? left : r0[e - 1];
       const float xp = e == 3 ? right : r0[e + 1];
       const float c = r0[e];
-      float tx = (xm - 2.f * c + xp) * A.ih2[0];
-      float ty = (ym[e] - 2.f * c + yp[e]) * A.ih2[1];
-      float tz = (rm[e] - 2.f * c + rp[e]) * A.ih2[2];
+      float tx = d2term(xm, c, xp, A.ih2[0]);
+      float ty = d2term(ym[e], c, yp[e], A.ih2[1]);
+      float tz = d2term(rm[e], c, rp[e], A.ih2[2]);
       const int x = x0 + e;
       const bool pin = inb && x >= 1 && x <= nx - 2;
       if (xstrip && pin) {
@@ -1294,10 +1350,11 @@ __device__ __forceinline__ void ac3d_body(const StepArgs& A) {
         s2.xi_base = (long long)y * P + x;
         tz = cpml_axis_term(tz, rm[e], c, rp[e], z, nz, H, A.ih[2], s2);
       }
-      const float lap = (tx + ty) + tz;
-      outD[e] = f[e] * lap;
-      outd[e] = o[e] + outD[e];
-      outp[e] = c + outd[e];
+      const float lap = radd(radd(tx, ty), tz);
+      outD[e] = rmul(f[e], lap);
+      outd[e] = radd(o[e], outD[e]);
+      outp[e] = radd(c, outd[e]);
+    }
     }
     if (inb) {
       if (ckp) {
@@ -1363,7 +1420,7 @@ __global__ void __launch_bounds__(32 * NW, 24 / NW) k_ac3d_step(const StepArgs A
 }
 template <int MODE, int NW = 4>
 __global__ void __launch_bounds__(32 * NW) k_ac3d_fwd(const StepArgs A) {
-  ac3d_body<MODE, NW>(A);
+  ac3d_body<MODE, NW, true>(A);
 }
 
 // ---------------------------------------------------------------------------

@@ -1,9 +1,9 @@
 """Two time steps per stencil launch (k_ac2d_pair: forward, recompute and
-adjoint kinds) against one step per launch.
+adjoint kinds, tuning variant 1024) against one step per launch (the default).
 
 The two-step kernel rounds exactly as two one-step launches do, so traces,
 misfits and gradients must be bit-identical whether the library pairs steps
-(the default) or not (tuning variant 1024), across grid shapes that leave
+or not, across grid shapes that leave
 partial warps and bands, free surface or not, halo 0, several sources (two on
 one point), receivers on several rows, odd and even checkpoint periods (which
 mix paired and single steps), BF16 recompute buffers and checkpoints, and
@@ -18,7 +18,7 @@ from cases import Case, GpuRun, make_shot, oracle_forward, rel_l2, smooth_model,
 
 pytestmark = pytest.mark.gpu
 
-NO_PAIR = 1024
+PAIR = 1024
 
 
 def _case(nx, nz, halo, freetop, seed):
@@ -62,21 +62,21 @@ def test_two_step_forward_is_bitwise_one_step(sw, oracle, nx, nz, halo, freetop,
     shots = [_shot(case, 301, seed=k) for k in range(3)]
     shots[1].nt = 250  # a shorter record: the active set changes mid-run
     out = {}
-    for v in (tzsel << 11, NO_PAIR):
+    for v in (PAIR | tzsel << 11, 0):
         run = GpuRun(sw, case, variant=v)
         run.ctx.profile(True)
         out[v] = run.forward(shots)
         n = _launches(run)
         run.ctx.profile(False)
         run.close()
-        if v == NO_PAIR:
+        if v == 0:
             assert n == 301
         else:
             assert n < 0.6 * 301, n  # steps were paired
-    for a, b in zip(out[tzsel << 11], out[NO_PAIR]):
+    for a, b in zip(out[PAIR | tzsel << 11], out[0]):
         assert np.array_equal(a, b)
     ref = oracle_forward(oracle, sw, case, shots[0])
-    assert rel_l2(out[NO_PAIR][0], ref) < 1e-5
+    assert rel_l2(out[0][0], ref) < 1e-5
 
 
 @pytest.mark.parametrize("check_freq,bf16", [(1, 0), (10, 0), (7, 0), (10, 1), (6, 2)])
@@ -90,19 +90,19 @@ def test_two_step_gradient_is_bitwise_one_step(sw, check_freq, bf16):
         s.observed = np.asfortranarray(o, dtype=np.float64)
     obs_run.close()
     out = {}
-    for v in (0, NO_PAIR):
+    for v in (PAIR, 0):
         run = GpuRun(sw, case, gradient=True, check_freq=check_freq, variant=v, bf16=bf16)
         run.ctx.profile(True)
         out[v] = run.gradient(shots)
         adj = _launches(run, 1)
         run.ctx.profile(False)
         run.close()
-        if v == NO_PAIR:
+        if v == 0:
             assert adj == 240
         else:
             assert adj < 0.75 * 240, adj  # adjoint steps were paired
-    g0, m0, t0 = out[0]
-    g1, m1, t1 = out[NO_PAIR]
+    g0, m0, t0 = out[PAIR]
+    g1, m1, t1 = out[0]
     assert m0 == m1
     assert np.array_equal(g0, g1), rel_l2(g0, g1)
     for a, b in zip(t0, t1):
@@ -113,7 +113,7 @@ def test_two_step_snapshots_are_bitwise_one_step(sw):
     case = _case(150, 70, 10, False, seed=9)
     shot = _shot(case, 200, seed=3)
     snaps = {}
-    for v in (0, NO_PAIR):
+    for v in (PAIR, 0):
         run = GpuRun(sw, case, variant=v)
         arr, keep, outs = run._structs([shot], False)
         buf = np.zeros((200 // 3) * case.vp.size, np.float32)
@@ -121,8 +121,8 @@ def test_two_step_snapshots_are_bitwise_one_step(sw):
         run.ctx.check(run.ctx.lib.sw_acoustic_forward_snapshots(run.h, 1, arr, 0, 3, ptrs), "snapshots")
         snaps[v] = (buf, outs[0])
         run.close()
-    assert np.array_equal(snaps[0][0], snaps[NO_PAIR][0])
-    assert np.array_equal(snaps[0][1], snaps[NO_PAIR][1])
+    assert np.array_equal(snaps[PAIR][0], snaps[0][0])
+    assert np.array_equal(snaps[PAIR][1], snaps[0][1])
 
 
 def test_boundary_source_falls_back_to_one_step(sw, oracle):
@@ -131,7 +131,7 @@ def test_boundary_source_falls_back_to_one_step(sw, oracle):
     case = _case(90, 60, 5, False, seed=2)
     ex = [h * (n - 1) for n, h in zip(case.vp.shape, case.h)]
     shot = make_shot(case.h, ex, 150, case.dt, 15.0, [[0.0, 0.5 * ex[1]]], [[0.5 * ex[0], 0.3 * ex[1]]])
-    run = GpuRun(sw, case)
+    run = GpuRun(sw, case, variant=PAIR)
     run.ctx.profile(True)
     tr = run.forward([shot])[0]
     n = _launches(run)
