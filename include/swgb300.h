@@ -280,6 +280,10 @@ typedef struct {
   const double* rec_pos;   /* (nrec, 2) metres, for muting; host memory */
   const float* invcov;     /* gradient: NULL, or the full inverse covariance (nt, nt) column-major, applied to
                               each component; takes precedence over invcov_diag */
+  int32_t misfit_kind;      /* gradient: 0 = L2Misfit, 1 = CCTSMisfit per component trace
+                               (src/inversion/misfits/CCTSMisfit.jl:30-44, :63-80; windows and inverse
+                               covariances are then unused, nt <= 13000) */
+  double misfit_dt;         /* CCTSMisfit.dt (misfit_kind 1) */
 } sw_elastic_shot;
 
 /* One elastic simulation (a set of preallocated device fields).  gradient = 1

@@ -95,6 +95,8 @@ struct SwElasticShot
     src_pos::Ptr{Float64}
     rec_pos::Ptr{Float64}
     invcov::Ptr{Float32}
+    misfit_kind::Int32       # 0 L2Misfit, 1 CCTSMisfit (per component trace)
+    misfit_dt::Float64       # CCTSMisfit.dt
 end
 
 last_error(ctx::Ptr{Cvoid}) =

@@ -50,6 +50,8 @@ struct ElasticShotBuffers
     sp::Matrix{Float64}
     rp::Matrix{Float64}
     kind::Int32
+    mkind::Int32
+    mdt::Float64
 end
 
 function elastic_shot_buffers(model, shot, misfit)
@@ -58,15 +60,14 @@ function elastic_shot_buffers(model, shot, misfit)
     tabs = (csr(s1ij, s1c), csr(s2ij, s2c), csr(ruxij, ruxc), csr(ruzij, ruzc))
     kind = shot isa SeismicWaves.MomentTensorShot ? Int32(0) : Int32(1)
     momtens = kind == 0 ? Float32.(hcat([[m.Mxx, m.Mzz, m.Mxz] for m in shot.srcs.momtens]...)) : zeros(Float32, 3, 0)
-    obs, icd, icf, win = nothing, nothing, nothing, Int32[]
+    obs, icd, icf, win, mkind, mdt = nothing, nothing, nothing, Int32[], Int32(0), 0.0
     if misfit !== nothing
-        misfit isa SeismicWaves.L2Misfit || error("the GB300 elastic gradient takes L2 misfits")
-        icd, icf, win, _, _ = misfit_fields(misfit)
+        icd, icf, win, mkind, mdt = misfit_fields(misfit)
         obs = Float32.(misfit.observed)
     end
     tr = zeros(Float32, size(shot.recs.seismograms))
     return ElasticShotBuffers(tabs, Float32.(scal), momtens, tr, cpml_block(model), obs, icd, icf, win,
-                              Float64.(shot.srcs.positions), Float64.(shot.recs.positions), kind)
+                              Float64.(shot.srcs.positions), Float64.(shot.recs.positions), kind, mkind, mdt)
 end
 
 pt(t) = SwPointTable(pointer(t[1]), pointer(t[2]), pointer(t[3]))
@@ -76,7 +77,7 @@ sw_struct(b::ElasticShotBuffers) =
                   isempty(b.momtens) ? Ptr{Float32}(C_NULL) : pointer(b.momtens), (pt(b.tabs[1]), pt(b.tabs[2])),
                   Int32(size(b.rp, 1)), (pt(b.tabs[3]), pt(b.tabs[4])), pointer(b.tr), pointer(b.cp), optptr(b.obs),
                   optptr(b.icd), Int32(length(b.win) ÷ 2), isempty(b.win) ? Ptr{Int32}(C_NULL) : pointer(b.win),
-                  pointer(b.sp), pointer(b.rp), optptr(b.icf))
+                  pointer(b.sp), pointer(b.rp), optptr(b.icf), b.mkind, b.mdt)
 
 function save_snapshots!(model::GB300Elastic{T}, buf::Vector{Float32}, nt::Int) where {T}
     nx, nz = model.grid.size

@@ -73,7 +73,7 @@ def load():
                                                P, P, i]
         lib.oracle_elastic_forward.restype = i
         lib.oracle_elastic_gradient.argtypes = [i, P, P, d, i, i, P, P, P, i, i, P, i, i, i, P, P, P, P, P, i, P,
-                                                P, P, P, P, i, i, P, i, i, i, P, P, P, P, P, P, P, i]
+                                                P, P, P, P, i, i, P, i, i, i, P, P, P, P, P, P, P, i, i, d]
         lib.oracle_elastic_gradient.restype = i
         lib.oracle_vd_forward.argtypes = [i, P, P, d, i, P, P, i, P, i, i, P, P, i, P, P, i, i, P]
         lib.oracle_vd_forward.restype = i
@@ -286,9 +286,10 @@ def elastic_forward(lam, mu, rho, h, dt, halo, freetop, cpml, shot, *, interp_rh
 
 def elastic_gradient(lam, mu, rho, h, dt, halo, freetop, cpml, shot, observed, *, invcov=None, windows=(),
                      check_freq=1, mute_src=0, mute_rec=0, src_pos=None, rec_pos=None, interp_rho=0,
-                     interp_mu=0, f32=False, nthreads=0):
+                     interp_mu=0, f32=False, nthreads=0, ccts_dt=None):
     """swgradient_1shot! (elastic 2D) plus calcmisfit.  Returns
-    (dict(rho=, lambda=, mu=) float64 (nx, nz), misfit, traces (nt, 2, nrec))."""
+    (dict(rho=, lambda=, mu=) float64 (nx, nz), misfit, traces (nt, 2, nrec)).
+    ``ccts_dt``: CCTSMisfit(ccts_dt) per component trace instead of the L2 misfit."""
     (lam, mu, rho, n, hh, kind, tf, nt, nsrc, mt, sc, sij, scoef, nrec, rcn, rij, rcoef,
      cp) = _elastic_common(lam, mu, rho, h, cpml, shot)
     observed = np.asfortranarray(observed, dtype=np.float64)
@@ -313,7 +314,8 @@ def elastic_gradient(lam, mu, rho, h, dt, halo, freetop, cpml, shot, observed, *
                                         _p(rij), _p(rcoef), _p(observed), _p(ic), ikind, nwin, _p(win),
                                         int(check_freq), int(mute_src), int(mute_rec), _p(sp), _p(rp),
                                         _p(traces), _p(g["rho"]), _p(g["lambda"]), _p(g["mu"]), _p(misfit),
-                                        int(nthreads or max_threads()))
+                                        int(nthreads or max_threads()), 0 if ccts_dt is None else 1,
+                                        float(ccts_dt or 0.0))
     if rc != 0:
         raise RuntimeError(f"oracle_elastic_gradient failed ({rc})")
     return g, float(misfit[0]), traces

@@ -537,7 +537,7 @@ int run_gradient(const int* n, const double* h, double dt, int halo, int freetop
                  const double* observed, const double* invcov, int invcov_kind, int nwin, const int* windows,
                  int check_freq, int mute_src, int mute_rec, const double* src_pos, const double* rec_pos,
                  double* traces_out, double* g_rho, double* g_lam, double* g_mu, double* misfit_out,
-                 int nthreads) {
+                 int nthreads, int ccts, double ccts_dt) {
   const int nt = sh.nt, nx = n[0], nz = n[1];
   if (check_freq < 1 || check_freq >= nt) return 1;  // LinearCheckpointer assertion
   ElasticSim<T> sim(nx, nz, h, dt, halo, freetop != 0, nthreads);
@@ -595,6 +595,15 @@ int run_gradient(const int* n, const double* h, double dt, int halo, int freetop
   double msf = 0;
   for (long q = 0; q < ntot; ++q) msf += res[q] * cres[q];
   *misfit_out = msf / 2;
+  if (ccts) {  // CCTSMisfit{T,3}: per receiver and component, dtau^2/2 and dtau/N ds/dt (CCTSMisfit.jl:30-44, :63-80)
+    std::vector<double> syn(nt);
+    msf = 0;
+    for (long c = 0; c < 2L * sh.nrec; ++c) {
+      for (int t = 0; t < nt; ++t) syn[t] = (double)tr[t + c * nt];
+      msf += oracle::ccts_trace(observed + c * nt, syn.data(), nt, ccts_dt, cres.data() + c * nt);
+    }
+    *misfit_out = msf;
+  }
   std::vector<T> adjsrc(ntot);
   for (long q = 0; q < ntot; ++q) adjsrc[q] = (T)(-cres[q]);
 
@@ -765,17 +774,18 @@ int oracle_elastic_gradient(int use_f32, const int* n, const double* h, double d
                             const double* rec_coef, const double* observed, const double* invcov,
                             int invcov_kind, int nwin, const int* windows, int check_freq, int mute_src,
                             int mute_rec, const double* src_pos, const double* rec_pos, double* traces_out,
-                            double* g_rho, double* g_lam, double* g_mu, double* misfit_out, int nthreads) {
+                            double* g_rho, double* g_lam, double* g_mu, double* misfit_out, int nthreads,
+                            int ccts, double ccts_dt) {
   if (n[0] < 5 || n[1] < 5 || (kind != 0 && kind != 1)) return 1;
   ElShot sh = make_shot<double>(nt, kind, nsrc, srctf, momtens, src_cnt, src_ij, src_coef, nrec, rec_cnt,
                                 rec_ij, rec_coef);
   if (use_f32)
     return run_gradient<float>(n, h, dt, halo, freetop, lam, mu, rho, irho, imu, cpml, sh, observed, invcov,
                                invcov_kind, nwin, windows, check_freq, mute_src, mute_rec, src_pos, rec_pos,
-                               traces_out, g_rho, g_lam, g_mu, misfit_out, nthreads);
+                               traces_out, g_rho, g_lam, g_mu, misfit_out, nthreads, ccts, ccts_dt);
   return run_gradient<double>(n, h, dt, halo, freetop, lam, mu, rho, irho, imu, cpml, sh, observed, invcov,
                               invcov_kind, nwin, windows, check_freq, mute_src, mute_rec, src_pos, rec_pos,
-                              traces_out, g_rho, g_lam, g_mu, misfit_out, nthreads);
+                              traces_out, g_rho, g_lam, g_mu, misfit_out, nthreads, ccts, ccts_dt);
 }
 
 }  // extern "C"

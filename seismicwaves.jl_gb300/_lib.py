@@ -64,7 +64,7 @@ class SwElasticShot(ctypes.Structure):
     _fields_ = [("nt", i32), ("kind", i32), ("nsrc", i32), ("srctf", vp_), ("momtens", vp_),
                 ("src", SwPointTable * 2), ("nrec", i32), ("rec", SwPointTable * 2), ("traces", vp_),
                 ("cpml", vp_), ("observed", vp_), ("invcov_diag", vp_), ("nwin", i32), ("windows", vp_),
-                ("src_pos", vp_), ("rec_pos", vp_), ("invcov", vp_)]
+                ("src_pos", vp_), ("rec_pos", vp_), ("invcov", vp_), ("misfit_kind", i32), ("misfit_dt", f64)]
 
 
 class SwError(RuntimeError):

@@ -1,6 +1,7 @@
-// Cross-correlation time-shift misfit (CCTSMisfit, src/inversion/misfits/CCTSMisfit.jl:17-61)
-// on the device, shared by the scalar-receiver paths (constant- and
-// variable-density acoustic).
+// Cross-correlation time-shift misfit (CCTSMisfit, src/inversion/misfits/CCTSMisfit.jl:17-80)
+// on the device, shared by the acoustic paths (constant and variable density,
+// one trace per receiver) and the elastic one (one trace per receiver and
+// component: the (nt, 2, nrec) records are 2 nrec traces of nt samples).
 //
 // Per trace (observed u, synthetic v, nt samples):
 //   xcorr(u, v) = conv(u, reverse(v)) (DSP.jl), 2 nt - 1 values; at 1-based
@@ -9,7 +10,10 @@
 //   dchi/du = dtau / N * ds/dt, ds/dt central differences (first sample
 //   (v[2] - 0) / 2dt, last sample 0), N = trapezoidal integral of (ds/dt)^2
 //   over the times dt .. nt dt.
-// The adjoint source is -dchi/du times the receiver's prescale factor.
+// The adjoint source is -dchi/du times the receiver's prescale factor (1
+// without a prescale field); amax (if given) takes the running maximum of
+// its magnitude as float bits (the elastic path scales its adjoint sources by
+// a power of two chosen from it).
 //
 // One block per trace.  u and a zero-padded copy of v (3 nt - 2 values) sit
 // in shared memory; lane l of warp w evaluates the 8 lags
@@ -46,7 +50,8 @@ inline size_t ccts_smem_bytes(int nt) { return (size_t)(4 * nt) * sizeof(float);
 // gridDim = (max receivers, shots); partial[shot * gridDim.x + r] = dtau^2 (0 when unused)
 __global__ void __launch_bounds__(CCTS_THREADS) k_ccts(const CctsShot* __restrict__ shots,
                                                        const float* __restrict__ prescale,
-                                                       double* __restrict__ partial) {
+                                                       double* __restrict__ partial,
+                                                       unsigned int* __restrict__ amax = nullptr) {
   extern __shared__ float sm[];
   const int r = blockIdx.x, s = blockIdx.y;
   const CctsShot S = shots[s];
@@ -133,9 +138,17 @@ __global__ void __launch_bounds__(CCTS_THREADS) k_ccts(const CctsShot* __restric
     __syncthreads();
   }
   const double f = dtau / rn[0];
-  const float pre = prescale[S.rec_lin[r]];
+  const float pre = prescale ? prescale[S.rec_lin[r]] : 1.0f;
   float* adj = S.adj + (long long)r * nt;
-  for (int t = threadIdx.x; t < nt; t += blockDim.x) adj[t] = (-(float)(f * dsdt(t))) * pre;
+  float mx = 0.0f;
+  for (int t = threadIdx.x; t < nt; t += blockDim.x) {
+    adj[t] = (-(float)(f * dsdt(t))) * pre;
+    mx = fmaxf(mx, fabsf(adj[t]));
+  }
+  if (amax) {
+    for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(amax, __float_as_uint(mx));  // non-negative floats order like their bits
+  }
   if (threadIdx.x == 0) *part = dtau * dtau;  // the sum kernels apply the 1/2
 }
 

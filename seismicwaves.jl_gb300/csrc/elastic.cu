@@ -52,6 +52,7 @@
 #include <vector>
 
 #include "internal.h"
+#include "ccts.cuh"
 
 namespace swgb {
 namespace el {
@@ -677,6 +678,7 @@ struct ShotDesc {
   const float* icd;          // dense inverse covariance (nt, nt) or null
   float* resid;              // dense case: masked residuals (nt, 2 nrec)
   const float* cres;         // dense case: C^-1 r (nt, 2 nrec), from the dense product (dense.cu)
+  int mkind;                 // 0 L2, 1 CCTS (k_ccts writes this shot's adjoint source)
 };
 
 // sigma_xx += Mxx w tf, sigma_zz += Mzz w tf (table 0), sigma_xz += Mxz w tf (table 1)
@@ -786,7 +788,7 @@ __global__ void k_el_misfit(const ShotDesc* __restrict__ desc, double* __restric
                             unsigned int* __restrict__ amax) {
   const int shot = blockIdx.y;
   const ShotDesc& D = desc[shot];
-  const long long total = (long long)D.nt * 2 * D.nrec;
+  const long long total = D.mkind == 1 ? 0 : (long long)D.nt * 2 * D.nrec;  // CCTS shots: k_ccts
   double acc = 0.0;
   float mx = 0.0f;
   for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < total;
@@ -1238,6 +1240,7 @@ struct sw_elastic {
   int tz = 8;  // rows per block of the stencil kernels (8, 16 or 32; 8 measured fastest)
   bool vec = true;  // four x points per thread (k_el_*4) instead of one
   DevMem d_scales;        // [0] the forward sources' common scale, [1] the adjoint source's scale
+  DevMem d_ccts, d_partial2;  // CCTS descriptors and per-trace misfit terms
   DevMem d_gout, d_mout;  // gradient / misfit of the host-buffer path (stable addresses for the graphs)
   // CUDA graphs of a group's whole gradient (forward, misfit, adjoint,
   // reduction), keyed by what the captured launches depend on
@@ -1379,6 +1382,17 @@ void validate_shot(const sw_elastic* es, const sw_elastic_shot& s, int k, bool g
   if (grad) {
     if (!s.observed) { os << "shot " << k << ": observed traces are required"; fail(SW_ERR_ARG, os.str()); }
     if (es->gp.check_freq >= s.nt) fail(SW_ERR_ARG, "Checkpointing frequency must be smaller than the number of timesteps!");
+    if (s.misfit_kind != 0 && s.misfit_kind != 1) {
+      os << "shot " << k << ": misfit_kind must be 0 (L2) or 1 (CCTS)";
+      fail(SW_ERR_ARG, os.str());
+    }
+    if (s.misfit_kind == 1) {
+      if (!(s.misfit_dt > 0)) fail(SW_ERR_ARG, "Timestep size must be positive!");
+      if (s.nt > 13000) {
+        os << "shot " << k << ": the device CCTS misfit takes records of at most 13000 samples";
+        fail(SW_ERR_UNSUPPORTED, os.str());
+      }
+    }
     for (int w = 0; w < s.nwin; ++w) {
       const int a = s.windows[2 * w], b = s.windows[2 * w + 1];
       if (!(1 <= a && a <= b && b <= s.nt))
@@ -1622,6 +1636,7 @@ void build_tables(sw_elastic* es, const sw_elastic_shot* shots, const std::vecto
     D.ic = (grad && s.invcov_diag) ? es->d_ic.as<float>() + ic_off[k] : nullptr;
     D.mask = o.has_mask ? FL + o.mask : nullptr;
     D.adjsrc = grad ? es->d_adj.as<float>() + tr_off[k] : nullptr;
+    D.mkind = grad ? s.misfit_kind : 0;
   }
   long long icd_o = 0, dres_o = 0;
   for (int k = 0; k < S; ++k) {
@@ -2198,6 +2213,28 @@ void elastic_gradient(sw_elastic* es, int nshots, const sw_elastic_shot* shots, 
     const int nblk = 64;
     ensure(es, es->d_partial, (size_t)nblk * S * sizeof(double), "misfit partials");
     ensure(es, es->d_amax, 16, "max reduction");
+    size_t ccts_smem = 0;
+    int ccts_rec = 0;
+    {  // CCTS shots: one trace per receiver component, no prescale
+      std::vector<int> kind(S), nt(S), nrec(S);
+      std::vector<double> mdt(S);
+      std::vector<const float*> tr(S), obs(S);
+      std::vector<float*> adj(S);
+      std::vector<const long long*> rl(S, nullptr);
+      for (int k = 0; k < S; ++k) {
+        const sw_elastic_shot& s = shots[group[k].orig];
+        kind[k] = s.misfit_kind;
+        mdt[k] = s.misfit_dt;
+        nt[k] = desc[k].nt;
+        nrec[k] = 2 * desc[k].nrec;
+        tr[k] = desc[k].tr;
+        obs[k] = desc[k].obs;
+        adj[k] = desc[k].adjsrc;
+      }
+      ensure(es, es->d_ccts, (size_t)S * sizeof(CctsShot), "CCTS table");
+      ccts_rec = upload_ccts(es->ctx, es->d_ccts.as<CctsShot>(), kind, mdt, nt, nrec, tr, obs, adj, rl, &ccts_smem);
+      if (ccts_rec) ensure(es, es->d_partial2, (size_t)ccts_rec * S * sizeof(double), "CCTS partials");
+    }
     {
       const std::vector<float> sc = {sf_ref, 1.0f};
       upload(es, es->d_scales, sc, "source scales");
@@ -2242,6 +2279,14 @@ void elastic_gradient(sw_elastic* es, int nshots, const sw_elastic_shot* shots, 
         k_el_misfit<<<dim3(nblk, S), 256, 0, st>>>(R.ddesc, es->d_partial.as<double>(), es->d_amax.as<unsigned>());
         check_cuda(cudaGetLastError(), "misfit launch");
         k_el_misfit_sum<<<1, 256, 0, st>>>(es->d_partial.as<double>(), nblk * S, mout, first_group ? 0 : 1);
+        if (ccts_rec) {  // CCTS shots: misfit terms and adjoint sources per component trace
+          k_ccts<<<dim3(ccts_rec, S), CCTS_THREADS, ccts_smem, st>>>(es->d_ccts.as<CctsShot>(), nullptr,
+                                                                     es->d_partial2.as<double>(),
+                                                                     es->d_amax.as<unsigned>());
+          check_cuda(cudaGetLastError(), "CCTS misfit launch");
+          k_el_misfit_sum<<<1, 256, 0, st>>>(es->d_partial2.as<double>(), ccts_rec * S, mout, 1);
+          check_cuda(cudaGetLastError(), "CCTS misfit sum launch");
+        }
         check_cuda(cudaGetLastError(), "misfit sum launch");
         es->ctx->prof.end(st, KK_OTHER, ev);
       }

@@ -387,6 +387,8 @@ class ElasticIsoCPMLWaveSimulation:
                 assert obs.shape == (nt, 2, nrec), "observed data shape must be (nt, 2, nrec)"
                 st.observed = obs.ctypes.data
                 arrs.append(obs)
+                if getattr(m, "kind", 0) == 1:  # CCTSMisfit, per component trace
+                    st.misfit_kind, st.misfit_dt = 1, m.dt
                 diag = m.invcov_diagonal()
                 if diag is not None:
                     diag = np.ascontiguousarray(diag, dtype=np.float32)
@@ -449,8 +451,6 @@ class ElasticIsoCPMLWaveSimulation:
     def run_gradient(self, shots, misfits):
         assert self.gradient, "The wavesim object was not built for gradient computations. (Was `gradient=true` specified?)"
         assert len(misfits) == len(shots)
-        if any(getattr(m, "kind", 0) == 1 for m in misfits):
-            raise NotImplementedError("the GB300 elastic gradient takes the L2 misfit (CCTSMisfit: acoustic paths)")
         self.init_shots(shots)
         structs, keep = self._shot_structs(shots, misfits)
         g = {k: np.zeros(self.grid.size, dtype=np.float64, order="F") for k in ("rho", "lambda", "mu")}

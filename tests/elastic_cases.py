@@ -130,13 +130,13 @@ def oracle_forward(case, shot, f32=False):
 
 
 def oracle_gradient(case, shot, observed, *, check_freq=1, invcov=None, windows=(), mute_src=0, mute_rec=0,
-                    f32=False):
+                    f32=False, ccts_dt=None):
     import oracle
     return oracle.elastic_gradient(case.lam, case.mu, case.rho, (case.h, case.h), case.dt, case.halo, case.freetop,
                                    cpml(case, shot), oracle_shot(case, shot), observed, invcov=invcov,
                                    windows=windows, check_freq=check_freq, mute_src=mute_src, mute_rec=mute_rec,
                                    src_pos=shot.src, rec_pos=shot.rec, interp_rho=case.interp_rho,
-                                   interp_mu=case.interp_mu, f32=f32)
+                                   interp_mu=case.interp_mu, f32=f32, ccts_dt=ccts_dt)
 
 
 class GpuElastic:
@@ -165,7 +165,7 @@ class GpuElastic:
             self.ctx.lib.sw_elastic_destroy(self.h)
             self.h = ctypes.c_void_p()
 
-    def _structs(self, shots, observed=None, invcov=None, windows=None):
+    def _structs(self, shots, observed=None, invcov=None, windows=None, ccts_dt=None):
         L = sw._lib
         keep, structs = [], (L.SwElasticShot * len(shots))()
         for k, shot in enumerate(shots):
@@ -191,6 +191,8 @@ class GpuElastic:
                 obs = np.asfortranarray(observed[k], dtype=np.float32)
                 st.observed = obs.ctypes.data
                 arrs.append(obs)
+                if ccts_dt is not None:
+                    st.misfit_kind, st.misfit_dt = 1, ccts_dt
                 if invcov is not None and invcov[k] is not None:
                     if np.ndim(invcov[k]) == 2:  # dense (nt, nt)
                         ic = np.asfortranarray(invcov[k], dtype=np.float32)
@@ -215,8 +217,8 @@ class GpuElastic:
         self.ctx.check(self.ctx.lib.sw_elastic_forward(self.h, len(shots), structs, 0), "sw_elastic_forward")
         return [k[0].astype(np.float64) for k in keep]
 
-    def gradient(self, shots, observed, invcov=None, windows=None):
-        structs, keep = self._structs(shots, observed, invcov, windows)
+    def gradient(self, shots, observed, invcov=None, windows=None, ccts_dt=None):
+        structs, keep = self._structs(shots, observed, invcov, windows, ccts_dt)
         nx, nz = self.case.nx, self.case.nz
         g = {k: np.zeros((nx, nz), dtype=np.float64, order="F") for k in ("rho", "lambda", "mu")}
         m = np.zeros(1)

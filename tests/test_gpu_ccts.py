@@ -1,6 +1,7 @@
 """GPU parity of the device CCTS misfit (k_ccts) on the constant- and
-variable-density acoustic gradients, against the FP64 oracle's restatement
-of CCTSMisfit.jl:17-80.  The per-trace time shifts are integers times dt, so
+variable-density acoustic gradients and on the elastic gradient (one trace
+per receiver component), against the FP64 oracle's restatement of
+CCTSMisfit.jl:17-80.  The per-trace time shifts are integers times dt, so
 the misfit matches to FP64 rounding once every argmax agrees; the gradient is
 held to the usual 1e-5."""
 import numpy as np
@@ -68,6 +69,27 @@ def test_ccts_gradient_variable_density_matches_oracle(ctx):
     run.close()
     errs = {k: rel_l2(g[k], gref[k]) for k in g}
     print(f"CCTS VD: misfit {m:.6e} vs {mref:.6e}, " + " ".join(f"{k} {v:.2e}" for k, v in errs.items()))
+    assert mref > 0 and m == pytest.approx(mref, rel=1e-9)
+    for k, v in errs.items():
+        assert v < 1e-5, k
+
+
+def test_ccts_gradient_elastic_matches_oracle(ctx):
+    """CCTSMisfit{T,3} on vector receivers (CCTSMisfit.jl:30-44, :63-80): a
+    time shift per receiver and component, summed into the misfit; the
+    adjoint sources carry the elastic path's power-of-two scale."""
+    import elastic_cases as EC
+    case = EC.small_case(nt=500, seed=3)
+    shot = case.shots[0]
+    pert = EC.ElCase(case.nx, case.nz, case.h, case.dt, case.halo, case.lam * 1.15, case.mu * 0.9, case.rho,
+                     [shot], freetop=case.freetop, sinc=case.sinc)
+    obs = EC.oracle_forward(pert, shot).astype(np.float32).astype(np.float64)
+    gref, mref, _ = EC.oracle_gradient(case, shot, obs, check_freq=20, ccts_dt=case.dt)
+    run = EC.GpuElastic(ctx, case, gradient=True, check_freq=20)
+    g, m, _ = run.gradient([shot], [obs], ccts_dt=case.dt)
+    run.close()
+    errs = {k: rel_l2(g[k], gref[k]) for k in g}
+    print(f"CCTS elastic: misfit {m:.6e} vs {mref:.6e}, " + " ".join(f"{k} {v:.2e}" for k, v in errs.items()))
     assert mref > 0 and m == pytest.approx(mref, rel=1e-9)
     for k, v in errs.items():
         assert v < 1e-5, k

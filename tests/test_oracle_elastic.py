@@ -197,3 +197,22 @@ def test_elastic_gradients_finite_difference():
         fd = (ms[0] - ms[1]) / (2 * eps)
         an = float(np.sum(g[name] * dv))
         assert abs(fd) > 0 and abs(an - fd) <= 1e-4 * abs(fd), name
+
+
+def test_elastic_ccts_misfit_matches_host_definition():
+    """The oracle's elastic CCTS misfit equals the host restatement of
+    CCTSMisfit{T,3} (seismicwaves.jl_gb300/api.py, numpy correlate) on the
+    oracle's own traces: one time shift per receiver and component."""
+    import elastic_cases as EC
+
+    import __graft_entry__
+    sw = __graft_entry__.load_package()
+    case = EC.small_case(nt=240, nx=70, nz=60, halo=10, seed=4)
+    shot = case.shots[0]
+    pert = EC.ElCase(case.nx, case.nz, case.h, case.dt, case.halo, case.lam * 1.2, case.mu, case.rho * 0.9,
+                     [shot], freetop=case.freetop, sinc=case.sinc)
+    obs = EC.oracle_forward(pert, shot)
+    _, m, tr = EC.oracle_gradient(case, shot, obs, check_freq=10, ccts_dt=case.dt)
+    mis = sw.CCTSMisfit(case.dt, observed=obs)
+    recs = type("R", (), {"seismograms": tr})()
+    assert m > 0 and m == pytest.approx(mis.calcmisfit(recs), rel=1e-12)
