@@ -49,7 +49,8 @@ def _args():
     p.add_argument("--nt", type=int, default=0, help="cap every shot's time steps (small profiling cases)")
     p.add_argument("--tz", type=int, default=0, help="stencil tile height (0 = library heuristic)")
     p.add_argument("--variant", type=int, default=-1, help="2D stencil variant (-1 = library default)")
-    p.add_argument("--autotune", action="store_true", help="pick variant and band height with the autotuner")
+    p.add_argument("--no-autotune", action="store_true",
+                   help="skip the autotuner (it runs by default unless --tz or --variant is given)")
     p.add_argument("--forward-only", action="store_true", help="time the batched forward instead of the gradient")
     p.add_argument("--bf16", type=int, default=0, help="acoustic snapshot_bf16 (0 FP32, 1 BF16 recompute buffer, "
                                                       "2 also BF16 checkpoints)")
@@ -154,6 +155,28 @@ class ClockSampler:
 
 
 # ----------------------------------------------------------------------------- GPU driver
+def _cap(arr, nt_cap):
+    """Cap every shot's time steps (short autotuning trials)."""
+    if nt_cap:
+        for st in arr:
+            st.nt = min(st.nt, nt_cap)
+
+
+def _tune_tz(R, w, kind, candidates):
+    """Band height of a variable-density or elastic simulation from capped gradient trials (2 K + 2 steps)."""
+    from seismicwaves_gb300 import tune
+
+    setter = R.lib.sw_acoustic_vd_set_tuning if kind == "vd" else R.lib.sw_elastic_set_tuning
+    idx = list(range(len(w.shots)))
+    cap = 2 * w.check_freq + 2
+    t0 = time.perf_counter()
+    tz, timings = tune.autotune_tz((kind, w.name, len(idx)), lambda t: R.ctx.check(setter(R.h, t), "set_tuning"),
+                                   lambda: R.gradient_device(idx, cap), candidates)
+    return tz, {"tz": tz, "trial_ms": {str(t): round(x * 1e3, 3) for t, x in timings.items()},
+                "tuning_s": round(time.perf_counter() - t0, 2),
+                "what": f"band height from batched gradients capped at {cap} steps, best of 2 per candidate"}
+
+
 class GradientRun:
     """The workload's shots as C-ABI structs over device (or pinned host) buffers."""
 
@@ -337,9 +360,10 @@ class ElasticRun:
         self.ctx.check(self.lib.sw_elastic_forward(self.h, len(idx), arr, 1), "observed forward")
         self.set_material(self.w.lam, self.w.mu, self.w.rho)
 
-    def gradient_device(self, idx):
+    def gradient_device(self, idx, nt_cap=0):
         arr = self.structs(idx, [x.data_ptr() for x in self.tf_d], [x.data_ptr() for x in self.tr_d],
                            [x.data_ptr() for x in self.obs_d])
+        _cap(arr, nt_cap)
         n = self.grad_d.numel() // 3
         p = self.grad_d.data_ptr()
         self.ctx.check(self.lib.sw_elastic_gradient(self.h, len(idx), arr, 1, p, p + 8 * n, p + 16 * n,
@@ -421,9 +445,10 @@ class VDRun(GradientRun):
         self.ctx.check(self.lib.sw_acoustic_vd_forward(self.h, len(idx), arr, 1), "observed forward")
         self.set_material(self.w.vp, self.w.rho)
 
-    def gradient_device(self, idx):
+    def gradient_device(self, idx, nt_cap=0):
         arr = self.structs(idx, [x.data_ptr() for x in self.tf_d], [x.data_ptr() for x in self.tr_d],
                            [x.data_ptr() for x in self.obs_d])
+        _cap(arr, nt_cap)
         n = self.grad_d.numel() // 2
         p = self.grad_d.data_ptr()
         self.ctx.check(self.lib.sw_acoustic_vd_gradient(self.h, len(idx), arr, 1, p, p + 8 * n,
@@ -485,9 +510,12 @@ def measure_vd(a, name="acoustic_vd2d_2001x801", shots=0, nt_cap=0, steps=None, 
     warmup = a.warmup if warmup is None else warmup
     sw, w = _workload(name, shots, nt_cap)
     R = VDRun(sw, w, device)
+    tuned, tz = None, a.tz or 8
     if a.tz:
         R.ctx.check(R.lib.sw_acoustic_vd_set_tuning(R.h, a.tz), "sw_acoustic_vd_set_tuning")
     R.make_observed()
+    if not (a.tz or a.no_autotune):
+        tz, tuned = _tune_tz(R, w, "vd", (8, 16, 32))
     nshots = len(w.shots)
     allidx = list(range(nshots))
     pts = float(w.point_steps())
@@ -531,7 +559,7 @@ def measure_vd(a, name="acoustic_vd2d_2001x801", shots=0, nt_cap=0, steps=None, 
            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
            "config": {"workload": w.name, "grid": list(w.vp.shape), "h_m": w.h[0], "shots": nshots,
                       "nt": max(s.nt for s in w.shots), "check_freq": w.check_freq, "halo": w.halo,
-                      "tz": a.tz or 8,
+                      "tz": tz, "tuning": tuned,
                       "cache": "inputs larger than L2 (each step streams several GB of wavefield state)",
                       "precision": "fp32 wavefields and stencil, fp32 sums over one checkpoint window, "
                                    "fp64 window totals, misfit and shot sum"},
@@ -746,6 +774,16 @@ def _extra_acoustic3d(a, device):
     R = GradientRun(sw, w, device, bf16=1)
     R.make_observed()
     idx = list(range(len(w.shots)))
+    tuned = None
+    if not a.no_autotune:
+        from seismicwaves_gb300 import tune
+
+        arr = R.structs(idx, [x.data_ptr() for x in R.tf_d], [x.data_ptr() for x in R.tr_d], None)
+        t0 = time.perf_counter()
+        r = tune.autotune(R.ctx, R.h, (w.vp.shape, w.halo), arr, len(idx), 3, steps=12, on_device=1)
+        tuned = {"variant": r["variant"], "tz": r["tz"], "tuning_s": round(time.perf_counter() - t0, 2),
+                 "trial_ms": {"/".join(map(str, k)): round(t * 1e3, 3) for k, t in r["trial_s"].items()},
+                 "what": "batched forwards of 12 steps, best of 2 per candidate"}
     R.gradient_device(idx)
     torch.cuda.synchronize(R.dev)
     clocks = ClockSampler(device)
@@ -765,7 +803,7 @@ def _extra_acoustic3d(a, device):
     out = {"workload": w.name, "grid": list(w.vp.shape), "shots": len(w.shots), "nt": max(s.nt for s in w.shots),
            "check_freq": w.check_freq, "buffer": "bf16 recompute buffer", "value": pts / t / 1e9, "unit": UNIT,
            "ms_per_step": t * 1e3, "shots_per_s": len(w.shots) / t, "steps": 1, "warmup": 1, "kernels": kern,
-           "clocks": clk}
+           "clocks": clk, "tuning": tuned}
     R.lib.sw_wavesim_destroy(R.h)
     return out
 
@@ -806,15 +844,28 @@ def run_gb300(a):
         R.ctx.check(R.lib.sw_wavesim_set_tuning(R.h, a.tz, max(a.variant, 0)), "sw_wavesim_set_tuning")
     R.make_observed()
     tuned = None
-    if a.autotune:
+    veff = a.variant
+    if not (a.no_autotune or a.tz or a.variant >= 0):
         from seismicwaves_gb300 import tune
 
         allidx0 = list(range(len(w.shots)))
-        arr = R.structs(allidx0, [x.data_ptr() for x in R.tf_d], [x.data_ptr() for x in R.tr_d], None)
-        choice, timings = tune.autotune(R.ctx, R.h, (w.vp.shape, w.halo), arr, len(allidx0), w.vp.ndim,
-                                        on_device=1)
-        tuned = {"variant": choice[0], "tz": choice[1],
-                 "trial_ms": {f"{v}/{tz}": round(t * 1e3, 3) for (v, tz), t in timings.items()}}
+        arr = R.structs(allidx0, [x.data_ptr() for x in R.tf_d], [x.data_ptr() for x in R.tr_d],
+                        [x.data_ptr() for x in R.obs_d])
+        t0 = time.perf_counter()
+        r = tune.autotune(R.ctx, R.h, (w.vp.shape, w.halo), arr, len(allidx0), w.vp.ndim, on_device=1,
+                          gradient_out=(R.grad_d.data_ptr(), R.mis_d.data_ptr()), check_freq=w.check_freq)
+        veff = r["variant"]
+        bands = r["band_heights"]
+        tuned = {"variant": r["variant"], "tz": r["tz"],
+                 "band_heights": dict(zip(("forward", "recompute", "adjoint"), bands)) if bands else None,
+                 "trial_ms": {"/".join(map(str, k)): round(t * 1e3, 3) for k, t in r["trial_s"].items()},
+                 "per_kind_ms": {f"{v}/{tz}": {n: round(x, 3) for n, x in d.items()}
+                                 for (v, tz), d in r["per_kind_ms"].items()},
+                 "band_ms": {str(tz): {n: round(x, 3) for n, x in d.items()} for tz, d in r["band_ms"].items()},
+                 "tuning_s": round(time.perf_counter() - t0, 2),
+                 "what": "trials: batched gradients of the workload's shots capped at 2 K + 2 steps; each "
+                         "candidate's best of 2 timed trials, per-kind ms from one event-timed trial; then "
+                         "each stencil kind's band height from its own time"}
     nshots = len(w.shots)
     allidx = list(range(nshots))
     pts = float(w.point_steps())
@@ -884,13 +935,13 @@ def run_gb300(a):
     # roofline of the dominant kernel (largest total time among the stencil kinds)
     nd = w.vp.ndim
     base = "k_ac2d_step" if nd == 2 else "k_ac3d_step"
-    if nd == 2 and a.variant >= 0 and (a.variant & 256) and nshots >= 4:
+    if nd == 2 and veff >= 0 and (veff & 256) and nshots >= 4:
         adj, adj_what = "k_ac2d_adj_grp", "adjoint + correlation (4 shots per block, Kahan sums)"
     elif nd == 2:
         adj, adj_what = base + "<3>", "adjoint + correlation (plain FP32 sums, FP64 flush every 32 steps)"
     else:
         adj, adj_what = base + "<2>", "adjoint + correlation (Kahan sums)"
-    two = "k_ac2d_pair (two steps per launch) / " if (nd == 2 and a.variant >= 0 and a.variant & 1024) else ""
+    two = "k_ac2d_pair (two steps per launch) / " if (nd == 2 and veff >= 0 and veff & 1024) else ""
     kinds = {0: (f"{two}{base}<0/1> forward", f"{base}<1>", "forward"),
              4: (f"{two}{base}<1> recompute (writes D)", f"{base}<1>", "recompute"),
              1: (f"{two}{adj} {adj_what}", adj, "adjoint")}
@@ -934,7 +985,7 @@ def run_gb300(a):
                        "cache": "inputs larger than L2 (each step streams tens of GB of wavefield state)",
                        "precision": "fp32 wavefields and stencil, "
                                     + ("fp32 correlation sums flushed to fp64 every 32 steps"
-                                       if (nd == 2 and not (a.variant >= 0 and (a.variant & 256)))
+                                       if (nd == 2 and not (veff >= 0 and (veff & 256)))
                                        else "Kahan fp32 correlation")
                                     + ", fp64 misfit and shot sum"
                                     + (", bf16 recompute buffer" if a.bf16 >= 1 else "")
@@ -978,9 +1029,12 @@ def measure_elastic(a, name="elastic2d_1200x600", shots=0, nt_cap=0, steps=None,
     warmup = a.warmup if warmup is None else warmup
     sw, w = _workload(name, shots, nt_cap)
     R = ElasticRun(sw, w, device)
+    tuned, tz = None, a.tz or 8
     if a.tz:
         R.ctx.check(R.lib.sw_elastic_set_tuning(R.h, a.tz), "sw_elastic_set_tuning")
     R.make_observed()
+    if not (a.tz or a.no_autotune):
+        tz, tuned = _tune_tz(R, w, "elastic", (8, 16, 32, 72))
     nshots = len(w.shots)
     allidx = list(range(nshots))
     pts = float(w.point_steps())
@@ -1021,7 +1075,7 @@ def measure_elastic(a, name="elastic2d_1200x600", shots=0, nt_cap=0, steps=None,
            "config": {"workload": w.name, "grid": list(w.lam.shape), "h_m": w.h[0], "shots": nshots,
                       "nt": max(s.nt for s in w.shots), "receivers": w.shots[0].rec_pos.shape[0],
                       "check_freq": w.check_freq, "halo": w.halo, "sources": "explosive moment tensor, sinc spread",
-                      "tz": a.tz or 8,
+                      "tz": tz, "tuning": tuned,
                       "cache": "inputs larger than L2 (each step streams several GB of wavefield state)",
                       "precision": "fp32 wavefields and stencil, Kahan fp32 correlation, fp64 misfit and shot sum"},
            "shots_per_s": nshots * steps / t_dev, "plain": pl,

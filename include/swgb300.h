@@ -216,6 +216,14 @@ int sw_acoustic_forward_snapshots(sw_wavesim* ws, int32_t nshots, const sw_acous
  * Results do not depend on any of them beyond rounding. */
 int sw_wavesim_set_tuning(sw_wavesim* ws, int32_t tz, int32_t variant);
 
+/* Band height (rows per block along the marching axis) of the one-step
+ * stencil per kind: the forward (and the forward of the gradient), the
+ * recompute of the gradient's adjoint phase, and the adjoint; 0 = the tz of
+ * sw_wavesim_set_tuning (or its heuristic).  Lets an autotuner pick each
+ * kind's band from that kind's own timing; results do not change.  No
+ * reference counterpart. */
+int sw_wavesim_set_band_heights(sw_wavesim* ws, int32_t tz_forward, int32_t tz_recompute, int32_t tz_adjoint);
+
 /* CUDA graphs (on by default): a batch's whole device-side time loop
  * (forward; for the gradient also misfit, adjoint and shot sum) is captured
  * into a graph on the second call with the same batch layout and replayed on

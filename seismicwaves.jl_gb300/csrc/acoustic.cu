@@ -460,6 +460,7 @@ struct sw_wavesim {
   DevMem d_icd, d_dres;  // dense inverse covariances; residuals and C^-1 r of those shots
   DevMem d_mute, d_mute_ptr;
   int tile_tz = 0;  // 0 = heuristic
+  int kind_tz[3] = {0, 0, 0};  // band height per stencil kind (forward, recompute, adjoint); 0 = tile_tz
   int variant = 0;  // 2D stencil: 0 = register-pipelined, 1 = TMA
   int pf = 0;       // 2D stencil: L2 prefetch distance in rows (0 = off)
   bool cpa = false; // 2D stencil (4 warps): rows staged through shared memory by cp.async
@@ -550,7 +551,8 @@ void run_graph(sw_wavesim* ws, std::vector<long long> key, Work&& work) {
 std::vector<long long> group_key(const sw_wavesim* ws, const std::vector<HostShot>& group, bool grad) {
   std::vector<long long> k = {grad ? 1 : 0, ws->grp, ws->variant, ws->tile_tz, ws->pf, ws->adjw ? 1 : 0,
                               ws->cpa ? 1 : 0, ws->pair_ok ? 1 : 0, ws->pair_adj_ok ? 1 : 0, ws->pair_tz,
-                              ws->pair_occ, (long long)group.size()};
+                              ws->pair_occ, ws->kind_tz[0], ws->kind_tz[1], ws->kind_tz[2],
+                              (long long)group.size()};
   for (const auto& h : group) k.push_back(h.nt);
   return k;
 }
@@ -970,7 +972,9 @@ int block_warps(const sw_wavesim* ws) { return (ws->variant & 3) == 2 ? 8 : (ws-
 // 3D: y rows (warps) per block, 4 or (variant 2) 8.
 int block_rows3d(const sw_wavesim* ws) { return (ws->variant & 3) == 2 ? 8 : 4; }
 
-StepCtx make_step_ctx(sw_wavesim* ws, int S) {
+enum { TZ_FORWARD = 0, TZ_RECOMPUTE = 1, TZ_ADJOINT = 2 };
+
+StepCtx make_step_ctx(sw_wavesim* ws, int S, int kind = TZ_FORWARD) {
   StepCtx c{ws, 0, 0, 1, 0};
   const int sms = ws->ctx->num_sms > 0 ? ws->ctx->num_sms : 148;
   const int nint = ws->n[ws->N - 1] - 2;  // interior extent of the marching axis
@@ -982,7 +986,7 @@ StepCtx make_step_ctx(sw_wavesim* ws, int S) {
     const int nw = block_rows3d(ws);
     c.tiles_y = (ws->n[1] - 2 + nw - 1) / nw;
   }
-  int TZ = ws->tile_tz;
+  int TZ = ws->kind_tz[kind] > 0 ? ws->kind_tz[kind] : ws->tile_tz;
   if (TZ <= 0) {
     if (ws->N == 2 && (ws->variant & 3) != 1) {
       // register-pipelined 2D stencil: short bands keep every SM at full
@@ -1514,7 +1518,7 @@ void adjoint_group(sw_wavesim* ws, const std::vector<HostShot>& group) {
     if (K > 1 && it % K == 0) {
       // recover segment m: forward steps (m-1)K+1 .. mK from the checkpoint at (m-1)K
       const int m = it / K;
-      const StepCtx c = make_step_ctx(ws, Sa);
+      const StepCtx c = make_step_ctx(ws, Sa, TZ_RECOMPUTE);
       float* cbase;
       long long cstride;
       if (m - 1 >= 1) {
@@ -1571,7 +1575,7 @@ void adjoint_group(sw_wavesim* ws, const std::vector<HostShot>& group) {
     // falls between them and the active shots stay the same
     const bool two = ws->pair_adj_ok && ws->adjw && it - 1 >= 1 && active_count(group, it - 1) == Sa &&
                      !(K > 1 && (it - 1) % K == 0) && (it - 1) % 32 != 0;
-    const StepCtx c = two ? make_pair_ctx(ws, Sa) : make_step_ctx(ws, Sa);
+    const StepCtx c = two ? make_pair_ctx(ws, Sa) : make_step_ctx(ws, Sa, TZ_ADJOINT);
     StepArgs a = base_args(ws, c, Sa);
     set_io(ws, a, ast, two, true);
     const long long dslot = K == 1 ? it - 1 : (it - 1) % K;
@@ -1998,6 +2002,11 @@ void wavesim_set_tuning(sw_wavesim* ws, int tz, int variant) {
   static const int pair_tz[8] = {0, 8, 16, 32, 64, 128, 4, 0};
   ws->pair_tz = pair_tz[(variant >> 11) & 7];
   ws->pair_occ = (variant >> 14) & 3;
+}
+void wavesim_set_band_heights(sw_wavesim* ws, int tz_forward, int tz_recompute, int tz_adjoint) {
+  ws->kind_tz[TZ_FORWARD] = tz_forward;
+  ws->kind_tz[TZ_RECOMPUTE] = tz_recompute;
+  ws->kind_tz[TZ_ADJOINT] = tz_adjoint;
 }
 void wavesim_use_graphs(sw_wavesim* ws, bool on) {
   ws->use_graphs = on;

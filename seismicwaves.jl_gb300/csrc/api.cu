@@ -18,6 +18,7 @@ void acoustic_forward(sw_wavesim* ws, int nshots, const sw_acoustic_shot* shots,
 void acoustic_gradient(sw_wavesim* ws, int nshots, const sw_acoustic_shot* shots, bool on_device, double* grad,
                        double* misfit);
 void wavesim_set_tuning(sw_wavesim* ws, int tz, int variant);
+void wavesim_set_band_heights(sw_wavesim* ws, int tz_forward, int tz_recompute, int tz_adjoint);
 void wavesim_use_graphs(sw_wavesim* ws, bool on);
 void acoustic_forward_snapshots(sw_wavesim* ws, int nshots, const sw_acoustic_shot* shots, bool on_device,
                                 int snapevery, float* const* snapshots);
@@ -300,6 +301,14 @@ int sw_profile_read(sw_ctx* ctx, int32_t kind, double* total_ms, int64_t* launch
 int sw_wavesim_set_tuning(sw_wavesim* ws, int32_t tz, int32_t variant) {
   if (!ws || tz < 0 || variant < 0 || variant >= (1 << 16)) return SW_ERR_ARG;
   swgb::wavesim_set_tuning(ws, tz, variant);
+  return SW_OK;
+}
+
+int sw_wavesim_set_band_heights(sw_wavesim* ws, int32_t tz_forward, int32_t tz_recompute, int32_t tz_adjoint) {
+  if (!ws || tz_forward < 0 || tz_recompute < 0 || tz_adjoint < 0 || tz_forward > 4096 || tz_recompute > 4096 ||
+      tz_adjoint > 4096)
+    return SW_ERR_ARG;
+  swgb::wavesim_set_band_heights(ws, tz_forward, tz_recompute, tz_adjoint);
   return SW_OK;
 }
 
