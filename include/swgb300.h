@@ -224,6 +224,15 @@ int sw_wavesim_set_tuning(sw_wavesim* ws, int32_t tz, int32_t variant);
  * reference counterpart. */
 int sw_wavesim_set_band_heights(sw_wavesim* ws, int32_t tz_forward, int32_t tz_recompute, int32_t tz_adjoint);
 
+/* Bounded waits of the TMA stencil (tuning variant 1): every mbarrier wait
+ * gives up after wait_cycles SM clock cycles (default 4e9, about 2 s), sets
+ * the context's error flag and leaves; the call then returns SW_ERR_TIMEOUT
+ * and the context stays usable.  withhold_stage >= 0 is a test hook: the
+ * producer warp of the launch's first block stops before issuing that stage
+ * of its row pipeline, so the consumers' wait on it runs out (nothing is in
+ * flight when they leave); -1 = off.  No reference counterpart. */
+int sw_wavesim_set_wait_test(sw_wavesim* ws, int64_t wait_cycles, int32_t withhold_stage);
+
 /* CUDA graphs (on by default): a batch's whole device-side time loop
  * (forward; for the gradient also misfit, adjoint and shot sum) is captured
  * into a graph on the second call with the same batch layout and replayed on

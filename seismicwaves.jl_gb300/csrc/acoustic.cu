@@ -460,6 +460,8 @@ struct sw_wavesim {
   DevMem d_icd, d_dres;  // dense inverse covariances; residuals and C^-1 r of those shots
   DevMem d_mute, d_mute_ptr;
   int tile_tz = 0;  // 0 = heuristic
+  long long wait_cycles = TMA_TIMEOUT_CYCLES;  // limit of one bounded device-side wait
+  int withhold = -1;                           // test hook of the TMA stencil (StepArgs::withhold)
   int kind_tz[3] = {0, 0, 0};  // band height per stencil kind (forward, recompute, adjoint); 0 = tile_tz
   int variant = 0;  // 2D stencil: 0 = register-pipelined, 1 = TMA
   int pf = 0;       // 2D stencil: L2 prefetch distance in rows (0 = off)
@@ -1249,6 +1251,8 @@ StepArgs base_args(sw_wavesim* ws, const StepCtx& c, int S) {
   a.tiles_z = c.tiles_z;
   a.TZ = c.TZ;
   a.err = ws->ctx->err.as<int>();
+  a.wait_cycles = ws->wait_cycles;
+  a.withhold = ws->withhold;
   a.pf = ws->pf;
   a.dbf16 = (ws->gradient && ws->gp.snapshot_bf16 >= 1) ? 1 : 0;
   return a;
@@ -2007,6 +2011,10 @@ void wavesim_set_band_heights(sw_wavesim* ws, int tz_forward, int tz_recompute, 
   ws->kind_tz[TZ_FORWARD] = tz_forward;
   ws->kind_tz[TZ_RECOMPUTE] = tz_recompute;
   ws->kind_tz[TZ_ADJOINT] = tz_adjoint;
+}
+void wavesim_set_wait_test(sw_wavesim* ws, long long wait_cycles, int withhold) {
+  ws->wait_cycles = wait_cycles;
+  ws->withhold = withhold;
 }
 void wavesim_use_graphs(sw_wavesim* ws, bool on) {
   ws->use_graphs = on;

@@ -65,6 +65,8 @@ struct StepArgs {
   int nshots;
   int tiles_x, tiles_y, tiles_z, TZ;
   int* err;                                        // set to 1 when a bounded wait gives up
+  long long wait_cycles;                           // limit of one bounded wait (clock64 cycles)
+  int withhold;  // TMA stencil test hook: block 0's producer never issues this stage (-1 = none)
   int pf;                                          // 2D stencil: rows ahead prefetched into L2 (0 = off)
   int dbf16;                                       // Dout / dcorr hold BF16 (the pointers are __nv_bfloat16 arrays)
 };
@@ -1437,7 +1439,7 @@ __global__ void __launch_bounds__(32 * NW) k_ac3d_fwd(const StepArgs A) {
 // ---------------------------------------------------------------------------
 constexpr int TMA_W = 512;            // x points per CTA tile
 constexpr int TMA_PROW = TMA_W + 8;   // p row in shared memory: 4 halo floats each side
-constexpr long long TMA_TIMEOUT_CYCLES = 4000000000LL;  // ~2 s at 2 GHz
+constexpr long long TMA_TIMEOUT_CYCLES = 4000000000LL;  // default wait limit, ~2 s at 2 GHz
 
 // Stage ring per mode: consumers hold 3 stages (p rows z-1, z, z+1), the rest
 // are in flight.  7 stages of 6.2 KB (forward) and 4 CTAs per SM, 6 stages
@@ -1472,12 +1474,12 @@ __device__ __forceinline__ bool mbar_try_wait(unsigned long long* b, unsigned pa
       : "memory");
   return ok != 0;
 }
-// returns false when the wait gave up
-__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* b, unsigned parity) {
+// returns false when the wait gave up after `limit` cycles
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* b, unsigned parity, long long limit) {
   if (mbar_try_wait(b, parity)) return true;
   const long long t0 = clock64();
   while (!mbar_try_wait(b, parity))
-    if (clock64() - t0 > TMA_TIMEOUT_CYCLES) return false;
+    if (clock64() - t0 > limit) return false;
   return true;
 }
 __device__ __forceinline__ void tma_load_1d(void* dst, const void* src, unsigned bytes, unsigned long long* b) {
@@ -1529,7 +1531,10 @@ __global__ void __launch_bounds__(160, TmaLayout<MODE>::MIN_BLOCKS) k_ac2d_tma(c
     const int aw = min(TMA_W, P - X0);
     for (int j = 0; j < nst; ++j) {
       const int slot = j % TMA_NS;
-      if (j >= TMA_NS && !mbar_wait_bounded(&empty[slot], ((j / TMA_NS) - 1) & 1)) {
+      // test hook: stop before stage `withhold` (every copy issued so far is
+      // consumed, so none is in flight when the consumers give up and leave)
+      if (j == A.withhold && blockIdx.x == 0) return;
+      if (j >= TMA_NS && !mbar_wait_bounded(&empty[slot], ((j / TMA_NS) - 1) & 1, A.wait_cycles)) {
         if (A.err) atomicExch(A.err, 1);
         return;
       }
@@ -1584,11 +1589,11 @@ __global__ void __launch_bounds__(160, TmaLayout<MODE>::MIN_BLOCKS) k_ac2d_tma(c
   for (int k = 0; k < rows; ++k) {
     bool ok = true;
     if (k == 0) {
-      ok = ok && mbar_wait_bounded(&full[0], 0);
-      ok = ok && mbar_wait_bounded(&full[1 % TMA_NS], 0);
+      ok = ok && mbar_wait_bounded(&full[0], 0, A.wait_cycles);
+      ok = ok && mbar_wait_bounded(&full[1 % TMA_NS], 0, A.wait_cycles);
     }
     const int j2 = k + 2;
-    ok = ok && mbar_wait_bounded(&full[j2 % TMA_NS], (j2 / TMA_NS) & 1);
+    ok = ok && mbar_wait_bounded(&full[j2 % TMA_NS], (j2 / TMA_NS) & 1, A.wait_cycles);
     if (!__all_sync(FULL, ok)) {
       if (lane == 0 && A.err) atomicExch(A.err, 1);
       return;

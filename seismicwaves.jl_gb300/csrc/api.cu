@@ -19,6 +19,7 @@ void acoustic_gradient(sw_wavesim* ws, int nshots, const sw_acoustic_shot* shots
                        double* misfit);
 void wavesim_set_tuning(sw_wavesim* ws, int tz, int variant);
 void wavesim_set_band_heights(sw_wavesim* ws, int tz_forward, int tz_recompute, int tz_adjoint);
+void wavesim_set_wait_test(sw_wavesim* ws, long long wait_cycles, int withhold);
 void wavesim_use_graphs(sw_wavesim* ws, bool on);
 void acoustic_forward_snapshots(sw_wavesim* ws, int nshots, const sw_acoustic_shot* shots, bool on_device,
                                 int snapevery, float* const* snapshots);
@@ -301,6 +302,12 @@ int sw_profile_read(sw_ctx* ctx, int32_t kind, double* total_ms, int64_t* launch
 int sw_wavesim_set_tuning(sw_wavesim* ws, int32_t tz, int32_t variant) {
   if (!ws || tz < 0 || variant < 0 || variant >= (1 << 16)) return SW_ERR_ARG;
   swgb::wavesim_set_tuning(ws, tz, variant);
+  return SW_OK;
+}
+
+int sw_wavesim_set_wait_test(sw_wavesim* ws, int64_t wait_cycles, int32_t withhold_stage) {
+  if (!ws || wait_cycles < 1000 || wait_cycles > 100000000000LL || withhold_stage < -1) return SW_ERR_ARG;
+  swgb::wavesim_set_wait_test(ws, wait_cycles, withhold_stage);
   return SW_OK;
 }
 

@@ -262,6 +262,7 @@ int run(const sw_acoustic_params* p, const float* vp, const sw_acoustic_shot* s,
   a.tiles_y = 1;
   a.tiles_z = tiles_z;
   a.TZ = TZ;
+  a.withhold = -1;
   int pc = 0, pk = 0;
   for (int it = 1; it <= s->nt; ++it) {
     a.pcur = FieldArg{pb[pc], F};
