@@ -26,10 +26,6 @@ def bench():
 
 # (kernel, workload, algorithmic bytes per interior point and shot, points)
 CASES = [
-    ("k_ac2d_step<3>", "acoustic2d_2001x801", 28 + 4 / 8, 1999 * 799),
-    ("k_ac2d_step<1> recompute", "acoustic2d_2001x801", 20 + 4 / 8, 1999 * 799),
-    ("k_ac2d_step<0>", "acoustic2d_2001x801", 16 + 4 / 8, 1999 * 799),
-    ("k_ac2d_adj_grp", "acoustic2d_2001x801", 24 + 4 / 8, 1999 * 799),
     ("k_vd_v + k_vd_p<corr> adjoint", "acoustic_vd2d_2001x801", 68 + 12 / 8, 1999 * 799),
 ]
 
@@ -47,6 +43,19 @@ def test_traffic_lookup_matches_algorithmic_bytes(bench, kernel, workload, bpp, 
 def test_traffic_lookup_unknown_kernel(bench):
     assert bench._traffic_from_profiles("k_no_such_kernel", "acoustic2d_2001x801") is None
     assert bench._traffic_from_profiles("k_ac2d_step<3>", "no_such_workload") is None
+
+
+@pytest.mark.parametrize("kind", ["recompute", "adjoint"])
+def test_traffic_ratio_of_the_2d_kinds(bench, kind):
+    """The 2D gradient kinds' DRAM/algorithmic ratio comes from the committed
+    16-shot capture: below 1 (no re-reads), above 0.5."""
+    r = bench._traffic_ratio_from_profiles(kind, "acoustic2d_2001x801")
+    assert r is not None and 0.5 <= r <= 1.05, r
+
+
+def test_traffic_ratio_unknown(bench):
+    assert bench._traffic_ratio_from_profiles("forward", "acoustic2d_2001x801") is None
+    assert bench._traffic_ratio_from_profiles("adjoint", "no_such_workload") is None
 
 
 def test_profile_summaries_name_their_command():
