@@ -28,7 +28,7 @@
  *   sw_wavesim_create / sw_wavesim_destroy
  *       build_wavesim -> AcousticCDCPMLWaveSimulation (src/apis/build.jl:18-40,
  *       src/models/acoustic/acou_models.jl:90-202): preallocated device fields
- *   sw_wavesim_set_vp
+ *   sw_wavesim_set_vp, sw_wavesim_set_vp64
  *       set_wavesim_matprop! -> update_matprop! -> precompute_fact!
  *       (src/apis/utils.jl:3-8, src/models/acoustic/acou_models.jl:53-60)
  *   sw_acoustic_forward
@@ -172,6 +172,13 @@ int sw_wavesim_destroy(sw_wavesim* ws);
 /* set_wavesim_matprop!: vp has prod(n) entries (column-major). */
 int sw_wavesim_set_vp(sw_wavesim* ws, const float* vp, int32_t on_device);
 
+/* set_wavesim_matprop! with a Float64 model (the reference's arrays): fact =
+ * vp^2 dt^2 is formed from the FP64 values, so the compensated forward of
+ * sw_wavesim_set_precision keeps its full precision; the stencils that take
+ * vp itself use its FP32 rounding.  The FP64 model stays on the device until
+ * sw_wavesim_set_vp replaces it. */
+int sw_wavesim_set_vp64(sw_wavesim* ws, const double* vp, int32_t on_device);
+
 /* run_swforward!: all shots advance together (shots that do not fit in device
  * memory at once run in consecutive groups). */
 int sw_acoustic_forward(sw_wavesim* ws, int32_t nshots, const sw_acoustic_shot* shots, int32_t on_device);
@@ -223,6 +230,20 @@ int sw_wavesim_set_tuning(sw_wavesim* ws, int32_t tz, int32_t variant);
  * kind's band from that kind's own timing; results do not change.  No
  * reference counterpart. */
 int sw_wavesim_set_band_heights(sw_wavesim* ws, int32_t tz_forward, int32_t tz_recompute, int32_t tz_adjoint);
+
+/* Arithmetic of the forward passes (sw_acoustic_forward and the forward of
+ * sw_acoustic_gradient), 2D and 3D: 0 = FP32 state (default); 1 =
+ * compensated: p and d held as unevaluated sums of two FP32 numbers, fact =
+ * vp^2 dt^2 and 1/h^2 as FP32 pairs of their FP64 values, the second
+ * differences, the increment and both state updates evaluated with
+ * error-free transformations (about 48 significant bits; the C-PML memory
+ * variables stay FP32).  Traces and misfits then agree with an FP64
+ * simulation to ~1e-7 at several thousand steps, where FP32 state drifts to
+ * ~1e-6; the forward takes about twice the bytes and several times the
+ * arithmetic.  The gradient's recompute and adjoint stay FP32 (they start
+ * from checkpoints rounded to FP32).  No reference counterpart: the
+ * reference runs in the precision of its arrays (Float64 on the CPU). */
+int sw_wavesim_set_precision(sw_wavesim* ws, int32_t mode);
 
 /* Bounded waits of the TMA stencil (tuning variant 1): every mbarrier wait
  * gives up after wait_cycles SM clock cycles (default 4e9, about 2 s), sets

@@ -24,6 +24,7 @@ EXPORTS = [
     "sw_version", "sw_ctx_create", "sw_ctx_destroy", "sw_ctx_last_error", "sw_ctx_stream",
     "sw_cpml_coefficients", "sw_wavesim_create", "sw_wavesim_destroy", "sw_wavesim_set_vp",
     "sw_acoustic_forward", "sw_acoustic_gradient", "sw_wavesim_set_tuning", "sw_wavesim_set_band_heights",
+    "sw_wavesim_set_precision", "sw_wavesim_set_vp64",
     "sw_wavesim_set_wait_test",
     "sw_profile_enable",
     "sw_profile_read", "sw_acoustic2d_forward_noalloc", "sw_elastic_create", "sw_elastic_destroy",
@@ -104,6 +105,8 @@ def load() -> ctypes.CDLL:
     lib.sw_acoustic_gradient.argtypes = [vp_, i32, P(SwAcousticShot), i32, vp_, vp_]
     lib.sw_wavesim_set_tuning.argtypes = [vp_, i32, i32]
     lib.sw_wavesim_set_band_heights.argtypes = [vp_, i32, i32, i32]
+    lib.sw_wavesim_set_precision.argtypes = [vp_, i32]
+    lib.sw_wavesim_set_vp64.argtypes = [vp_, vp_, i32]
     lib.sw_wavesim_set_wait_test.argtypes = [vp_, ctypes.c_int64, i32]
     lib.sw_profile_enable.argtypes = [vp_, i32]
     lib.sw_profile_read.argtypes = [vp_, i32, P(f64), P(ctypes.c_int64), P(f64)]

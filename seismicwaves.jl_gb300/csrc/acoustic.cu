@@ -91,7 +91,8 @@ __global__ void k_inject_record(const ShotDesc* __restrict__ desc, const long lo
                                 const int* __restrict__ ptr, const int* __restrict__ ids,
                                 const int* __restrict__ bslot, const long long* __restrict__ rec_lin,
                                 FieldArg pnew, FieldArg dnew, FieldArg dfield, int d_first, int it, int record,
-                                int dbf16, const int* __restrict__ rec_stash, FieldArg stash, int it_stash) {
+                                int dbf16, const int* __restrict__ rec_stash, FieldArg stash, int it_stash,
+                                FieldArg plo, FieldArg dlo) {
   const int shot = blockIdx.x;
   const ShotDesc D = desc[shot];
   if (it > D.nt) return;
@@ -113,6 +114,21 @@ __global__ void k_inject_record(const ShotDesc* __restrict__ desc, const long lo
       float sd;
       pn[lin] = ring_update(D.ring, slot, it, add, &sd);
       if (dd) dst1(dd, lin, sd, dbf16);
+    } else if (plo.p) {  // compensated state: p and d get the sources without rounding
+      float* pl = plo.p + (long long)shot * plo.s;
+      float* dl = dlo.p + (long long)shot * dlo.s;
+      ff pv{pn[lin], pl[lin]}, dv{dn[lin], dl[lin]}, av{0.f, 0.f};
+      for (int k = k0; k < k1; ++k) {
+        const ff v{D.tf[(long long)(it - 1) + (long long)ids[k] * D.nt], 0.f};
+        pv = ff_add(pv, v);
+        dv = ff_add(dv, v);
+        av = ff_add(av, v);
+      }
+      pn[lin] = pv.hi;
+      pl[lin] = pv.lo;
+      dn[lin] = dv.hi;
+      dl[lin] = dv.lo;
+      if (dd) dst1(dd, lin, dld1(dd, lin, dbf16) + ff_round(av), dbf16);
     } else {
       float acc = pn[lin];
       for (int k = k0; k < k1; ++k) {
@@ -127,8 +143,11 @@ __global__ void k_inject_record(const ShotDesc* __restrict__ desc, const long lo
   }
   if (!record) return;
   __syncthreads();
-  for (int r = threadIdx.x; r < D.nrec; r += blockDim.x)
-    D.tr[(long long)(it - 1) + (long long)r * D.nt] = pn[rec_lin[D.rec_off + r]];
+  const float* pnl = plo.p ? plo.p + (long long)shot * plo.s : nullptr;
+  for (int r = threadIdx.x; r < D.nrec; r += blockDim.x) {
+    const long long q = rec_lin[D.rec_off + r];
+    D.tr[(long long)(it - 1) + (long long)r * D.nt] = pnl ? __fadd_rn(pn[q], pnl[q]) : pn[q];
+  }
 }
 
 // Adjoint injection at the receivers (adjoint_onestep_CPML! -> inject_sources!
@@ -401,12 +420,32 @@ __global__ void k_ck_unpack(const __nv_bfloat16* __restrict__ src, long long sho
 
 // fact = dt^2 vp^2 into the padded layout; vp kept unpadded (float).
 __global__ void k_set_fact(const float* __restrict__ vp, int n0, long long npts, int P, double dt2,
-                           float* __restrict__ fact) {
+                           float* __restrict__ fact, float* __restrict__ fact_lo) {
   for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < npts;
        c += (long long)gridDim.x * blockDim.x) {
     const long long rowi = c / n0;
     const double v = (double)vp[c];
-    fact[rowi * P + (c - rowi * n0)] = (float)(dt2 * v * v);
+    const double f = dt2 * v * v;
+    const float hi = (float)f;
+    fact[rowi * P + (c - rowi * n0)] = hi;
+    if (fact_lo) fact_lo[rowi * P + (c - rowi * n0)] = (float)(f - (double)hi);  // compensated step
+  }
+}
+
+// fact from FP64 velocities: the FP32 rounding of vp for the kernels that
+// take vp, fact = dt^2 vp^2 in FP64 split into its FP32 rounding and (with a
+// low-part buffer) the remainder.
+__global__ void k_set_fact64(const double* __restrict__ vp64, int n0, long long npts, int P, double dt2,
+                             float* __restrict__ vp, float* __restrict__ fact, float* __restrict__ fact_lo) {
+  for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < npts;
+       c += (long long)gridDim.x * blockDim.x) {
+    const long long rowi = c / n0;
+    const double v = vp64[c];
+    const double f = dt2 * v * v;
+    const float hi = (float)f;
+    vp[c] = (float)v;
+    fact[rowi * P + (c - rowi * n0)] = hi;
+    if (fact_lo) fact_lo[rowi * P + (c - rowi * n0)] = (float)(f - (double)hi);
   }
 }
 
@@ -460,6 +499,10 @@ struct sw_wavesim {
   DevMem d_icd, d_dres;  // dense inverse covariances; residuals and C^-1 r of those shots
   DevMem d_mute, d_mute_ptr;
   int tile_tz = 0;  // 0 = heuristic
+  int precision = 0;                          // 1: compensated (double-FP32) forward steps (k_ac_hp)
+  DevMem plo[2], dlo, fact_lo;                 // their low parts of p (ping-pong), d and fact
+  DevMem vp64;                                 // FP64 vp of sw_wavesim_set_vp64 (fact's low part comes from it)
+  int hp_cap = 0;                              // shots the low-part buffers hold
   long long wait_cycles = TMA_TIMEOUT_CYCLES;  // limit of one bounded device-side wait
   int withhold = -1;                           // test hook of the TMA stencil (StepArgs::withhold)
   int kind_tz[3] = {0, 0, 0};  // band height per stencil kind (forward, recompute, adjoint); 0 = tile_tz
@@ -553,7 +596,7 @@ void run_graph(sw_wavesim* ws, std::vector<long long> key, Work&& work) {
 std::vector<long long> group_key(const sw_wavesim* ws, const std::vector<HostShot>& group, bool grad) {
   std::vector<long long> k = {grad ? 1 : 0, ws->grp, ws->variant, ws->tile_tz, ws->pf, ws->adjw ? 1 : 0,
                               ws->cpa ? 1 : 0, ws->pair_ok ? 1 : 0, ws->pair_adj_ok ? 1 : 0, ws->pair_tz,
-                              ws->pair_occ, ws->kind_tz[0], ws->kind_tz[1], ws->kind_tz[2],
+                              ws->pair_occ, ws->kind_tz[0], ws->kind_tz[1], ws->kind_tz[2], ws->precision,
                               (long long)group.size()};
   for (const auto& h : group) k.push_back(h.nt);
   return k;
@@ -798,7 +841,7 @@ void build_tables(sw_wavesim* ws, const sw_acoustic_shot* shots, const std::vect
   // points and PAIR_MAXRR receiver rows per shot.
   T.pair.assign(S, PairShot{});
   T.recstash.assign(T.rec.size(), 0);
-  T.pair_ok = ws->N == 2 && ws->pair_on && (ws->variant & 3) == 0 && !ws->cpa;
+  T.pair_ok = ws->N == 2 && ws->pair_on && (ws->variant & 3) == 0 && !ws->cpa && ws->precision == 0;
   for (int k = 0; k < S && T.pair_ok; ++k) {
     const ShotDesc& D = T.desc[k];
     PairShot& ps = T.pair[k];
@@ -872,9 +915,42 @@ void build_tables(sw_wavesim* ws, const sw_acoustic_shot* shots, const std::vect
                "mask upload");
 }
 
+size_t per_shot_bytes(const sw_wavesim* ws, bool grad, int max_nt);
+
+// Device memory held by the per-shot buffers (counted back into the budget of
+// plan_groups and ensure_state).
+size_t owned_bytes(const sw_wavesim* ws) {
+  size_t owned = 0;
+  for (int b = 0; b < 2; ++b) owned += ws->pb[b].bytes + ws->ab[b].bytes + ws->plo[b].bytes;
+  owned += ws->db.bytes + ws->adb.bytes + ws->g.bytes + ws->gc.bytes + ws->dbuf.bytes + ws->ck.bytes + ws->dlo.bytes;
+  owned += ws->db2.bytes + ws->adb2.bytes + ws->ck16.bytes + ws->ck_stage.bytes;
+  for (int k = 0; k < 2; ++k)
+    for (int d = 0; d < 3; ++d) owned += ws->psi[k][d].bytes + ws->apsi[k][d].bytes;
+  return owned;
+}
+
 void ensure_state(sw_wavesim* ws, int S, bool grad, int max_nt) {
   const long long F = ws->F;
   cudaStream_t st = ws->ctx->stream;
+  // A gradient group smaller than the state capacity (left by a larger
+  // forward batch) gets state sized to the group when the gradient buffers
+  // of the whole capacity would not fit.
+  bool shrink = false;
+  if (grad && S < ws->cap) {
+    size_t free_b = 0, total_b = 0;
+    check_cuda(cudaMemGetInfo(&free_b, &total_b), "cudaMemGetInfo");
+    shrink = (double)per_shot_bytes(ws, true, max_nt) * ws->cap > 0.85 * (double)(free_b + owned_bytes(ws));
+  }
+  if (shrink) {
+    ws->dbuf.release();
+    ws->ck.release();
+    ws->ck16.release();
+    ws->ck_stage.release();
+    for (int b = 0; b < 2; ++b) ws->plo[b].release();
+    ws->dlo.release();
+    ws->hp_cap = 0;
+    ws->cap = 0;
+  }
   if (S > ws->cap) {
     for (int b = 0; b < 2; ++b) dev_alloc(ws->pb[b], (size_t)S * F * sizeof(float), "pressure field", st);
     dev_alloc(ws->db, (size_t)S * F * sizeof(float), "pressure increment", st);
@@ -906,6 +982,12 @@ void ensure_state(sw_wavesim* ws, int S, bool grad, int max_nt) {
     ws->cap = S;
     ws->d_slots = 0;
     ws->ck_slots = 0;
+    ++ws->gen;
+  }
+  if (ws->precision == 1 && ws->hp_cap < ws->cap) {
+    for (int b = 0; b < 2; ++b) dev_alloc(ws->plo[b], (size_t)ws->cap * F * sizeof(float), "pressure low part", st);
+    dev_alloc(ws->dlo, (size_t)ws->cap * F * sizeof(float), "increment low part", st);
+    ws->hp_cap = ws->cap;
     ++ws->gen;
   }
   if (grad) {
@@ -949,6 +1031,7 @@ size_t per_shot_bytes(const sw_wavesim* ws, bool grad, int max_nt) {
   if (ws->gradient) floats = 2 * floats + 2 * ws->F;
   if (ws->N == 2) floats += ws->F + 2 * ws->strip_total;  // second d / xi buffers, scratch strips
   if (ws->N == 2 && ws->gradient) floats += ws->F + ws->strip_total;  // second adjoint d / xi buffers
+  if (ws->precision == 1) floats += 3 * ws->F;  // low parts of p (two buffers) and d
   if (grad) {
     const int K = ws->gp.check_freq;
     const long long dsl = (K == 1 ? (long long)max_nt : K) * ws->F;
@@ -1012,6 +1095,26 @@ StepCtx make_step_ctx(sw_wavesim* ws, int S, int kind = TZ_FORWARD) {
   return c;
 }
 
+// Compensated forward step (k_ac_hp): 2D blocks of 512 x points, 3D blocks of
+// 128 x points and 4 y rows; bands of 32 rows, shorter while the launch would
+// have fewer than 8 blocks per SM, 4 rows at least.
+StepCtx make_hp_ctx(sw_wavesim* ws, int S) {
+  StepCtx c{ws, 0, 0, 1, 0};
+  const int sms = ws->ctx->num_sms > 0 ? ws->ctx->num_sms : 148;
+  if (ws->N == 2) {
+    c.tiles_x = (int)((ws->P + 511) / 512);
+  } else {
+    c.tiles_x = (int)((ws->P + 127) / 128);
+    c.tiles_y = (ws->n[1] - 2 + 3) / 4;
+  }
+  const int nint = ws->n[ws->N - 1] - 2;
+  int TZ = 32;
+  while (TZ > 4 && (long long)S * c.tiles_x * c.tiles_y * ((nint + TZ - 1) / TZ) < 8LL * sms) TZ /= 2;
+  c.TZ = TZ;
+  c.tiles_z = (nint + TZ - 1) / TZ;
+  return c;
+}
+
 // Two-step launches: warps of PAIR_OUT x points, 4 per block; bands of 32
 // rows (the band halo of the first step repeats 2 of every 34 rows), shorter
 // bands where 32-row ones would leave the GPU with less than two waves of
@@ -1050,6 +1153,14 @@ double pair_bytes(const sw_wavesim* ws, int S, int n_dwrite, bool ckpt, bool adj
   if (ckpt) b += 8.0 * pts * S + 8.0 * strip * S;
   if (adjoint) b += (2.0 * dsz + 8.0) * pts * S;
   return b;
+}
+
+// Extra bytes of a compensated forward launch: per interior point and shot R
+// plo[n], W plo[n+1], R/W dlo; the low part of fact once for the launch.
+double hp_extra_bytes(const sw_wavesim* ws, int S) {
+  double pts = 1.0;
+  for (int d = 0; d < ws->N; ++d) pts *= (double)(ws->n[d] - 2);
+  return (16.0 * S + 4.0) * pts;
 }
 
 // Algorithmic bytes of one stencil launch (FP32 words): per interior point and
@@ -1149,6 +1260,17 @@ struct Launcher {
     cudaEvent_t ev = nullptr;
     const int kind = (MODE == MODE_ADJ || MODE == MODE_ADJW) ? KK_ADJOINT : (recompute ? KK_RECOMPUTE : KK_STENCIL);
     ws->ctx->prof.begin(st, kind, bytes, &ev);
+    if constexpr (MODE == MODE_FWD || MODE == MODE_FWD_D) {
+      if (ws->precision == 1 && !recompute) {  // compensated forward (context from make_hp_ctx)
+        if (ws->N == 2)
+          k_ac_hp<MODE, 2><<<(unsigned)blocks, 128, 0, st>>>(a);
+        else
+          k_ac_hp<MODE, 3><<<(unsigned)blocks, 128, 0, st>>>(a);
+        check_cuda(cudaGetLastError(), "compensated stencil launch");
+        ws->ctx->prof.end(st, kind, ev);
+        return;
+      }
+    }
     if constexpr (MODE == MODE_ADJW) {  // 2D register-pipelined or cp.async-staged stencil only
       const int nw = block_warps(ws);
       if (nw == 4 && ws->cpa) {
@@ -1251,6 +1373,14 @@ StepArgs base_args(sw_wavesim* ws, const StepCtx& c, int S) {
   a.tiles_z = c.tiles_z;
   a.TZ = c.TZ;
   a.err = ws->ctx->err.as<int>();
+  if (ws->precision == 1) {
+    a.fact_lo = ws->fact_lo.as<float>();
+    for (int d = 0; d < ws->N; ++d) {
+      const double ih2 = 1.0 / (ws->prm.h[d] * ws->prm.h[d]);
+      a.ih2[d] = (float)ih2;
+      a.ih2_lo[d] = (float)(ih2 - (double)(float)ih2);
+    }
+  }
   a.wait_cycles = ws->wait_cycles;
   a.withhold = ws->withhold;
   a.pf = ws->pf;
@@ -1293,6 +1423,11 @@ void zero_state(sw_wavesim* ws, int S, bool adjoint) {
       check_cuda(cudaMemsetAsync((adjoint ? ws->axi2 : ws->xi2)[d].p, 0, (size_t)S * ws->xsz[d] * sizeof(float), st),
                  "reset xi");
   }
+  if (!adjoint && ws->precision == 1) {
+    for (int k = 0; k < 2; ++k)
+      check_cuda(cudaMemsetAsync(ws->plo[k].p, 0, (size_t)S * ws->F * sizeof(float), st), "reset p low part");
+    check_cuda(cudaMemsetAsync(ws->dlo.p, 0, (size_t)S * ws->F * sizeof(float), st), "reset d low part");
+  }
   check_cuda(cudaMemsetAsync(ws->d_ring.p, 0, ws->d_ring.bytes, st), "reset rings");
 }
 
@@ -1312,7 +1447,8 @@ void download_traces(sw_wavesim* ws, const sw_acoustic_shot* shots, const std::v
 }
 
 void launch_inject(sw_wavesim* ws, int Sa, const FieldArg& pnew, const FieldArg& dnew, const FieldArg& Dw,
-                   int d_first, int it, int record, int it_stash = 0) {
+                   int d_first, int it, int record, int it_stash = 0, const FieldArg& plo = FieldArg{nullptr, 0},
+                   const FieldArg& dlo = FieldArg{nullptr, 0}) {
   cudaStream_t st = ws->ctx->stream;
   cudaEvent_t ev = nullptr;
   ws->ctx->prof.begin(st, KK_SRCREC, 0.0, &ev);
@@ -1321,7 +1457,7 @@ void launch_inject(sw_wavesim* ws, int Sa, const FieldArg& pnew, const FieldArg&
                                       ws->d_ids.as<int>(), ws->d_bslot.as<int>(), ws->d_rec.as<long long>(), pnew,
                                       dnew, Dw, d_first, it, record,
                                       (ws->gradient && ws->gp.snapshot_bf16 >= 1) ? 1 : 0,
-                                      ws->d_recstash.as<int>(), stash, it_stash);
+                                      ws->d_recstash.as<int>(), stash, it_stash, plo, dlo);
   check_cuda(cudaGetLastError(), "inject/record launch");
   ws->ctx->prof.end(st, KK_SRCREC, ev);
 }
@@ -1374,6 +1510,11 @@ void set_io(sw_wavesim* ws, StepArgs& a, FwdState& s, bool two, bool adjoint) {
   DevMem* db[2] = {adjoint ? &ws->adb : &ws->db, adjoint ? &ws->adb2 : &ws->db2};
   a.pcur = fa(pb[s.p], F);
   a.pnew = fa(pb[1 - s.p], F);
+  if (!adjoint && ws->precision == 1) {
+    a.plo_cur = fa(ws->plo[s.p], F);
+    a.plo_new = fa(ws->plo[1 - s.p], F);
+    a.dlo = fa(ws->dlo, F);
+  }
   a.din = fa(*db[s.d], F);
   a.dout = fa(*db[dn], F);
   for (int d = 0; d < ws->N; ++d) {
@@ -1439,7 +1580,7 @@ void forward_group(sw_wavesim* ws, const std::vector<HostShot>& group, bool grad
     bool two = ws->pair_ok && it + 1 <= max_nt && active_count(group, it + 1) == Sa &&
                !(snap && it % ws->snapevery == 0);
     if (two && grad) two = !(K > 1 && it % K == 0) && d_first_of(it + 1, Sa) == d_first;
-    const StepCtx c = two ? make_pair_ctx(ws, Sa) : make_step_ctx(ws, Sa);
+    const StepCtx c = two ? make_pair_ctx(ws, Sa) : ws->precision == 1 ? make_hp_ctx(ws, Sa) : make_step_ctx(ws, Sa);
     StepArgs a = base_args(ws, c, Sa);
     set_io(ws, a, sta, two, false);
     int ck_slot = -1;
@@ -1479,12 +1620,14 @@ void forward_group(sw_wavesim* ws, const std::vector<HostShot>& group, bool grad
         L.pair<MODE_FWD>(a, b, bytes);
       launch_inject(ws, Sa, a.pnew, a.dout, grad ? b.Dout2 : FieldArg{nullptr, 0}, d_first, it + 1, 1, it);
     } else {
-      const double bytes = stencil_bytes(ws, Sa, grad ? MODE_FWD_D : MODE_FWD, n_dwrite, ckpt);
+      double bytes = stencil_bytes(ws, Sa, grad ? MODE_FWD_D : MODE_FWD, n_dwrite, ckpt);
+      if (ws->precision == 1) bytes += hp_extra_bytes(ws, Sa);
       if (grad)
         L.step<MODE_FWD_D>(a, c, bytes);
       else
         L.step<MODE_FWD>(a, c, bytes);
-      launch_inject(ws, Sa, a.pnew, a.dout, grad ? a.Dout : FieldArg{nullptr, 0}, d_first, it, 1);
+      launch_inject(ws, Sa, a.pnew, a.dout, grad ? a.Dout : FieldArg{nullptr, 0}, d_first, it, 1, 0, a.plo_new,
+                    a.dlo);
     }
     if (ck_slot >= 0) pack_checkpoint(ws, Sa, ck_slot);
     const int it_end = two ? it + 1 : it;
@@ -1639,12 +1782,7 @@ std::vector<std::vector<HostShot>> plan_groups(sw_wavesim* ws, const std::vector
   size_t free_b = 0, total_b = 0;
   check_cuda(cudaMemGetInfo(&free_b, &total_b), "cudaMemGetInfo");
   // keep the buffers already allocated in the budget
-  size_t owned = 0;
-  for (int b = 0; b < 2; ++b) owned += ws->pb[b].bytes + ws->ab[b].bytes;
-  owned += ws->db.bytes + ws->adb.bytes + ws->g.bytes + ws->gc.bytes + ws->dbuf.bytes + ws->ck.bytes;
-  for (int k = 0; k < 2; ++k)
-    for (int d = 0; d < 3; ++d) owned += ws->psi[k][d].bytes + ws->apsi[k][d].bytes;
-  const double budget = 0.85 * (double)(free_b + owned);
+  const double budget = 0.85 * (double)(free_b + owned_bytes(ws));
   std::vector<std::vector<HostShot>> groups;
   size_t i = 0;
   while (i < order.size()) {
@@ -1749,13 +1887,41 @@ void wavesim_set_vp(sw_wavesim* ws, const float* vp, bool on_device) {
   check_cuda(cudaMemcpyAsync(ws->vp.p, vp, ws->npts * sizeof(float),
                              on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, st),
              "vp upload");
+  ws->vp64.release();  // the FP32 values are the model now
   const double dt = ws->prm.dt;
   cudaEvent_t ev = nullptr;
   ws->ctx->prof.begin(st, KK_OTHER, 0.0, &ev);
   k_set_fact<<<std::min<long long>((ws->npts + 255) / 256, 4096), 256, 0, st>>>(
-      ws->vp.as<float>(), ws->n[0], ws->npts, ws->P, dt * dt, ws->fact.as<float>());
+      ws->vp.as<float>(), ws->n[0], ws->npts, ws->P, dt * dt, ws->fact.as<float>(),
+      ws->precision == 1 ? ws->fact_lo.as<float>() : nullptr);
   check_cuda(cudaGetLastError(), "fact launch");
   ws->ctx->prof.end(st, KK_OTHER, ev);
+  ws->has_vp = true;
+}
+
+void launch_fact64(sw_wavesim* ws) {
+  cudaStream_t st = ws->ctx->stream;
+  cudaEvent_t ev = nullptr;
+  ws->ctx->prof.begin(st, KK_OTHER, 0.0, &ev);
+  k_set_fact64<<<std::min<long long>((ws->npts + 255) / 256, 4096), 256, 0, st>>>(
+      ws->vp64.as<double>(), ws->n[0], ws->npts, ws->P, ws->prm.dt * ws->prm.dt, ws->vp.as<float>(),
+      ws->fact.as<float>(), ws->precision == 1 ? ws->fact_lo.as<float>() : nullptr);
+  check_cuda(cudaGetLastError(), "fact launch");
+  ws->ctx->prof.end(st, KK_OTHER, ev);
+}
+
+void wavesim_set_vp64(sw_wavesim* ws, const double* vp, bool on_device) {
+  if (!vp) fail(SW_ERR_ARG, "vp is NULL");
+  cudaStream_t st = ws->ctx->stream;
+  if (!on_device) {
+    for (long long c = 0; c < ws->npts; ++c)
+      if (!(vp[c] > 0)) fail(SW_ERR_ARG, "Pressure velocity material property must be positive!");
+  }
+  if (!ws->vp64.p) dev_alloc(ws->vp64, (size_t)ws->npts * sizeof(double), "vp (FP64)", st);
+  check_cuda(cudaMemcpyAsync(ws->vp64.p, vp, ws->npts * sizeof(double),
+                             on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, st),
+             "vp upload");
+  launch_fact64(ws);
   ws->has_vp = true;
 }
 
@@ -2011,6 +2177,25 @@ void wavesim_set_band_heights(sw_wavesim* ws, int tz_forward, int tz_recompute, 
   ws->kind_tz[TZ_FORWARD] = tz_forward;
   ws->kind_tz[TZ_RECOMPUTE] = tz_recompute;
   ws->kind_tz[TZ_ADJOINT] = tz_adjoint;
+}
+void wavesim_set_precision(sw_wavesim* ws, int mode) {
+  if (mode == ws->precision) return;
+  ws->precision = mode;
+  ws->drop_graphs();
+  if (mode == 1 && !ws->fact_lo.p) {
+    cudaStream_t st = ws->ctx->stream;
+    dev_alloc(ws->fact_lo, (size_t)ws->F * sizeof(float), "fact low part", st);
+    check_cuda(cudaMemsetAsync(ws->fact_lo.p, 0, (size_t)ws->F * sizeof(float), st), "fact low part");
+    if (ws->has_vp && ws->vp64.p) {
+      launch_fact64(ws);
+    } else if (ws->has_vp) {
+      k_set_fact<<<std::min<long long>((ws->npts + 255) / 256, 4096), 256, 0, st>>>(
+          ws->vp.as<float>(), ws->n[0], ws->npts, ws->P, ws->prm.dt * ws->prm.dt, ws->fact.as<float>(),
+          ws->fact_lo.as<float>());
+      check_cuda(cudaGetLastError(), "fact launch");
+    }
+    check_cuda(cudaStreamSynchronize(st), "set precision");
+  }
 }
 void wavesim_set_wait_test(sw_wavesim* ws, long long wait_cycles, int withhold) {
   ws->wait_cycles = wait_cycles;

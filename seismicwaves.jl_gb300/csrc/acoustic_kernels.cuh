@@ -69,6 +69,10 @@ struct StepArgs {
   int withhold;  // TMA stencil test hook: block 0's producer never issues this stage (-1 = none)
   int pf;                                          // 2D stencil: rows ahead prefetched into L2 (0 = off)
   int dbf16;                                       // Dout / dcorr hold BF16 (the pointers are __nv_bfloat16 arrays)
+  // compensated step (k_ac_hp): low parts of p[n], p[n+1] and d (in place), of fact and of 1/h^2
+  FieldArg plo_cur, plo_new, dlo;
+  const float* fact_lo;
+  float ih2_lo[3];
 };
 
 struct StripIO {
@@ -1690,6 +1694,271 @@ __global__ void __launch_bounds__(160, TmaLayout<MODE>::MIN_BLOCKS) k_ac2d_tma(c
           }
         }
       }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Compensated (double-FP32) forward step: sw_wavesim_set_precision(ws, 1).
+//
+// FP32 state loses about 1e-6 of relative trace accuracy over a few thousand
+// steps, and most of it comes from the cancellation in the second
+// differences (a smooth wave's p[x-1] - 2 p[x] + p[x+1] is a few percent of
+// p, so its FP32 rounding is ~30 eps of the result), then from the FP32
+// rounding of p, of the increment d and of fact = vp^2 dt^2.  This step keeps
+// p and d as unevaluated sums hi + lo of two FP32 numbers and fact and 1/h^2
+// as hi + lo pairs of their FP64 values, and evaluates the increment
+// d[n+1] - d[n] = fact * lap(p) and both state updates with error-free
+// transformations: Knuth's TwoSum, the FMA form of Dekker's TwoProduct
+// (a*b - fl(a*b) = fma(a, b, -fl(a*b))) and Dekker's Fast2Sum
+// renormalisation (the double-double arithmetic of Dekker 1971 and of the QD
+// library of Hida, Li and Bailey), about 48 bits of significand.  The C-PML
+// memory variables stay FP32: their correction to the second difference is
+// small where the damping starts and is added to the compensated value.
+// Same algorithm and update order as the FP32 step (k_ac2d_step / ac3d_body);
+// checkpoints and the D slots get the rounded hi + lo values.
+// ---------------------------------------------------------------------------
+struct ff {
+  float hi, lo;
+};
+__device__ __forceinline__ ff two_sum(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  const float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+  return {s, e};
+}
+__device__ __forceinline__ ff fast_two_sum(float a, float b) {  // |a| >= |b| or a == 0
+  const float s = __fadd_rn(a, b);
+  return {s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+__device__ __forceinline__ ff ff_add(ff a, ff b) {
+  const ff s = two_sum(a.hi, b.hi);
+  const ff t = two_sum(a.lo, b.lo);
+  ff r = fast_two_sum(s.hi, __fadd_rn(s.lo, t.hi));
+  return fast_two_sum(r.hi, __fadd_rn(r.lo, t.lo));
+}
+__device__ __forceinline__ ff ff_mul(ff a, ff b) {
+  const float p = __fmul_rn(a.hi, b.hi);
+  float e = __fmaf_rn(a.hi, b.hi, -p);
+  e = __fmaf_rn(a.hi, b.lo, __fmaf_rn(a.lo, b.hi, e));
+  return fast_two_sum(p, e);
+}
+__device__ __forceinline__ float ff_round(ff a) { return __fadd_rn(a.hi, a.lo); }
+
+// p[l] - 2 p[c] + p[r] of compensated values, compensated
+__device__ __forceinline__ ff ff_d2(float lh, float ll, float ch, float cl, float rh, float rl) {
+  const ff s = two_sum(lh, rh);
+  const ff t = two_sum(s.hi, __fmul_rn(-2.f, ch));  // -2 ch is exact
+  const float lo = __fadd_rn(__fadd_rn(s.lo, t.lo), __fadd_rn(__fadd_rn(ll, rl), __fmul_rn(-2.f, cl)));
+  return fast_two_sum(t.hi, lo);
+}
+
+// The C-PML correction of one axis (dpsi + xi), with the memory variables
+// advanced as in cpml_axis_term from the rounded second difference d2.
+__device__ __forceinline__ float cpml_axis_corr(float d2, float pl, float p0, float pr, int x, int n, int halo,
+                                                float ih, const StripIO& s) {
+  int qr;
+  bool first;
+  if (x < halo) {
+    qr = x;
+    first = (x == 1);
+  } else if (x >= n - halo) {
+    qr = x + 1 - n + 2 * halo;
+    first = (x == n - halo);
+  } else {
+    return 0.f;
+  }
+  const int ql = qr - 1;
+  const long long il = s.psi_base + (long long)ql * s.psi_step;
+  const long long ir = s.psi_base + (long long)qr * s.psi_step;
+  const float oldl = s.psi_in[il];
+  const float oldr = s.psi_in[ir];
+  const float newl = radd(rmul(s.bh[ql], oldl), rmul(s.ah[ql], rmul(rsub(p0, pl), ih)));
+  const float newr = radd(rmul(s.bh[qr], oldr), rmul(s.ah[qr], rmul(rsub(pr, p0), ih)));
+  s.psi_out[ir] = newr;
+  if (s.ck_psi) s.ck_psi[ir] = oldr;
+  if (first) {
+    s.psi_out[il] = newl;
+    if (s.ck_psi) s.ck_psi[il] = oldl;
+  }
+  const float dpsi = rmul(rsub(newr, newl), ih);
+  const long long iq = s.xi_base + (long long)qr * s.xi_step;
+  const float xo = s.xi_in[iq];
+  if (s.ck_xi) s.ck_xi[iq] = xo;
+  const float xn = radd(rmul(s.b[qr], xo), rmul(s.a[qr], radd(d2, dpsi)));
+  s.xi_out[iq] = xn;
+  return radd(dpsi, xn);
+}
+
+// One warp = 128 x points (4 per thread) of one row (2D) or of one y row
+// (3D), marching a band of TZ rows of the last axis; 4 warps per block (2D:
+// 512 x points; 3D: 4 y rows).  Forward modes only (MODE_FWD, MODE_FWD_D).
+template <int MODE, int NDIM>
+__global__ void __launch_bounds__(128) k_ac_hp(const StepArgs A) {
+  static_assert(MODE == MODE_FWD || MODE == MODE_FWD_D, "compensated step: forward modes only");
+  constexpr unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int S = A.nshots;
+  const int shot = blockIdx.x % S;
+  int tile = blockIdx.x / S;
+  const int nx = A.n0, P = A.P, H = A.halo;
+  const int nm = NDIM == 2 ? A.n1 : A.n2;  // marching axis
+  const int ny = NDIM == 3 ? A.n1 : 1;
+  int wx0, y = 0;
+  if (NDIM == 2) {
+    wx0 = (tile % A.tiles_x) * 512 + warp * 128;
+    tile /= A.tiles_x;
+  } else {
+    wx0 = (tile % A.tiles_x) * 128;
+    tile /= A.tiles_x;
+    y = 1 + (tile % A.tiles_y) * 4 + warp;
+    tile /= A.tiles_y;
+  }
+  const int z_begin = 1 + tile * A.TZ;
+  const int z_end = min(z_begin + A.TZ, nm - 1);
+  if (z_begin >= z_end || wx0 >= P || (NDIM == 3 && y > ny - 2)) return;  // warp-uniform
+  const int x0 = wx0 + lane * 4;
+  const bool inb = x0 < P;
+  const int xa = inb ? x0 : P - 4;
+  const long long plane = NDIM == 2 ? (long long)P : (long long)P * ny;  // stride of the marching axis
+  const long long rowoff = NDIM == 2 ? xa : (long long)y * P + xa;
+
+  const float* __restrict__ pc = fptr(A.pcur, shot);
+  const float* __restrict__ pcl = fptr(A.plo_cur, shot);
+  float* __restrict__ pn = fptr(A.pnew, shot);
+  float* __restrict__ pnl = fptr(A.plo_new, shot);
+  float* dd = fptr(A.dout, shot);  // in place: din == dout
+  float* ddl = fptr(A.dlo, shot);
+  const float* __restrict__ fh = A.fact;
+  const float* __restrict__ fl = A.fact_lo;
+  const int na = 2 * H + 2, nh = 2 * H;
+  float* ckp = fptr(A.ck_p, shot);
+  float* ckd = fptr(A.ck_d, shot);
+  float* Dw = nullptr;
+  if (MODE == MODE_FWD_D && shot >= A.d_first) Dw = dptr(A.Dout, shot, A.dbf16);
+  const bool xstrip = inb && (x0 < H || x0 + 3 >= nx - H);
+  const bool ystrip = NDIM == 3 && ((y < H) || (y >= ny - H));
+  const int ax_m = NDIM - 1;  // index of the marching axis in ih / ih2
+  const ff ih2x{A.ih2[0], A.ih2_lo[0]}, ih2m{A.ih2[ax_m], A.ih2_lo[ax_m]};
+  const ff ih2y{A.ih2[1], A.ih2_lo[1]};
+
+  float rmh[4], rml[4], r0h[4], r0l[4], rph[4], rpl[4];
+  {
+    const long long idx = (long long)z_begin * plane + rowoff;
+    ld4(rmh, pc + idx - plane);
+    ld4(rml, pcl + idx - plane);
+    ld4(r0h, pc + idx);
+    ld4(r0l, pcl + idx);
+  }
+  for (int z = z_begin; z < z_end; ++z) {
+    const long long idx = (long long)z * plane + rowoff;
+    ld4(rph, pc + idx + plane);
+    ld4(rpl, pcl + idx + plane);
+    float oh[4], ol[4], fa[4], fb[4];
+    ld4rw(oh, dd + idx);
+    ld4rw(ol, ddl + idx);
+    ld4(fa, fh + idx);
+    ld4(fb, fl + idx);
+    float ymh[4], yml[4], yph[4], ypl[4];
+    if (NDIM == 3) {
+      ld4(ymh, pc + idx - P);
+      ld4(yml, pcl + idx - P);
+      ld4(yph, pc + idx + P);
+      ld4(ypl, pcl + idx + P);
+    }
+    float lh = __shfl_up_sync(FULL, r0h[3], 1), ll = __shfl_up_sync(FULL, r0l[3], 1);
+    float rh = __shfl_down_sync(FULL, r0h[0], 1), rl = __shfl_down_sync(FULL, r0l[0], 1);
+    if (lane == 0) {
+      lh = xa > 0 ? pc[idx - 1] : 0.f;
+      ll = xa > 0 ? pcl[idx - 1] : 0.f;
+    }
+    if (lane == 31) {
+      rh = xa + 4 < P ? pc[idx + 4] : 0.f;
+      rl = xa + 4 < P ? pcl[idx + 4] : 0.f;
+    }
+    const bool mstrip = (z < H) || (z >= nm - H);
+    float outph[4], outpl[4], outdh[4], outdl[4], outD[4];
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+      const float xmh = e == 0 ? lh : r0h[e - 1], xml = e == 0 ? ll : r0l[e - 1];
+      const float xph = e == 3 ? rh : r0h[e + 1], xpl = e == 3 ? rl : r0l[e + 1];
+      const float ch = r0h[e], cl = r0l[e];
+      const int x = x0 + e;
+      const bool pin = inb && x >= 1 && x <= nx - 2;
+      ff dx = ff_d2(xmh, xml, ch, cl, xph, xpl);
+      ff dm = ff_d2(rmh[e], rml[e], ch, cl, rph[e], rpl[e]);
+      ff tx = ff_mul(dx, ih2x), tm = ff_mul(dm, ih2m);
+      if (xstrip && pin) {
+        StripIO s0 = NDIM == 2 ? strip_io(A, 0, shot, 1) : strip_io(A, 0, shot, 1);
+        if (NDIM == 2) {
+          s0.psi_base = (long long)z * nh;
+          s0.xi_base = (long long)z * na;
+        } else {
+          s0.psi_base = ((long long)z * ny + y) * nh;
+          s0.xi_base = ((long long)z * ny + y) * na;
+        }
+        tx = ff_add(tx, ff{cpml_axis_corr(ff_round(tx), xmh, ch, xph, x, nx, H, A.ih[0], s0), 0.f});
+      }
+      if (mstrip && pin) {
+        StripIO sm = strip_io(A, ax_m, shot, plane);
+        if (NDIM == 2) {
+          sm.psi_base = x;
+          sm.xi_base = x;
+        } else {
+          sm.psi_base = (long long)y * P + x;
+          sm.xi_base = (long long)y * P + x;
+        }
+        tm = ff_add(tm, ff{cpml_axis_corr(ff_round(tm), rmh[e], ch, rph[e], z, nm, H, A.ih[ax_m], sm), 0.f});
+      }
+      ff lap = ff_add(tx, tm);
+      if (NDIM == 3) {
+        ff ty = ff_mul(ff_d2(ymh[e], yml[e], ch, cl, yph[e], ypl[e]), ih2y);
+        if (ystrip && pin) {
+          StripIO s1 = strip_io(A, 1, shot, P);
+          s1.psi_base = (long long)z * nh * P + x;
+          s1.xi_base = (long long)z * na * P + x;
+          ty = ff_add(ty, ff{cpml_axis_corr(ff_round(ty), ymh[e], ch, yph[e], y, ny, H, A.ih[1], s1), 0.f});
+        }
+        lap = ff_add(lap, ty);
+      }
+      const ff D = ff_mul(ff{fa[e], fb[e]}, lap);
+      const ff dn = ff_add(ff{oh[e], ol[e]}, D);
+      const ff pnw = ff_add(ff{ch, cl}, dn);
+      outD[e] = ff_round(D);
+      outdh[e] = dn.hi;
+      outdl[e] = dn.lo;
+      outph[e] = pnw.hi;
+      outpl[e] = pnw.lo;
+    }
+    if (inb) {
+      if (ckp) {
+        float cp4[4], cd4[4];
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+          cp4[e] = __fadd_rn(r0h[e], r0l[e]);
+          cd4[e] = __fadd_rn(oh[e], ol[e]);
+        }
+        st4(ckp + idx, cp4);
+        st4(ckd + idx, cd4);
+      }
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        const int x = x0 + e;
+        if (x >= 1 && x <= nx - 2) {
+          pn[idx + e] = outph[e];
+          pnl[idx + e] = outpl[e];
+          dd[idx + e] = outdh[e];
+          ddl[idx + e] = outdl[e];
+          if (MODE == MODE_FWD_D && Dw) dst1(Dw, idx + e, outD[e], A.dbf16);
+        }
+      }
+    }
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+      rmh[e] = r0h[e];
+      rml[e] = r0l[e];
+      r0h[e] = rph[e];
+      r0l[e] = rpl[e];
     }
   }
 }

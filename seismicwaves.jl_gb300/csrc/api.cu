@@ -20,6 +20,8 @@ void acoustic_gradient(sw_wavesim* ws, int nshots, const sw_acoustic_shot* shots
 void wavesim_set_tuning(sw_wavesim* ws, int tz, int variant);
 void wavesim_set_band_heights(sw_wavesim* ws, int tz_forward, int tz_recompute, int tz_adjoint);
 void wavesim_set_wait_test(sw_wavesim* ws, long long wait_cycles, int withhold);
+void wavesim_set_precision(sw_wavesim* ws, int mode);
+void wavesim_set_vp64(sw_wavesim* ws, const double* vp, bool on_device);
 void wavesim_use_graphs(sw_wavesim* ws, bool on);
 void acoustic_forward_snapshots(sw_wavesim* ws, int nshots, const sw_acoustic_shot* shots, bool on_device,
                                 int snapevery, float* const* snapshots);
@@ -255,6 +257,15 @@ int sw_wavesim_set_vp(sw_wavesim* ws, const float* vp, int32_t on_device) {
   });
 }
 
+int sw_wavesim_set_vp64(sw_wavesim* ws, const double* vp, int32_t on_device) {
+  if (!ws) return SW_ERR_ARG;
+  sw_ctx* ctx = swgb::wavesim_ctx(ws);
+  return guarded(ctx, [&] {
+    swgb::check_cuda(cudaSetDevice(ctx->device), "cudaSetDevice");
+    swgb::wavesim_set_vp64(ws, vp, on_device != 0);
+  });
+}
+
 int sw_acoustic_forward(sw_wavesim* ws, int32_t nshots, const sw_acoustic_shot* shots, int32_t on_device) {
   if (!ws) return SW_ERR_ARG;
   sw_ctx* ctx = swgb::wavesim_ctx(ws);
@@ -303,6 +314,11 @@ int sw_wavesim_set_tuning(sw_wavesim* ws, int32_t tz, int32_t variant) {
   if (!ws || tz < 0 || variant < 0 || variant >= (1 << 16)) return SW_ERR_ARG;
   swgb::wavesim_set_tuning(ws, tz, variant);
   return SW_OK;
+}
+
+int sw_wavesim_set_precision(sw_wavesim* ws, int32_t mode) {
+  if (!ws || mode < 0 || mode > 1) return SW_ERR_ARG;
+  return guarded(swgb::wavesim_ctx(ws), [&] { swgb::wavesim_set_precision(ws, mode); });
 }
 
 int sw_wavesim_set_wait_test(sw_wavesim* ws, int64_t wait_cycles, int32_t withhold_stage) {

@@ -106,7 +106,7 @@ class GpuRun:
     """Drives libswgb300 directly through its C ABI for one case."""
 
     def __init__(self, sw, case: Case, gradient=False, check_freq=1, mute_src=0, mute_rec=0, variant=0, tz=0,
-                 bf16=False):
+                 bf16=False, precision=0):
         L = sw._lib
         self.sw, self.case, self.L = sw, case, L
         self.ctx = L.Context(0)
@@ -122,8 +122,13 @@ class GpuRun:
         self.h = ctypes.c_void_p()
         self.ctx.check(self.ctx.lib.sw_wavesim_create(self.ctx.h, ctypes.byref(prm), int(gradient),
                                                       ctypes.byref(gp), ctypes.byref(self.h)), "create")
-        vp32 = np.asfortranarray(case.vp, dtype=np.float32)
-        self.ctx.check(self.ctx.lib.sw_wavesim_set_vp(self.h, vp32.ctypes.data, 0), "set_vp")
+        if precision:  # 1: compensated (double-FP32) forward steps, fact from the FP64 model
+            self.ctx.check(self.ctx.lib.sw_wavesim_set_precision(self.h, int(precision)), "set_precision")
+            vp64 = np.asfortranarray(case.vp, dtype=np.float64)
+            self.ctx.check(self.ctx.lib.sw_wavesim_set_vp64(self.h, vp64.ctypes.data, 0), "set_vp64")
+        else:
+            vp32 = np.asfortranarray(case.vp, dtype=np.float32)
+            self.ctx.check(self.ctx.lib.sw_wavesim_set_vp(self.h, vp32.ctypes.data, 0), "set_vp")
         if variant or tz:
             self.ctx.check(self.ctx.lib.sw_wavesim_set_tuning(self.h, int(tz), int(variant)), "set_tuning")
 

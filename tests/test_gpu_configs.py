@@ -115,12 +115,20 @@ def test_acoustic2d_2001x801_batch_matches_oracle(sw, oracle):
         trefs.append(tk)
     bound = _misfit_bound(tr, trefs, [s.observed for s in shots])
     errs = (abs(msf - mref) / mref, rel_l2(g, gref))
-    print(f"acoustic2d_2001x801, shots {sel} (nt {[s.nt for s in shots]}): traces "
+    # the compensated forward (sw_wavesim_set_precision 1) on the same batch
+    hp = GpuRun(sw, case, gradient=True, check_freq=w.check_freq, precision=1)
+    g_hp, msf_hp, tr_hp = hp.gradient(shots)
+    hp.close()
+    hp_errs = (abs(msf_hp - mref) / mref, rel_l2(g_hp, gref), max(rel_l2(a, b) for a, b in zip(tr_hp, trefs)))
+    print(f"acoustic2d_2001x801, shots {sel} (nt {[s.nt for s in shots]}): FP32 traces "
           f"{[f'{rel_l2(a, b):.2e}' for a, b in zip(tr, trefs)]} misfit {errs[0]:.3e} (trace-implied bound "
-          f"{bound:.3e})  batched gradient {errs[1]:.3e}  per-shot gradients {[f'{e:.2e}' for e in gerrs]}")
-    assert errs[0] <= max(MISFIT_TOL, 1.1 * bound)
+          f"{bound:.3e})  batched gradient {errs[1]:.3e}  per-shot gradients {[f'{e:.2e}' for e in gerrs]}; "
+          f"compensated: traces <= {hp_errs[2]:.2e} misfit {hp_errs[0]:.3e} gradient {hp_errs[1]:.3e}")
+    assert errs[0] <= max(MISFIT_TOL, 1.1 * bound)  # FP32 state: about 2e-6 at these record lengths
     assert errs[1] < GRAD_TOL
     assert max(gerrs) < GRAD_TOL
+    assert hp_errs[0] < MISFIT_TOL  # the misfit bar, met by the compensated forward
+    assert hp_errs[1] < GRAD_TOL and hp_errs[2] < TRACE_TOL
 
 
 def test_acoustic2d_2001x801_all_shots_consistency(sw):
@@ -221,15 +229,19 @@ def test_acoustic3d_generator_200_matches_oracle(sw, oracle):
     _gpu_observed(sw, case, w.vp_observed, shots)
     gref, mref, tref = oracle_gradient(oracle, sw, case, shots[0], check_freq=50)
     out = {}
-    for bf16 in (0, 1):
-        run = GpuRun(sw, case, gradient=True, check_freq=50, bf16=bf16)
-        out[bf16] = run.gradient(shots)
+    for bf16, prec in ((0, 0), (1, 0), (0, 1)):
+        run = GpuRun(sw, case, gradient=True, check_freq=50, bf16=bf16, precision=prec)
+        out[(bf16, prec)] = run.gradient(shots)
         run.close()
-    g, msf, tr = out[0]
+    g, msf, tr = out[(0, 0)]
+    g_hp, msf_hp, tr_hp = out[(0, 1)]
     bound = _misfit_bound(tr, [tref], [shots[0].observed])
-    errs = (rel_l2(tr[0], tref), abs(msf - mref) / mref, rel_l2(g, gref), rel_l2(out[1][0], gref))
+    errs = (rel_l2(tr[0], tref), abs(msf - mref) / mref, rel_l2(g, gref), rel_l2(out[(1, 0)][0], gref))
+    hp_errs = (rel_l2(tr_hp[0], tref), abs(msf_hp - mref) / mref, rel_l2(g_hp, gref))
     print(f"acoustic3d 200^3: traces {errs[0]:.3e} misfit {errs[1]:.3e} (trace-implied bound {bound:.3e}) "
-          f"gradient {errs[2]:.3e}, with the BF16 buffer {errs[3]:.3e}")
+          f"gradient {errs[2]:.3e}, with the BF16 buffer {errs[3]:.3e}; compensated forward: traces "
+          f"{hp_errs[0]:.3e} misfit {hp_errs[1]:.3e} gradient {hp_errs[2]:.3e}")
     assert errs[0] < TRACE_TOL and errs[1] <= max(MISFIT_TOL, 1.1 * bound)
     assert errs[2] < GRAD_TOL
     assert errs[3] < 5e-3
+    assert hp_errs[0] < TRACE_TOL and hp_errs[1] < MISFIT_TOL and hp_errs[2] < GRAD_TOL
