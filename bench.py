@@ -796,7 +796,8 @@ def _extra_acoustic3d(a, device):
     prof = {k: R.ctx.profile_read(k) for k in (0, 1, 4)}
     pts = float(w.point_steps())
     peak, _ = _peak()
-    names = {0: "k_ac3d_step<1> forward", 4: "k_ac3d_step<1> recompute", 1: "k_ac3d_step<2> adjoint + correlation"}
+    k3 = "k_ac3d_inner + k_ac3d_shell"
+    names = {0: f"{k3} <1> forward", 4: f"{k3} <1> recompute", 1: f"{k3} <2> adjoint + correlation"}
     kern = {names[k]: {"ms": prof[k][0], "GB_per_s": prof[k][2] / (prof[k][0] / 1e3) / 1e9 if prof[k][0] else None,
                        "frac": prof[k][2] / (prof[k][0] / 1e3) / 1e9 / peak if prof[k][0] else None}
             for k in prof}
@@ -934,7 +935,7 @@ def run_gb300(a):
         return
     # roofline of the dominant kernel (largest total time among the stencil kinds)
     nd = w.vp.ndim
-    base = "k_ac2d_step" if nd == 2 else "k_ac3d_step"
+    base = "k_ac2d_step" if nd == 2 else "k_ac3d_inner + k_ac3d_shell"
     if nd == 2 and veff >= 0 and (veff & 256) and nshots >= 4:
         adj, adj_what = "k_ac2d_adj_grp", "adjoint + correlation (4 shots per block, Kahan sums)"
     elif nd == 2:

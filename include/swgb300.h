@@ -126,6 +126,9 @@ typedef struct {
  * freetop_axis = 1 applies the free-surface override of the first half. */
 int sw_cpml_coefficients(double vel_max, double dt, int32_t halo, double rcoef, double h, double f0,
                          int32_t freetop_axis, float* a, float* a_h, float* b, float* b_h);
+/* The same coefficients in FP64 (sw_acoustic_shot.cpml64 of the compensated forward). */
+int sw_cpml_coefficients64(double vel_max, double dt, int32_t halo, double rcoef, double h, double f0,
+                           int32_t freetop_axis, double* a, double* a_h, double* b, double* b_h);
 
 /* One shot (ScalarShot) as possrcrec_scaletf hands it to the backend:
  * nearest-grid-point indices and the scaled source time functions. */
@@ -150,6 +153,8 @@ typedef struct {
   int32_t misfit_kind;      /* gradient: 0 = L2Misfit, 1 = CCTSMisfit (src/inversion/misfits/CCTSMisfit.jl:17-61;
                                windows and inverse covariances are then unused, nt <= 13000) */
   double misfit_dt;         /* CCTSMisfit.dt (misfit_kind 1) */
+  const double* cpml64;     /* NULL, or the cpml coefficients in FP64 (host memory): the compensated forward
+                               (sw_wavesim_set_precision 1) evaluates the C-PML strips with them */
 } sw_acoustic_shot;
 
 /* GradParameters. */

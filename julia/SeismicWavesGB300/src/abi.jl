@@ -46,6 +46,7 @@ struct SwAcousticShot
     invcov::Ptr{Float32}     # dense (nt, nt) C^-1 or C_NULL (takes precedence over invcov_diag)
     misfit_kind::Int32       # 0 L2Misfit, 1 CCTSMisfit
     misfit_dt::Float64       # CCTSMisfit.dt
+    cpml64::Ptr{Float64}     # C_NULL or the cpml coefficients in Float64 (compensated forward)
 end
 
 # GradParameters (sw_grad_params)

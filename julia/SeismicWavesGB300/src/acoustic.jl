@@ -96,7 +96,7 @@ sw_struct(b::ScalarShotBuffers) =
     SwAcousticShot(Int32(size(b.tr, 1)), Int32(size(b.si, 1)), pointer(b.si), pointer(b.tf), Int32(size(b.ri, 1)),
                    pointer(b.ri), pointer(b.tr), pointer(b.cp), optptr(b.obs), optptr(b.icd),
                    Int32(length(b.win) ÷ 2), isempty(b.win) ? Ptr{Int32}(C_NULL) : pointer(b.win),
-                   pointer(b.sp), pointer(b.rp), optptr(b.icf), b.kind, b.mdt)
+                   pointer(b.sp), pointer(b.rp), optptr(b.icf), b.kind, b.mdt, Ptr{Float64}(C_NULL))
 
 const GB300Acoustic = Union{GB300CD, GB300VD}
 

@@ -22,7 +22,7 @@ STATUS_NAMES = {
 # Every function declared in include/swgb300.h (checked by the test-suite).
 EXPORTS = [
     "sw_version", "sw_ctx_create", "sw_ctx_destroy", "sw_ctx_last_error", "sw_ctx_stream",
-    "sw_cpml_coefficients", "sw_wavesim_create", "sw_wavesim_destroy", "sw_wavesim_set_vp",
+    "sw_cpml_coefficients", "sw_cpml_coefficients64", "sw_wavesim_create", "sw_wavesim_destroy", "sw_wavesim_set_vp",
     "sw_acoustic_forward", "sw_acoustic_gradient", "sw_wavesim_set_tuning", "sw_wavesim_set_band_heights",
     "sw_wavesim_set_precision", "sw_wavesim_set_vp64",
     "sw_wavesim_set_wait_test",
@@ -46,7 +46,7 @@ class SwAcousticShot(ctypes.Structure):
     _fields_ = [("nt", i32), ("nsrc", i32), ("src_idx", vp_), ("srctf", vp_), ("nrec", i32),
                 ("rec_idx", vp_), ("traces", vp_), ("cpml", vp_), ("observed", vp_),
                 ("invcov_diag", vp_), ("nwin", i32), ("windows", vp_), ("src_pos", vp_), ("rec_pos", vp_),
-                ("invcov", vp_), ("misfit_kind", i32), ("misfit_dt", f64)]
+                ("invcov", vp_), ("misfit_kind", i32), ("misfit_dt", f64), ("cpml64", vp_)]
 
 
 class SwGradParams(ctypes.Structure):
@@ -98,6 +98,7 @@ def load() -> ctypes.CDLL:
     lib.sw_ctx_stream.argtypes = [vp_]
     lib.sw_ctx_stream.restype = vp_
     lib.sw_cpml_coefficients.argtypes = [f64, f64, i32, f64, f64, f64, i32, vp_, vp_, vp_, vp_]
+    lib.sw_cpml_coefficients64.argtypes = [f64, f64, i32, f64, f64, f64, i32, vp_, vp_, vp_, vp_]
     lib.sw_wavesim_create.argtypes = [vp_, P(SwAcousticParams), i32, P(SwGradParams), P(vp_)]
     lib.sw_wavesim_destroy.argtypes = [vp_]
     lib.sw_wavesim_set_vp.argtypes = [vp_, vp_, i32]
@@ -168,6 +169,22 @@ class Context:
             self.close()
         except Exception:
             pass
+
+
+def cpml_coefficients64(vel_max, dt, halo, rcoef, h, f0, freetop_axis):
+    """sw_cpml_coefficients64 -> (a, a_h, b, b_h) float64 arrays."""
+    import numpy as np
+    lib = load()
+    a = np.zeros(2 * (halo + 1))
+    b = np.zeros(2 * (halo + 1))
+    ah = np.zeros(max(2 * halo, 1))
+    bh = np.zeros(max(2 * halo, 1))
+    rc = lib.sw_cpml_coefficients64(float(vel_max), float(dt), int(halo), float(rcoef), float(h), float(f0),
+                                    int(bool(freetop_axis)), a.ctypes.data, ah.ctypes.data, b.ctypes.data,
+                                    bh.ctypes.data)
+    if rc != SW_OK:
+        raise SwError(rc, "sw_cpml_coefficients64: invalid arguments")
+    return a, ah[: 2 * halo], b, bh[: 2 * halo]
 
 
 def cpml_coefficients(vel_max, dt, halo, rcoef, h, f0, freetop_axis):

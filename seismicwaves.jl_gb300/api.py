@@ -461,16 +461,18 @@ class AcousticCDCPMLWaveSimulation:
                     warnings.warn(f"Position {p} is inside the CPML region!")
 
     # -- per-shot host preprocessing -------------------------------------------
-    def cpml_block(self, domfreq: float) -> np.ndarray:
-        """init_bdc!: this shot's coefficients, [a, a_h, b, b_h] per axis."""
+    def cpml_block(self, domfreq: float, fp64: bool = False) -> np.ndarray:
+        """init_bdc!: this shot's coefficients, [a, a_h, b, b_h] per axis (FP32, or FP64 for the
+        compensated forward)."""
         cp = self.cpmlparams
         vmax = float(np.max(self.matprop.vp)) if cp.vel_max is None else float(cp.vel_max)
         N = len(self.grid.size)
+        coeffs = _lib.cpml_coefficients64 if fp64 else _lib.cpml_coefficients
         parts = []
         for d in range(N):
-            parts += _lib.cpml_coefficients(vmax, self.dt, cp.halo, cp.rcoef, self.grid.spacing[d], domfreq,
-                                            cp.freeboundtop and d == N - 1)
-        return np.concatenate(parts).astype(np.float32)
+            parts += coeffs(vmax, self.dt, cp.halo, cp.rcoef, self.grid.spacing[d], domfreq,
+                            cp.freeboundtop and d == N - 1)
+        return np.concatenate(parts).astype(np.float64 if fp64 else np.float32)
 
     def find_nearest_grid_points(self, positions) -> np.ndarray:
         return nearest_grid_points(positions, self.grid.spacing)
@@ -495,6 +497,10 @@ class AcousticCDCPMLWaveSimulation:
             st.src_idx, st.rec_idx = possrcs.ctypes.data, posrecs.ctypes.data
             st.srctf, st.traces, st.cpml = scal.ctypes.data, traces.ctypes.data, cp.ctypes.data
             arrs = [possrcs, posrecs, scal, traces, cp]
+            if self.runparams.compensated:
+                cp64 = self.cpml_block(shot.srcs.domfreq, fp64=True)
+                st.cpml64 = cp64.ctypes.data
+                arrs.append(cp64)
             if misfits is not None:
                 m = misfits[k]
                 obs = np.asfortranarray(m.observed, dtype=np.float32)

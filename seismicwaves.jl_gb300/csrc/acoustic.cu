@@ -478,6 +478,8 @@ struct sw_wavesim {
   DevMem d_pair, d_recstash, d_stash;     // two-step launches: per-shot source / receiver-row table,
                                           // receiver -> stash index, first-step pressure of receiver rows
   bool pair_on = false;                   // 2D: two time steps per launch where possible (tuning variant)
+  bool split3d = true;                    // 3D: inner rows and strip rows as two launches (variant bit 16: one)
+  bool inner_np = false;                  // 3D inner rows without the software pipeline (variant bit 17)
   int pair_tz = 0;                        // rows per block of the two-step kernel (0 = heuristic)
   int pair_occ = 0;                       // resident-block bound of the two-step kernel (0 = default, 1, 2)
   bool pair_ok = false;                   // the current group's shots allow two-step launches
@@ -502,6 +504,7 @@ struct sw_wavesim {
   int precision = 0;                          // 1: compensated (double-FP32) forward steps (k_ac_hp)
   DevMem plo[2], dlo, fact_lo;                 // their low parts of p (ping-pong), d and fact
   DevMem vp64;                                 // FP64 vp of sw_wavesim_set_vp64 (fact's low part comes from it)
+  DevMem psi64[2][3], xi64[3], d_cpml64;       // compensated step: FP64 C-PML memory variables, coefficients
   int hp_cap = 0;                              // shots the low-part buffers hold
   long long wait_cycles = TMA_TIMEOUT_CYCLES;  // limit of one bounded device-side wait
   int withhold = -1;                           // test hook of the TMA stencil (StepArgs::withhold)
@@ -597,6 +600,7 @@ std::vector<long long> group_key(const sw_wavesim* ws, const std::vector<HostSho
   std::vector<long long> k = {grad ? 1 : 0, ws->grp, ws->variant, ws->tile_tz, ws->pf, ws->adjw ? 1 : 0,
                               ws->cpa ? 1 : 0, ws->pair_ok ? 1 : 0, ws->pair_adj_ok ? 1 : 0, ws->pair_tz,
                               ws->pair_occ, ws->kind_tz[0], ws->kind_tz[1], ws->kind_tz[2], ws->precision,
+                              ws->split3d ? 1 : 0, ws->inner_np ? 1 : 0,
                               (long long)group.size()};
   for (const auto& h : group) k.push_back(h.nt);
   return k;
@@ -766,6 +770,7 @@ void build_tables(sw_wavesim* ws, const sw_acoustic_shot* shots, const std::vect
   const int na = 2 * ws->prm.halo + 2, nh = 2 * ws->prm.halo;
   const int cstride = ws->N * (2 * na + 2 * nh);
   std::vector<float> cpml((size_t)S * cstride);
+  std::vector<double> cpml64(ws->precision == 1 ? (size_t)S * cstride : 0);
   std::vector<float> masks;
   long long tf_o = 0, tr_o = 0, ic_o = 0;
   for (int k = 0; k < S; ++k) {
@@ -786,6 +791,8 @@ void build_tables(sw_wavesim* ws, const sw_acoustic_shot* shots, const std::vect
       T.rec.push_back(lin_of(ws, I));
     }
     std::memcpy(&cpml[(size_t)k * cstride], s.cpml, sizeof(float) * cstride);
+    if (ws->precision == 1)  // FP64 coefficients of the compensated step (the FP32 ones widened if absent)
+      for (int q = 0; q < cstride; ++q) cpml64[(size_t)k * cstride + q] = s.cpml64 ? s.cpml64[q] : (double)s.cpml[q];
     const long long ntf = (long long)s.nt * s.nsrc, ntr = (long long)s.nt * s.nrec;
     if (on_device) {
       D.tf = s.srctf;
@@ -910,6 +917,7 @@ void build_tables(sw_wavesim* ws, const sw_acoustic_shot* shots, const std::vect
   upload(ws, ws->d_ids, T.ids, "point ids");
   upload(ws, ws->d_rec, T.rec, "receiver table");
   upload(ws, ws->d_cpml, cpml, "cpml coefficients");
+  if (ws->precision == 1) upload(ws, ws->d_cpml64, cpml64, "cpml coefficients (FP64)");
   if (!masks.empty())
     check_cuda(cudaMemcpyAsync(ws->d_mask.p, masks.data(), masks.size() * sizeof(float), cudaMemcpyHostToDevice, st),
                "mask upload");
@@ -924,6 +932,7 @@ size_t owned_bytes(const sw_wavesim* ws) {
   for (int b = 0; b < 2; ++b) owned += ws->pb[b].bytes + ws->ab[b].bytes + ws->plo[b].bytes;
   owned += ws->db.bytes + ws->adb.bytes + ws->g.bytes + ws->gc.bytes + ws->dbuf.bytes + ws->ck.bytes + ws->dlo.bytes;
   owned += ws->db2.bytes + ws->adb2.bytes + ws->ck16.bytes + ws->ck_stage.bytes;
+  for (int d = 0; d < 3; ++d) owned += ws->psi64[0][d].bytes + ws->psi64[1][d].bytes + ws->xi64[d].bytes;
   for (int k = 0; k < 2; ++k)
     for (int d = 0; d < 3; ++d) owned += ws->psi[k][d].bytes + ws->apsi[k][d].bytes;
   return owned;
@@ -948,6 +957,11 @@ void ensure_state(sw_wavesim* ws, int S, bool grad, int max_nt) {
     ws->ck_stage.release();
     for (int b = 0; b < 2; ++b) ws->plo[b].release();
     ws->dlo.release();
+    for (int d = 0; d < 3; ++d) {
+      ws->psi64[0][d].release();
+      ws->psi64[1][d].release();
+      ws->xi64[d].release();
+    }
     ws->hp_cap = 0;
     ws->cap = 0;
   }
@@ -987,6 +1001,11 @@ void ensure_state(sw_wavesim* ws, int S, bool grad, int max_nt) {
   if (ws->precision == 1 && ws->hp_cap < ws->cap) {
     for (int b = 0; b < 2; ++b) dev_alloc(ws->plo[b], (size_t)ws->cap * F * sizeof(float), "pressure low part", st);
     dev_alloc(ws->dlo, (size_t)ws->cap * F * sizeof(float), "increment low part", st);
+    for (int d = 0; d < ws->N; ++d) {
+      for (int k = 0; k < 2; ++k)
+        dev_alloc(ws->psi64[k][d], (size_t)ws->cap * ws->psz[d] * sizeof(double), "psi (FP64)", st);
+      dev_alloc(ws->xi64[d], (size_t)ws->cap * ws->xsz[d] * sizeof(double), "xi (FP64)", st);
+    }
     ws->hp_cap = ws->cap;
     ++ws->gen;
   }
@@ -1031,7 +1050,10 @@ size_t per_shot_bytes(const sw_wavesim* ws, bool grad, int max_nt) {
   if (ws->gradient) floats = 2 * floats + 2 * ws->F;
   if (ws->N == 2) floats += ws->F + 2 * ws->strip_total;  // second d / xi buffers, scratch strips
   if (ws->N == 2 && ws->gradient) floats += ws->F + ws->strip_total;  // second adjoint d / xi buffers
-  if (ws->precision == 1) floats += 3 * ws->F;  // low parts of p (two buffers) and d
+  if (ws->precision == 1) {  // low parts of p (two buffers) and d; FP64 psi (two buffers) and xi
+    floats += 3 * ws->F;
+    for (int d = 0; d < ws->N; ++d) floats += 4 * ws->psz[d] + 2 * ws->xsz[d];
+  }
   if (grad) {
     const int K = ws->gp.check_freq;
     const long long dsl = (K == 1 ? (long long)max_nt : K) * ws->F;
@@ -1250,6 +1272,32 @@ void launch_pair(long long blocks, cudaStream_t st, const StepArgs& a, const Pai
   k_ac2d_pair<MODE, 4, MB><<<(unsigned)blocks, 128, 0, st>>>(a, b);
 }
 
+// Grid of the two-launch 3D step (the host side of ac3d_work): per axis the
+// rows [1, a) and [b, n-1) hold the C-PML strips.
+struct Split3d {
+  int tiles_y1, tiles_z1;  // region 1: y groups x z bands over [a, b) x [a, b)
+  int shell_units;         // region 2: (z band, y group) units per x tile
+};
+void split_axis_host(int n, int H, int& a, int& b) {
+  a = std::min(std::max(H, 1), n - 1);
+  b = std::max(n - std::max(H, 1), a);
+}
+Split3d split3d(const sw_wavesim* ws, int TZ, int NW) {
+  const int ny = ws->n[1], nz = ws->n[2], H = ws->prm.halo;
+  int ay, by, az, bz;
+  split_axis_host(ny, H, ay, by);
+  split_axis_host(nz, H, az, bz);
+  Split3d r;
+  r.tiles_y1 = (by - ay + NW - 1) / NW;
+  r.tiles_z1 = (bz - az + TZ - 1) / TZ;
+  if (r.tiles_y1 == 0 || r.tiles_z1 == 0) r.tiles_y1 = r.tiles_z1 = 0;
+  const int gy_all = (ny - 2 + NW - 1) / NW;
+  const int nb_lo = (az - 1 + TZ - 1) / TZ, nb_hi = (nz - 1 - bz + TZ - 1) / TZ;
+  const int gyl = (ay - 1 + NW - 1) / NW, gyh = (ny - 1 - by + NW - 1) / NW;
+  r.shell_units = (nb_lo + nb_hi) * gy_all + ((bz - az + TZ - 1) / TZ) * (gyl + gyh);
+  return r;
+}
+
 struct Launcher {
   sw_wavesim* ws;
   cudaStream_t st;
@@ -1306,6 +1354,26 @@ struct Launcher {
         k_ac2d_step<MODE, 8><<<(unsigned)blocks, 256, 0, st>>>(a);
       else
         k_ac2d_step<MODE, 16><<<(unsigned)blocks, 512, 0, st>>>(a);
+    } else if (ws->split3d) {
+      // rows outside the y / z strips, then the strip rows (k_ac3d_inner, k_ac3d_shell)
+      const int nw = block_rows3d(ws);
+      const Split3d sp = split3d(ws, c.TZ, nw);
+      StepArgs a1 = a;
+      a1.tiles_y = sp.tiles_y1;
+      a1.tiles_z = sp.tiles_z1;
+      const long long b1 = (long long)a.nshots * c.tiles_x * sp.tiles_y1 * sp.tiles_z1;
+      const long long b2 = (long long)a.nshots * c.tiles_x * sp.shell_units;
+      if (b1 > 0 && ws->inner_np) {
+        if (nw == 8) k_ac3d_inner_np<MODE, 8><<<(unsigned)b1, 256, 0, st>>>(a1);
+        else k_ac3d_inner_np<MODE><<<(unsigned)b1, 128, 0, st>>>(a1);
+      } else if (b1 > 0) {
+        if (nw == 8) k_ac3d_inner<MODE, 8><<<(unsigned)b1, 256, 0, st>>>(a1);
+        else k_ac3d_inner<MODE><<<(unsigned)b1, 128, 0, st>>>(a1);
+      }
+      if (b2 > 0) {
+        if (nw == 8) k_ac3d_shell<MODE, 8><<<(unsigned)b2, 256, 0, st>>>(a);
+        else k_ac3d_shell<MODE><<<(unsigned)b2, 128, 0, st>>>(a);
+      }
     } else {
       const int nw = block_rows3d(ws);
       if constexpr (MODE == MODE_FWD) {
@@ -1375,6 +1443,8 @@ StepArgs base_args(sw_wavesim* ws, const StepCtx& c, int S) {
   a.err = ws->ctx->err.as<int>();
   if (ws->precision == 1) {
     a.fact_lo = ws->fact_lo.as<float>();
+    a.cpml64 = ws->d_cpml64.as<double>();
+    for (int d = 0; d < ws->N; ++d) a.ihd[d] = 1.0 / ws->prm.h[d];
     for (int d = 0; d < ws->N; ++d) {
       const double ih2 = 1.0 / (ws->prm.h[d] * ws->prm.h[d]);
       a.ih2[d] = (float)ih2;
@@ -1427,6 +1497,11 @@ void zero_state(sw_wavesim* ws, int S, bool adjoint) {
     for (int k = 0; k < 2; ++k)
       check_cuda(cudaMemsetAsync(ws->plo[k].p, 0, (size_t)S * ws->F * sizeof(float), st), "reset p low part");
     check_cuda(cudaMemsetAsync(ws->dlo.p, 0, (size_t)S * ws->F * sizeof(float), st), "reset d low part");
+    for (int d = 0; d < ws->N; ++d) {
+      for (int k = 0; k < 2; ++k)
+        check_cuda(cudaMemsetAsync(ws->psi64[k][d].p, 0, (size_t)S * ws->psz[d] * sizeof(double), st), "reset psi");
+      check_cuda(cudaMemsetAsync(ws->xi64[d].p, 0, (size_t)S * ws->xsz[d] * sizeof(double), st), "reset xi");
+    }
   }
   check_cuda(cudaMemsetAsync(ws->d_ring.p, 0, ws->d_ring.bytes, st), "reset rings");
 }
@@ -1514,6 +1589,11 @@ void set_io(sw_wavesim* ws, StepArgs& a, FwdState& s, bool two, bool adjoint) {
     a.plo_cur = fa(ws->plo[s.p], F);
     a.plo_new = fa(ws->plo[1 - s.p], F);
     a.dlo = fa(ws->dlo, F);
+    for (int d = 0; d < ws->N; ++d) {
+      a.psi64_in[d] = Field64{ws->psi64[s.k][d].as<double>(), ws->psz[d]};
+      a.psi64_out[d] = Field64{ws->psi64[1 - s.k][d].as<double>(), ws->psz[d]};
+      a.xi64[d] = Field64{ws->xi64[d].as<double>(), ws->xsz[d]};
+    }
   }
   a.din = fa(*db[s.d], F);
   a.dout = fa(*db[dn], F);
@@ -2172,6 +2252,8 @@ void wavesim_set_tuning(sw_wavesim* ws, int tz, int variant) {
   static const int pair_tz[8] = {0, 8, 16, 32, 64, 128, 4, 0};
   ws->pair_tz = pair_tz[(variant >> 11) & 7];
   ws->pair_occ = (variant >> 14) & 3;
+  ws->split3d = (variant & 65536) == 0;
+  ws->inner_np = (variant & 131072) != 0;
 }
 void wavesim_set_band_heights(sw_wavesim* ws, int tz_forward, int tz_recompute, int tz_adjoint) {
   ws->kind_tz[TZ_FORWARD] = tz_forward;

@@ -48,6 +48,11 @@ namespace swgb {
 // steps (k_flush_grad).
 enum StepMode { MODE_FWD = 0, MODE_FWD_D = 1, MODE_ADJ = 2, MODE_ADJW = 3 };
 
+struct Field64 {  // FP64 per-shot array: shot k at p + k * s
+  double* p;
+  long long s;
+};
+
 struct StepArgs {
   int n0, n1, n2;  // grid points per axis (n2 = 1 in 2D; the depth axis is n1 in 2D, n2 in 3D)
   int P;           // pitch of axis 0 in floats
@@ -69,10 +74,14 @@ struct StepArgs {
   int withhold;  // TMA stencil test hook: block 0's producer never issues this stage (-1 = none)
   int pf;                                          // 2D stencil: rows ahead prefetched into L2 (0 = off)
   int dbf16;                                       // Dout / dcorr hold BF16 (the pointers are __nv_bfloat16 arrays)
-  // compensated step (k_ac_hp): low parts of p[n], p[n+1] and d (in place), of fact and of 1/h^2
+  // compensated step (k_ac_hp): low parts of p[n], p[n+1] and d (in place), of fact and of 1/h^2;
+  // FP64 C-PML coefficients (stride cpml_stride), memory variables and 1/h
   FieldArg plo_cur, plo_new, dlo;
   const float* fact_lo;
   float ih2_lo[3];
+  const double* cpml64;
+  Field64 psi64_in[3], psi64_out[3], xi64[3];
+  double ihd[3];
 };
 
 struct StripIO {
@@ -1238,7 +1247,68 @@ __device__ __forceinline__ StripIO strip_io(const StepArgs& A, int d, int shot, 
   return s;
 }
 
-template <int MODE, int NW, bool FAST = false>
+// Split of the (y, z) rows for the two-launch 3D step: per axis the rows
+// [1, a) and [b, n-1) lie in (or next to) the C-PML strips, [a, b) outside.
+__device__ __forceinline__ void split_axis(int n, int H, int& a, int& b) {
+  a = min(max(H, 1), n - 1);
+  b = max(n - max(H, 1), a);
+}
+
+// Work of one warp in the 3D step: (y row, z band) for a block index.
+// REGION 0: the whole grid (tiles_y x tiles_z bands).  REGION 1: rows with y
+// and z outside the C-PML strips (tiles_y x tiles_z over [a, b) of each).
+// REGION 2: the rest -- z slabs (z in [1, a) or [b, nz-1), every y) then y
+// slabs (z in [a, b), y in [1, a) or [b, ny-1)) -- enumerated per x tile.
+template <int NW, int REGION>
+__device__ __forceinline__ bool ac3d_work(const StepArgs& A, int tile, int warp, int& y, int& z_begin, int& z_end) {
+  const int ny = A.n1, nz = A.n2, H = A.halo, TZ = A.TZ;
+  if (REGION == 0) {
+    const int tyi = tile % A.tiles_y, tzi = tile / A.tiles_y;
+    y = 1 + tyi * NW + warp;
+    z_begin = 1 + tzi * TZ;
+    z_end = min(z_begin + TZ, nz - 1);
+    return z_begin < z_end && y <= ny - 2;
+  }
+  int ay, by, az, bz;
+  split_axis(ny, H, ay, by);
+  split_axis(nz, H, az, bz);
+  if (REGION == 1) {
+    const int tyi = tile % A.tiles_y, tzi = tile / A.tiles_y;
+    y = ay + tyi * NW + warp;
+    z_begin = az + tzi * TZ;
+    z_end = min(z_begin + TZ, bz);
+    return z_begin < z_end && y < by;
+  }
+  const int gy_all = (ny - 2 + NW - 1) / NW;
+  const int nb_lo = (az - 1 + TZ - 1) / TZ, nb_hi = (nz - 1 - bz + TZ - 1) / TZ;
+  const int uz = (nb_lo + nb_hi) * gy_all;
+  if (tile < uz) {
+    const int kz = tile / gy_all, gy = tile % gy_all;
+    y = 1 + gy * NW + warp;
+    if (kz < nb_lo) {
+      z_begin = 1 + kz * TZ;
+      z_end = min(z_begin + TZ, az);
+    } else {
+      z_begin = bz + (kz - nb_lo) * TZ;
+      z_end = min(z_begin + TZ, nz - 1);
+    }
+    return z_begin < z_end && y <= ny - 2;
+  }
+  tile -= uz;
+  const int gyl = (ay - 1 + NW - 1) / NW, gyh = (ny - 1 - by + NW - 1) / NW;
+  if (gyl + gyh == 0) return false;
+  const int kz = tile / (gyl + gyh), g = tile % (gyl + gyh);
+  z_begin = az + kz * TZ;
+  z_end = min(z_begin + TZ, bz);
+  if (g < gyl) {
+    y = 1 + g * NW + warp;
+    return z_begin < z_end && y < ay;
+  }
+  y = by + (g - gyl) * NW + warp;
+  return z_begin < z_end && y <= ny - 2;
+}
+
+template <int MODE, int NW, bool FAST = false, int REGION = 0, bool PIPE = true>
 __device__ __forceinline__ void ac3d_body(const StepArgs& A) {
   constexpr unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -1247,13 +1317,10 @@ __device__ __forceinline__ void ac3d_body(const StepArgs& A) {
   int tile = blockIdx.x / S;
   const int txi = tile % A.tiles_x;
   tile /= A.tiles_x;
-  const int tyi = tile % A.tiles_y, tzi = tile / A.tiles_y;
   const int nx = A.n0, ny = A.n1, nz = A.n2, P = A.P, H = A.halo;
-  const int y = 1 + tyi * NW + warp;  // one y row per warp, NW rows per block
-  const int z_begin = 1 + tzi * A.TZ;
-  const int z_end = min(z_begin + A.TZ, nz - 1);
+  int y, z_begin, z_end;  // one y row per warp, NW rows per block
+  if (!ac3d_work<NW, REGION>(A, tile, warp, y, z_begin, z_end)) return;  // warp-uniform
   const int wx0 = txi * 128;
-  if (z_begin >= z_end || y > ny - 2) return;  // warp-uniform
   const int x0 = wx0 + lane * 4;
   const bool inb = x0 < P;
   const int xa = inb ? x0 : P - 4;
@@ -1267,7 +1334,7 @@ __device__ __forceinline__ void ac3d_body(const StepArgs& A) {
   const int na = 2 * H + 2, nh = 2 * H;
 
   const bool xstrip = inb && (x0 < H || x0 + 3 >= nx - H);
-  const bool ystrip = (y < H) || (y >= ny - H);
+  const bool ystrip = REGION != 1 && ((y < H) || (y >= ny - H));  // region 1: never
   // the warp's 128 x points and its y row interior and outside the strips
   const bool fastxy = wx0 >= plain_lo(H) && wx0 + 127 <= plain_hi(nx, H) && y >= plain_lo(H) && y <= plain_hi(ny, H);
   const bool vec_interior = (x0 >= 1) && (x0 + 3 <= nx - 2);
@@ -1289,18 +1356,26 @@ __device__ __forceinline__ void ac3d_body(const StepArgs& A) {
     const long long idx = (long long)z_begin * plane + rowoff;
     ld4(rm, pc + idx - plane);
     ld4(r0, pc + idx);
-    ld4(rp, pc + idx + plane);
-    ld4(ym, pc + idx - P);
-    ld4(yp, pc + idx + P);
-    ld4rw(o, di + idx);
-    ld4(f, fa + idx);
+    if (PIPE) {
+      ld4(rp, pc + idx + plane);
+      ld4(ym, pc + idx - P);
+      ld4(yp, pc + idx + P);
+      ld4rw(o, di + idx);
+      ld4(f, fa + idx);
+    }
   }
   for (int z = z_begin; z < z_end; ++z) {
     const long long base = (long long)z * plane;
     const long long idx = base + rowoff;
-    const bool more = z + 1 < z_end;
+    const bool more = PIPE && z + 1 < z_end;
     float rpn[4], ymn[4], ypn[4], on[4], fn[4];
-    if (more) {
+    if (!PIPE) {  // no software pipeline: fewer registers, more resident warps
+      ld4(rp, pc + idx + plane);
+      ld4(ym, pc + idx - P);
+      ld4(yp, pc + idx + P);
+      ld4rw(o, di + idx);
+      ld4(f, fa + idx);
+    } else if (more) {
       const long long nidx = idx + plane;
       ld4(rpn, pc + nidx + plane);
       ld4(ymn, pc + nidx - P);
@@ -1312,7 +1387,7 @@ __device__ __forceinline__ void ac3d_body(const StepArgs& A) {
     float right = __shfl_down_sync(FULL, r0[0], 1);
     if (lane == 0) left = xa > 0 ? pc[idx - 1] : 0.f;
     if (lane == 31) right = xa + 4 < P ? pc[idx + 4] : 0.f;
-    const bool zstrip = (z < H) || (z >= nz - H);
+    const bool zstrip = REGION != 1 && ((z < H) || (z >= nz - H));  // region 1: never
     float outp[4], outd[4], outD[4];
     if (FAST && fastxy && z >= plain_lo(H) && z <= plain_hi(nz, H)) {
       // warp-uniform: every point interior and outside the strips
@@ -1427,6 +1502,22 @@ __global__ void __launch_bounds__(32 * NW, 24 / NW) k_ac3d_step(const StepArgs A
 template <int MODE, int NW = 4>
 __global__ void __launch_bounds__(32 * NW) k_ac3d_fwd(const StepArgs A) {
   ac3d_body<MODE, NW, true>(A);
+}
+// Two-launch 3D step: rows outside the y and z strips (no y / z C-PML code,
+// fewer registers), then the rows of the strips.  Every point is computed by
+// exactly one of the two launches with the arithmetic of ac3d_body.
+template <int MODE, int NW = 4>
+__global__ void __launch_bounds__(32 * NW, 24 / NW) k_ac3d_inner(const StepArgs A) {
+  ac3d_body<MODE, NW, false, 1>(A);
+}
+// the same without the software pipeline, at 8 resident blocks of 4 warps
+template <int MODE, int NW = 4>
+__global__ void __launch_bounds__(32 * NW, 32 / NW) k_ac3d_inner_np(const StepArgs A) {
+  ac3d_body<MODE, NW, false, 1, false>(A);
+}
+template <int MODE, int NW = 4>
+__global__ void __launch_bounds__(32 * NW, 16 / NW) k_ac3d_shell(const StepArgs A) {
+  ac3d_body<MODE, NW, false, 2>(A);
 }
 
 // ---------------------------------------------------------------------------
@@ -1712,9 +1803,9 @@ __global__ void __launch_bounds__(160, TmaLayout<MODE>::MIN_BLOCKS) k_ac2d_tma(c
 // transformations: Knuth's TwoSum, the FMA form of Dekker's TwoProduct
 // (a*b - fl(a*b) = fma(a, b, -fl(a*b))) and Dekker's Fast2Sum
 // renormalisation (the double-double arithmetic of Dekker 1971 and of the QD
-// library of Hida, Li and Bailey), about 48 bits of significand.  The C-PML
-// memory variables stay FP32: their correction to the second difference is
-// small where the damping starts and is added to the compensated value.
+// library of Hida, Li and Bailey), about 48 bits of significand.  In the
+// C-PML strips (where sources and receivers often sit) the memory variables
+// and coefficients are FP64 and their correction is evaluated in FP64.
 // Same algorithm and update order as the FP32 step (k_ac2d_step / ac3d_body);
 // checkpoints and the D slots get the rounded hi + lo values.
 // ---------------------------------------------------------------------------
@@ -1753,10 +1844,43 @@ __device__ __forceinline__ ff ff_d2(float lh, float ll, float ch, float cl, floa
   return fast_two_sum(t.hi, lo);
 }
 
-// The C-PML correction of one axis (dpsi + xi), with the memory variables
-// advanced as in cpml_axis_term from the rounded second difference d2.
-__device__ __forceinline__ float cpml_axis_corr(float d2, float pl, float p0, float pr, int x, int n, int halo,
-                                                float ih, const StripIO& s) {
+// The C-PML correction of one axis (dpsi + xi) in FP64: the update of
+// cpml_axis_term with FP64 memory variables and coefficients and the
+// compensated pressures (hi + lo is exact in FP64), returned as an FP32 pair.
+struct Strip64 {
+  const double* psi_in;
+  double* psi_out;
+  float* ck_psi;
+  const double* xi_in;
+  double* xi_out;
+  float* ck_xi;
+  const double *a, *ah, *b, *bh;
+  long long psi_step, xi_step, psi_base, xi_base;
+};
+__device__ __forceinline__ Strip64 strip64_io(const StepArgs& A, int d, int shot, long long step) {
+  const int H = A.halo;
+  const int na = 2 * H + 2, nh = 2 * H, L = 2 * na + 2 * nh;
+  const double* cp = A.cpml64 + (long long)shot * A.cpml_stride + (long long)d * L;
+  Strip64 s;
+  s.psi_in = A.psi64_in[d].p + (long long)shot * A.psi64_in[d].s;
+  s.psi_out = A.psi64_out[d].p + (long long)shot * A.psi64_out[d].s;
+  s.xi_in = A.xi64[d].p + (long long)shot * A.xi64[d].s;
+  s.xi_out = const_cast<double*>(s.xi_in);  // in place
+  s.ck_psi = fptr(A.ck_psi[d], shot);
+  s.ck_xi = fptr(A.ck_xi[d], shot);
+  s.a = cp;
+  s.ah = cp + na;
+  s.b = cp + na + nh;
+  s.bh = cp + 2 * na + nh;
+  s.psi_step = step;
+  s.xi_step = step;
+  s.psi_base = 0;
+  s.xi_base = 0;
+  return s;
+}
+__device__ __forceinline__ double ff_d(ff a) { return (double)a.hi + (double)a.lo; }
+__device__ __forceinline__ ff cpml_axis_corr64(ff d2, ff pl, ff p0, ff pr, int x, int n, int halo, double ih,
+                                               const Strip64& s) {
   int qr;
   bool first;
   if (x < halo) {
@@ -1766,28 +1890,31 @@ __device__ __forceinline__ float cpml_axis_corr(float d2, float pl, float p0, fl
     qr = x + 1 - n + 2 * halo;
     first = (x == n - halo);
   } else {
-    return 0.f;
+    return ff{0.f, 0.f};
   }
   const int ql = qr - 1;
   const long long il = s.psi_base + (long long)ql * s.psi_step;
   const long long ir = s.psi_base + (long long)qr * s.psi_step;
-  const float oldl = s.psi_in[il];
-  const float oldr = s.psi_in[ir];
-  const float newl = radd(rmul(s.bh[ql], oldl), rmul(s.ah[ql], rmul(rsub(p0, pl), ih)));
-  const float newr = radd(rmul(s.bh[qr], oldr), rmul(s.ah[qr], rmul(rsub(pr, p0), ih)));
+  const double P0 = ff_d(p0);
+  const double oldl = s.psi_in[il];
+  const double oldr = s.psi_in[ir];
+  const double newl = s.bh[ql] * oldl + s.ah[ql] * ((P0 - ff_d(pl)) * ih);
+  const double newr = s.bh[qr] * oldr + s.ah[qr] * ((ff_d(pr) - P0) * ih);
   s.psi_out[ir] = newr;
-  if (s.ck_psi) s.ck_psi[ir] = oldr;
+  if (s.ck_psi) s.ck_psi[ir] = (float)oldr;
   if (first) {
     s.psi_out[il] = newl;
-    if (s.ck_psi) s.ck_psi[il] = oldl;
+    if (s.ck_psi) s.ck_psi[il] = (float)oldl;
   }
-  const float dpsi = rmul(rsub(newr, newl), ih);
+  const double dpsi = (newr - newl) * ih;
   const long long iq = s.xi_base + (long long)qr * s.xi_step;
-  const float xo = s.xi_in[iq];
-  if (s.ck_xi) s.ck_xi[iq] = xo;
-  const float xn = radd(rmul(s.b[qr], xo), rmul(s.a[qr], radd(d2, dpsi)));
+  const double xo = s.xi_in[iq];
+  if (s.ck_xi) s.ck_xi[iq] = (float)xo;
+  const double xn = s.b[qr] * xo + s.a[qr] * (ff_d(d2) + dpsi);
   s.xi_out[iq] = xn;
-  return radd(dpsi, xn);
+  const double corr = dpsi + xn;
+  const float hi = (float)corr;
+  return ff{hi, (float)(corr - (double)hi)};
 }
 
 // One warp = 128 x points (4 per thread) of one row (2D) or of one y row
@@ -1889,7 +2016,7 @@ __global__ void __launch_bounds__(128) k_ac_hp(const StepArgs A) {
       ff dm = ff_d2(rmh[e], rml[e], ch, cl, rph[e], rpl[e]);
       ff tx = ff_mul(dx, ih2x), tm = ff_mul(dm, ih2m);
       if (xstrip && pin) {
-        StripIO s0 = NDIM == 2 ? strip_io(A, 0, shot, 1) : strip_io(A, 0, shot, 1);
+        Strip64 s0 = strip64_io(A, 0, shot, 1);
         if (NDIM == 2) {
           s0.psi_base = (long long)z * nh;
           s0.xi_base = (long long)z * na;
@@ -1897,10 +2024,10 @@ __global__ void __launch_bounds__(128) k_ac_hp(const StepArgs A) {
           s0.psi_base = ((long long)z * ny + y) * nh;
           s0.xi_base = ((long long)z * ny + y) * na;
         }
-        tx = ff_add(tx, ff{cpml_axis_corr(ff_round(tx), xmh, ch, xph, x, nx, H, A.ih[0], s0), 0.f});
+        tx = ff_add(tx, cpml_axis_corr64(tx, ff{xmh, xml}, ff{ch, cl}, ff{xph, xpl}, x, nx, H, A.ihd[0], s0));
       }
       if (mstrip && pin) {
-        StripIO sm = strip_io(A, ax_m, shot, plane);
+        Strip64 sm = strip64_io(A, ax_m, shot, plane);
         if (NDIM == 2) {
           sm.psi_base = x;
           sm.xi_base = x;
@@ -1908,16 +2035,18 @@ __global__ void __launch_bounds__(128) k_ac_hp(const StepArgs A) {
           sm.psi_base = (long long)y * P + x;
           sm.xi_base = (long long)y * P + x;
         }
-        tm = ff_add(tm, ff{cpml_axis_corr(ff_round(tm), rmh[e], ch, rph[e], z, nm, H, A.ih[ax_m], sm), 0.f});
+        tm = ff_add(tm, cpml_axis_corr64(tm, ff{rmh[e], rml[e]}, ff{ch, cl}, ff{rph[e], rpl[e]}, z, nm, H,
+                                         A.ihd[ax_m], sm));
       }
       ff lap = ff_add(tx, tm);
       if (NDIM == 3) {
         ff ty = ff_mul(ff_d2(ymh[e], yml[e], ch, cl, yph[e], ypl[e]), ih2y);
         if (ystrip && pin) {
-          StripIO s1 = strip_io(A, 1, shot, P);
+          Strip64 s1 = strip64_io(A, 1, shot, P);
           s1.psi_base = (long long)z * nh * P + x;
           s1.xi_base = (long long)z * na * P + x;
-          ty = ff_add(ty, ff{cpml_axis_corr(ff_round(ty), ymh[e], ch, yph[e], y, ny, H, A.ih[1], s1), 0.f});
+          ty = ff_add(ty, cpml_axis_corr64(ty, ff{ymh[e], yml[e]}, ff{ch, cl}, ff{yph[e], ypl[e]}, y, ny, H, A.ihd[1],
+                                           s1));
         }
         lap = ff_add(lap, ty);
       }

@@ -219,6 +219,20 @@ int sw_cpml_coefficients(double vel_max, double dt, int32_t halo, double rcoef, 
   return SW_OK;
 }
 
+int sw_cpml_coefficients64(double vel_max, double dt, int32_t halo, double rcoef, double h, double f0,
+                           int32_t freetop_axis, double* a, double* a_h, double* b, double* b_h) {
+  if (halo < 0 || !(dt > 0) || !(h > 0) || !a || !b || (halo > 0 && (!a_h || !b_h))) return SW_ERR_ARG;
+  const int na = 2 * (halo + 1), nh = 2 * halo;
+  double* tmp = new (std::nothrow) double[2 * na + 2 * nh + 4];
+  if (!tmp) return SW_ERR_OOM;
+  swgb::cpml_axis_coefficients(vel_max, dt, halo, rcoef, h, f0, freetop_axis != 0, tmp, tmp + na, tmp + na + nh,
+                               tmp + 2 * na + nh);
+  for (int k = 0; k < na; ++k) { a[k] = tmp[k]; b[k] = tmp[na + nh + k]; }
+  for (int k = 0; k < nh; ++k) { a_h[k] = tmp[na + k]; b_h[k] = tmp[2 * na + nh + k]; }
+  delete[] tmp;
+  return SW_OK;
+}
+
 int sw_wavesim_create(sw_ctx* ctx, const sw_acoustic_params* params, int32_t gradient, const sw_grad_params* gparams,
                       sw_wavesim** out) {
   if (!ctx || !out) return SW_ERR_ARG;
@@ -311,7 +325,7 @@ int sw_profile_read(sw_ctx* ctx, int32_t kind, double* total_ms, int64_t* launch
 }
 
 int sw_wavesim_set_tuning(sw_wavesim* ws, int32_t tz, int32_t variant) {
-  if (!ws || tz < 0 || variant < 0 || variant >= (1 << 16)) return SW_ERR_ARG;
+  if (!ws || tz < 0 || variant < 0 || variant >= (1 << 18)) return SW_ERR_ARG;
   swgb::wavesim_set_tuning(ws, tz, variant);
   return SW_OK;
 }

@@ -10,7 +10,8 @@ read from the library's per-kind event timing -- and short forwards
 otherwise (3D, where gradient trials would be long).  Candidates for 2D: the
 register-pipelined stencil with 4-, 8- or 16-row bands and with 8 warps per
 block, the cp.async-staged stencil, two time steps per launch, and the
-grouped adjoint; for 3D the band height and 8 y rows per block.  A second
+grouped adjoint; for 3D the band height, 8 y rows per block, the inner
+rows without the software pipeline and the single-launch step.  A second
 stage then picks the band height of the forward, recompute and adjoint
 stencils separately, each from its own per-kind time
 (sw_wavesim_set_band_heights).  Results are cached per (grid, halo, shots,
@@ -32,7 +33,8 @@ _cache: dict = {}
 
 # (variant, tz) of sw_wavesim_set_tuning
 CANDIDATES_2D = [(0, 4), (0, 8), (0, 16), (2, 8), (512, 8), (1024, 0), (256, 8)]
-CANDIDATES_3D = [(0, 8), (0, 16), (0, 32), (2, 8)]
+# 3D: 131072 = inner rows without the software pipeline, 65536 = one launch per step
+CANDIDATES_3D = [(0, 8), (0, 16), (0, 32), (2, 8), (131072, 8), (131072, 16), (65536, 16)]
 KIND_NAMES = {0: "forward", 4: "recompute", 1: "adjoint"}
 # band heights tried per stencil kind after the variant is chosen (2D gradients)
 TZ_KIND_2D = (4, 8, 16)

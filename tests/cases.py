@@ -122,6 +122,7 @@ class GpuRun:
         self.h = ctypes.c_void_p()
         self.ctx.check(self.ctx.lib.sw_wavesim_create(self.ctx.h, ctypes.byref(prm), int(gradient),
                                                       ctypes.byref(gp), ctypes.byref(self.h)), "create")
+        self.precision = precision
         if precision:  # 1: compensated (double-FP32) forward steps, fact from the FP64 model
             self.ctx.check(self.ctx.lib.sw_wavesim_set_precision(self.h, int(precision)), "set_precision")
             vp64 = np.asfortranarray(case.vp, dtype=np.float64)
@@ -145,6 +146,15 @@ class GpuRun:
             st.src_idx, st.rec_idx, st.srctf, st.traces, st.cpml = (si.ctypes.data, ri.ctypes.data,
                                                                    scal.ctypes.data, tr.ctypes.data, cp.ctypes.data)
             items = [si, ri, scal, tr, cp]
+            if self.precision:  # the FP64 coefficients of the compensated forward
+                vmax = float(np.max(self.case.vp))
+                parts = []
+                for d in range(self.case.ndim):
+                    parts += L.cpml_coefficients64(vmax, self.case.dt, self.case.halo, self.case.rcoef, self.case.h[d],
+                                                   shot.f0, self.case.freetop and d == self.case.ndim - 1)
+                cp64 = np.concatenate(parts)
+                st.cpml64 = cp64.ctypes.data
+                items.append(cp64)
             if grad:
                 obs = np.asfortranarray(shot.observed, dtype=np.float32)
                 st.observed = obs.ctypes.data

@@ -46,3 +46,9 @@ def test_cpml_coefficients_match_oracle(sw, oracle, halo, freetop):
     assert np.all(b > 0) and np.all(b <= 1) and np.all(a <= 0)
     if freetop:
         assert np.all(a[: na // 2] == 0) and np.all(b[: na // 2] == 1)
+    # the FP64 entry point (compensated forward) gives the oracle's values to FP64 rounding and
+    # rounds to the FP32 ones
+    a6, ah6, b6, bh6 = sw._lib.cpml_coefficients64(vmax, dt, halo, rcoef, h, f0, freetop)
+    np.testing.assert_allclose(np.concatenate([a6, ah6, b6, bh6]), blk, rtol=1e-13, atol=1e-300)
+    for x32, x64 in ((a, a6), (ah, ah6), (b, b6), (bh, bh6)):
+        assert np.array_equal(x32, x64.astype(np.float32))
