@@ -165,7 +165,9 @@ typedef struct {
   int32_t compute_misfit;
   int32_t snapshot_bf16;    /* 0: FP32 snapshots; 1: the recompute buffer (the second time differences
                                kept between checkpoints) in BF16; 2: also the checkpoints' (p, d) in
-                               per-snapshot-scaled BF16.  Acoustic path only. */
+                               per-snapshot-scaled BF16; 3 (3D only): the recompute buffer in FP16 with
+                               a power-of-two scale per row and 128-point x tile (8x BF16's precision
+                               in the same 2 bytes, plus one byte per 128 points).  Acoustic path. */
 } sw_grad_params;
 
 /* build_wavesim.  `gradient` = 1 allows sw_acoustic_gradient.  Device memory

@@ -81,6 +81,30 @@ __device__ __forceinline__ float ring_update(float* ring, int slot, int it, floa
   return v;
 }
 
+// Sets (add = false) or adds to (add = true) the FP16 D value at lin and
+// re-encodes the point's 128-point tile when the new tile maximum calls for
+// another exponent (sources added after the stencil wrote the tile).
+__device__ void d16_put(float* d, signed char* ex, long long lin, float v, bool add, int P) {
+  __half* h = reinterpret_cast<__half*>(d);
+  const long long row = lin / P;
+  const int x = (int)(lin - row * P);
+  const int ntx = (P + 127) / 128;
+  signed char* ep = ex + row * ntx + (x >> 7);
+  const int e = *ep;
+  const long long t0 = row * P + (x & ~127), t1 = row * P + min((x | 127) + 1, P);
+  const float nv = add ? __half2float(h[lin]) * pow2f(-e) + v : v;
+  float m = fabsf(nv);
+  for (long long q = t0; q < t1; ++q)
+    if (q != lin) m = fmaxf(m, fabsf(__half2float(h[q]) * pow2f(-e)));
+  const int e2 = dexp_of(m);
+  if (e2 != e) {
+    for (long long q = t0; q < t1; ++q)
+      if (q != lin) h[q] = __float2half_rn(h_enc(__half2float(h[q]) * pow2f(-e), e2));
+    *ep = (signed char)e2;
+  }
+  h[lin] = __float2half_rn(h_enc(nv, e2));
+}
+
 // inject_sources! + record_receivers! for every active shot: one block per
 // shot.  Duplicated points are summed in source order by one thread, like the
 // reference's serial loop.  Interior points add the source to p[n+1] and to
@@ -92,7 +116,7 @@ __global__ void k_inject_record(const ShotDesc* __restrict__ desc, const long lo
                                 const int* __restrict__ bslot, const long long* __restrict__ rec_lin,
                                 FieldArg pnew, FieldArg dnew, FieldArg dfield, int d_first, int it, int record,
                                 int dbf16, const int* __restrict__ rec_stash, FieldArg stash, int it_stash,
-                                FieldArg plo, FieldArg dlo) {
+                                FieldArg plo, FieldArg dlo, FieldArgE dexp, int P) {
   const int shot = blockIdx.x;
   const ShotDesc D = desc[shot];
   if (it > D.nt) return;
@@ -104,6 +128,11 @@ __global__ void k_inject_record(const ShotDesc* __restrict__ desc, const long lo
   float* pn = pnew.p + (long long)shot * pnew.s;
   float* dn = dnew.p + (long long)shot * dnew.s;
   float* dd = (dfield.p && shot >= d_first) ? dptr(dfield, shot, dbf16) : nullptr;
+  float* dd16 = nullptr;  // FP16 D slots: updated below by one thread (tile exponents)
+  if (dbf16 == 2) {
+    dd16 = dd;
+    dd = nullptr;
+  }
   for (int u = threadIdx.x; u < D.nsp; u += blockDim.x) {
     const long long lin = pts[D.sp_off + u];
     float add = 0.f;
@@ -141,6 +170,22 @@ __global__ void k_inject_record(const ShotDesc* __restrict__ desc, const long lo
       if (dd) dst1(dd, lin, dld1(dd, lin, dbf16) + add, dbf16);
     }
   }
+  if (dbf16 == 2) __syncthreads();  // block-uniform: the rings above are updated
+  if (dd16 && threadIdx.x == 0) {
+    signed char* ex = dexp.p + (long long)shot * dexp.s;
+    for (int u = 0; u < D.nsp; ++u) {
+      const long long lin = pts[D.sp_off + u];
+      const int k0 = ptr[D.sp_ptr + u], k1 = ptr[D.sp_ptr + u + 1];
+      float add = 0.f;
+      for (int k = k0; k < k1; ++k) add += D.tf[(long long)(it - 1) + (long long)ids[k] * D.nt];
+      const int slot = bslot[D.sp_off + u];
+      if (slot >= 0)  // boundary node: D is the ring's second difference, read back from the ring
+        d16_put(dd16, ex, lin, D.ring[3 * slot + it % 3] - 2.f * D.ring[3 * slot + (it + 2) % 3] +
+                                     D.ring[3 * slot + (it + 1) % 3], false, P);
+      else
+        d16_put(dd16, ex, lin, add, true, P);
+    }
+  }
   if (!record) return;
   __syncthreads();
   const float* pnl = plo.p ? plo.p + (long long)shot * plo.s : nullptr;
@@ -156,7 +201,8 @@ __global__ void k_inject_record(const ShotDesc* __restrict__ desc, const long lo
 // here (boundary nodes, which the stencil skips, add their full lambda * D).
 __device__ void adj_inject_shot(const ShotDesc& D, const long long* __restrict__ pts, const int* __restrict__ ptr,
                                 const int* __restrict__ ids, const int* __restrict__ bslot, float* lp, float* ld,
-                                const float* dp, int dbf16, float* gp, float* cp, int it);
+                                const float* dp, int dbf16, float* gp, float* cp, int it, const signed char* ex,
+                                int P);
 
 // One block per accumulator group (grp consecutive shots share one gradient
 // pair); the group's shots are handled one after the other, so receivers of
@@ -164,7 +210,7 @@ __device__ void adj_inject_shot(const ShotDesc& D, const long long* __restrict__
 __global__ void k_adj_inject(const ShotDesc* __restrict__ desc, const long long* __restrict__ pts,
                              const int* __restrict__ ptr, const int* __restrict__ ids,
                              const int* __restrict__ bslot, FieldArg lam, FieldArg lamd, FieldArg dcorr, FieldArg g,
-                             FieldArg gc, int it, int nshots, int grp, int dbf16) {
+                             FieldArg gc, int it, int nshots, int grp, int dbf16, FieldArgE dexp, int P) {
   float* gp = g.p + (long long)blockIdx.x * g.s;
   float* cp = gc.p ? gc.p + (long long)blockIdx.x * gc.s : nullptr;  // null: plain FP32 sums
   for (int j = 0; j < grp; ++j) {
@@ -172,13 +218,15 @@ __global__ void k_adj_inject(const ShotDesc* __restrict__ desc, const long long*
     if (shot >= nshots) break;
     if (j > 0) __syncthreads();
     adj_inject_shot(desc[shot], pts, ptr, ids, bslot, lam.p + (long long)shot * lam.s,
-                    lamd.p + (long long)shot * lamd.s, dptr(dcorr, shot, dbf16), dbf16, gp, cp, it);
+                    lamd.p + (long long)shot * lamd.s, dptr(dcorr, shot, dbf16), dbf16, gp, cp, it,
+                    dexp.p ? dexp.p + (long long)shot * dexp.s : nullptr, P);
   }
 }
 
 __device__ void adj_inject_shot(const ShotDesc& D, const long long* __restrict__ pts, const int* __restrict__ ptr,
                                 const int* __restrict__ ids, const int* __restrict__ bslot, float* lp, float* ld,
-                                const float* dp, int dbf16, float* gp, float* cp, int it) {
+                                const float* dp, int dbf16, float* gp, float* cp, int it, const signed char* ex,
+                                int P) {
   if (it > D.nt) return;
   for (int u = threadIdx.x; u < D.nrp; u += blockDim.x) {
     const long long lin = pts[D.rp_off + u];
@@ -202,13 +250,15 @@ __device__ void adj_inject_shot(const ShotDesc& D, const long long* __restrict__
       ld[lin] += add;
       corr = add;
     }
+    // FP16 D slots: the exponent of the point's 128-point tile
+    const int e = ex ? ex[(lin / P) * ((P + 127) / 128) + ((lin % P) >> 7)] : 0;
     if (cp) {
       float gv = gp[lin], cv = cp[lin];
-      kahan_add(gv, cv, corr * dld1(dp, lin, dbf16));
+      kahan_add(gv, cv, corr * dld1(dp, lin, dbf16, e));
       gp[lin] = gv;
       cp[lin] = cv;
     } else {
-      gp[lin] = __fmaf_rn(corr, dld1(dp, lin, dbf16), gp[lin]);
+      gp[lin] = __fmaf_rn(corr, dld1(dp, lin, dbf16, e), gp[lin]);
     }
   }
 }
@@ -479,7 +529,7 @@ struct sw_wavesim {
                                           // receiver -> stash index, first-step pressure of receiver rows
   bool pair_on = false;                   // 2D: two time steps per launch where possible (tuning variant)
   bool split3d = true;                    // 3D: inner rows and strip rows as two launches (variant bit 16: one)
-  bool inner_np = false;                  // 3D inner rows without the software pipeline (variant bit 17)
+  bool inner_np = false;                  // 3D: the three launches without the software pipeline (variant bit 17)
   int pair_tz = 0;                        // rows per block of the two-step kernel (0 = heuristic)
   int pair_occ = 0;                       // resident-block bound of the two-step kernel (0 = default, 1, 2)
   bool pair_ok = false;                   // the current group's shots allow two-step launches
@@ -489,6 +539,7 @@ struct sw_wavesim {
   DevMem ab[2], adb, apsi[2][3], axi[3];  // adjoint state
   DevMem g, gc;
   DevMem dbuf;                         // D slots
+  DevMem dexp;                         // FP16 D slots (snapshot_bf16 3): exponent per row and 128-point x tile
   long long d_slots = 0;
   DevMem ck;                           // checkpoint slots (with BF16 snapshots: the psi / xi strips only)
   long long ck_slots = 0;
@@ -925,6 +976,21 @@ void build_tables(sw_wavesim* ws, const sw_acoustic_shot* shots, const std::vect
 
 size_t per_shot_bytes(const sw_wavesim* ws, bool grad, int max_nt);
 
+// Exponent array of the FP16 D slots: per slot rows x x-tiles bytes, slots of a shot contiguous.
+long long dexp_slot(const sw_wavesim* ws) {
+  long long rows = 1;
+  for (int d = 1; d < ws->N; ++d) rows *= ws->n[d];
+  return rows * ((ws->P + 127) / 128);
+}
+// The exponents of the D slot that `D` (a dslot_arg result) points to.
+FieldArgE dexp_for(const sw_wavesim* ws, const FieldArg& D) {
+  if (!D.p || ws->gp.snapshot_bf16 != 3) return FieldArgE{nullptr, 0};
+  const long long off = reinterpret_cast<const __half*>(D.p) - ws->dbuf.as<__half>();
+  const long long Fe = dexp_slot(ws);
+  return FieldArgE{ws->dexp.as<signed char>() + (off / ws->F) * Fe, ws->d_slots * Fe};
+}
+
+
 // Device memory held by the per-shot buffers (counted back into the budget of
 // plan_groups and ensure_state).
 size_t owned_bytes(const sw_wavesim* ws) {
@@ -1016,13 +1082,17 @@ void ensure_state(sw_wavesim* ws, int S, bool grad, int max_nt) {
       ws->dbuf.release();
       const size_t esz = ws->gp.snapshot_bf16 >= 1 ? sizeof(__nv_bfloat16) : sizeof(float);
       dev_alloc(ws->dbuf, (size_t)ws->cap * dslots * F * esz, "D buffer", st);
+      if (ws->gp.snapshot_bf16 == 3) {
+        dev_alloc(ws->dexp, (size_t)ws->cap * dslots * dexp_slot(ws), "D exponents", st);
+        check_cuda(cudaMemsetAsync(ws->dexp.p, 0, ws->dexp.bytes, st), "D exponents");
+      }
       ws->d_slots = dslots;
       ++ws->gen;
     }
     const long long cks = K == 1 ? 0 : max_nt / K;
     if (cks > ws->ck_slots) {
       ws->ck.release();
-      const bool bf = ws->gp.snapshot_bf16 >= 2;
+      const bool bf = ws->gp.snapshot_bf16 == 2;
       const long long slot = bf ? ws->strip_total : 2 * F + ws->strip_total;
       dev_alloc(ws->ck, (size_t)ws->cap * cks * slot * sizeof(float), "checkpoints", st);
       if (bf) {
@@ -1059,7 +1129,7 @@ size_t per_shot_bytes(const sw_wavesim* ws, bool grad, int max_nt) {
     const long long dsl = (K == 1 ? (long long)max_nt : K) * ws->F;
     floats += ws->gp.snapshot_bf16 >= 1 ? (dsl + 1) / 2 : dsl;  // BF16 D slots take half
     if (K > 1) {
-      if (ws->gp.snapshot_bf16 >= 2)  // BF16 (p, d) = one float's worth per point, plus the FP32 stage
+      if (ws->gp.snapshot_bf16 == 2)  // BF16 (p, d) = one float's worth per point, plus the FP32 stage
         floats += (long long)(max_nt / K) * (ws->F + ws->strip_total) + 2 * ws->F;
       else
         floats += (long long)(max_nt / K) * (2 * ws->F + ws->strip_total);
@@ -1276,7 +1346,8 @@ void launch_pair(long long blocks, cudaStream_t st, const StepArgs& a, const Pai
 // rows [1, a) and [b, n-1) hold the C-PML strips.
 struct Split3d {
   int tiles_y1, tiles_z1;  // region 1: y groups x z bands over [a, b) x [a, b)
-  int shell_units;         // region 2: (z band, y group) units per x tile
+  int zslab_units;         // region 2: (z band, y group) units per x tile
+  int yslab_units;         // region 3: the same for the y slabs
 };
 void split_axis_host(int n, int H, int& a, int& b) {
   a = std::min(std::max(H, 1), n - 1);
@@ -1294,7 +1365,8 @@ Split3d split3d(const sw_wavesim* ws, int TZ, int NW) {
   const int gy_all = (ny - 2 + NW - 1) / NW;
   const int nb_lo = (az - 1 + TZ - 1) / TZ, nb_hi = (nz - 1 - bz + TZ - 1) / TZ;
   const int gyl = (ay - 1 + NW - 1) / NW, gyh = (ny - 1 - by + NW - 1) / NW;
-  r.shell_units = (nb_lo + nb_hi) * gy_all + ((bz - az + TZ - 1) / TZ) * (gyl + gyh);
+  r.zslab_units = (nb_lo + nb_hi) * gy_all;
+  r.yslab_units = ((bz - az + TZ - 1) / TZ) * (gyl + gyh);
   return r;
 }
 
@@ -1302,7 +1374,12 @@ struct Launcher {
   sw_wavesim* ws;
   cudaStream_t st;
   template <int MODE>
-  void step(const StepArgs& a, const StepCtx& c, double bytes, bool recompute = false) {
+  void step(const StepArgs& a0, const StepCtx& c, double bytes, bool recompute = false) {
+    StepArgs a = a0;
+    if (a.dbf16 == 2) {  // the exponents of the FP16 D slots read / written
+      a.Dexp = dexp_for(ws, a.Dout);
+      a.dcorr_exp = dexp_for(ws, a.dcorr);
+    }
     check_vector_alignment(a);
     const long long blocks = (long long)a.nshots * c.tiles_x * c.tiles_y * c.tiles_z;
     cudaEvent_t ev = nullptr;
@@ -1355,14 +1432,15 @@ struct Launcher {
       else
         k_ac2d_step<MODE, 16><<<(unsigned)blocks, 512, 0, st>>>(a);
     } else if (ws->split3d) {
-      // rows outside the y / z strips, then the strip rows (k_ac3d_inner, k_ac3d_shell)
+      // rows outside the y / z strips, the z slabs, the y slabs (k_ac3d_inner, k_ac3d_zslab, k_ac3d_yslab)
       const int nw = block_rows3d(ws);
       const Split3d sp = split3d(ws, c.TZ, nw);
       StepArgs a1 = a;
       a1.tiles_y = sp.tiles_y1;
       a1.tiles_z = sp.tiles_z1;
       const long long b1 = (long long)a.nshots * c.tiles_x * sp.tiles_y1 * sp.tiles_z1;
-      const long long b2 = (long long)a.nshots * c.tiles_x * sp.shell_units;
+      const long long b2 = (long long)a.nshots * c.tiles_x * sp.zslab_units;
+      const long long b3 = (long long)a.nshots * c.tiles_x * sp.yslab_units;
       if (b1 > 0 && ws->inner_np) {
         if (nw == 8) k_ac3d_inner_np<MODE, 8><<<(unsigned)b1, 256, 0, st>>>(a1);
         else k_ac3d_inner_np<MODE><<<(unsigned)b1, 128, 0, st>>>(a1);
@@ -1370,9 +1448,19 @@ struct Launcher {
         if (nw == 8) k_ac3d_inner<MODE, 8><<<(unsigned)b1, 256, 0, st>>>(a1);
         else k_ac3d_inner<MODE><<<(unsigned)b1, 128, 0, st>>>(a1);
       }
-      if (b2 > 0) {
-        if (nw == 8) k_ac3d_shell<MODE, 8><<<(unsigned)b2, 256, 0, st>>>(a);
-        else k_ac3d_shell<MODE><<<(unsigned)b2, 128, 0, st>>>(a);
+      if (b2 > 0 && ws->inner_np) {
+        if (nw == 8) k_ac3d_zslab<MODE, 8, false><<<(unsigned)b2, 256, 0, st>>>(a);
+        else k_ac3d_zslab<MODE, 4, false><<<(unsigned)b2, 128, 0, st>>>(a);
+      } else if (b2 > 0) {
+        if (nw == 8) k_ac3d_zslab<MODE, 8><<<(unsigned)b2, 256, 0, st>>>(a);
+        else k_ac3d_zslab<MODE><<<(unsigned)b2, 128, 0, st>>>(a);
+      }
+      if (b3 > 0 && ws->inner_np) {
+        if (nw == 8) k_ac3d_yslab<MODE, 8, false><<<(unsigned)b3, 256, 0, st>>>(a);
+        else k_ac3d_yslab<MODE, 4, false><<<(unsigned)b3, 128, 0, st>>>(a);
+      } else if (b3 > 0) {
+        if (nw == 8) k_ac3d_yslab<MODE, 8><<<(unsigned)b3, 256, 0, st>>>(a);
+        else k_ac3d_yslab<MODE><<<(unsigned)b3, 128, 0, st>>>(a);
       }
     } else {
       const int nw = block_rows3d(ws);
@@ -1454,7 +1542,8 @@ StepArgs base_args(sw_wavesim* ws, const StepCtx& c, int S) {
   a.wait_cycles = ws->wait_cycles;
   a.withhold = ws->withhold;
   a.pf = ws->pf;
-  a.dbf16 = (ws->gradient && ws->gp.snapshot_bf16 >= 1) ? 1 : 0;
+  a.dbf16 = (ws->gradient && ws->gp.snapshot_bf16 >= 1) ? (ws->gp.snapshot_bf16 == 3 ? 2 : 1) : 0;
+  a.ntx = (int)((ws->P + 127) / 128);
   return a;
 }
 
@@ -1531,8 +1620,8 @@ void launch_inject(sw_wavesim* ws, int Sa, const FieldArg& pnew, const FieldArg&
   k_inject_record<<<Sa, 128, 0, st>>>(ws->d_desc.as<ShotDesc>(), ws->d_pts.as<long long>(), ws->d_ptr.as<int>(),
                                       ws->d_ids.as<int>(), ws->d_bslot.as<int>(), ws->d_rec.as<long long>(), pnew,
                                       dnew, Dw, d_first, it, record,
-                                      (ws->gradient && ws->gp.snapshot_bf16 >= 1) ? 1 : 0,
-                                      ws->d_recstash.as<int>(), stash, it_stash, plo, dlo);
+                                      (ws->gradient && ws->gp.snapshot_bf16 >= 1) ? (ws->gp.snapshot_bf16 == 3 ? 2 : 1) : 0,
+                                      ws->d_recstash.as<int>(), stash, it_stash, plo, dlo, dexp_for(ws, Dw), ws->P);
   check_cuda(cudaGetLastError(), "inject/record launch");
   ws->ctx->prof.end(st, KK_SRCREC, ev);
 }
@@ -1638,7 +1727,7 @@ void forward_group(sw_wavesim* ws, const std::vector<HostShot>& group, bool grad
   const int max_nt = group.front().nt;
   const int K = grad ? ws->gp.check_freq : 0;
   const long long F = ws->F;
-  const bool bf16 = grad && ws->gp.snapshot_bf16 >= 2;
+  const bool bf16 = grad && ws->gp.snapshot_bf16 == 2;
   const long long slot = bf16 ? ws->strip_total : 2 * F + ws->strip_total;
   FwdState sta;
   Launcher L{ws, st};
@@ -1732,7 +1821,7 @@ void adjoint_group(sw_wavesim* ws, const std::vector<HostShot>& group) {
   const int max_nt = group.front().nt;
   const int K = ws->gp.check_freq;
   const long long F = ws->F;
-  const bool bf16 = ws->gp.snapshot_bf16 >= 2;
+  const bool bf16 = ws->gp.snapshot_bf16 == 2;
   const long long slot = bf16 ? ws->strip_total : 2 * F + ws->strip_total;
   Launcher L{ws, st};
   zero_state(ws, S, true);
@@ -1843,7 +1932,8 @@ void adjoint_group(sw_wavesim* ws, const std::vector<HostShot>& group) {
     ws->ctx->prof.begin(st, KK_SRCREC, 0.0, &ev);
     k_adj_inject<<<(Sa + ws->grp - 1) / ws->grp, 128, 0, st>>>(
         ws->d_desc.as<ShotDesc>(), ws->d_pts.as<long long>(), ws->d_ptr.as<int>(), ws->d_ids.as<int>(),
-        ws->d_bslot.as<int>(), a.pnew, a.dout, dcorr_last, a.g, a.gc, it_last, Sa, ws->grp, a.dbf16);
+        ws->d_bslot.as<int>(), a.pnew, a.dout, dcorr_last, a.g, a.gc, it_last, Sa, ws->grp, a.dbf16,
+        dexp_for(ws, dcorr_last), ws->P);
     check_cuda(cudaGetLastError(), "adjoint inject launch");
     ws->ctx->prof.end(st, KK_SRCREC, ev);
     if (ws->adjw && (it_last - 1) % 32 == 0) {  // at most 32 terms per FP32 sum
@@ -1931,7 +2021,9 @@ void wavesim_init(sw_wavesim* ws, sw_ctx* ctx, const sw_acoustic_params* p, int 
     if (ws->gp.check_freq < 1) fail(SW_ERR_ARG, "check_freq must be positive");
     if (ws->gp.mute_radius_src < 0 || ws->gp.mute_radius_rec < 0)
       fail(SW_ERR_ARG, "mutearoundpoint!(): The smoothing radius must be positive.");
-    if (ws->gp.snapshot_bf16 < 0 || ws->gp.snapshot_bf16 > 2) fail(SW_ERR_ARG, "snapshot_bf16 must be 0, 1 or 2");
+    if (ws->gp.snapshot_bf16 < 0 || ws->gp.snapshot_bf16 > 3) fail(SW_ERR_ARG, "snapshot_bf16 must be 0, 1, 2 or 3");
+    if (ws->gp.snapshot_bf16 == 3 && ws->N != 3)
+      fail(SW_ERR_UNSUPPORTED, "snapshot_bf16 = 3 (FP16 recompute buffer) is available for 3D simulations");
   }
   ws->N = p->ndim;
   for (int d = 0; d < 3; ++d) ws->n[d] = d < p->ndim ? p->n[d] : 1;

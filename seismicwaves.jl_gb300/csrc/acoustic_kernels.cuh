@@ -38,6 +38,7 @@
 #pragma once
 
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
 
 #include "internal.h"
 
@@ -47,6 +48,11 @@ namespace swgb {
 // (no Kahan compensation), which the host flushes into FP64 totals every few
 // steps (k_flush_grad).
 enum StepMode { MODE_FWD = 0, MODE_FWD_D = 1, MODE_ADJ = 2, MODE_ADJW = 3 };
+
+struct FieldArgE {  // int8 per-shot array (exponents of the FP16 D slots): shot k at p + k * s
+  signed char* p;
+  long long s;
+};
 
 struct Field64 {  // FP64 per-shot array: shot k at p + k * s
   double* p;
@@ -73,7 +79,9 @@ struct StepArgs {
   long long wait_cycles;                           // limit of one bounded wait (clock64 cycles)
   int withhold;  // TMA stencil test hook: block 0's producer never issues this stage (-1 = none)
   int pf;                                          // 2D stencil: rows ahead prefetched into L2 (0 = off)
-  int dbf16;                                       // Dout / dcorr hold BF16 (the pointers are __nv_bfloat16 arrays)
+  int dbf16;  // Dout / dcorr: 0 FP32, 1 BF16, 2 FP16 scaled by 2^e per row and 128-point x tile (3D)
+  FieldArgE Dexp, dcorr_exp;  // dbf16 == 2: the exponents e of Dout / dcorr, [row][x tile]
+  int ntx;                    // x tiles of 128 points per row of the exponent arrays
   // compensated step (k_ac_hp): low parts of p[n], p[n+1] and d (in place), of fact and of 1/h^2;
   // FP64 C-PML coefficients (stride cpml_stride), memory variables and 1/h
   FieldArg plo_cur, plo_new, dlo;
@@ -118,8 +126,34 @@ __device__ __forceinline__ float* dptr(const FieldArg& f, int shot, int bf) {
   if (bf) return reinterpret_cast<float*>(reinterpret_cast<__nv_bfloat16*>(f.p) + (long long)shot * f.s);
   return f.p + (long long)shot * f.s;
 }
-__device__ __forceinline__ void dld4(float (&v)[4], const float* p, long long idx, int bf) {
-  if (bf) {
+// FP16 D (dbf16 == 2): every 128-point x tile of a row is stored as
+// round(D * 2^e) with e chosen from the tile's largest |D| so that it maps
+// into [2^10, 2^11) (32x head room below FP16's largest value for the
+// sources added afterwards; relative precision 2^-11 down to 2^-24 of the
+// tile maximum).
+__device__ __forceinline__ int dexp_of(float amax) {
+  if (!(amax > 0.f)) return 0;
+  const int ex = (int)((__float_as_uint(amax) >> 23) & 255u) - 127;  // amax in [2^ex, 2^(ex+1))
+  return max(-100, min(100, 10 - ex));
+}
+__device__ __forceinline__ float pow2f(int e) { return __uint_as_float((unsigned)(e + 127) << 23); }
+__device__ __forceinline__ float h_enc(float v, int e) {  // scaled and clamped to FP16's finite range
+  return fminf(fmaxf(v * pow2f(e), -65504.f), 65504.f);
+}
+// e of one warp's tile (all lanes call it; lanes without points pass valid = false)
+__device__ __forceinline__ int warp_dexp(const float (&v)[4], bool valid) {
+  const float m = valid ? fmaxf(fmaxf(fabsf(v[0]), fabsf(v[1])), fmaxf(fabsf(v[2]), fabsf(v[3]))) : 0.f;
+  return dexp_of(__uint_as_float(__reduce_max_sync(0xffffffffu, __float_as_uint(m))));
+}
+
+__device__ __forceinline__ void dld4(float (&v)[4], const float* p, long long idx, int bf, int e = 0) {
+  if (bf == 2) {
+    const uint2 u = __ldg(reinterpret_cast<const uint2*>(reinterpret_cast<const __half*>(p) + idx));
+    const float2 a = __half22float2(*reinterpret_cast<const __half2*>(&u.x));
+    const float2 b = __half22float2(*reinterpret_cast<const __half2*>(&u.y));
+    const float s = pow2f(-e);
+    v[0] = a.x * s; v[1] = a.y * s; v[2] = b.x * s; v[3] = b.y * s;
+  } else if (bf) {
     const uint2 u = __ldg(reinterpret_cast<const uint2*>(reinterpret_cast<const __nv_bfloat16*>(p) + idx));
     const float2 a = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&u.x));
     const float2 b = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&u.y));
@@ -128,8 +162,15 @@ __device__ __forceinline__ void dld4(float (&v)[4], const float* p, long long id
     ld4(v, p + idx);
   }
 }
-__device__ __forceinline__ void dst4(float* p, long long idx, const float (&v)[4], int bf) {
-  if (bf) {
+__device__ __forceinline__ void dst4(float* p, long long idx, const float (&v)[4], int bf, int e = 0) {
+  if (bf == 2) {
+    const __half2 a = __floats2half2_rn(h_enc(v[0], e), h_enc(v[1], e));
+    const __half2 b = __floats2half2_rn(h_enc(v[2], e), h_enc(v[3], e));
+    uint2 u;
+    u.x = *reinterpret_cast<const unsigned*>(&a);
+    u.y = *reinterpret_cast<const unsigned*>(&b);
+    *reinterpret_cast<uint2*>(reinterpret_cast<__half*>(p) + idx) = u;
+  } else if (bf) {
     const __nv_bfloat162 a = __floats2bfloat162_rn(v[0], v[1]);
     const __nv_bfloat162 b = __floats2bfloat162_rn(v[2], v[3]);
     uint2 u;
@@ -140,11 +181,13 @@ __device__ __forceinline__ void dst4(float* p, long long idx, const float (&v)[4
     st4(p + idx, v);
   }
 }
-__device__ __forceinline__ void dst1(float* p, long long idx, float v, int bf) {
-  if (bf) reinterpret_cast<__nv_bfloat16*>(p)[idx] = __float2bfloat16_rn(v);
+__device__ __forceinline__ void dst1(float* p, long long idx, float v, int bf, int e = 0) {
+  if (bf == 2) reinterpret_cast<__half*>(p)[idx] = __float2half_rn(h_enc(v, e));
+  else if (bf) reinterpret_cast<__nv_bfloat16*>(p)[idx] = __float2bfloat16_rn(v);
   else p[idx] = v;
 }
-__device__ __forceinline__ float dld1(const float* p, long long idx, int bf) {
+__device__ __forceinline__ float dld1(const float* p, long long idx, int bf, int e = 0) {
+  if (bf == 2) return __half2float(reinterpret_cast<const __half*>(p)[idx]) * pow2f(-e);
   if (bf) return __bfloat162float(reinterpret_cast<const __nv_bfloat16*>(p)[idx]);
   return p[idx];
 }
@@ -1257,8 +1300,9 @@ __device__ __forceinline__ void split_axis(int n, int H, int& a, int& b) {
 // Work of one warp in the 3D step: (y row, z band) for a block index.
 // REGION 0: the whole grid (tiles_y x tiles_z bands).  REGION 1: rows with y
 // and z outside the C-PML strips (tiles_y x tiles_z over [a, b) of each).
-// REGION 2: the rest -- z slabs (z in [1, a) or [b, nz-1), every y) then y
-// slabs (z in [a, b), y in [1, a) or [b, ny-1)) -- enumerated per x tile.
+// REGION 2: the z slabs (z in [1, a) or [b, nz-1), every y).  REGION 3: the
+// y slabs (z in [a, b), y in [1, a) or [b, ny-1)).  Slabs are enumerated per
+// x tile as (z band, y group) units.
 template <int NW, int REGION>
 __device__ __forceinline__ bool ac3d_work(const StepArgs& A, int tile, int warp, int& y, int& z_begin, int& z_end) {
   const int ny = A.n1, nz = A.n2, H = A.halo, TZ = A.TZ;
@@ -1280,9 +1324,8 @@ __device__ __forceinline__ bool ac3d_work(const StepArgs& A, int tile, int warp,
     return z_begin < z_end && y < by;
   }
   const int gy_all = (ny - 2 + NW - 1) / NW;
-  const int nb_lo = (az - 1 + TZ - 1) / TZ, nb_hi = (nz - 1 - bz + TZ - 1) / TZ;
-  const int uz = (nb_lo + nb_hi) * gy_all;
-  if (tile < uz) {
+  const int nb_lo = (az - 1 + TZ - 1) / TZ;
+  if (REGION == 2) {
     const int kz = tile / gy_all, gy = tile % gy_all;
     y = 1 + gy * NW + warp;
     if (kz < nb_lo) {
@@ -1294,7 +1337,6 @@ __device__ __forceinline__ bool ac3d_work(const StepArgs& A, int tile, int warp,
     }
     return z_begin < z_end && y <= ny - 2;
   }
-  tile -= uz;
   const int gyl = (ay - 1 + NW - 1) / NW, gyh = (ny - 1 - by + NW - 1) / NW;
   if (gyl + gyh == 0) return false;
   const int kz = tile / (gyl + gyh), g = tile % (gyl + gyh);
@@ -1334,7 +1376,8 @@ __device__ __forceinline__ void ac3d_body(const StepArgs& A) {
   const int na = 2 * H + 2, nh = 2 * H;
 
   const bool xstrip = inb && (x0 < H || x0 + 3 >= nx - H);
-  const bool ystrip = REGION != 1 && ((y < H) || (y >= ny - H));  // region 1: never
+  // region 1: never in a y strip; region 3: always
+  const bool ystrip = REGION == 3 || (REGION != 1 && ((y < H) || (y >= ny - H)));
   // the warp's 128 x points and its y row interior and outside the strips
   const bool fastxy = wx0 >= plain_lo(H) && wx0 + 127 <= plain_hi(nx, H) && y >= plain_lo(H) && y <= plain_hi(ny, H);
   const bool vec_interior = (x0 >= 1) && (x0 + 3 <= nx - 2);
@@ -1387,7 +1430,8 @@ __device__ __forceinline__ void ac3d_body(const StepArgs& A) {
     float right = __shfl_down_sync(FULL, r0[0], 1);
     if (lane == 0) left = xa > 0 ? pc[idx - 1] : 0.f;
     if (lane == 31) right = xa + 4 < P ? pc[idx + 4] : 0.f;
-    const bool zstrip = REGION != 1 && ((z < H) || (z >= nz - H));  // region 1: never
+    // regions 1 and 3: never in a z strip; region 2: always
+    const bool zstrip = REGION == 2 || (REGION != 1 && REGION != 3 && ((z < H) || (z >= nz - H)));
     float outp[4], outd[4], outD[4];
     if (FAST && fastxy && z >= plain_lo(H) && z <= plain_hi(nz, H)) {
       // warp-uniform: every point interior and outside the strips
@@ -1437,6 +1481,13 @@ __device__ __forceinline__ void ac3d_body(const StepArgs& A) {
       outp[e] = radd(c, outd[e]);
     }
     }
+    // FP16 D slots: the exponent of this warp's tile of row (y, z)
+    const long long erow = ((long long)z * ny + y) * A.ntx + txi;
+    int de = 0;
+    if (MODE == MODE_FWD_D && A.dbf16 == 2 && Dw) {
+      de = warp_dexp(outD, inb);
+      if (lane == 0) A.Dexp.p[(long long)shot * A.Dexp.s + erow] = (signed char)de;
+    }
     if (inb) {
       if (ckp) {
         st4(ckp + idx, r0);
@@ -1444,7 +1495,7 @@ __device__ __forceinline__ void ac3d_body(const StepArgs& A) {
       }
       if (MODE == MODE_ADJ) {
         float dv[4], g4[4], c4[4];
-        dld4(dv, dcr, idx, A.dbf16);
+        dld4(dv, dcr, idx, A.dbf16, A.dbf16 == 2 ? A.dcorr_exp.p[(long long)shot * A.dcorr_exp.s + erow] : 0);
         ld4rw(g4, gg + idx);
         ld4rw(c4, gcp + idx);
 #pragma unroll
@@ -1462,7 +1513,7 @@ __device__ __forceinline__ void ac3d_body(const StepArgs& A) {
       if (vec_interior) {
         st4(pn + idx, outp);
         st4(dn + idx, outd);
-        if (MODE == MODE_FWD_D && Dw) dst4(Dw, idx, outD, A.dbf16);
+        if (MODE == MODE_FWD_D && Dw) dst4(Dw, idx, outD, A.dbf16, de);
       } else {
 #pragma unroll
         for (int e = 0; e < 4; ++e) {
@@ -1470,7 +1521,7 @@ __device__ __forceinline__ void ac3d_body(const StepArgs& A) {
           if (x >= 1 && x <= nx - 2) {
             pn[idx + e] = outp[e];
             dn[idx + e] = outd[e];
-            if (MODE == MODE_FWD_D && Dw) dst1(Dw, idx + e, outD[e], A.dbf16);
+            if (MODE == MODE_FWD_D && Dw) dst1(Dw, idx + e, outD[e], A.dbf16, de);
           }
         }
       }
@@ -1503,9 +1554,10 @@ template <int MODE, int NW = 4>
 __global__ void __launch_bounds__(32 * NW) k_ac3d_fwd(const StepArgs A) {
   ac3d_body<MODE, NW, true>(A);
 }
-// Two-launch 3D step: rows outside the y and z strips (no y / z C-PML code,
-// fewer registers), then the rows of the strips.  Every point is computed by
-// exactly one of the two launches with the arithmetic of ac3d_body.
+// Three-launch 3D step: rows outside the y and z strips (no y / z C-PML code,
+// fewer registers), the z slabs (z strip code only where it applies), the y
+// slabs.  Every point is computed by exactly one launch with the arithmetic
+// of ac3d_body.
 template <int MODE, int NW = 4>
 __global__ void __launch_bounds__(32 * NW, 24 / NW) k_ac3d_inner(const StepArgs A) {
   ac3d_body<MODE, NW, false, 1>(A);
@@ -1515,9 +1567,14 @@ template <int MODE, int NW = 4>
 __global__ void __launch_bounds__(32 * NW, 32 / NW) k_ac3d_inner_np(const StepArgs A) {
   ac3d_body<MODE, NW, false, 1, false>(A);
 }
-template <int MODE, int NW = 4>
-__global__ void __launch_bounds__(32 * NW, 16 / NW) k_ac3d_shell(const StepArgs A) {
-  ac3d_body<MODE, NW, false, 2>(A);
+// (the z slabs fit 6 blocks per SM without the software pipeline, 4 with it)
+template <int MODE, int NW = 4, bool PIPE = true>
+__global__ void __launch_bounds__(32 * NW, PIPE ? 16 / NW : 24 / NW) k_ac3d_zslab(const StepArgs A) {
+  ac3d_body<MODE, NW, false, 2, PIPE>(A);
+}
+template <int MODE, int NW = 4, bool PIPE = true>
+__global__ void __launch_bounds__(32 * NW, 16 / NW) k_ac3d_yslab(const StepArgs A) {
+  ac3d_body<MODE, NW, false, 3, PIPE>(A);
 }
 
 // ---------------------------------------------------------------------------
@@ -2059,6 +2116,12 @@ __global__ void __launch_bounds__(128) k_ac_hp(const StepArgs A) {
       outph[e] = pnw.hi;
       outpl[e] = pnw.lo;
     }
+    int de = 0;  // FP16 D slots (3D): the exponent of this warp's tile
+    if (MODE == MODE_FWD_D && A.dbf16 == 2 && Dw) {
+      de = warp_dexp(outD, inb);
+      const long long erow = ((long long)z * ny + y) * A.ntx + (wx0 >> 7);
+      if (lane == 0) A.Dexp.p[(long long)shot * A.Dexp.s + erow] = (signed char)de;
+    }
     if (inb) {
       if (ckp) {
         float cp4[4], cd4[4];
@@ -2078,7 +2141,7 @@ __global__ void __launch_bounds__(128) k_ac_hp(const StepArgs A) {
           pnl[idx + e] = outpl[e];
           dd[idx + e] = outdh[e];
           ddl[idx + e] = outdl[e];
-          if (MODE == MODE_FWD_D && Dw) dst1(Dw, idx + e, outD[e], A.dbf16);
+          if (MODE == MODE_FWD_D && Dw) dst1(Dw, idx + e, outD[e], A.dbf16, de);
         }
       }
     }

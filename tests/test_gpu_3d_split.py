@@ -1,5 +1,5 @@
-"""The 3D step as two launches (rows outside the y / z C-PML strips, then the
-strip rows: k_ac3d_inner / k_ac3d_inner_np + k_ac3d_shell, the default)
+"""The 3D step as three launches (rows outside the y / z C-PML strips, the z
+slabs, the y slabs: k_ac3d_inner / k_ac3d_inner_np, k_ac3d_zslab, k_ac3d_yslab; the default)
 against the single-launch kernels (tuning variant bit 16).  Every point is
 computed by exactly one launch with the same arithmetic, so traces, misfit
 and gradient must be bit-identical, for the pipelined and unpipelined inner
@@ -37,7 +37,7 @@ CASES = [  # shape, halo, freetop
     ((70, 50, 45), 6, True),
     ((61, 40, 33), 5, False),
     ((50, 36, 15), 6, True),   # the smallest depth for this halo: three inner rows
-    ((40, 30, 28), 0, False),  # no strips: the shell launch covers nothing
+    ((40, 30, 28), 0, False),  # no strips: the slab launches cover nothing
 ]
 
 

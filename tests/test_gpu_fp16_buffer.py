@@ -1,0 +1,72 @@
+"""The FP16 recompute buffer of 3D gradients (snapshot_bf16 = 3: D stored as
+FP16 with a power-of-two exponent per row and 128-point x tile) against the
+FP32 buffer and the BF16 one on the same inputs.  The forward does not read
+the buffer, so traces and misfit are bit-identical across the three; the
+gradient must be several times closer to the FP32-buffer gradient than the
+BF16 one is.  Cases: sources inside and outside the C-PML layer, a source on
+the free surface (its node's D comes from the injection ring), checkpoint
+periods 1 and 9, the three-launch and single-launch 3D steps, the
+compensated forward; 2D simulations reject the mode."""
+import numpy as np
+import pytest
+
+from cases import Case, GpuRun, make_shot, rel_l2, smooth_model, stable_dt
+
+pytestmark = pytest.mark.gpu
+
+
+def _setup(sw, n=(64, 56, 48), halo=8, src_depth=0.3, seed=21):
+    vp = smooth_model(n, 1800.0, 3000.0, seed)
+    h = (10.0, 10.0, 10.0)
+    case = Case(vp=vp, h=h, dt=stable_dt(vp, h), halo=halo, freetop=True)
+    ex = [hh * (k - 1) for k, hh in zip(vp.shape, h)]
+    rec = [[x, y, 0.1 * ex[2]] for x in np.linspace(0.1, 0.9, 9) * ex[0] for y in (0.3 * ex[1], 0.6 * ex[1])]
+    shots = [make_shot(h, ex, 220, case.dt, 14.0, [[0.45 * ex[0], 0.5 * ex[1], src_depth * ex[2]]], rec),
+             make_shot(h, ex, 190, case.dt, 14.0, [[0.6 * ex[0], 0.4 * ex[1], 0.05 * ex[2]]], rec)]
+    obs_case = Case(vp=np.asfortranarray(vp * 1.04), h=h, dt=case.dt, halo=halo, freetop=True)
+    run = GpuRun(sw, obs_case)
+    for s, o in zip(shots, run.forward(shots)):
+        s.observed = np.asfortranarray(o, dtype=np.float64)
+    run.close()
+    return case, shots
+
+
+def _grad(sw, case, shots, bf16, check_freq, variant=0, precision=0):
+    run = GpuRun(sw, case, gradient=True, check_freq=check_freq, bf16=bf16, variant=variant, precision=precision)
+    out = run.gradient(shots)
+    run.close()
+    return out
+
+
+@pytest.mark.parametrize("check_freq,variant", [(9, 0), (1, 0), (9, 65536), (9, 131072)])
+def test_fp16_buffer_closer_than_bf16(sw, check_freq, variant):
+    case, shots = _setup(sw)
+    g0, m0, t0 = _grad(sw, case, shots, 0, check_freq, variant)
+    g1, m1, t1 = _grad(sw, case, shots, 1, check_freq, variant)
+    g3, m3, t3 = _grad(sw, case, shots, 3, check_freq, variant)
+    assert m3 == m0 == m1
+    assert all(np.array_equal(a, b) for a, b in zip(t3, t0))
+    e1, e3 = rel_l2(g1, g0), rel_l2(g3, g0)
+    print(f"K={check_freq} variant {variant}: BF16 buffer {e1:.2e}, FP16 buffer {e3:.2e}")
+    assert e3 < e1 / 4
+    assert e3 < 5e-4
+
+
+def test_fp16_buffer_boundary_source_and_compensated_forward(sw):
+    """A source on the free surface (z = 0: the ring path writes its D) and the
+    compensated forward writing the FP16 slots."""
+    case, shots = _setup(sw, src_depth=0.0, seed=5)
+    g0, m0, _ = _grad(sw, case, shots, 0, 9)
+    g3, m3, _ = _grad(sw, case, shots, 3, 9)
+    assert m3 == m0 and rel_l2(g3, g0) < 5e-4
+    gh0, mh0, _ = _grad(sw, case, shots, 0, 9, precision=1)
+    gh3, mh3, _ = _grad(sw, case, shots, 3, 9, precision=1)
+    assert mh3 == mh0 and rel_l2(gh3, gh0) < 5e-4
+
+
+def test_fp16_buffer_is_3d_only(sw):
+    vp = smooth_model((80, 60), 1800.0, 3000.0, 2)
+    case = Case(vp=vp, h=(10.0, 10.0), dt=stable_dt(vp, (10.0, 10.0)), halo=6, freetop=False)
+    with pytest.raises(sw._lib.SwError) as e:
+        GpuRun(sw, case, gradient=True, check_freq=5, bf16=3)
+    assert "3D" in str(e.value)
