@@ -2022,7 +2022,7 @@ void wavesim_init(sw_wavesim* ws, sw_ctx* ctx, const sw_acoustic_params* p, int 
     if (ws->gp.mute_radius_src < 0 || ws->gp.mute_radius_rec < 0)
       fail(SW_ERR_ARG, "mutearoundpoint!(): The smoothing radius must be positive.");
     if (ws->gp.snapshot_bf16 < 0 || ws->gp.snapshot_bf16 > 3) fail(SW_ERR_ARG, "snapshot_bf16 must be 0, 1, 2 or 3");
-    if (ws->gp.snapshot_bf16 == 3 && ws->N != 3)
+    if (ws->gp.snapshot_bf16 == 3 && p->ndim != 3)
       fail(SW_ERR_UNSUPPORTED, "snapshot_bf16 = 3 (FP16 recompute buffer) is available for 3D simulations");
   }
   ws->N = p->ndim;
