@@ -279,6 +279,53 @@ __device__ __forceinline__ float cpml_axis_term(float d2, float pl, float p0, fl
   return radd(t, xn);
 }
 
+// cpml_axis_term for four consecutive x points of an axis whose strip cell
+// does not depend on x (the y and z axes of the 3D step): the same
+// arithmetic per point, with psi, xi and their checkpoint copies moved as
+// float4 (the base indices point at the first of the four points; the two
+// outermost columns, which no point reads, get their values too).
+__device__ __forceinline__ void cpml_axis_term4(float (&t)[4], const float (&pl)[4], const float (&p0)[4],
+                                                const float (&pr)[4], int v, int n, int halo, float ih,
+                                                const StripIO& s) {
+  int qr;
+  bool first;
+  if (v < halo) {
+    qr = v;
+    first = (v == 1);
+  } else if (v >= n - halo) {
+    qr = v + 1 - n + 2 * halo;
+    first = (v == n - halo);
+  } else {
+    return;
+  }
+  const int ql = qr - 1;
+  const long long il = s.psi_base + (long long)ql * s.psi_step;
+  const long long ir = s.psi_base + (long long)qr * s.psi_step;
+  const long long iq = s.xi_base + (long long)qr * s.xi_step;
+  const float bhl = s.bh[ql], ahl = s.ah[ql], bhr = s.bh[qr], ahr = s.ah[qr], bq = s.b[qr], aq = s.a[qr];
+  float oldl[4], oldr[4], xo[4], newl[4], newr[4], xn[4];
+  ld4rw(oldl, s.psi_in + il);
+  ld4rw(oldr, s.psi_in + ir);
+  ld4rw(xo, s.xi_in + iq);
+#pragma unroll
+  for (int e = 0; e < 4; ++e) {
+    newl[e] = radd(rmul(bhl, oldl[e]), rmul(ahl, rmul(rsub(p0[e], pl[e]), ih)));
+    newr[e] = radd(rmul(bhr, oldr[e]), rmul(ahr, rmul(rsub(pr[e], p0[e]), ih)));
+    const float dpsi = rmul(rsub(newr[e], newl[e]), ih);
+    const float tt = radd(t[e], dpsi);
+    xn[e] = radd(rmul(bq, xo[e]), rmul(aq, tt));
+    t[e] = radd(tt, xn[e]);
+  }
+  st4(s.psi_out + ir, newr);
+  if (s.ck_psi) st4(s.ck_psi + ir, oldr);
+  if (first) {
+    st4(s.psi_out + il, newl);
+    if (s.ck_psi) st4(s.ck_psi + il, oldl);
+  }
+  if (s.ck_xi) st4(s.ck_xi + iq, xo);
+  st4(s.xi_out + iq, xn);
+}
+
 // TMA prefetch of a contiguous global range into L2 (no registers, no
 // completion to wait for).  Address 16-byte aligned, size a multiple of 16.
 __device__ __forceinline__ void l2_prefetch(const void* p, unsigned bytes) {
@@ -1447,39 +1494,44 @@ __device__ __forceinline__ void ac3d_body(const StepArgs& A) {
         outp[e] = radd(c, outd[e]);
       }
     } else {
+      float tx[4], ty[4], tz[4];
 #pragma unroll
-    for (int e = 0; e < 4; ++e) {
-      const float xm = e == 0 ? left : r0[e - 1];
-      const float xp = e == 3 ? right : r0[e + 1];
-      const float c = r0[e];
-      float tx = d2term(xm, c, xp, A.ih2[0]);
-      float ty = d2term(ym[e], c, yp[e], A.ih2[1]);
-      float tz = d2term(rm[e], c, rp[e], A.ih2[2]);
-      const int x = x0 + e;
-      const bool pin = inb && x >= 1 && x <= nx - 2;
-      if (xstrip && pin) {
-        StripIO s0 = strip_io(A, 0, shot, 1);
-        s0.psi_base = ((long long)z * ny + y) * nh;
-        s0.xi_base = ((long long)z * ny + y) * na;
-        tx = cpml_axis_term(tx, xm, c, xp, x, nx, H, A.ih[0], s0);
+      for (int e = 0; e < 4; ++e) {
+        const float xm = e == 0 ? left : r0[e - 1];
+        const float xp = e == 3 ? right : r0[e + 1];
+        const float c = r0[e];
+        tx[e] = d2term(xm, c, xp, A.ih2[0]);
+        ty[e] = d2term(ym[e], c, yp[e], A.ih2[1]);
+        tz[e] = d2term(rm[e], c, rp[e], A.ih2[2]);
+        const int x = x0 + e;
+        if (xstrip && inb && x >= 1 && x <= nx - 2) {
+          StripIO s0 = strip_io(A, 0, shot, 1);
+          s0.psi_base = ((long long)z * ny + y) * nh;
+          s0.xi_base = ((long long)z * ny + y) * na;
+          tx[e] = cpml_axis_term(tx[e], xm, c, xp, x, nx, H, A.ih[0], s0);
+        }
       }
-      if (ystrip && pin) {
+      // the y and z strips: the strip cell is the same for the four points
+      // (it depends on y or z only), so their memory variables move as float4
+      if (ystrip && inb) {
         StripIO s1 = strip_io(A, 1, shot, P);
-        s1.psi_base = (long long)z * nh * P + x;
-        s1.xi_base = (long long)z * na * P + x;
-        ty = cpml_axis_term(ty, ym[e], c, yp[e], y, ny, H, A.ih[1], s1);
+        s1.psi_base = (long long)z * nh * P + xa;
+        s1.xi_base = (long long)z * na * P + xa;
+        cpml_axis_term4(ty, ym, r0, yp, y, ny, H, A.ih[1], s1);
       }
-      if (zstrip && pin) {
+      if (zstrip && inb) {
         StripIO s2 = strip_io(A, 2, shot, (long long)ny * P);
-        s2.psi_base = (long long)y * P + x;
-        s2.xi_base = (long long)y * P + x;
-        tz = cpml_axis_term(tz, rm[e], c, rp[e], z, nz, H, A.ih[2], s2);
+        s2.psi_base = (long long)y * P + xa;
+        s2.xi_base = (long long)y * P + xa;
+        cpml_axis_term4(tz, rm, r0, rp, z, nz, H, A.ih[2], s2);
       }
-      const float lap = radd(radd(tx, ty), tz);
-      outD[e] = rmul(f[e], lap);
-      outd[e] = radd(o[e], outD[e]);
-      outp[e] = radd(c, outd[e]);
-    }
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        const float lap = radd(radd(tx[e], ty[e]), tz[e]);
+        outD[e] = rmul(f[e], lap);
+        outd[e] = radd(o[e], outD[e]);
+        outp[e] = radd(r0[e], outd[e]);
+      }
     }
     // FP16 D slots: the exponent of this warp's tile of row (y, z)
     const long long erow = ((long long)z * ny + y) * A.ntx + txi;

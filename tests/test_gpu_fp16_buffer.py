@@ -56,9 +56,12 @@ def test_fp16_buffer_boundary_source_and_compensated_forward(sw):
     """A source on the free surface (z = 0: the ring path writes its D) and the
     compensated forward writing the FP16 slots."""
     case, shots = _setup(sw, src_depth=0.0, seed=5)
-    g0, m0, _ = _grad(sw, case, shots, 0, 9)
-    g3, m3, _ = _grad(sw, case, shots, 3, 9)
+    # a source on the outermost line needs check_freq 1 (the library rejects it otherwise, as
+    # the reference's recompute reads a stale buffer there)
+    g0, m0, _ = _grad(sw, case, shots, 0, 1)
+    g3, m3, _ = _grad(sw, case, shots, 3, 1)
     assert m3 == m0 and rel_l2(g3, g0) < 5e-4
+    case, shots = _setup(sw, seed=5)
     gh0, mh0, _ = _grad(sw, case, shots, 0, 9, precision=1)
     gh3, mh3, _ = _grad(sw, case, shots, 3, 9, precision=1)
     assert mh3 == mh0 and rel_l2(gh3, gh0) < 5e-4
