@@ -46,7 +46,7 @@
  *   sw_acoustic_vd_create / sw_acoustic_vd_destroy
  *       build_wavesim -> AcousticVDStaggeredCPMLWaveSimulation (src/apis/build.jl:60-72,
  *       src/models/acoustic/acou_models.jl:311-454)
- *   sw_acoustic_vd_set_material
+ *   sw_acoustic_vd_set_material, sw_acoustic_vd_set_material64
  *       update_matprop! -> precompute_fact! (acou_models.jl:283-300)
  *   sw_acoustic_vd_forward
  *       run_swforward! + swforward_1shot! (VD) + forward_onestep_CPML!
@@ -400,6 +400,20 @@ int sw_acoustic_vd_gradient(sw_acoustic_vd* vd, int32_t nshots, const sw_acousti
 /* Rows per thread block of the VD stencil kernels: 8, 16 or 32 (0 = default
  * 8).  A tuning knob of this backend; results do not depend on it. */
 int sw_acoustic_vd_set_tuning(sw_acoustic_vd* vd, int32_t tz);
+
+/* Compensated forward of the variable-density path (mode 1; 0 = FP32, the
+ * default): p, vx and vz as unevaluated sums of two FP32 numbers, fact_m0 /
+ * fact_m1 and 1/dx, 1/dz as FP32 pairs of their FP64 values, the staggered
+ * differences and both updates in double-FP32, the C-PML memory variables
+ * and coefficients (sw_acoustic_shot.cpml64, or the FP32 ones widened) in
+ * FP64.  The gradient's recompute and adjoint stay FP32.  No reference
+ * counterpart (the reference runs in the precision of its arrays). */
+int sw_acoustic_vd_set_precision(sw_acoustic_vd* vd, int32_t mode);
+
+/* sw_acoustic_vd_set_material with Float64 arrays (host memory): the
+ * material factors are formed from the FP64 values, so the compensated
+ * forward keeps their full precision. */
+int sw_acoustic_vd_set_material64(sw_acoustic_vd* vd, const double* vp, const double* rho);
 
 /* 2D forward of one shot that allocates no device memory.  Has no
  * counterpart in the reference: it exists for callers that cannot let a

@@ -32,6 +32,7 @@ EXPORTS = [
     "sw_wavesim_use_graphs", "sw_acoustic_forward_snapshots", "sw_elastic_forward_snapshots",
     "sw_acoustic_vd_create", "sw_acoustic_vd_destroy", "sw_acoustic_vd_set_material", "sw_acoustic_vd_forward",
     "sw_acoustic_vd_forward_snapshots", "sw_acoustic_vd_gradient", "sw_acoustic_vd_set_tuning",
+    "sw_acoustic_vd_set_precision", "sw_acoustic_vd_set_material64",
 ]
 
 i32, f64, vp_ = ctypes.c_int32, ctypes.c_double, ctypes.c_void_p
@@ -128,6 +129,8 @@ def load() -> ctypes.CDLL:
     lib.sw_acoustic_vd_forward_snapshots.argtypes = [vp_, i32, P(SwAcousticShot), i32, i32, P(vp_)]
     lib.sw_acoustic_vd_gradient.argtypes = [vp_, i32, P(SwAcousticShot), i32, vp_, vp_, vp_]
     lib.sw_acoustic_vd_set_tuning.argtypes = [vp_, i32]
+    lib.sw_acoustic_vd_set_precision.argtypes = [vp_, i32]
+    lib.sw_acoustic_vd_set_material64.argtypes = [vp_, vp_, vp_]
     _lib = lib
     return lib
 

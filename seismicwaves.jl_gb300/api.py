@@ -263,11 +263,13 @@ class RunParameters:
     """src/models/genparameters.jl:25-46 (parall selects the backend; only :GB300 here).
 
     compensated (an addition of this backend, False by default): the forward
-    passes of the constant-density acoustic simulation keep p and d as pairs
-    of FP32 numbers and form fact from the FP64 model
-    (sw_wavesim_set_precision / sw_wavesim_set_vp64): traces and misfit
-    within ~1e-7 of an FP64 run at thousands of steps instead of ~1e-6, at
-    several times the forward's cost.
+    passes of the acoustic simulations (constant density: p and d; variable
+    density: p, vx and vz) keep their state as pairs of FP32 numbers and form
+    the material factors from the FP64 model (sw_wavesim_set_precision /
+    sw_wavesim_set_vp64, sw_acoustic_vd_set_precision /
+    sw_acoustic_vd_set_material64): traces and misfit within ~1e-8 of an
+    FP64 run at thousands of steps instead of ~1e-6, at several times the
+    forward's cost.
     """
     parall: str = _BACKEND
     snapevery: int | None = None

@@ -41,6 +41,7 @@
 #include <cuda_fp16.h>
 
 #include "internal.h"
+#include "ff.cuh"
 
 namespace swgb {
 
@@ -1918,33 +1919,6 @@ __global__ void __launch_bounds__(160, TmaLayout<MODE>::MIN_BLOCKS) k_ac2d_tma(c
 // Same algorithm and update order as the FP32 step (k_ac2d_step / ac3d_body);
 // checkpoints and the D slots get the rounded hi + lo values.
 // ---------------------------------------------------------------------------
-struct ff {
-  float hi, lo;
-};
-__device__ __forceinline__ ff two_sum(float a, float b) {
-  const float s = __fadd_rn(a, b);
-  const float bb = __fsub_rn(s, a);
-  const float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
-  return {s, e};
-}
-__device__ __forceinline__ ff fast_two_sum(float a, float b) {  // |a| >= |b| or a == 0
-  const float s = __fadd_rn(a, b);
-  return {s, __fsub_rn(b, __fsub_rn(s, a))};
-}
-__device__ __forceinline__ ff ff_add(ff a, ff b) {
-  const ff s = two_sum(a.hi, b.hi);
-  const ff t = two_sum(a.lo, b.lo);
-  ff r = fast_two_sum(s.hi, __fadd_rn(s.lo, t.hi));
-  return fast_two_sum(r.hi, __fadd_rn(r.lo, t.lo));
-}
-__device__ __forceinline__ ff ff_mul(ff a, ff b) {
-  const float p = __fmul_rn(a.hi, b.hi);
-  float e = __fmaf_rn(a.hi, b.hi, -p);
-  e = __fmaf_rn(a.hi, b.lo, __fmaf_rn(a.lo, b.hi, e));
-  return fast_two_sum(p, e);
-}
-__device__ __forceinline__ float ff_round(ff a) { return __fadd_rn(a.hi, a.lo); }
-
 // p[l] - 2 p[c] + p[r] of compensated values, compensated
 __device__ __forceinline__ ff ff_d2(float lh, float ll, float ch, float cl, float rh, float rl) {
   const ff s = two_sum(lh, rh);

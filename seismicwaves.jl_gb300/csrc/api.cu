@@ -48,6 +48,8 @@ void vd_forward_snapshots(sw_acoustic_vd* vd, int nshots, const sw_acoustic_shot
 void vd_gradient(sw_acoustic_vd* vd, int nshots, const sw_acoustic_shot* shots, bool on_device, double* g_vp,
                  double* g_rho, double* misfit);
 void vd_set_tuning(sw_acoustic_vd* vd, int tz);
+void vd_set_precision(sw_acoustic_vd* vd, int mode);
+void vd_set_material64(sw_acoustic_vd* vd, const double* vp, const double* rho);
 sw_ctx* vd_ctx(sw_acoustic_vd* vd);
 sw_acoustic_vd* vd_new();
 void vd_delete(sw_acoustic_vd* vd);
@@ -502,6 +504,20 @@ int sw_acoustic_vd_gradient(sw_acoustic_vd* vd, int32_t nshots, const sw_acousti
   return guarded(ctx, [&] {
     swgb::check_cuda(cudaSetDevice(ctx->device), "cudaSetDevice");
     swgb::vd_gradient(vd, nshots, shots, on_device != 0, grad_vp, grad_rho, misfit);
+  });
+}
+
+int sw_acoustic_vd_set_precision(sw_acoustic_vd* vd, int32_t mode) {
+  if (!vd || mode < 0 || mode > 1) return SW_ERR_ARG;
+  return guarded(swgb::vd_ctx(vd), [&] { swgb::vd_set_precision(vd, mode); });
+}
+
+int sw_acoustic_vd_set_material64(sw_acoustic_vd* vd, const double* vp, const double* rho) {
+  if (!vd) return SW_ERR_ARG;
+  sw_ctx* ctx = swgb::vd_ctx(vd);
+  return guarded(ctx, [&] {
+    swgb::check_cuda(cudaSetDevice(ctx->device), "cudaSetDevice");
+    swgb::vd_set_material64(vd, vp, rho);
   });
 }
 

@@ -48,6 +48,7 @@
 
 #include "internal.h"
 #include "ccts.cuh"
+#include "ff.cuh"
 
 namespace swgb {
 namespace vd {
@@ -371,6 +372,236 @@ __global__ void __launch_bounds__(BX) k_vd_v(const VArgs A) {
 }
 
 // ---------------------------------------------------------------------------
+// Compensated forward step (sw_acoustic_vd_set_precision(vd, 1)): p, vx and
+// vz as double-FP32 values (high parts in the usual arrays, low parts in their
+// own), fact_m0 / fact_m1 and 1/dx, 1/dz as FP32 pairs of their FP64 values,
+// the staggered differences c2 (f3 - f2) + c1 (f1 - f4) and both updates in
+// double-FP32 (ff.cuh), the C-PML memory variables and coefficients in FP64.
+// Same update order and index rules as k_vd_p / k_vd_v; forward modes only
+// (the recompute and the adjoint stay FP32, starting from FP32-rounded
+// checkpoints).
+// ---------------------------------------------------------------------------
+struct HArgs {
+  Geo g;
+  const float* pin; float* pout;     // p high parts [shot][F] (pin may equal pout)
+  float* plo;                        // p low parts [shot][F], updated in place
+  float* vx; float* vz;              // velocity high parts
+  float* vxl; float* vzl;            // velocity low parts
+  double* xi_x; double* xi_z;        // pressure-update memory variables (FP64)
+  double* psi_x; double* psi_z;      // velocity-update memory variables (FP64)
+  long long xs, zs;
+  const float* m0; const float* m0l;
+  const float* m1x; const float* m1xl;
+  const float* m1z; const float* m1zl;
+  const double* cp; int cps;         // FP64 coefficients per shot, as cp of PArgs
+  float idxl, idzl;                  // low parts of 1/dx, 1/dz (the high parts are g.idx, g.idz)
+};
+
+// c1 f1 - c2 f2 + c2 f3 - c1 f4 = c2 (f3 - f2) + c1 (f1 - f4), times 1/h
+__device__ __forceinline__ ff ffd4(ff f1, ff f2, ff f3, ff f4, ff inv) {
+  constexpr double C1 = 1.0 / 24.0;
+  const ff c1{(float)C1, (float)(C1 - (double)(float)C1)};
+  const ff c2{1.125f, 0.f};  // 27/24, exact
+  return ff_mul(ff_add(ff_mul(ff_sub(f3, f2), c2), ff_mul(ff_sub(f1, f4), c1)), inv);
+}
+// psi = b psi + a dv; returns dv + psi (cpml_upd in FP64)
+__device__ __forceinline__ ff cpml_upd64(double* psi, double a, double b, ff dv) {
+  const double d = ff_to_d(dv);
+  const double nv = b * (*psi) + a * d;
+  *psi = nv;
+  return d_to_ff(d + nv);
+}
+
+template <int TZ>
+__global__ void __launch_bounds__(BX) k_vd_p_hp(const HArgs A) {
+  const Geo g = A.g;
+  const int s = blockIdx.z;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int wx0 = (blockIdx.x * 4 + warp) * 128;
+  const int j0 = blockIdx.y * TZ + 1;
+  const int j1 = min(j0 + TZ - 1, g.nz);
+  if (j0 > j1 || wx0 >= g.nx) return;  // warp uniform
+  const int i0 = wx0 + lane * 4 + 1;
+  const bool ldok = i0 <= g.nx + 2;
+  const long long so = (long long)s * g.F;
+  const float* vx = A.vx + so;
+  const float* vz = A.vz + so;
+  const float* vxl = A.vxl + so;
+  const float* vzl = A.vzl + so;
+  const float* pin = A.pin + so;
+  float* pout = A.pout + so;
+  float* plo = A.plo + so;
+  const int na = 2 * g.halo + 2, nh = 2 * g.halo;
+  const double* cx = A.cp + (long long)s * A.cps;
+  const double* cz = cx + 2 * na + 2 * nh;
+  double* xix = A.xi_x + (long long)s * A.xs;
+  double* xiz = A.xi_z + (long long)s * A.zs;
+  const int P = g.P;
+  const bool xstrip = i0 <= g.halo + 1 || i0 + 3 >= g.nx - g.halo;
+  const ff idx{g.idx, A.idxl}, idz{g.idz, A.idzl};
+  long long c = g.lin(i0, j0);
+  F4 z0 = ld4p(vz, c - 2 * P, ldok), z1 = ld4p(vz, c - P, ldok), z2 = ld4p(vz, c, ldok), z3 = ld4p(vz, c + P, ldok);
+  F4 l0 = ld4p(vzl, c - 2 * P, ldok), l1 = ld4p(vzl, c - P, ldok), l2 = ld4p(vzl, c, ldok), l3 = ld4p(vzl, c + P, ldok);
+  for (int j = j0; j <= j1; ++j, c += P) {
+    const bool more = j + 1 <= j1;
+    const F4 zn = ld4p(vz, c + 2 * P, ldok && more), ln = ld4p(vzl, c + 2 * P, ldok && more);
+    const F4 X = ld4p(vx, c, ldok), XL = ld4p(vxl, c, ldok);
+    float xa[7], xb[7];  // vx at i0-2 .. i0+4 (row j): high and low parts
+    xa[0] = __shfl_up_sync(FULL, X.v[2], 1);
+    xa[1] = __shfl_up_sync(FULL, X.v[3], 1);
+    xa[6] = __shfl_down_sync(FULL, X.v[0], 1);
+    xb[0] = __shfl_up_sync(FULL, XL.v[2], 1);
+    xb[1] = __shfl_up_sync(FULL, XL.v[3], 1);
+    xb[6] = __shfl_down_sync(FULL, XL.v[0], 1);
+    if (lane == 0) {
+      xa[0] = ldz(vx, c - 2, ldok);
+      xa[1] = ldz(vx, c - 1, ldok);
+      xb[0] = ldz(vxl, c - 2, ldok);
+      xb[1] = ldz(vxl, c - 1, ldok);
+    }
+    if (lane == 31) {
+      xa[6] = ldz(vx, c + 4, ldok);
+      xb[6] = ldz(vxl, c + 4, ldok);
+    }
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+      xa[2 + e] = X.v[e];
+      xb[2 + e] = XL.v[e];
+    }
+    const F4 PI = ld4p(pin, c, ldok), PL = ld4p(plo, c, ldok);
+    const F4 M0 = ld4z(A.m0, c, ldok), M0L = ld4z(A.m0l, c, ldok);
+    const bool jin = j >= 2 && j <= g.nz - 1;
+    const int kz = jin ? k_pres(j, g.nz, g.halo) : 0;
+    float oh[4], ol[4];
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+      const int i = i0 + e;
+      if (jin && i >= 2 && i <= g.nx - 1) {
+        ff dvx = ffd4(ff{xa[e], xb[e]}, ff{xa[e + 1], xb[e + 1]}, ff{xa[e + 2], xb[e + 2]}, ff{xa[e + 3], xb[e + 3]},
+                      idx);
+        ff dvz = ffd4(ff{z0.v[e], l0.v[e]}, ff{z1.v[e], l1.v[e]}, ff{z2.v[e], l2.v[e]}, ff{z3.v[e], l3.v[e]}, idz);
+        if (xstrip) {
+          const int kx = k_pres(i, g.nx, g.halo);
+          if (kx) dvx = cpml_upd64(xix + (long long)(j - 1) * g.W + (kx - 1), cx[kx - 1], cx[na + nh + kx - 1], dvx);
+        }
+        if (kz) dvz = cpml_upd64(xiz + (long long)(kz - 1) * P + (i - 1), cz[kz - 1], cz[na + nh + kz - 1], dvz);
+        const ff o = ff_sub(ff{PI.v[e], PL.v[e]}, ff_mul(ff{M0.v[e], M0L.v[e]}, ff_add(dvx, dvz)));
+        oh[e] = o.hi;
+        ol[e] = o.lo;
+      } else {
+        oh[e] = PI.v[e];
+        ol[e] = PL.v[e];
+      }
+    }
+    if (ldok) {
+#pragma unroll
+      for (int e = 0; e < 4; ++e)
+        if (i0 + e <= g.nx) {
+          pout[c + e] = oh[e];
+          plo[c + e] = ol[e];
+        }
+    }
+    z0 = z1; z1 = z2; z2 = z3; z3 = zn;
+    l0 = l1; l1 = l2; l2 = l3; l3 = ln;
+  }
+}
+
+template <int TZ>
+__global__ void __launch_bounds__(BX) k_vd_v_hp(const HArgs A) {
+  const Geo g = A.g;
+  const int s = blockIdx.z;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int wx0 = (blockIdx.x * 4 + warp) * 128;
+  const int j0 = blockIdx.y * TZ + 1;
+  const int j1 = min(j0 + TZ - 1, g.nz);
+  if (j0 > j1 || wx0 >= g.nx) return;
+  const int i0 = wx0 + lane * 4 + 1;
+  const bool ldok = i0 <= g.nx + 2;
+  const long long so = (long long)s * g.F;
+  const float* p = A.pout + so;  // the pressure just updated
+  const float* pl = A.plo + so;
+  float* vx = A.vx + so;
+  float* vz = A.vz + so;
+  float* vxl = A.vxl + so;
+  float* vzl = A.vzl + so;
+  const int na = 2 * g.halo + 2, nh = 2 * g.halo;
+  const double* cx = A.cp + (long long)s * A.cps;
+  const double* cz = cx + 2 * na + 2 * nh;
+  double* psx = A.psi_x + (long long)s * A.xs;
+  double* psz = A.psi_z + (long long)s * A.zs;
+  const int P = g.P;
+  const bool xstrip = i0 <= g.halo || i0 + 3 >= g.nx - g.halo;
+  const ff idx{g.idx, A.idxl}, idz{g.idz, A.idzl};
+  long long c = g.lin(i0, j0);
+  F4 w0 = ld4p(p, c - P, ldok), w1 = ld4p(p, c, ldok), w2 = ld4p(p, c + P, ldok), w3 = ld4p(p, c + 2 * P, ldok);
+  F4 u0 = ld4p(pl, c - P, ldok), u1 = ld4p(pl, c, ldok), u2 = ld4p(pl, c + P, ldok), u3 = ld4p(pl, c + 2 * P, ldok);
+  for (int j = j0; j <= j1; ++j, c += P) {
+    const bool more = j + 1 <= j1;
+    const F4 wn = ld4p(p, c + 3 * P, ldok && more), un = ld4p(pl, c + 3 * P, ldok && more);
+    float pa[7], pb[7];  // p at i0-1 .. i0+5 (row j): high and low parts
+    pa[0] = __shfl_up_sync(FULL, w1.v[3], 1);
+    pa[5] = __shfl_down_sync(FULL, w1.v[0], 1);
+    pa[6] = __shfl_down_sync(FULL, w1.v[1], 1);
+    pb[0] = __shfl_up_sync(FULL, u1.v[3], 1);
+    pb[5] = __shfl_down_sync(FULL, u1.v[0], 1);
+    pb[6] = __shfl_down_sync(FULL, u1.v[1], 1);
+    if (lane == 0) {
+      pa[0] = ldz(p, c - 1, ldok);
+      pb[0] = ldz(pl, c - 1, ldok);
+    }
+    if (lane == 31) {
+      pa[5] = ldz(p, c + 4, ldok);
+      pa[6] = ldz(p, c + 5, ldok);
+      pb[5] = ldz(pl, c + 4, ldok);
+      pb[6] = ldz(pl, c + 5, ldok);
+    }
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+      pa[1 + e] = w1.v[e];
+      pb[1 + e] = u1.v[e];
+    }
+    if (ldok) {
+      const F4 VX = ld4rw(vx, c), VXL = ld4rw(vxl, c), MX = ld4z(A.m1x, c, true), MXL = ld4z(A.m1xl, c, true);
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        const int i = i0 + e;
+        if (i > g.nx - 1) continue;
+        ff d = ffd4(ff{pa[e], pb[e]}, ff{pa[e + 1], pb[e + 1]}, ff{pa[e + 2], pb[e + 2]}, ff{pa[e + 3], pb[e + 3]}, idx);
+        if (xstrip) {
+          const int kx = k_vel(i, g.nx, g.halo);
+          if (kx) d = cpml_upd64(psx + (long long)(j - 1) * g.W + (kx - 1), cx[na + kx - 1], cx[2 * na + nh + kx - 1], d);
+        }
+        const ff nv = ff_sub(ff{VX.v[e], VXL.v[e]}, ff_mul(ff{MX.v[e], MXL.v[e]}, d));
+        vx[c + e] = nv.hi;
+        vxl[c + e] = nv.lo;
+      }
+      if (j <= g.nz - 1) {
+        const int kz = k_vel(j, g.nz, g.halo);
+        const F4 VZ = ld4rw(vz, c), VZL = ld4rw(vzl, c), MZ = ld4z(A.m1z, c, true), MZL = ld4z(A.m1zl, c, true);
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+          const int i = i0 + e;
+          if (i > g.nx) continue;
+          ff d = ffd4(ff{w0.v[e], u0.v[e]}, ff{w1.v[e], u1.v[e]}, ff{w2.v[e], u2.v[e]}, ff{w3.v[e], u3.v[e]}, idz);
+          if (kz) d = cpml_upd64(psz + (long long)(kz - 1) * P + (i - 1), cz[na + kz - 1], cz[2 * na + nh + kz - 1], d);
+          const ff nv = ff_sub(ff{VZ.v[e], VZL.v[e]}, ff_mul(ff{MZ.v[e], MZL.v[e]}, d));
+          vz[c + e] = nv.hi;
+          vzl[c + e] = nv.lo;
+        }
+      }
+    }
+    w0 = w1; w1 = w2; w2 = w3; w3 = wn;
+    u0 = u1; u1 = u2; u2 = u3; u3 = un;
+  }
+}
+
+// FP64 memory variables into the FP32 checkpoint strips (compensated forward)
+__global__ void k_vd_d2f(const double* __restrict__ src, float* __restrict__ dst, long long n) {
+  for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x)
+    dst[q] = (float)src[q];
+}
+
+// ---------------------------------------------------------------------------
 // Sources, receivers, misfit, reductions
 // ---------------------------------------------------------------------------
 struct ShotDesc {
@@ -398,20 +629,32 @@ struct ShotDesc {
 // inject_sources! then record_receivers! (the velocity update in between does
 // not touch p): one block per active shot; a point that several sources share
 // receives them in source order.
-__global__ void k_vd_srcrec(const ShotDesc* __restrict__ desc, int it, long long F, float* p, int record) {
+__global__ void k_vd_srcrec(const ShotDesc* __restrict__ desc, int it, long long F, float* p, int record,
+                            float* plo) {
   const ShotDesc D = desc[blockIdx.x];
   if (it > D.nt) return;  // block uniform
   float* pp = p + (long long)blockIdx.x * F;
+  float* pl = plo ? plo + (long long)blockIdx.x * F : nullptr;  // compensated forward: low parts
   for (int u = threadIdx.x; u < D.nsp; u += blockDim.x) {
     const long long c = D.sp_lin[u];
+    if (pl) {
+      ff v{pp[c], pl[c]};
+      for (int k = D.sp_ptr[u]; k < D.sp_ptr[u + 1]; ++k)
+        v = ff_add(v, ff{D.tf[(long long)(it - 1) + (long long)D.sp_ids[k] * D.nt], 0.f});
+      pp[c] = v.hi;
+      pl[c] = v.lo;
+      continue;
+    }
     float v = pp[c];
     for (int k = D.sp_ptr[u]; k < D.sp_ptr[u + 1]; ++k) v += D.tf[(long long)(it - 1) + (long long)D.sp_ids[k] * D.nt];
     pp[c] = v;
   }
   if (!record) return;
   __syncthreads();
-  for (int r = threadIdx.x; r < D.nrec; r += blockDim.x)
-    D.tr[(long long)(it - 1) + (long long)r * D.nt] = pp[D.rec_lin[r]];
+  for (int r = threadIdx.x; r < D.nrec; r += blockDim.x) {
+    const long long q = D.rec_lin[r];
+    D.tr[(long long)(it - 1) + (long long)r * D.nt] = pl ? __fadd_rn(pp[q], pl[q]) : pp[q];
+  }
 }
 
 // Adjoint injection at the receivers and the matching share of the pressure
@@ -645,6 +888,12 @@ struct sw_acoustic_vd {
   int snapevery = 0;
   float* const* snap_out = nullptr;
   int tz = 8;
+  // compensated forward (precision 1): low parts of p, vx, vz and of the
+  // material factors, FP64 memory variables and coefficients
+  int precision = 0;
+  int hp_cap = 0;
+  DevMem plo, vxl, vzl, xi64[2], psi64[2], m0l, m1xl, m1zl, d_cp64;
+  std::vector<float> m0l_h, m1xl_h, m1zl_h;
 };
 
 namespace {
@@ -742,6 +991,16 @@ void ensure_state(sw_acoustic_vd* vd, int S, bool grad, int max_nt, int ngroups)
       vd->acc.release();
     }
     vd->cap = S;
+  }
+  if (vd->precision == 1 && vd->hp_cap < vd->cap) {
+    for (DevMem* m : {&vd->plo, &vd->vxl, &vd->vzl})
+      dev_alloc(*m, (size_t)vd->cap * F * sizeof(float), "VD low parts", st);
+    for (int d = 0; d < 2; ++d) {
+      const long long w = d == 0 ? vd->xs : vd->zs;
+      dev_alloc(vd->xi64[d], (size_t)vd->cap * w * sizeof(double), "VD memory variables (FP64)", st);
+      dev_alloc(vd->psi64[d], (size_t)vd->cap * w * sizeof(double), "VD memory variables (FP64)", st);
+    }
+    vd->hp_cap = vd->cap;
   }
   if (grad) {
     const int K = vd->gp.check_freq;
@@ -870,6 +1129,7 @@ void build_tables(sw_acoustic_vd* vd, const sw_acoustic_shot* shots, const std::
   if (ic_total) ensure(vd, vd->d_ic, (size_t)ic_total * sizeof(float), "inverse covariance");
   const cudaMemcpyKind kind = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
   std::vector<float> cps(S * (size_t)vd->cps);
+  std::vector<double> cps64(vd->precision == 1 ? S * (size_t)vd->cps : 0);
   for (int k = 0; k < S; ++k) {
     const sw_acoustic_shot& s = shots[group[k].orig];
     check_cuda(cudaMemcpyAsync(vd->d_tf.as<float>() + tf_off[k], s.srctf, (size_t)s.nt * s.nsrc * sizeof(float), kind, st),
@@ -882,8 +1142,11 @@ void build_tables(sw_acoustic_vd* vd, const sw_acoustic_shot* shots, const std::
                    "invcov upload");
     }
     std::copy(s.cpml, s.cpml + vd->cps, cps.begin() + (size_t)k * vd->cps);
+    if (vd->precision == 1)  // FP64 coefficients of the compensated forward (the FP32 ones widened if absent)
+      for (int q = 0; q < vd->cps; ++q) cps64[(size_t)k * vd->cps + q] = s.cpml64 ? s.cpml64[q] : (double)s.cpml[q];
   }
   upload(vd, vd->d_cp, cps, "C-PML coefficients");
+  if (vd->precision == 1) upload(vd, vd->d_cp64, cps64, "C-PML coefficients (FP64)");
   check_cuda(cudaMemsetAsync(vd->d_tr.p, 0, (size_t)std::max<long long>(tr_total, 4) * sizeof(float), st), "traces clear");
   const long long* LL = vd->d_ll.as<long long>();
   const int* IN = vd->d_int.as<int>();
@@ -980,6 +1243,15 @@ void zero_state(sw_acoustic_vd* vd, int S, bool adjoint) {
   DevMem* f = adjoint ? vd->ast : vd->st;
   for (int k = 0; k < 3; ++k)
     check_cuda(cudaMemsetAsync(f[k].p, 0, (size_t)S * vd->g.F * sizeof(float), st), "state clear");
+  if (!adjoint && vd->precision == 1) {
+    for (DevMem* m : {&vd->plo, &vd->vxl, &vd->vzl})
+      check_cuda(cudaMemsetAsync(m->p, 0, (size_t)S * vd->g.F * sizeof(float), st), "low parts clear");
+    for (int d = 0; d < 2; ++d) {
+      const long long w = d == 0 ? vd->xs : vd->zs;
+      check_cuda(cudaMemsetAsync(vd->xi64[d].p, 0, (size_t)S * w * sizeof(double), st), "xi clear");
+      check_cuda(cudaMemsetAsync(vd->psi64[d].p, 0, (size_t)S * w * sizeof(double), st), "psi clear");
+    }
+  }
   for (int d = 0; d < 2; ++d) {
     const long long w = d == 0 ? vd->xs : vd->zs;
     check_cuda(cudaMemsetAsync((adjoint ? vd->axi : vd->xi)[d].p, 0, (size_t)S * w * sizeof(float), st), "xi clear");
@@ -1058,14 +1330,70 @@ struct Run {
   double adj_bytes(int S) const { return (double)vd->g.nx * vd->g.nz * (S * 68.0 + 12.0); }
 
   // forward_onestep_CPML!: p (pin -> pout), injection + recording, velocities
+  HArgs hargs(const float* pin, float* pout) const {
+    HArgs a{};
+    a.g = vd->g;
+    a.pin = pin;
+    a.pout = pout;
+    a.plo = vd->plo.as<float>();
+    a.vx = vd->st[1].as<float>();
+    a.vz = vd->st[2].as<float>();
+    a.vxl = vd->vxl.as<float>();
+    a.vzl = vd->vzl.as<float>();
+    a.xi_x = vd->xi64[0].as<double>();
+    a.xi_z = vd->xi64[1].as<double>();
+    a.psi_x = vd->psi64[0].as<double>();
+    a.psi_z = vd->psi64[1].as<double>();
+    a.xs = vd->xs;
+    a.zs = vd->zs;
+    a.m0 = vd->m0.as<float>();
+    a.m0l = vd->m0l.as<float>();
+    a.m1x = vd->m1x.as<float>();
+    a.m1xl = vd->m1xl.as<float>();
+    a.m1z = vd->m1z.as<float>();
+    a.m1zl = vd->m1zl.as<float>();
+    a.cp = vd->d_cp64.as<double>();
+    a.cps = vd->cps;
+    const double ix = 1.0 / vd->prm.h[0], iz = 1.0 / vd->prm.h[1];
+    a.idxl = (float)(ix - (double)(float)ix);
+    a.idzl = (float)(iz - (double)(float)iz);
+    return a;
+  }
+  // compensated forward_onestep_CPML! (k_vd_p_hp, injection with low parts, k_vd_v_hp)
+  void forward_step_hp(int S, int it, const float* pin, float* pout, bool record, int kind) const {
+    const HArgs a = hargs(pin, pout);
+    const int TZ = 8;
+    const dim3 grid((vd->g.nx + 511) / 512, (vd->g.nz + TZ - 1) / TZ, S);
+    cudaEvent_t ev = nullptr;
+    vd->ctx->prof.begin(st, kind, fwd_bytes(S) + hp_extra_bytes(S), &ev);
+    k_vd_p_hp<TZ><<<grid, BX, 0, st>>>(a);
+    check_cuda(cudaGetLastError(), "compensated pressure update launch");
+    vd->ctx->prof.end(st, kind, ev);
+    vd->ctx->prof.begin(st, KK_SRCREC, 0.0, &ev);
+    k_vd_srcrec<<<S, 128, 0, st>>>(ddesc, it, vd->g.F, pout, record ? 1 : 0, vd->plo.as<float>());
+    check_cuda(cudaGetLastError(), "injection launch");
+    vd->ctx->prof.end(st, KK_SRCREC, ev);
+    vd->ctx->prof.begin(st, kind, 0.0, &ev);
+    k_vd_v_hp<TZ><<<grid, BX, 0, st>>>(a);
+    check_cuda(cudaGetLastError(), "compensated velocity update launch");
+    vd->ctx->prof.end(st, kind, ev);
+  }
+  // extra bytes of the compensated step per node and shot: R/W the low parts of p, vx, vz (24),
+  // R the low parts of the factors once (12)
+  double hp_extra_bytes(int S) const { return (double)vd->g.nx * vd->g.nz * (S * 24.0 + 12.0); }
+
   void forward_step(int S, int it, const float* pin, float* pout, bool record, int kind) const {
     if (S <= 0) return;
+    if (vd->precision == 1 && kind == KK_STENCIL) {  // the forward pass (the recompute stays FP32)
+      forward_step_hp(S, it, pin, pout, record, kind);
+      return;
+    }
     cudaEvent_t ev = nullptr;
     vd->ctx->prof.begin(st, kind, fwd_bytes(S), &ev);
     launch_p(pargs(false, pin, pout), S, false);
     vd->ctx->prof.end(st, kind, ev);
     vd->ctx->prof.begin(st, KK_SRCREC, 0.0, &ev);
-    k_vd_srcrec<<<S, 128, 0, st>>>(ddesc, it, vd->g.F, pout, record ? 1 : 0);
+    k_vd_srcrec<<<S, 128, 0, st>>>(ddesc, it, vd->g.F, pout, record ? 1 : 0, nullptr);
     check_cuda(cudaGetLastError(), "injection launch");
     vd->ctx->prof.end(st, KK_SRCREC, ev);
     vd->ctx->prof.begin(st, kind, 0.0, &ev);
@@ -1179,8 +1507,25 @@ void vd_init(sw_acoustic_vd* vd, sw_ctx* ctx, const sw_acoustic_params* p, int i
   dev_alloc(vd->rho_d, (size_t)g.nx * g.nz * sizeof(double), "rho", ctx->stream);
 }
 
-// update_matprop! + precompute_fact! (acou_models.jl:273-300)
-void vd_set_material(sw_acoustic_vd* vd, const float* vp, const float* rho) {
+void vd_upload_low(sw_acoustic_vd* vd) {
+  cudaStream_t st = vd->ctx->stream;
+  const size_t F = (size_t)vd->g.F;
+  for (DevMem* m : {&vd->m0l, &vd->m1xl, &vd->m1zl})
+    if (!m->p) dev_alloc(*m, F * sizeof(float), "VD material low parts", st);
+  check_cuda(cudaMemcpyAsync(vd->m0l.p, vd->m0l_h.data(), F * sizeof(float), cudaMemcpyHostToDevice, st), "upload");
+  check_cuda(cudaMemcpyAsync(vd->m1xl.p, vd->m1xl_h.data(), F * sizeof(float), cudaMemcpyHostToDevice, st), "upload");
+  check_cuda(cudaMemcpyAsync(vd->m1zl.p, vd->m1zl_h.data(), F * sizeof(float), cudaMemcpyHostToDevice, st), "upload");
+  check_cuda(cudaStreamSynchronize(st), "material upload");
+}
+
+void vd_set_precision(sw_acoustic_vd* vd, int mode) {
+  vd->precision = mode;
+  if (mode == 1 && vd->has_mat) vd_upload_low(vd);
+}
+
+// update_matprop! + precompute_fact! (acou_models.jl:273-300); T = float or double
+template <typename T>
+void vd_set_material_t(sw_acoustic_vd* vd, const T* vp, const T* rho) {
   if (!vp || !rho) fail(SW_ERR_ARG, "vp and rho are required");
   const Geo& g = vd->g;
   const long long np = (long long)g.nx * g.nz;
@@ -1190,6 +1535,13 @@ void vd_set_material(sw_acoustic_vd* vd, const float* vp, const float* rho) {
   }
   auto M = [&](int i, int j) { return (size_t)(i - 1) + (size_t)(j - 1) * g.nx; };
   std::vector<float> m0(g.F, 0.0f), mx(g.F, 0.0f), mz(g.F, 0.0f);
+  vd->m0l_h.assign(g.F, 0.0f);  // low parts of the factors (compensated forward)
+  vd->m1xl_h.assign(g.F, 0.0f);
+  vd->m1zl_h.assign(g.F, 0.0f);
+  auto split = [](double v, float& hi, float& lo) {
+    hi = (float)v;
+    lo = (float)(v - (double)hi);
+  };
   std::vector<double> vpd(np), rd(np);
   const double dt = vd->prm.dt;
   // 1/rho at a half point: arithmetic mean of 1/rho, or its harmonic mean (= 1 / mean of rho)
@@ -1202,9 +1554,9 @@ void vd_set_material(sw_acoustic_vd* vd, const float* vp, const float* rho) {
       const long long q = g.lin(i, j);
       vpd[c] = vp[c];
       rd[c] = rho[c];
-      m0[q] = (float)((double)vp[c] * vp[c] * rho[c] * dt);
-      if (i <= g.nx - 1) mx[q] = (float)(m1(c, M(i + 1, j)) * dt);
-      if (j <= g.nz - 1) mz[q] = (float)(m1(c, M(i, j + 1)) * dt);
+      split((double)vp[c] * vp[c] * rho[c] * dt, m0[q], vd->m0l_h[q]);
+      if (i <= g.nx - 1) split(m1(c, M(i + 1, j)) * dt, mx[q], vd->m1xl_h[q]);
+      if (j <= g.nz - 1) split(m1(c, M(i, j + 1)) * dt, mz[q], vd->m1zl_h[q]);
     }
   cudaStream_t st = vd->ctx->stream;
   auto up = [&](DevMem& m, const void* src, size_t bytes) {
@@ -1217,7 +1569,10 @@ void vd_set_material(sw_acoustic_vd* vd, const float* vp, const float* rho) {
   up(vd->rho_d, rd.data(), rd.size() * sizeof(double));
   check_cuda(cudaStreamSynchronize(st), "material upload");
   vd->has_mat = true;
+  if (vd->precision == 1) vd_upload_low(vd);
 }
+void vd_set_material(sw_acoustic_vd* vd, const float* vp, const float* rho) { vd_set_material_t(vd, vp, rho); }
+void vd_set_material64(sw_acoustic_vd* vd, const double* vp, const double* rho) { vd_set_material_t(vd, vp, rho); }
 
 void vd_forward(sw_acoustic_vd* vd, int nshots, const sw_acoustic_shot* shots, bool on_device) {
   if (!vd->has_mat) fail(SW_ERR_STATE, "material properties not set (sw_acoustic_vd_set_material)");
@@ -1326,6 +1681,16 @@ void vd_gradient(sw_acoustic_vd* vd, int nshots, const sw_acoustic_shot* shots, 
       for (int f = 0; f < 3; ++f) copy(b + (size_t)f * cap * F, vd->st[f].p, (size_t)S * F * sizeof(float), "checkpoint save");
       float* sp[4];
       strip_ptrs(b, sp);
+      if (vd->precision == 1) {  // the compensated forward keeps FP64 memory variables
+        const double* src[4] = {vd->xi64[0].as<double>(), vd->psi64[0].as<double>(), vd->xi64[1].as<double>(),
+                                vd->psi64[1].as<double>()};
+        for (int q = 0; q < 4; ++q) {
+          const long long n = (long long)S * (q < 2 ? vd->xs : vd->zs);
+          k_vd_d2f<<<(unsigned)std::min<long long>((n + 255) / 256, 1024), 256, 0, st>>>(src[q], sp[q], n);
+          check_cuda(cudaGetLastError(), "checkpoint strip conversion");
+        }
+        return;
+      }
       copy(sp[0], vd->xi[0].p, (size_t)S * vd->xs * sizeof(float), "checkpoint save");
       copy(sp[1], vd->psi[0].p, (size_t)S * vd->xs * sizeof(float), "checkpoint save");
       copy(sp[2], vd->xi[1].p, (size_t)S * vd->zs * sizeof(float), "checkpoint save");

@@ -108,6 +108,8 @@ class AcousticVDStaggeredCPMLWaveSimulation(AcousticCDCPMLWaveSimulation):
         self.ctx.check(self.ctx.lib.sw_acoustic_vd_create(self.ctx.h, ctypes.byref(prm), self._interp, int(gradient),
                                                           ctypes.byref(gp), ctypes.byref(self._h)),
                        "sw_acoustic_vd_create")
+        if runparams.compensated:
+            self.ctx.check(self.ctx.lib.sw_acoustic_vd_set_precision(self._h, 1), "sw_acoustic_vd_set_precision")
 
     def __del__(self):
         try:
@@ -142,6 +144,12 @@ class AcousticVDStaggeredCPMLWaveSimulation(AcousticCDCPMLWaveSimulation):
             raise ValueError("the interpolation method is fixed when the wavesim is built")
         self.matprop = VpRhoAcousticVDMaterialProperties(np.array(matprop.vp, copy=True), np.array(matprop.rho, copy=True),
                                                          matprop.interp_method)
+        if self.runparams.compensated:  # the factors from the FP64 model
+            vp64 = np.asfortranarray(matprop.vp, dtype=np.float64)
+            rho64 = np.asfortranarray(matprop.rho, dtype=np.float64)
+            self.ctx.check(self.ctx.lib.sw_acoustic_vd_set_material64(self._h, vp64.ctypes.data, rho64.ctypes.data),
+                           "sw_acoustic_vd_set_material64")
+            return
         vp32 = np.asfortranarray(matprop.vp, dtype=np.float32)
         rho32 = np.asfortranarray(matprop.rho, dtype=np.float32)
         self.ctx.check(self.ctx.lib.sw_acoustic_vd_set_material(self._h, vp32.ctypes.data, rho32.ctypes.data),

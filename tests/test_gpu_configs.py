@@ -172,14 +172,22 @@ def test_acoustic_vd2d_2001x801_shot_matches_oracle(sw, oracle):
     run = GpuVD(ctx, case, gradient=True, check_freq=w.check_freq)
     g, msf, tr = run.gradient([shot], [obs])
     run.close()
+    hp = GpuVD(ctx, case, gradient=True, check_freq=w.check_freq, precision=1)  # the compensated forward
+    g_hp, msf_hp, tr_hp = hp.gradient([shot], [obs])
+    hp.close()
     ctx.close()
     gref, mref, tref = vd_gradient(case, shot, obs, check_freq=w.check_freq)
     errs = (rel_l2(tr[0], tref), abs(msf - mref) / mref, rel_l2(g["vp"], gref["vp"]), rel_l2(g["rho"], gref["rho"]))
+    hp_errs = (rel_l2(tr_hp[0], tref), abs(msf_hp - mref) / mref, rel_l2(g_hp["vp"], gref["vp"]),
+               rel_l2(g_hp["rho"], gref["rho"]))
     bound = _misfit_bound(tr, [tref], [obs])
     print(f"acoustic_vd2d_2001x801 (nt {shot.nt}): traces {errs[0]:.3e} misfit {errs[1]:.3e} (trace-implied "
-          f"bound {bound:.3e}) vp {errs[2]:.3e} rho {errs[3]:.3e}")
-    assert errs[0] < TRACE_TOL and errs[1] <= max(MISFIT_TOL, 1.1 * bound)
+          f"bound {bound:.3e}) vp {errs[2]:.3e} rho {errs[3]:.3e}; compensated: traces {hp_errs[0]:.3e} misfit "
+          f"{hp_errs[1]:.3e} vp {hp_errs[2]:.3e} rho {hp_errs[3]:.3e}")
+    assert errs[0] < TRACE_TOL and errs[1] <= max(MISFIT_TOL, 1.1 * bound)  # FP32 state: about 1.8e-6
     assert errs[2] < GRAD_TOL and errs[3] < GRAD_TOL
+    assert hp_errs[0] < TRACE_TOL and hp_errs[1] < MISFIT_TOL  # the misfit bar, met by the compensated forward
+    assert hp_errs[2] < GRAD_TOL and hp_errs[3] < GRAD_TOL
 
 
 def test_elastic2d_1200x600_batch_matches_oracle(sw):

@@ -92,7 +92,7 @@ def oracle_gradient(case, shot, observed, *, check_freq=1, invcov=None, windows=
 class GpuVD:
     """One sw_acoustic_vd through the C ABI (host buffers)."""
 
-    def __init__(self, lib_ctx, case: VDCase, gradient=False, check_freq=1, mute_src=0, mute_rec=0):
+    def __init__(self, lib_ctx, case: VDCase, gradient=False, check_freq=1, mute_src=0, mute_rec=0, precision=0):
         self.ctx = lib_ctx
         self.case = case
         L = sw._lib
@@ -107,10 +107,18 @@ class GpuVD:
         self.ctx.check(self.ctx.lib.sw_acoustic_vd_create(self.ctx.h, ctypes.byref(prm), int(case.interp),
                                                           int(gradient), ctypes.byref(gp), ctypes.byref(self.h)),
                        "sw_acoustic_vd_create")
-        vp = np.asfortranarray(case.vp, dtype=np.float32)
-        rho = np.asfortranarray(case.rho, dtype=np.float32)
-        self.ctx.check(self.ctx.lib.sw_acoustic_vd_set_material(self.h, vp.ctypes.data, rho.ctypes.data),
-                       "sw_acoustic_vd_set_material")
+        self.precision = precision
+        if precision:  # compensated forward: the factors from the FP64 model
+            self.ctx.check(self.ctx.lib.sw_acoustic_vd_set_precision(self.h, int(precision)), "set_precision")
+            vp64 = np.asfortranarray(case.vp, dtype=np.float64)
+            rho64 = np.asfortranarray(case.rho, dtype=np.float64)
+            self.ctx.check(self.ctx.lib.sw_acoustic_vd_set_material64(self.h, vp64.ctypes.data, rho64.ctypes.data),
+                           "sw_acoustic_vd_set_material64")
+        else:
+            vp = np.asfortranarray(case.vp, dtype=np.float32)
+            rho = np.asfortranarray(case.rho, dtype=np.float32)
+            self.ctx.check(self.ctx.lib.sw_acoustic_vd_set_material(self.h, vp.ctypes.data, rho.ctypes.data),
+                           "sw_acoustic_vd_set_material")
 
     def close(self):
         if self.h:
@@ -132,6 +140,10 @@ class GpuVD:
             st.src_idx, st.srctf, st.rec_idx = si.ctypes.data, tf.ctypes.data, ri.ctypes.data
             st.traces, st.cpml = tr.ctypes.data, cp.ctypes.data
             arrs = [si, ri, tf, tr, cp]
+            if self.precision:  # FP64 coefficients of the compensated forward
+                cp64 = np.ascontiguousarray(cpml(self.case, shot), dtype=np.float64)
+                st.cpml64 = cp64.ctypes.data
+                arrs.append(cp64)
             if observed is not None:
                 obs = np.asfortranarray(observed[k], dtype=np.float32)
                 st.observed = obs.ctypes.data
