@@ -1439,8 +1439,19 @@ struct Launcher {
       a1.tiles_y = sp.tiles_y1;
       a1.tiles_z = sp.tiles_z1;
       const long long b1 = (long long)a.nshots * c.tiles_x * sp.tiles_y1 * sp.tiles_z1;
-      const long long b2 = (long long)a.nshots * c.tiles_x * sp.zslab_units;
-      const long long b3 = (long long)a.nshots * c.tiles_x * sp.yslab_units;
+      // the slabs are thin: shorter bands while a slab launch would fill less
+      // than two waves of 4 blocks per SM (small batches), 4 rows at least
+      const int sms = ws->ctx->num_sms > 0 ? ws->ctx->num_sms : 148;
+      int tzs = c.TZ;
+      Split3d ss = sp;
+      while (tzs > 4 && (long long)a.nshots * c.tiles_x * std::min(ss.zslab_units, ss.yslab_units) < 8LL * sms) {
+        tzs /= 2;
+        ss = split3d(ws, tzs, nw);
+      }
+      StepArgs a2 = a;
+      a2.TZ = tzs;
+      const long long b2 = (long long)a.nshots * c.tiles_x * ss.zslab_units;
+      const long long b3 = (long long)a.nshots * c.tiles_x * ss.yslab_units;
       if (b1 > 0 && ws->inner_np) {
         if (nw == 8) k_ac3d_inner_np<MODE, 8><<<(unsigned)b1, 256, 0, st>>>(a1);
         else k_ac3d_inner_np<MODE><<<(unsigned)b1, 128, 0, st>>>(a1);
@@ -1449,18 +1460,18 @@ struct Launcher {
         else k_ac3d_inner<MODE><<<(unsigned)b1, 128, 0, st>>>(a1);
       }
       if (b2 > 0 && ws->inner_np) {
-        if (nw == 8) k_ac3d_zslab<MODE, 8, false><<<(unsigned)b2, 256, 0, st>>>(a);
-        else k_ac3d_zslab<MODE, 4, false><<<(unsigned)b2, 128, 0, st>>>(a);
+        if (nw == 8) k_ac3d_zslab<MODE, 8, false><<<(unsigned)b2, 256, 0, st>>>(a2);
+        else k_ac3d_zslab<MODE, 4, false><<<(unsigned)b2, 128, 0, st>>>(a2);
       } else if (b2 > 0) {
-        if (nw == 8) k_ac3d_zslab<MODE, 8><<<(unsigned)b2, 256, 0, st>>>(a);
-        else k_ac3d_zslab<MODE><<<(unsigned)b2, 128, 0, st>>>(a);
+        if (nw == 8) k_ac3d_zslab<MODE, 8><<<(unsigned)b2, 256, 0, st>>>(a2);
+        else k_ac3d_zslab<MODE><<<(unsigned)b2, 128, 0, st>>>(a2);
       }
       if (b3 > 0 && ws->inner_np) {
-        if (nw == 8) k_ac3d_yslab<MODE, 8, false><<<(unsigned)b3, 256, 0, st>>>(a);
-        else k_ac3d_yslab<MODE, 4, false><<<(unsigned)b3, 128, 0, st>>>(a);
+        if (nw == 8) k_ac3d_yslab<MODE, 8, false><<<(unsigned)b3, 256, 0, st>>>(a2);
+        else k_ac3d_yslab<MODE, 4, false><<<(unsigned)b3, 128, 0, st>>>(a2);
       } else if (b3 > 0) {
-        if (nw == 8) k_ac3d_yslab<MODE, 8><<<(unsigned)b3, 256, 0, st>>>(a);
-        else k_ac3d_yslab<MODE><<<(unsigned)b3, 128, 0, st>>>(a);
+        if (nw == 8) k_ac3d_yslab<MODE, 8><<<(unsigned)b3, 256, 0, st>>>(a2);
+        else k_ac3d_yslab<MODE><<<(unsigned)b3, 128, 0, st>>>(a2);
       }
     } else {
       const int nw = block_rows3d(ws);
