@@ -921,13 +921,18 @@ def run_gb300(a):
     t_e2e = max_over_ranks(R.timed(R.gradient_host, a.steps), dist, R.dev)
     e2e = whole_job_rate(pts, a.steps, world, t_e2e) / 1e9
 
-    # plain per-shot path: the same library, one shot per call
+    # plain per-shot path: the same library, one shot per call, with the library's own launch
+    # shapes for a single shot (the batch's tuning does not carry over)
     plain = None
     if not a.no_plain:
+        if tuned:
+            R.ctx.check(R.lib.sw_wavesim_set_tuning(R.h, 0, 0), "sw_wavesim_set_tuning")
+            R.ctx.check(R.lib.sw_wavesim_set_band_heights(R.h, 0, 0, 0), "sw_wavesim_set_band_heights")
         R.gradient_device([0])
         t_plain = R.timed(lambda: [R.gradient_device([i]) for i in allidx], 1)
         plain = {"value": pts / t_plain / 1e9, "unit": UNIT, "shots_per_s": nshots / t_plain,
-                 "ms_per_step": t_plain * 1e3, "what": "same kernels, one shot per call"}
+                 "ms_per_step": t_plain * 1e3,
+                 "what": "same kernels, one shot per call, the library's default launch shapes for one shot"}
 
     parity = None
     if rank == 0 and not a.no_parity and w.vp.ndim == 2:
