@@ -1802,7 +1802,9 @@ void forward_group(sw_wavesim* ws, const std::vector<HostShot>& group, bool grad
     } else {
       double bytes = stencil_bytes(ws, Sa, grad ? MODE_FWD_D : MODE_FWD, n_dwrite, ckpt);
       if (ws->precision == 1) bytes += hp_extra_bytes(ws, Sa);
-      if (grad)
+      // steps before the top segment write no D: the plain forward kernel does the same work
+      // without the D store path
+      if (grad && n_dwrite > 0)
         L.step<MODE_FWD_D>(a, c, bytes);
       else
         L.step<MODE_FWD>(a, c, bytes);
