@@ -356,7 +356,7 @@ __device__ __forceinline__ void st4v(float* p, long long c, const float (&v)[4])
   *reinterpret_cast<float4*>(p + c) = make_float4(v[0], v[1], v[2], v[3]);
 }
 
-template <int TZ, bool FP = true>
+template <int TZ>
 __global__ void __launch_bounds__(BX, 6) k_el_stress4(const Args A) {
   const Geo g = A.g;
   const int s = blockIdx.z;
@@ -382,8 +382,6 @@ __global__ void __launch_bounds__(BX, 6) k_el_stress4(const Args A) {
   const bool xstrip = i0 <= g.halo + 1 || i0 + 3 >= g.nx - 1 - g.halo;
   const bool xx_all = i0 >= 2 && i0 + 3 <= g.nx - 1;  // all four points are sigma_xx nodes
   const bool xz_all = i0 + 3 <= g.nx - 1;             // all four points are sigma_xz nodes
-  // the warp's 128 points (i = wx0+1 .. wx0+128) all nodes and outside the x strips
-  const bool wfast = wx0 > g.halo && wx0 + 128 <= g.nx - 2 - g.halo;
   long long c = g.lin(i0, j0);
   F4 xu0 = ld4z(ux, c - P, ldok), xu1 = ld4z(ux, c, ldok), xu2 = ld4z(ux, c + P, ldok), xu3 = ld4z(ux, c + 2 * P, ldok);
   F4 zu0 = ld4z(uz, c - 2 * P, ldok), zu1 = ld4z(uz, c - P, ldok), zu2 = ld4z(uz, c, ldok), zu3 = ld4z(uz, c + P, ldok);
@@ -419,28 +417,6 @@ __global__ void __launch_bounds__(BX, 6) k_el_stress4(const Args A) {
     const int kF = cpml_full(j, g.nz, g.halo, colF);  // duz/dz at sigma_xx nodes (uz has nz-1 points)
     const int kH = cpml_half(j, g.nz, g.halo, colH);  // dux/dz at sigma_xz nodes (ux has nz points)
     float oxx[4], ozz[4], oxz[4];
-    if (FP && wfast && !kF && !kH && j >= 3) {
-      // warp-uniform: every point of the warp is a sigma_xx and sigma_xz node outside the C-PML
-      // strips and below the free-surface rows; the same arithmetic without the per-point tests
-#pragma unroll
-      for (int e = 0; e < 4; ++e) {
-        const float l = L4.v[e], m = M4.v[e];
-        const float l2m = l + 2.0f * m;
-        const float dux = d4(ua[e], ua[e + 1], ua[e + 2], ua[e + 3], g.idx);
-        const float duz = d4(zu0.v[e], zu1.v[e], zu2.v[e], zu3.v[e], g.idz);
-        oxx[e] = l2m * dux + l * duz;
-        ozz[e] = l * dux + l2m * duz;
-        const float dzx = d4(za[e], za[e + 1], za[e + 2], za[e + 3], g.idx);
-        const float dxz = d4(xu0.v[e], xu1.v[e], xu2.v[e], xu3.v[e], g.idz);
-        oxz[e] = MIJ.v[e] * (dzx + dxz);
-      }
-      st4v(sxx, c, oxx);
-      st4v(szz, c, ozz);
-      st4v(sxz, c, oxz);
-      xu0 = xu1; xu1 = xu2; xu2 = xu3; xu3 = xun;
-      zu0 = zu1; zu1 = zu2; zu2 = zu3; zu3 = zun;
-      continue;
-    }
 #pragma unroll
     for (int e = 0; e < 4; ++e) {
       const int i = i0 + e;
@@ -509,7 +485,7 @@ __global__ void __launch_bounds__(BX, 6) k_el_stress4(const Args A) {
   }
 }
 
-template <int TZ, bool FP = true>
+template <int TZ>
 __global__ void __launch_bounds__(BX, 5) k_el_disp4(const Args A) {
   const Geo g = A.g;
   const int s = blockIdx.z;
@@ -536,8 +512,6 @@ __global__ void __launch_bounds__(BX, 5) k_el_disp4(const Args A) {
   const bool xstrip = i0 <= g.halo + 1 || i0 + 3 >= g.nx - 1 - g.halo;
   const bool ux_all = i0 + 3 <= g.nx - 1;  // all four points are ux nodes
   const bool uz_all = i0 + 3 <= g.nx;      // all four points are uz nodes
-  // the warp's 128 points (i = wx0+1 .. wx0+128) all nodes and outside the x strips
-  const bool wfast = wx0 > g.halo && wx0 + 128 <= g.nx - 2 - g.halo;
   long long c = g.lin(i0, j0);
   F4 q0 = ld4z(sxz, c - 2 * P, ldok), q1 = ld4z(sxz, c - P, ldok), q2 = ld4z(sxz, c, ldok), q3 = ld4z(sxz, c + P, ldok);
   F4 w0 = ld4z(szz, c - P, ldok), w1 = ld4z(szz, c, ldok), w2 = ld4z(szz, c + P, ldok), w3 = ld4z(szz, c + 2 * P, ldok);
@@ -573,50 +547,6 @@ __global__ void __launch_bounds__(BX, 5) k_el_disp4(const Args A) {
     int colB = 0, colD = 0;
     const int kB = cpml_full(j, g.nz, g.halo, colB);  // dsxz/dz at ux nodes (sigma_xz has nz-1 points)
     const int kD = cpml_half(j, g.nz, g.halo, colD);  // dszz/dz at uz nodes (sigma_zz has nz points)
-    if (FP && wfast && !kB && !kD && j >= 3 && j <= g.nz - 1) {
-      // warp-uniform: every point a ux and uz node outside the C-PML strips and below the
-      // free-surface rows; the same arithmetic without the per-point tests
-      {
-        const F4 R = ld4z(A.dtr_i, c, true), U = ld4rwz(ux, c), DU = ld4rwz(dux, c);
-        float nu[4], ndu[4], Dv[4];
-#pragma unroll
-        for (int e = 0; e < 4; ++e) {
-          const float d1 = d4(xa[e], xa[e + 1], xa[e + 2], xa[e + 3], g.idx);
-          const float d2 = d4(q0.v[e], q1.v[e], q2.v[e], q3.v[e], g.idz);
-          Dv[e] = R.v[e] * (d1 + d2);
-          ndu[e] = DU.v[e] + Dv[e];
-          nu[e] = U.v[e] + ndu[e];
-        }
-        if (slots) {
-          st4v(A.sUx + so, c, U.v);
-          st4v(A.sDx + so, c, Dv);
-        }
-        st4v(ux, c, nu);
-        st4v(dux, c, ndu);
-      }
-      {
-        const F4 Rj = ld4z(A.dtr_j, c, true), V = ld4rwz(uz, c), DV = ld4rwz(duz, c);
-        float nv[4], ndv[4], Dz[4];
-#pragma unroll
-        for (int e = 0; e < 4; ++e) {
-          const float e1 = d4(qa[e], qa[e + 1], qa[e + 2], qa[e + 3], g.idx);
-          const float e2 = d4(w0.v[e], w1.v[e], w2.v[e], w3.v[e], g.idz);
-          Dz[e] = Rj.v[e] * (e1 + e2);
-          ndv[e] = DV.v[e] + Dz[e];
-          nv[e] = V.v[e] + ndv[e];
-        }
-        if (slots) {
-          st4v(A.sUz + so, c, V.v);
-          st4v(A.sDz + so, c, Dz);
-        }
-        st4v(uz, c, nv);
-        st4v(duz, c, ndv);
-      }
-      q0 = q1; q1 = q2; q2 = q3; q3 = qn;
-      w0 = w1; w1 = w2; w2 = w3; w3 = wn;
-      xc = xcn;
-      continue;
-    }
     if (ldok) {
       // ux nodes
       const F4 R = ld4z(A.dtr_i, c, true);
@@ -1309,7 +1239,6 @@ struct sw_elastic {
   float* const* snap_out = nullptr;  // per caller shot: nt/snapevery blocks [ux, uz, sxx, szz, sxz]
   int tz = 8;  // rows per block of the stencil kernels (8, 16 or 32; 8 measured fastest)
   bool vec = true;  // four x points per thread (k_el_*4) instead of one
-  bool fastp = true;  // the four-point kernels' warp-uniform interior path (tz + 128: off)
   DevMem d_scales;        // [0] the forward sources' common scale, [1] the adjoint source's scale
   DevMem d_ccts, d_partial2;  // CCTS descriptors and per-trace misfit terms
   DevMem d_gout, d_mout;  // gradient / misfit of the host-buffer path (stable addresses for the graphs)
@@ -1868,10 +1797,8 @@ template <int TZ>
 void launch_stencil_tz(const sw_elastic* es, cudaStream_t st, const Args& a, int S, bool stress) {
   if (es->vec) {  // four points per thread: 512 per block
     const dim3 grid((es->g.nx + 511) / 512, (es->g.nz + TZ - 1) / TZ, S);
-    if (stress && es->fastp) k_el_stress4<TZ><<<grid, BX, 0, st>>>(a);
-    else if (stress) k_el_stress4<TZ, false><<<grid, BX, 0, st>>>(a);
-    else if (es->fastp) k_el_disp4<TZ><<<grid, BX, 0, st>>>(a);
-    else k_el_disp4<TZ, false><<<grid, BX, 0, st>>>(a);
+    if (stress) k_el_stress4<TZ><<<grid, BX, 0, st>>>(a);
+    else k_el_disp4<TZ><<<grid, BX, 0, st>>>(a);
   } else {
     const dim3 grid((es->g.nx + BX - 1) / BX, (es->g.nz + TZ - 1) / TZ, S);
     if (stress) k_el_stress<TZ><<<grid, BX, 0, st>>>(a);
@@ -2312,8 +2239,7 @@ void elastic_gradient(sw_elastic* es, int nshots, const sw_elastic_shot* shots, 
       const std::vector<float> sc = {sf_ref, 1.0f};
       upload(es, es->d_scales, sc, "source scales");
     }
-    std::vector<long long> key = {S, ntmax, es->tz, es->vec ? 1 : 0, es->fastp ? 1 : 0, first_group ? 1 : 0,
-                                  mute ? 1 : 0,
+    std::vector<long long> key = {S, ntmax, es->tz, es->vec ? 1 : 0, first_group ? 1 : 0, mute ? 1 : 0,
                                   R.gx_src, R.gx_adj, R.gx_rec, (long long)(uintptr_t)out[0],
                                   (long long)(uintptr_t)out[1], (long long)(uintptr_t)out[2],
                                   (long long)(uintptr_t)mout};
@@ -2448,14 +2374,12 @@ void elastic_gradient(sw_elastic* es, int nshots, const sw_elastic_shot* shots, 
 }
 
 void elastic_set_tuning(sw_elastic* es, int tz) {
-  // tz = rows per block (8, 16, 32; 0 = 8); + 64 selects the one-point-per-thread kernels;
-  // + 128 switches off the warp-uniform interior path of the four-point kernels
+  // tz = rows per block (8, 16, 32; 0 = 8); + 64 selects the one-point-per-thread kernels
   const int rows = tz % 64;
-  if (tz < 0 || tz >= 256 || (rows != 0 && rows != 8 && rows != 16 && rows != 32))
-    fail(SW_ERR_ARG, "tz must be 0, 8, 16 or 32, optionally + 64 and + 128");
+  if (tz < 0 || tz >= 128 || (rows != 0 && rows != 8 && rows != 16 && rows != 32))
+    fail(SW_ERR_ARG, "tz must be 0, 8, 16 or 32, optionally + 64");
   es->tz = rows == 0 ? 8 : rows;
-  es->vec = (tz & 64) == 0;
-  es->fastp = (tz & 128) == 0;
+  es->vec = tz < 64;
 }
 sw_ctx* elastic_ctx(sw_elastic* es) { return es->ctx; }
 sw_elastic* elastic_new() { return new sw_elastic(); }
