@@ -56,6 +56,8 @@ def _args():
                                                       "2 also BF16 checkpoints)")
     p.add_argument("--no-parity", action="store_true", help="skip the FP64-oracle error of the benchmark's shortest shot")
     p.add_argument("--check-freq", type=int, default=0, help="override the checkpoint period (small profiling cases)")
+    p.add_argument("--precision", type=int, default=0,
+                   help="1: compensated (double-FP32) forward passes of the acoustic CD / VD gradient")
     p.add_argument("--no-extras", action="store_true",
                    help="skip the full-length 3D and elastic gradients that the default run times after the headline")
     return p.parse_args()
@@ -180,7 +182,7 @@ def _tune_tz(R, w, kind, candidates):
 class GradientRun:
     """The workload's shots as C-ABI structs over device (or pinned host) buffers."""
 
-    def __init__(self, sw, w, device, on_device=True, bf16=0):
+    def __init__(self, sw, w, device, on_device=True, bf16=0, precision=0):
         import torch
 
         L = sw._lib
@@ -200,6 +202,8 @@ class GradientRun:
         self.h = ctypes.c_void_p()
         self.ctx.check(self.lib.sw_wavesim_create(self.ctx.h, ctypes.byref(prm), 1, ctypes.byref(gp),
                                                   ctypes.byref(self.h)), "sw_wavesim_create")
+        if precision:  # compensated forward passes
+            self.ctx.check(self.lib.sw_wavesim_set_precision(self.h, precision), "sw_wavesim_set_precision")
         self.hf = ctypes.c_void_p()
         self.ctx.check(self.lib.sw_wavesim_create(self.ctx.h, ctypes.byref(prm), 0, None, ctypes.byref(self.hf)),
                        "sw_wavesim_create")
@@ -214,7 +218,14 @@ class GradientRun:
             for d in range(nd):
                 parts += L.cpml_coefficients(vmax, w.dt, w.halo, 1e-4, w.h[d], s.f0, w.freetop and d == nd - 1)
             cp = np.concatenate(parts).astype(np.float32)
-            self.host.append((si, ri, tf, cp))
+            if precision:  # the FP64 coefficients of the compensated forward
+                p64 = []
+                for d in range(nd):
+                    p64 += L.cpml_coefficients64(vmax, w.dt, w.halo, 1e-4, w.h[d], s.f0, w.freetop and d == nd - 1)
+                self.host.append((si, ri, tf, cp, np.concatenate(p64)))
+            else:
+                self.host.append((si, ri, tf, cp))
+        self.precision = precision
         # device-resident inputs and outputs
         t = torch
         self.vp_d = t.from_numpy(np.ascontiguousarray(w.vp.ravel(order="F"), dtype=np.float32)).to(self.dev)
@@ -228,10 +239,12 @@ class GradientRun:
     def structs(self, idx, tf, tr, obs):
         arr = (self.L.SwAcousticShot * len(idx))()
         for k, i in enumerate(idx):
-            si, ri, _, cp = self.host[i]
+            si, ri, _, cp = self.host[i][:4]
             st = arr[k]
             st.nt, st.nsrc, st.nrec = self.w.shots[i].nt, si.shape[0], ri.shape[0]
             st.src_idx, st.rec_idx, st.cpml = si.ctypes.data, ri.ctypes.data, cp.ctypes.data
+            if len(self.host[i]) > 4:
+                st.cpml64 = self.host[i][4].ctypes.data
             st.srctf, st.traces = tf[i], tr[i]
             if obs is not None:
                 st.observed = obs[i]
@@ -244,7 +257,11 @@ class GradientRun:
         arr = self.structs(idx, [x.data_ptr() for x in self.tf_d], [x.data_ptr() for x in self.obs_d], None)
         self.ctx.check(self.lib.sw_acoustic_forward(self.hf, len(idx), arr, 1), "observed forward")
         self.lib.sw_wavesim_destroy(self.hf)
-        self.ctx.check(self.lib.sw_wavesim_set_vp(self.h, self.vp_d.data_ptr(), 1), "set_vp")
+        if self.precision:  # the compensated forward takes the FP64 model
+            self.vp64 = np.asfortranarray(self.w.vp, dtype=np.float64)
+            self.ctx.check(self.lib.sw_wavesim_set_vp64(self.h, self.vp64.ctypes.data, 0), "set_vp64")
+        else:
+            self.ctx.check(self.lib.sw_wavesim_set_vp(self.h, self.vp_d.data_ptr(), 1), "set_vp")
 
     def forward_device(self, idx):
         arr = self.structs(idx, [x.data_ptr() for x in self.tf_d], [x.data_ptr() for x in self.tr_d], None)
@@ -259,19 +276,26 @@ class GradientRun:
     def setup_host(self):
         """Pinned host copies of the per-step inputs and outputs (end-to-end leg)."""
         t = self.torch
-        self.vp_h = self.vp_d.cpu().pin_memory()
+        if getattr(self, "precision", 0):  # FP64 model for the compensated forward
+            self.vp_h = t.from_numpy(np.ascontiguousarray(self.w.vp.ravel(order="F"), dtype=np.float64)).pin_memory()
+        else:
+            self.vp_h = self.vp_d.cpu().pin_memory()
         self.tf_h = [x.cpu().pin_memory() for x in self.tf_d]
         self.obs_h = [x.cpu().pin_memory() for x in self.obs_d]
         self.tr_h = [t.zeros(x.numel(), dtype=t.float32).pin_memory() for x in self.tr_d]
         self.grad_h = t.zeros(self.grad_d.numel(), dtype=t.float64).pin_memory()
         self.mis_h = t.zeros(1, dtype=t.float64).pin_memory()
-        h2d = self.vp_h.numel() * 4 + sum(x.numel() * 4 for x in self.tf_h) + sum(x.numel() * 4 for x in self.obs_h)
+        h2d = (self.vp_h.numel() * self.vp_h.element_size() + sum(x.numel() * 4 for x in self.tf_h)
+               + sum(x.numel() * 4 for x in self.obs_h))
         d2h = sum(x.numel() * 4 for x in self.tr_h) + self.grad_h.numel() * 8 + 8
         return h2d, d2h
 
     def gradient_host(self):
         idx = list(range(len(self.w.shots)))
-        self.ctx.check(self.lib.sw_wavesim_set_vp(self.h, self.vp_h.data_ptr(), 0), "set_vp")
+        if getattr(self, "precision", 0):
+            self.ctx.check(self.lib.sw_wavesim_set_vp64(self.h, self.vp_h.data_ptr(), 0), "set_vp64")
+        else:
+            self.ctx.check(self.lib.sw_wavesim_set_vp(self.h, self.vp_h.data_ptr(), 0), "set_vp")
         arr = self.structs(idx, [x.data_ptr() for x in self.tf_h], [x.data_ptr() for x in self.tr_h],
                            [x.data_ptr() for x in self.obs_h])
         self.ctx.check(self.lib.sw_acoustic_gradient(self.h, len(idx), arr, 0, self.grad_h.data_ptr(),
@@ -395,7 +419,7 @@ class ElasticRun:
 class VDRun(GradientRun):
     """The variable-density workload's shots as C-ABI structs (sw_acoustic_vd_*)."""
 
-    def __init__(self, sw, w, device):
+    def __init__(self, sw, w, device, precision=0):
         import torch
 
         L = sw._lib
@@ -415,6 +439,8 @@ class VDRun(GradientRun):
         self.h = ctypes.c_void_p()
         self.ctx.check(self.lib.sw_acoustic_vd_create(self.ctx.h, ctypes.byref(prm), 0, 1, ctypes.byref(gp),
                                                       ctypes.byref(self.h)), "sw_acoustic_vd_create")
+        if precision:  # compensated forward passes
+            self.ctx.check(self.lib.sw_acoustic_vd_set_precision(self.h, precision), "sw_acoustic_vd_set_precision")
         self.stream = torch.cuda.ExternalStream(self.ctx.stream, device=self.dev)
         vmax = float(np.max(w.vp))
         self.host = []
@@ -509,7 +535,7 @@ def measure_vd(a, name="acoustic_vd2d_2001x801", shots=0, nt_cap=0, steps=None, 
     steps = a.steps if steps is None else steps
     warmup = a.warmup if warmup is None else warmup
     sw, w = _workload(name, shots, nt_cap)
-    R = VDRun(sw, w, device)
+    R = VDRun(sw, w, device, precision=a.precision)
     tuned, tz = None, a.tz or 8
     if a.tz:
         R.ctx.check(R.lib.sw_acoustic_vd_set_tuning(R.h, a.tz), "sw_acoustic_vd_set_tuning")
@@ -562,7 +588,8 @@ def measure_vd(a, name="acoustic_vd2d_2001x801", shots=0, nt_cap=0, steps=None, 
                       "tz": tz, "tuning": tuned,
                       "cache": "inputs larger than L2 (each step streams several GB of wavefield state)",
                       "precision": "fp32 wavefields and stencil, fp32 sums over one checkpoint window, "
-                                   "fp64 window totals, misfit and shot sum"},
+                                   "fp64 window totals, misfit and shot sum"
+                                   + ("; compensated double-fp32 forward passes" if a.precision else "")},
            "shots_per_s": nshots * steps / t_dev, "plain": pl,
            "batched_vs_plain": (nshots * steps / t_dev / pl["shots_per_s"]) if pl else None,
            "clocks": clk,
@@ -689,7 +716,7 @@ def _parity_2d(R, sw, w):
     s = w.shots[idx]
     R.gradient_device([idx])
     R.torch.cuda.synchronize(R.dev)
-    si, ri, _, _ = R.host[idx]
+    si, ri = R.host[idx][:2]
     nrec = ri.shape[0]
     g = R.grad_d.cpu().numpy().reshape(w.vp.shape, order="F")
     mis = float(R.mis_d.item())
@@ -841,7 +868,7 @@ def run_gb300(a):
         torch.cuda.set_device(local)
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     sw, w = _workload(a.workload, a.shots, a.nt, a.check_freq)
-    R = GradientRun(sw, w, local, bf16=a.bf16)
+    R = GradientRun(sw, w, local, bf16=a.bf16, precision=a.precision)
     if a.tz or a.variant >= 0:
         R.ctx.check(R.lib.sw_wavesim_set_tuning(R.h, a.tz, max(a.variant, 0)), "sw_wavesim_set_tuning")
     R.make_observed()
@@ -995,6 +1022,7 @@ def run_gb300(a):
                                        if (nd == 2 and not (veff >= 0 and (veff & 256)))
                                        else "Kahan fp32 correlation")
                                     + ", fp64 misfit and shot sum"
+                                    + (", compensated double-fp32 forward passes" if a.precision else "")
                                     + (", bf16 recompute buffer" if a.bf16 >= 1 else "")
                                     + (", bf16 checkpoints" if a.bf16 >= 2 else ""),
                        "parallelism": f"replicas x{world}" if world > 1 else "1 GPU, all shots batched"},
