@@ -2159,15 +2159,23 @@ __global__ void __launch_bounds__(128) k_ac_hp(const StepArgs A) {
         st4(ckp + idx, cp4);
         st4(ckd + idx, cd4);
       }
+      if (x0 >= 1 && x0 + 3 <= nx - 2) {  // all four points interior: vector stores
+        st4(pn + idx, outph);
+        st4(pnl + idx, outpl);
+        st4(dd + idx, outdh);
+        st4(ddl + idx, outdl);
+        if (MODE == MODE_FWD_D && Dw) dst4(Dw, idx, outD, A.dbf16, de);
+      } else {
 #pragma unroll
-      for (int e = 0; e < 4; ++e) {
-        const int x = x0 + e;
-        if (x >= 1 && x <= nx - 2) {
-          pn[idx + e] = outph[e];
-          pnl[idx + e] = outpl[e];
-          dd[idx + e] = outdh[e];
-          ddl[idx + e] = outdl[e];
-          if (MODE == MODE_FWD_D && Dw) dst1(Dw, idx + e, outD[e], A.dbf16, de);
+        for (int e = 0; e < 4; ++e) {
+          const int x = x0 + e;
+          if (x >= 1 && x <= nx - 2) {
+            pn[idx + e] = outph[e];
+            pnl[idx + e] = outpl[e];
+            dd[idx + e] = outdh[e];
+            ddl[idx + e] = outdl[e];
+            if (MODE == MODE_FWD_D && Dw) dst1(Dw, idx + e, outD[e], A.dbf16, de);
+          }
         }
       }
     }

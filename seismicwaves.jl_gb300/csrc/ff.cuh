@@ -23,11 +23,12 @@ __device__ __forceinline__ ff fast_two_sum(float a, float b) {  // |a| >= |b| or
   const float s = __fadd_rn(a, b);
   return {s, __fsub_rn(b, __fsub_rn(s, a))};
 }
+// The QD library's "sloppy" addition: one TwoSum of the high parts, the low
+// parts added in FP32, one Fast2Sum; its error is a few units of 2^-46
+// relative to |a| + |b|, far below the FP32 roundings this arithmetic removes.
 __device__ __forceinline__ ff ff_add(ff a, ff b) {
   const ff s = two_sum(a.hi, b.hi);
-  const ff t = two_sum(a.lo, b.lo);
-  ff r = fast_two_sum(s.hi, __fadd_rn(s.lo, t.hi));
-  return fast_two_sum(r.hi, __fadd_rn(r.lo, t.lo));
+  return fast_two_sum(s.hi, __fadd_rn(s.lo, __fadd_rn(a.lo, b.lo)));
 }
 __device__ __forceinline__ ff ff_mul(ff a, ff b) {
   const float p = __fmul_rn(a.hi, b.hi);
