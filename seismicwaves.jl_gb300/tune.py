@@ -34,7 +34,7 @@ _cache: dict = {}
 # (variant, tz) of sw_wavesim_set_tuning
 CANDIDATES_2D = [(0, 4), (0, 8), (0, 16), (2, 8), (512, 8), (1024, 0), (256, 8)]
 # 3D: 131072 = inner rows without the software pipeline, 65536 = one launch per step
-CANDIDATES_3D = [(0, 8), (0, 16), (0, 32), (2, 8), (131072, 8), (131072, 16), (65536, 16)]
+CANDIDATES_3D = [(0, 8), (0, 16), (0, 32), (2, 8), (131072, 8), (131072, 16), (131074, 16), (65536, 16)]
 KIND_NAMES = {0: "forward", 4: "recompute", 1: "adjoint"}
 # band heights tried per stencil kind after the variant is chosen (2D gradients)
 TZ_KIND_2D = (4, 8, 16)
