@@ -1069,7 +1069,7 @@ def measure_elastic(a, name="elastic2d_1200x600", shots=0, nt_cap=0, steps=None,
         R.ctx.check(R.lib.sw_elastic_set_tuning(R.h, a.tz), "sw_elastic_set_tuning")
     R.make_observed()
     if not (a.tz or a.no_autotune):
-        tz, tuned = _tune_tz(R, w, "elastic", (8, 16, 32, 72))
+        tz, tuned = _tune_tz(R, w, "elastic", (8, 16, 32, 72, 136))
     nshots = len(w.shots)
     allidx = list(range(nshots))
     pts = float(w.point_steps())

@@ -485,8 +485,15 @@ __global__ void __launch_bounds__(BX, 6) k_el_stress4(const Args A) {
   }
 }
 
-template <int TZ>
-__global__ void __launch_bounds__(BX, 5) k_el_disp4(const Args A) {
+// COMP: 2 updates ux and uz; 0 only ux, 1 only uz (two launches with fewer
+// registers each: the uz half loads no sigma_xx and no sigma_xz column, the ux
+// half no sigma_zz)
+template <int COMP>
+struct ElDispBounds {
+  static constexpr int MINB = COMP == 2 ? 5 : 7;
+};
+template <int TZ, int COMP = 2>
+__global__ void __launch_bounds__(BX, ElDispBounds<COMP>::MINB) k_el_disp4(const Args A) {
   const Geo g = A.g;
   const int s = blockIdx.z;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -512,42 +519,62 @@ __global__ void __launch_bounds__(BX, 5) k_el_disp4(const Args A) {
   const bool xstrip = i0 <= g.halo + 1 || i0 + 3 >= g.nx - 1 - g.halo;
   const bool ux_all = i0 + 3 <= g.nx - 1;  // all four points are ux nodes
   const bool uz_all = i0 + 3 <= g.nx;      // all four points are uz nodes
+  constexpr bool DOX = COMP != 1, DOZ = COMP != 0;
   long long c = g.lin(i0, j0);
-  F4 q0 = ld4z(sxz, c - 2 * P, ldok), q1 = ld4z(sxz, c - P, ldok), q2 = ld4z(sxz, c, ldok), q3 = ld4z(sxz, c + P, ldok);
-  F4 w0 = ld4z(szz, c - P, ldok), w1 = ld4z(szz, c, ldok), w2 = ld4z(szz, c + P, ldok), w3 = ld4z(szz, c + 2 * P, ldok);
-  F4 xc = ld4z(sxx, c, ldok);
+  F4 q0{}, q1{}, q3{}, w0{}, w1{}, w2{}, w3{}, xc{};
+  if (DOX) {
+    q0 = ld4z(sxz, c - 2 * P, ldok);
+    q1 = ld4z(sxz, c - P, ldok);
+    q3 = ld4z(sxz, c + P, ldok);
+    xc = ld4z(sxx, c, ldok);
+  }
+  F4 q2 = ld4z(sxz, c, ldok);
+  if (DOZ) {
+    w0 = ld4z(szz, c - P, ldok);
+    w1 = ld4z(szz, c, ldok);
+    w2 = ld4z(szz, c + P, ldok);
+    w3 = ld4z(szz, c + 2 * P, ldok);
+  }
   for (int j = j0; j <= j1; ++j, c += P) {
     const bool more = j + 1 <= j1;
-    F4 qn = ld4z(sxz, c + 2 * P, ldok && more);
-    F4 wn = ld4z(szz, c + 3 * P, ldok && more);
-    F4 xcn = ld4z(sxx, c + P, ldok && more);
+    F4 qn{}, wn{}, xcn{};
+    if (DOX) {
+      qn = ld4z(sxz, c + 2 * P, ldok && more);
+      xcn = ld4z(sxx, c + P, ldok && more);
+    } else {
+      qn = ld4z(sxz, c + P, ldok && more);  // only row j+1 (next q2)
+    }
+    if (DOZ) wn = ld4z(szz, c + 3 * P, ldok && more);
     // sigma_xx at i0-1 .. i0+5, sigma_xz at i0-2 .. i0+4 (row j)
     float xa[7], qa[7];
-    xa[0] = __shfl_up_sync(FULL, xc.v[3], 1);
-    xa[5] = __shfl_down_sync(FULL, xc.v[0], 1);
-    xa[6] = __shfl_down_sync(FULL, xc.v[1], 1);
-    qa[0] = __shfl_up_sync(FULL, q2.v[2], 1);
-    qa[1] = __shfl_up_sync(FULL, q2.v[3], 1);
-    qa[6] = __shfl_down_sync(FULL, q2.v[0], 1);
-    if (lane == 0) {
-      xa[0] = ldz(sxx, c - 1, ldok);
-      qa[0] = ldz(sxz, c - 2, ldok);
-      qa[1] = ldz(sxz, c - 1, ldok);
-    }
-    if (lane == 31) {
-      xa[5] = ldz(sxx, c + 4, ldok);
-      xa[6] = ldz(sxx, c + 5, ldok);
-      qa[6] = ldz(sxz, c + 4, ldok);
-    }
+    if (DOX) {
+      xa[0] = __shfl_up_sync(FULL, xc.v[3], 1);
+      xa[5] = __shfl_down_sync(FULL, xc.v[0], 1);
+      xa[6] = __shfl_down_sync(FULL, xc.v[1], 1);
+      if (lane == 0) xa[0] = ldz(sxx, c - 1, ldok);
+      if (lane == 31) {
+        xa[5] = ldz(sxx, c + 4, ldok);
+        xa[6] = ldz(sxx, c + 5, ldok);
+      }
 #pragma unroll
-    for (int e = 0; e < 4; ++e) {
-      xa[1 + e] = xc.v[e];
-      qa[2 + e] = q2.v[e];
+      for (int e = 0; e < 4; ++e) xa[1 + e] = xc.v[e];
+    }
+    if (DOZ) {
+      qa[0] = __shfl_up_sync(FULL, q2.v[2], 1);
+      qa[1] = __shfl_up_sync(FULL, q2.v[3], 1);
+      qa[6] = __shfl_down_sync(FULL, q2.v[0], 1);
+      if (lane == 0) {
+        qa[0] = ldz(sxz, c - 2, ldok);
+        qa[1] = ldz(sxz, c - 1, ldok);
+      }
+      if (lane == 31) qa[6] = ldz(sxz, c + 4, ldok);
+#pragma unroll
+      for (int e = 0; e < 4; ++e) qa[2 + e] = q2.v[e];
     }
     int colB = 0, colD = 0;
     const int kB = cpml_full(j, g.nz, g.halo, colB);  // dsxz/dz at ux nodes (sigma_xz has nz-1 points)
     const int kD = cpml_half(j, g.nz, g.halo, colD);  // dszz/dz at uz nodes (sigma_zz has nz points)
-    if (ldok) {
+    if (ldok && DOX) {
       // ux nodes
       const F4 R = ld4z(A.dtr_i, c, true);
       F4 U = ld4rwz(ux, c), DU = ld4rwz(dux, c);
@@ -594,6 +621,8 @@ __global__ void __launch_bounds__(BX, 5) k_el_disp4(const Args A) {
             dux[c + e] = ndu[e];
           }
       }
+    }
+    if (ldok && DOZ) {
       // uz nodes
       if (j <= g.nz - 1) {
         const F4 Rj = ld4z(A.dtr_j, c, true);
@@ -641,9 +670,15 @@ __global__ void __launch_bounds__(BX, 5) k_el_disp4(const Args A) {
         }
       }
     }
-    q0 = q1; q1 = q2; q2 = q3; q3 = qn;
-    w0 = w1; w1 = w2; w2 = w3; w3 = wn;
-    xc = xcn;
+    if (DOX) {
+      q0 = q1; q1 = q2; q2 = q3; q3 = qn;
+      xc = xcn;
+    } else {
+      q2 = qn;
+    }
+    if (DOZ) {
+      w0 = w1; w1 = w2; w2 = w3; w3 = wn;
+    }
   }
 }
 
@@ -1239,6 +1274,7 @@ struct sw_elastic {
   float* const* snap_out = nullptr;  // per caller shot: nt/snapevery blocks [ux, uz, sxx, szz, sxz]
   int tz = 8;  // rows per block of the stencil kernels (8, 16 or 32; 8 measured fastest)
   bool vec = true;  // four x points per thread (k_el_*4) instead of one
+  bool split_disp = false;  // the displacement update as two launches, ux then uz (tz + 128)
   DevMem d_scales;        // [0] the forward sources' common scale, [1] the adjoint source's scale
   DevMem d_ccts, d_partial2;  // CCTS descriptors and per-trace misfit terms
   DevMem d_gout, d_mout;  // gradient / misfit of the host-buffer path (stable addresses for the graphs)
@@ -1797,8 +1833,14 @@ template <int TZ>
 void launch_stencil_tz(const sw_elastic* es, cudaStream_t st, const Args& a, int S, bool stress) {
   if (es->vec) {  // four points per thread: 512 per block
     const dim3 grid((es->g.nx + 511) / 512, (es->g.nz + TZ - 1) / TZ, S);
-    if (stress) k_el_stress4<TZ><<<grid, BX, 0, st>>>(a);
-    else k_el_disp4<TZ><<<grid, BX, 0, st>>>(a);
+    if (stress) {
+      k_el_stress4<TZ><<<grid, BX, 0, st>>>(a);
+    } else if (es->split_disp) {  // ux and uz updates as two launches
+      k_el_disp4<TZ, 0><<<grid, BX, 0, st>>>(a);
+      k_el_disp4<TZ, 1><<<grid, BX, 0, st>>>(a);
+    } else {
+      k_el_disp4<TZ><<<grid, BX, 0, st>>>(a);
+    }
   } else {
     const dim3 grid((es->g.nx + BX - 1) / BX, (es->g.nz + TZ - 1) / TZ, S);
     if (stress) k_el_stress<TZ><<<grid, BX, 0, st>>>(a);
@@ -2239,7 +2281,8 @@ void elastic_gradient(sw_elastic* es, int nshots, const sw_elastic_shot* shots, 
       const std::vector<float> sc = {sf_ref, 1.0f};
       upload(es, es->d_scales, sc, "source scales");
     }
-    std::vector<long long> key = {S, ntmax, es->tz, es->vec ? 1 : 0, first_group ? 1 : 0, mute ? 1 : 0,
+    std::vector<long long> key = {S, ntmax, es->tz, es->vec ? 1 : 0, es->split_disp ? 1 : 0, first_group ? 1 : 0,
+                                  mute ? 1 : 0,
                                   R.gx_src, R.gx_adj, R.gx_rec, (long long)(uintptr_t)out[0],
                                   (long long)(uintptr_t)out[1], (long long)(uintptr_t)out[2],
                                   (long long)(uintptr_t)mout};
@@ -2374,12 +2417,14 @@ void elastic_gradient(sw_elastic* es, int nshots, const sw_elastic_shot* shots, 
 }
 
 void elastic_set_tuning(sw_elastic* es, int tz) {
-  // tz = rows per block (8, 16, 32; 0 = 8); + 64 selects the one-point-per-thread kernels
+  // tz = rows per block (8, 16, 32; 0 = 8); + 64 selects the one-point-per-thread kernels;
+  // + 128 runs the four-point displacement update as two launches (ux, uz)
   const int rows = tz % 64;
-  if (tz < 0 || tz >= 128 || (rows != 0 && rows != 8 && rows != 16 && rows != 32))
-    fail(SW_ERR_ARG, "tz must be 0, 8, 16 or 32, optionally + 64");
+  if (tz < 0 || tz >= 256 || (rows != 0 && rows != 8 && rows != 16 && rows != 32))
+    fail(SW_ERR_ARG, "tz must be 0, 8, 16 or 32, optionally + 64 and + 128");
   es->tz = rows == 0 ? 8 : rows;
-  es->vec = tz < 64;
+  es->vec = (tz & 64) == 0;
+  es->split_disp = (tz & 128) != 0;
 }
 sw_ctx* elastic_ctx(sw_elastic* es) { return es->ctx; }
 sw_elastic* elastic_new() { return new sw_elastic(); }

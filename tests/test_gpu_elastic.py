@@ -159,3 +159,28 @@ def test_elastic_gradient_dense_invcov(ctx):
     assert abs(m - mref) <= MISFIT_TOL * abs(mref)
     for k in g:
         assert rel_l2(g[k], gref[k]) < GRAD_TOL, k
+
+
+@pytest.mark.parametrize("kind,freetop", [("mt", True), ("force", False)])
+def test_elastic_split_displacement_matches(ctx, kind, freetop):
+    """The displacement update as two launches (ux, then uz; sw_elastic_set_tuning
+    + 128) runs the same per-point arithmetic as the single launch: the traces
+    and gradients agree with it and with the oracle."""
+    case = small_case(kind, freetop=freetop, nt=360)
+    shot = case.shots[0]
+    obs = _observed(case, shot)
+    out = {}
+    for tz in (8, 136):
+        run = GpuElastic(ctx, case, gradient=True, check_freq=19)
+        run.ctx.check(run.ctx.lib.sw_elastic_set_tuning(run.h, tz), "sw_elastic_set_tuning")
+        out[tz] = run.gradient([shot], [obs])
+        run.close()
+    g0, m0, t0 = out[8]
+    g1, m1, t1 = out[136]
+    assert rel_l2(t1[0], t0[0]) < 1e-6 and abs(m1 - m0) <= 1e-6 * abs(m0)
+    for k in g0:
+        assert rel_l2(g1[k], g0[k]) < 1e-6, k
+    gref, mref, tref = oracle_gradient(case, shot, obs, check_freq=19)
+    assert rel_l2(t1[0], tref) < TRACE_TOL
+    for k in g1:
+        assert rel_l2(g1[k], gref[k]) < GRAD_TOL, k
