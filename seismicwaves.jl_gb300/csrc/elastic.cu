@@ -1274,7 +1274,7 @@ struct sw_elastic {
   float* const* snap_out = nullptr;  // per caller shot: nt/snapevery blocks [ux, uz, sxx, szz, sxz]
   int tz = 8;  // rows per block of the stencil kernels (8, 16 or 32; 8 measured fastest)
   bool vec = true;  // four x points per thread (k_el_*4) instead of one
-  bool split_disp = false;  // the displacement update as two launches, ux then uz (tz + 128)
+  bool split_disp = true;  // the displacement update as two launches, ux then uz (tz + 128: one launch)
   DevMem d_scales;        // [0] the forward sources' common scale, [1] the adjoint source's scale
   DevMem d_ccts, d_partial2;  // CCTS descriptors and per-trace misfit terms
   DevMem d_gout, d_mout;  // gradient / misfit of the host-buffer path (stable addresses for the graphs)
@@ -2418,13 +2418,13 @@ void elastic_gradient(sw_elastic* es, int nshots, const sw_elastic_shot* shots, 
 
 void elastic_set_tuning(sw_elastic* es, int tz) {
   // tz = rows per block (8, 16, 32; 0 = 8); + 64 selects the one-point-per-thread kernels;
-  // + 128 runs the four-point displacement update as two launches (ux, uz)
+  // + 128 runs the four-point displacement update as one launch instead of two (ux, uz)
   const int rows = tz % 64;
   if (tz < 0 || tz >= 256 || (rows != 0 && rows != 8 && rows != 16 && rows != 32))
     fail(SW_ERR_ARG, "tz must be 0, 8, 16 or 32, optionally + 64 and + 128");
   es->tz = rows == 0 ? 8 : rows;
   es->vec = (tz & 64) == 0;
-  es->split_disp = (tz & 128) != 0;
+  es->split_disp = (tz & 128) == 0;
 }
 sw_ctx* elastic_ctx(sw_elastic* es) { return es->ctx; }
 sw_elastic* elastic_new() { return new sw_elastic(); }

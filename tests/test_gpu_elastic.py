@@ -163,9 +163,9 @@ def test_elastic_gradient_dense_invcov(ctx):
 
 @pytest.mark.parametrize("kind,freetop", [("mt", True), ("force", False)])
 def test_elastic_split_displacement_matches(ctx, kind, freetop):
-    """The displacement update as two launches (ux, then uz; sw_elastic_set_tuning
-    + 128) runs the same per-point arithmetic as the single launch: the traces
-    and gradients agree with it and with the oracle."""
+    """The displacement update as two launches (ux, then uz; the default) runs
+    the same per-point arithmetic as the single launch (sw_elastic_set_tuning
+    + 128): the traces and gradients agree with it and with the oracle."""
     case = small_case(kind, freetop=freetop, nt=360)
     shot = case.shots[0]
     obs = _observed(case, shot)
