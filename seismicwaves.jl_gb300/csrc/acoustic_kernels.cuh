@@ -2003,8 +2003,11 @@ __device__ __forceinline__ ff cpml_axis_corr64(ff d2, ff pl, ff p0, ff pr, int x
 // One warp = 128 x points (4 per thread) of one row (2D) or of one y row
 // (3D), marching a band of TZ rows of the last axis; 4 warps per block (2D:
 // 512 x points; 3D: 4 y rows).  Forward modes only (MODE_FWD, MODE_FWD_D).
+// The 2D kernel is bounded for six blocks per SM (80 registers, a few bytes
+// of spills, faster than the unbounded allocation); a bound spills heavily in
+// 3D.
 template <int MODE, int NDIM>
-__global__ void __launch_bounds__(128) k_ac_hp(const StepArgs A) {
+__global__ void __launch_bounds__(128, NDIM == 2 ? 6 : 1) k_ac_hp(const StepArgs A) {
   static_assert(MODE == MODE_FWD || MODE == MODE_FWD_D, "compensated step: forward modes only");
   constexpr unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
