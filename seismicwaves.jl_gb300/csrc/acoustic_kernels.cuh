@@ -210,9 +210,11 @@ __device__ __forceinline__ void kahan_add(float& g, float& c, float y) {
 __device__ __forceinline__ float radd(float a, float b) { return __fadd_rn(a, b); }
 __device__ __forceinline__ float rsub(float a, float b) { return __fsub_rn(a, b); }
 __device__ __forceinline__ float rmul(float a, float b) { return __fmul_rn(a, b); }
-// (l - 2c + r) * ih2: the second difference along one axis
+// (l - 2c + r) * ih2: the second difference along one axis.  -2c is exact,
+// so l - 2c as one fused multiply-add rounds exactly as the product followed
+// by a rounded add (one instruction fewer per axis and point).
 __device__ __forceinline__ float d2term(float l, float c, float r, float ih2) {
-  return rmul(radd(radd(l, rmul(-2.f, c)), r), ih2);
+  return rmul(radd(__fmaf_rn(-2.f, c, l), r), ih2);
 }
 
 // One row of four interior points outside the damping strips advanced by one
@@ -514,8 +516,16 @@ __global__ void __launch_bounds__(32 * NW, (Ac2dBounds<MODE, NW>::MINB - (DP - 1
   // are issued before the stores of row z, so each warp keeps two rows of
   // loads in flight instead of waiting on every row.
   float rm[4], r0[4], rp[4], o[4], f[4], dv[4], g4[4], c4[4];
+  // The x neighbours of a lane's four points come from the neighbouring lanes
+  // by shuffles; lane 0 (left) and lane 31 (right) read theirs from memory,
+  // one value per row, loaded one row ahead (e0: row z) so that no row waits
+  // on its edge load (DP == 1).
+  const int eoff = lane == 0 ? xa - 1 : xa + 4;
+  const bool eload = (lane == 0 && xa > 0) || (lane == 31 && xa + 4 < P);
+  float e0 = 0.f;
   ld4(rm, pc + (long long)(z_begin - 1) * P + xa);
   ld4(r0, pc + (long long)z_begin * P + xa);
+  if (DP == 1 && eload) e0 = pc[(long long)z_begin * P + eoff];
   {
     const long long row = (long long)z_begin * P;
     ld4(rp, pc + row + P + xa);
@@ -553,7 +563,7 @@ __global__ void __launch_bounds__(32 * NW, (Ac2dBounds<MODE, NW>::MINB - (DP - 1
         if (MODE == MODE_ADJ) l2_prefetch(gcp + prow, seg);
       }
     }
-    float rpn[4], on[4], fn[4], dvn[4], g4n[4], c4n[4];
+    float rpn[4], on[4], fn[4], dvn[4], g4n[4], c4n[4], en = 0.f;
     const bool more = z + 1 < z_end;
     if constexpr (DP == 2) {
       if (z + 2 < z_end) {
@@ -564,6 +574,7 @@ __global__ void __launch_bounds__(32 * NW, (Ac2dBounds<MODE, NW>::MINB - (DP - 1
       }
     } else if (more) {
       const long long nrow = row + P;
+      if (eload) en = pc[nrow + eoff];
       ld4(rpn, pc + nrow + P + xa);
       ld4rw(on, di + nrow + xa);
       ld4(fn, fa + nrow + xa);
@@ -575,9 +586,15 @@ __global__ void __launch_bounds__(32 * NW, (Ac2dBounds<MODE, NW>::MINB - (DP - 1
     }
     float left = __shfl_up_sync(FULL, r0[3], 1);
     float right = __shfl_down_sync(FULL, r0[0], 1);
-    if (lane == 0) left = xa > 0 ? pc[row + xa - 1] : 0.f;
-    if (lane == 31) right = xa + 4 < P ? pc[row + xa + 4] : 0.f;
+    if constexpr (DP == 2) {
+      if (lane == 0) left = xa > 0 ? pc[row + xa - 1] : 0.f;
+      if (lane == 31) right = xa + 4 < P ? pc[row + xa + 4] : 0.f;
+    } else {
+      if (lane == 0) left = e0;
+      if (lane == 31) right = e0;
+    }
     R.update(z, rm, r0, rp, o, f, dv, g4, c4, left, right);
+    if constexpr (DP == 1) e0 = en;
 #pragma unroll
     for (int e = 0; e < 4; ++e) {
       rm[e] = r0[e];
