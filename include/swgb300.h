@@ -227,6 +227,11 @@ int sw_acoustic_forward_snapshots(sw_wavesim* ws, int32_t nshots, const sw_acous
  * block of that kernel (0 = heuristic: 32, fewer for small batches; 1 = 8,
  * 2 = 16, 3 = 32, 4 = 64, 5 = 128, 6 = 4) and bits 14-15 its resident-block
  * bound (0 = 6 forward / 5 adjoint blocks per SM, 1 = 4 / 3, 2 = 7 / 4).
+ * 3D: + 65536 runs the step as one launch instead of three (rows outside the
+ * y / z strips, the z slabs, the y slabs); + 131072 runs the three launches
+ * without the software pipeline.  2D, 4 warps per block: by default the
+ * 4-point lane groups that meet an x strip are advanced by a launch of their
+ * own after the stencil launch; + 262144 keeps them in the one launch.
  * Results do not depend on any of them beyond rounding. */
 int sw_wavesim_set_tuning(sw_wavesim* ws, int32_t tz, int32_t variant);
 

@@ -530,6 +530,7 @@ struct sw_wavesim {
   bool pair_on = false;                   // 2D: two time steps per launch where possible (tuning variant)
   bool split3d = true;                    // 3D: inner rows and strip rows as two launches (variant bit 16: one)
   bool inner_np = false;                  // 3D: the three launches without the software pipeline (variant bit 17)
+  bool xsplit = true;                     // 2D 4-warp stencil: x strips in their own launch (variant bit 18: not)
   int pair_tz = 0;                        // rows per block of the two-step kernel (0 = heuristic)
   int pair_occ = 0;                       // resident-block bound of the two-step kernel (0 = default, 1, 2)
   bool pair_ok = false;                   // the current group's shots allow two-step launches
@@ -651,7 +652,7 @@ std::vector<long long> group_key(const sw_wavesim* ws, const std::vector<HostSho
   std::vector<long long> k = {grad ? 1 : 0, ws->grp, ws->variant, ws->tile_tz, ws->pf, ws->adjw ? 1 : 0,
                               ws->cpa ? 1 : 0, ws->pair_ok ? 1 : 0, ws->pair_adj_ok ? 1 : 0, ws->pair_tz,
                               ws->pair_occ, ws->kind_tz[0], ws->kind_tz[1], ws->kind_tz[2], ws->precision,
-                              ws->split3d ? 1 : 0, ws->inner_np ? 1 : 0,
+                              ws->split3d ? 1 : 0, ws->inner_np ? 1 : 0, ws->xsplit ? 1 : 0,
                               (long long)group.size()};
   for (const auto& h : group) k.push_back(h.nt);
   return k;
@@ -1336,6 +1337,17 @@ void enable_pair_carveout() {
   done_for_device = dev;
 }
 
+// The 2D one-step stencil of 4-warp blocks with the x strips split off: the
+// lanes outside the x strips, then the lane groups that meet one.
+template <int MODE>
+void launch_2d_xsplit(long long blocks, cudaStream_t st, const StepArgs& a) {
+  k_ac2d_step<MODE, 4, 1, true><<<(unsigned)blocks, 128, 0, st>>>(a);
+  int nl, xr, ng;
+  xstrip_groups(a.n0, a.halo, a.P, nl, xr, ng);
+  const long long threads = (long long)ng * (a.n1 - 2) * a.nshots;
+  if (threads > 0) k_ac2d_xstrip<MODE><<<(unsigned)((threads + 127) / 128), 128, 0, st>>>(a);
+}
+
 template <int MODE, int MB>
 void launch_pair(long long blocks, cudaStream_t st, const StepArgs& a, const PairArgs& b) {
   enable_pair_carveout<MODE, MB>();
@@ -1401,7 +1413,9 @@ struct Launcher {
       if (nw == 4 && ws->cpa) {
         enable_cpa_carveout<MODE>();
         k_ac2d_cpa<MODE, 4><<<(unsigned)blocks, 128, 0, st>>>(a);
-      } else if (nw == 4)
+      } else if (nw == 4 && ws->xsplit)
+        launch_2d_xsplit<MODE>(blocks, st, a);
+      else if (nw == 4)
         k_ac2d_step<MODE, 4><<<(unsigned)blocks, 128, 0, st>>>(a);
       else if (nw == 8)
         k_ac2d_step<MODE, 8><<<(unsigned)blocks, 256, 0, st>>>(a);
@@ -1425,7 +1439,9 @@ struct Launcher {
         }
       }
       if (launched) {
-      } else if (nw == 4)
+      } else if (nw == 4 && ws->xsplit)
+        launch_2d_xsplit<MODE>(blocks, st, a);
+      else if (nw == 4)
         k_ac2d_step<MODE, 4><<<(unsigned)blocks, 128, 0, st>>>(a);
       else if (nw == 8)
         k_ac2d_step<MODE, 8><<<(unsigned)blocks, 256, 0, st>>>(a);
@@ -2359,6 +2375,7 @@ void wavesim_set_tuning(sw_wavesim* ws, int tz, int variant) {
   ws->pair_occ = (variant >> 14) & 3;
   ws->split3d = (variant & 65536) == 0;
   ws->inner_np = (variant & 131072) != 0;
+  ws->xsplit = (variant & 262144) == 0;
 }
 void wavesim_set_band_heights(sw_wavesim* ws, int tz_forward, int tz_recompute, int tz_adjoint) {
   ws->kind_tz[TZ_FORWARD] = tz_forward;

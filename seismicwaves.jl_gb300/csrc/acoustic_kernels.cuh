@@ -390,6 +390,12 @@ struct Ac2dRow {
     gcp = MODE == MODE_ADJ ? fptr(A.gc, shot) : nullptr;
   }
 
+  // XS (x strips split off): a lane whose four points meet an x strip
+  // (xstrip) stores nothing here; k_ac2d_xstrip advances those points.  Every
+  // other lane's points lie outside the x strips and inside the grid's
+  // interior, so a row outside the z strips takes the interior path in every
+  // warp and a z strip row needs only the z term.
+  template <bool XS = false>
   __device__ __forceinline__ void update(int z, const float (&rm)[4], const float (&r0)[4], const float (&rp)[4],
                                          const float (&o)[4], const float (&f)[4], const float (&dv)[4],
                                          float (&g4)[4], float (&c4)[4], float left, float right) {
@@ -398,8 +404,24 @@ struct Ac2dRow {
     sx.psi_base = (long long)z * (2 * H);
     sx.xi_base = (long long)z * (2 * H + 2);
     float outp[4], outd[4], outD[4];
-    if (fastx && z >= plain_lo(H) && z <= plain_hi(nz, H)) {
+    if ((XS || fastx) && z >= plain_lo(H) && z <= plain_hi(nz, H)) {
       row4_interior(rm, r0, rp, left, right, o, f, ih2x, ih2z, outp, outd, outD);
+    } else if (XS) {
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        const float c = r0[e];
+        const float tx = d2term(e == 0 ? left : r0[e - 1], c, e == 3 ? right : r0[e + 1], ih2x);
+        float tz = d2term(rm[e], c, rp[e], ih2z);
+        if (zstrip && inb && !xstrip) {
+          sz.psi_base = x0 + e;
+          sz.xi_base = x0 + e;
+          tz = cpml_axis_term(tz, rm[e], c, rp[e], z, nz, H, ihz, sz);
+        }
+        const float lap = radd(tx, tz);
+        outD[e] = rmul(f[e], lap);
+        outd[e] = radd(o[e], outD[e]);
+        outp[e] = radd(c, outd[e]);
+      }
     } else {
 #pragma unroll
       for (int e = 0; e < 4; ++e) {
@@ -422,7 +444,7 @@ struct Ac2dRow {
         outp[e] = radd(c, outd[e]);
       }
     }
-    if (!inb) return;
+    if (!inb || (XS && xstrip)) return;
     if (ckp) {
       st4(ckp + row + x0, r0);
       st4(ckd + row + x0, o);
@@ -482,7 +504,7 @@ struct Ac2dBounds {
                                                   : (NW == 4 ? 8 : NW == 8 ? 4 : 2);
 };
 
-template <int MODE, int NW, int DP = 1>
+template <int MODE, int NW, int DP = 1, bool XS = false>
 __global__ void __launch_bounds__(32 * NW, (Ac2dBounds<MODE, NW>::MINB - (DP - 1))) k_ac2d_step(const StepArgs A) {
   constexpr unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -593,7 +615,7 @@ __global__ void __launch_bounds__(32 * NW, (Ac2dBounds<MODE, NW>::MINB - (DP - 1
       if (lane == 0) left = e0;
       if (lane == 31) right = e0;
     }
-    R.update(z, rm, r0, rp, o, f, dv, g4, c4, left, right);
+    R.template update<XS>(z, rm, r0, rp, o, f, dv, g4, c4, left, right);
     if constexpr (DP == 1) e0 = en;
 #pragma unroll
     for (int e = 0; e < 4; ++e) {
@@ -617,6 +639,56 @@ __global__ void __launch_bounds__(32 * NW, (Ac2dBounds<MODE, NW>::MINB - (DP - 1
   }
 }
 
+
+// The 4-point lane groups that meet an x strip (x0 < H or x0 + 3 >= nx - H,
+// x0 = 0, 4, .. < P): nl groups x0 = 0 .. 4 (nl - 1) on the left, then the
+// groups from x0 = xr up to the padded row end; ng in all.
+__host__ __device__ __forceinline__ void xstrip_groups(int nx, int H, int P, int& nl, int& xr, int& ng) {
+  nl = (H + 3) / 4;
+  const int lo = nx - H - 3 > 0 ? nx - H - 3 : 0;
+  xr = ((lo + 3) / 4) * 4;
+  if (xr < 4 * nl) xr = 4 * nl;
+  ng = nl + (P - xr > 0 ? (P - xr) / 4 : 0);
+}
+
+// The points that k_ac2d_step<.., XS = true> leaves: one thread per (lane
+// group of the x strips, row, shot) loads its rows and runs the general path
+// of Ac2dRow (both strips per point), so every point is advanced by the same
+// arithmetic as in the single launch.
+template <int MODE>
+__global__ void __launch_bounds__(128) k_ac2d_xstrip(const StepArgs A) {
+  const int nx = A.n0, nz = A.n1, P = A.P, H = A.halo;
+  int nl, xr, ng;
+  xstrip_groups(nx, H, P, nl, xr, ng);
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int g = (int)(t % ng);
+  const long long rest = t / ng;
+  const int z = 1 + (int)(rest % (nz - 2));
+  const int shot = (int)(rest / (nz - 2));
+  if (shot >= A.nshots) return;
+  const int x0 = g < nl ? 4 * g : xr + 4 * (g - nl);
+  const float* __restrict__ pc = fptr(A.pcur, shot);
+  const float* di = fptr(A.din, shot);
+  const long long row = (long long)z * P;
+  float rm[4], r0[4], rp[4], o[4], f[4], dv[4] = {}, g4[4] = {}, c4[4] = {};
+  ld4(rm, pc + row - P + x0);
+  ld4(r0, pc + row + x0);
+  ld4(rp, pc + row + P + x0);
+  ld4rw(o, di + row + x0);
+  ld4(f, A.fact + row + x0);
+  const float left = x0 > 0 ? pc[row + x0 - 1] : 0.f;
+  const float right = x0 + 4 < P ? pc[row + x0 + 4] : 0.f;
+  Ac2dRow<MODE> R;
+  R.init(A, shot, x0);
+  R.fastx = false;
+  constexpr bool ADJ = MODE == MODE_ADJ || MODE == MODE_ADJW;
+  if (ADJ) {
+    dld4(dv, dptr(A.dcorr, shot, A.dbf16), row + x0, A.dbf16);
+    ld4rw(g4, R.gg + row + x0);
+    if (MODE == MODE_ADJ) ld4rw(c4, R.gcp + row + x0);
+  }
+  R.update(z, rm, r0, rp, o, f, dv, g4, c4, left, right);
+}
 
 // ---------------------------------------------------------------------------
 // 2D, two time steps per pass (temporal blocking) for the forward kinds and

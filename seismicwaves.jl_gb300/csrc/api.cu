@@ -327,7 +327,7 @@ int sw_profile_read(sw_ctx* ctx, int32_t kind, double* total_ms, int64_t* launch
 }
 
 int sw_wavesim_set_tuning(sw_wavesim* ws, int32_t tz, int32_t variant) {
-  if (!ws || tz < 0 || variant < 0 || variant >= (1 << 18)) return SW_ERR_ARG;
+  if (!ws || tz < 0 || variant < 0 || variant >= (1 << 19)) return SW_ERR_ARG;
   swgb::wavesim_set_tuning(ws, tz, variant);
   return SW_OK;
 }
