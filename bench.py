@@ -556,6 +556,7 @@ def measure_vd(a, name="acoustic_vd2d_2001x801", shots=0, nt_cap=0, steps=None, 
     R.timed(lambda: R.gradient_device(allidx), 1)
     R.ctx.profile(False)
     prof = {k: R.ctx.profile_read(k) for k in range(6)}
+    kernels_per_call = sum(R.ctx.profile_kernels(k) for k in range(6))
     h2d, d2h = R.setup_host()
     R.gradient_host()
     t_e2e = R.timed(R.gradient_host, steps)
@@ -595,7 +596,7 @@ def measure_vd(a, name="acoustic_vd2d_2001x801", shots=0, nt_cap=0, steps=None, 
            "clocks": clk,
            "e2e": {"value": pts * steps / t_e2e / 1e9, "unit": UNIT, "h2d_bytes_per_step": h2d,
                    "d2h_bytes_per_step": d2h},
-           "gpu_launches": sum(prof[k][1] for k in range(6)) * steps, "roofline": roof}
+           "gpu_launches": kernels_per_call * steps, "roofline": roof}
     if cpu:
         import oracle
 
@@ -937,6 +938,7 @@ def run_gb300(a):
     t_prof = R.timed(lambda: R.gradient_device(allidx), 1)
     R.ctx.profile(False)
     prof = {k: R.ctx.profile_read(k) for k in range(5)}
+    kernels_per_call = sum(R.ctx.profile_kernels(k) for k in range(5))
     t_dev = max_over_ranks(t_dev, dist, R.dev)
     barrier()
     value = whole_job_rate(pts, a.steps, world, t_dev) / 1e9
@@ -968,16 +970,23 @@ def run_gb300(a):
         return
     # roofline of the dominant kernel (largest total time among the stencil kinds)
     nd = w.vp.ndim
-    base = "k_ac2d_step" if nd == 2 else "k_ac3d_inner + k_ac3d_zslab + k_ac3d_yslab"
+    # 2D, 4-warp one-step stencil: the x strips run as a second launch unless variant bit 18 is set
+    xs = nd == 2 and not (veff >= 0 and veff & (262144 | 512 | 3))
+
+    def kname(m):
+        if nd == 3:
+            return f"k_ac3d_inner + k_ac3d_zslab + k_ac3d_yslab<{m}>"
+        return f"k_ac2d_step<{m}> + k_ac2d_xstrip<{m}>" if xs else f"k_ac2d_step<{m}>"
+
     if nd == 2 and veff >= 0 and (veff & 256) and nshots >= 4:
         adj, adj_what = "k_ac2d_adj_grp", "adjoint + correlation (4 shots per block, Kahan sums)"
     elif nd == 2:
-        adj, adj_what = base + "<3>", "adjoint + correlation (plain FP32 sums, FP64 flush every 32 steps)"
+        adj, adj_what = kname(3), "adjoint + correlation (plain FP32 sums, FP64 flush every 32 steps)"
     else:
-        adj, adj_what = base + "<2>", "adjoint + correlation (Kahan sums)"
+        adj, adj_what = kname(2), "adjoint + correlation (Kahan sums)"
     two = "k_ac2d_pair (two steps per launch) / " if (nd == 2 and veff >= 0 and veff & 1024) else ""
-    kinds = {0: (f"{two}{base}<0/1> forward", f"{base}<1>", "forward"),
-             4: (f"{two}{base}<1> recompute (writes D)", f"{base}<1>", "recompute"),
+    kinds = {0: (f"{two}{kname('0/1')} forward", kname(1), "forward"),
+             4: (f"{two}{kname(1)} recompute (writes D)", kname(1), "recompute"),
              1: (f"{two}{adj} {adj_what}", adj, "adjoint")}
     dom = max(kinds, key=lambda k: prof[k][0])
     ms_tot, launches, bytes_tot = prof[dom]
@@ -1007,7 +1016,8 @@ def run_gb300(a):
             "kernels": {kinds[k][0]: {"ms": prof[k][0], "launches": prof[k][1],
                                       "GB_per_s": (prof[k][2] / (prof[k][0] / 1e3) / 1e9) if prof[k][0] else None}
                         for k in kinds}}
-    total_launches = sum(prof[k][1] for k in range(5)) * a.steps  # per gradient x timed gradients
+    # kernels per gradient (a profiled step may launch several) x timed gradients
+    total_launches = kernels_per_call * a.steps
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
             "ms_per_step": t_dev * 1e3 / a.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32", "data": "synthetic",
@@ -1084,6 +1094,7 @@ def measure_elastic(a, name="elastic2d_1200x600", shots=0, nt_cap=0, steps=None,
     R.timed(lambda: R.gradient_device(allidx), 1)
     R.ctx.profile(False)
     prof = {k: R.ctx.profile_read(k) for k in range(6)}
+    kernels_per_call = sum(R.ctx.profile_kernels(k) for k in range(6))
     h2d, d2h = R.setup_host()
     R.gradient_host()
     t_e2e = R.timed(R.gradient_host, steps)
@@ -1118,7 +1129,7 @@ def measure_elastic(a, name="elastic2d_1200x600", shots=0, nt_cap=0, steps=None,
            "clocks": clk,
            "e2e": {"value": pts * steps / t_e2e / 1e9, "unit": UNIT, "h2d_bytes_per_step": h2d,
                    "d2h_bytes_per_step": d2h},
-           "gpu_launches": sum(prof[k][1] for k in range(6)) * steps, "roofline": roof}
+           "gpu_launches": kernels_per_call * steps, "roofline": roof}
     if cpu:
         import oracle
 

@@ -280,6 +280,11 @@ int sw_wavesim_use_graphs(sw_wavesim* ws, int32_t on);
  * bytes = algorithmic bytes. */
 int sw_profile_enable(sw_ctx* ctx, int32_t on);
 int sw_profile_read(sw_ctx* ctx, int32_t kind, double* total_ms, int64_t* launches, double* bytes);
+/* Kernel launches inside the brackets that sw_profile_read counts as
+ * `launches` (one bracket per step of a kind; the 2D step with its x strips,
+ * the 3D step as three launches, the variable-density adjoint pair and the
+ * elastic displacement pair launch several kernels). */
+int sw_profile_read_kernels(sw_ctx* ctx, int32_t kind, int64_t* kernels);
 
 /* ---------------------------------------------------------------------------
  * Isotropic elastic 2D (P-SV), 4th-order staggered displacement-stress scheme

@@ -27,7 +27,7 @@ EXPORTS = [
     "sw_wavesim_set_precision", "sw_wavesim_set_vp64",
     "sw_wavesim_set_wait_test",
     "sw_profile_enable",
-    "sw_profile_read", "sw_acoustic2d_forward_noalloc", "sw_elastic_create", "sw_elastic_destroy",
+    "sw_profile_read", "sw_profile_read_kernels", "sw_acoustic2d_forward_noalloc", "sw_elastic_create", "sw_elastic_destroy",
     "sw_elastic_set_material", "sw_elastic_forward", "sw_elastic_gradient", "sw_elastic_set_tuning",
     "sw_wavesim_use_graphs", "sw_acoustic_forward_snapshots", "sw_elastic_forward_snapshots",
     "sw_acoustic_vd_create", "sw_acoustic_vd_destroy", "sw_acoustic_vd_set_material", "sw_acoustic_vd_forward",
@@ -112,6 +112,7 @@ def load() -> ctypes.CDLL:
     lib.sw_wavesim_set_wait_test.argtypes = [vp_, ctypes.c_int64, i32]
     lib.sw_profile_enable.argtypes = [vp_, i32]
     lib.sw_profile_read.argtypes = [vp_, i32, P(f64), P(ctypes.c_int64), P(f64)]
+    lib.sw_profile_read_kernels.argtypes = [vp_, i32, P(ctypes.c_int64)]
     lib.sw_acoustic2d_forward_noalloc.argtypes = [P(SwAcousticParams), vp_, P(SwAcousticShot), vp_]
     lib.sw_elastic_create.argtypes = [vp_, P(SwElasticParams), i32, P(SwGradParams), P(vp_)]
     lib.sw_elastic_destroy.argtypes = [vp_]
@@ -161,6 +162,12 @@ class Context:
         self.check(self.lib.sw_profile_read(self.h, kind, ctypes.byref(ms), ctypes.byref(n), ctypes.byref(b)),
                    "sw_profile_read")
         return ms.value, n.value, b.value
+
+    def profile_kernels(self, kind: int) -> int:
+        """Kernel launches inside the timed brackets of `kind`."""
+        n = ctypes.c_int64()
+        self.check(self.lib.sw_profile_read_kernels(self.h, kind, ctypes.byref(n)), "sw_profile_read_kernels")
+        return n.value
 
     def close(self):
         if self.h:

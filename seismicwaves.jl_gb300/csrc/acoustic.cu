@@ -1339,13 +1339,16 @@ void enable_pair_carveout() {
 
 // The 2D one-step stencil of 4-warp blocks with the x strips split off: the
 // lanes outside the x strips, then the lane groups that meet one.
+// Returns the number of kernels launched.
 template <int MODE>
-void launch_2d_xsplit(long long blocks, cudaStream_t st, const StepArgs& a) {
+int launch_2d_xsplit(long long blocks, cudaStream_t st, const StepArgs& a) {
   k_ac2d_step<MODE, 4, 1, true><<<(unsigned)blocks, 128, 0, st>>>(a);
   int nl, xr, ng;
   xstrip_groups(a.n0, a.halo, a.P, nl, xr, ng);
   const long long threads = (long long)ng * (a.n1 - 2) * a.nshots;
-  if (threads > 0) k_ac2d_xstrip<MODE><<<(unsigned)((threads + 127) / 128), 128, 0, st>>>(a);
+  if (threads <= 0) return 1;
+  k_ac2d_xstrip<MODE><<<(unsigned)((threads + 127) / 128), 128, 0, st>>>(a);
+  return 2;
 }
 
 template <int MODE, int MB>
@@ -1397,6 +1400,7 @@ struct Launcher {
     cudaEvent_t ev = nullptr;
     const int kind = (MODE == MODE_ADJ || MODE == MODE_ADJW) ? KK_ADJOINT : (recompute ? KK_RECOMPUTE : KK_STENCIL);
     ws->ctx->prof.begin(st, kind, bytes, &ev);
+    int nk = 1;  // kernels launched for this step
     if constexpr (MODE == MODE_FWD || MODE == MODE_FWD_D) {
       if (ws->precision == 1 && !recompute) {  // compensated forward (context from make_hp_ctx)
         if (ws->N == 2)
@@ -1414,7 +1418,7 @@ struct Launcher {
         enable_cpa_carveout<MODE>();
         k_ac2d_cpa<MODE, 4><<<(unsigned)blocks, 128, 0, st>>>(a);
       } else if (nw == 4 && ws->xsplit)
-        launch_2d_xsplit<MODE>(blocks, st, a);
+        nk = launch_2d_xsplit<MODE>(blocks, st, a);
       else if (nw == 4)
         k_ac2d_step<MODE, 4><<<(unsigned)blocks, 128, 0, st>>>(a);
       else if (nw == 8)
@@ -1440,7 +1444,7 @@ struct Launcher {
       }
       if (launched) {
       } else if (nw == 4 && ws->xsplit)
-        launch_2d_xsplit<MODE>(blocks, st, a);
+        nk = launch_2d_xsplit<MODE>(blocks, st, a);
       else if (nw == 4)
         k_ac2d_step<MODE, 4><<<(unsigned)blocks, 128, 0, st>>>(a);
       else if (nw == 8)
@@ -1468,6 +1472,7 @@ struct Launcher {
       a2.TZ = tzs;
       const long long b2 = (long long)a.nshots * c.tiles_x * ss.zslab_units;
       const long long b3 = (long long)a.nshots * c.tiles_x * ss.yslab_units;
+      nk = (b1 > 0) + (b2 > 0) + (b3 > 0);
       if (b1 > 0 && ws->inner_np) {
         if (nw == 8) k_ac3d_inner_np<MODE, 8><<<(unsigned)b1, 256, 0, st>>>(a1);
         else k_ac3d_inner_np<MODE><<<(unsigned)b1, 128, 0, st>>>(a1);
@@ -1500,7 +1505,7 @@ struct Launcher {
       }
     }
     check_cuda(cudaGetLastError(), "stencil launch");
-    ws->ctx->prof.end(st, kind, ev);
+    ws->ctx->prof.end(st, kind, ev, nk);
   }
   // two time steps in one launch (2D)
   template <int MODE>

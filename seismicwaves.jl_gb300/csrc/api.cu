@@ -98,11 +98,11 @@ void Profiler::begin(cudaStream_t s, int kind, double b, cudaEvent_t* a_out) {
   *a_out = a;
 }
 
-void Profiler::end(cudaStream_t s, int kind, cudaEvent_t a) {
+void Profiler::end(cudaStream_t s, int kind, cudaEvent_t a, int nk) {
   if (!on || !a) return;
   cudaEvent_t b = get();
   check_cuda(cudaEventRecord(b, s), "cudaEventRecord");
-  pending.push_back(Pending{a, b, kind});
+  pending.push_back(Pending{a, b, kind, nk});
   if (pending.size() > 8192) resolve();
 }
 
@@ -114,6 +114,7 @@ void Profiler::resolve() {
     check_cuda(cudaEventElapsedTime(&ms, p.a, p.b), "cudaEventElapsedTime");
     total_ms[p.kind] += ms;
     launches[p.kind] += 1;
+    kernels[p.kind] += p.nk;
     pool.push_back(p.a);
     pool.push_back(p.b);
   }
@@ -310,6 +311,7 @@ int sw_profile_enable(sw_ctx* ctx, int32_t on) {
       for (int k = 0; k < swgb::KK_COUNT; ++k) {
         ctx->prof.total_ms[k] = 0;
         ctx->prof.launches[k] = 0;
+        ctx->prof.kernels[k] = 0;
         ctx->prof.bytes[k] = 0;
       }
     }
@@ -323,6 +325,14 @@ int sw_profile_read(sw_ctx* ctx, int32_t kind, double* total_ms, int64_t* launch
     if (total_ms) *total_ms = ctx->prof.total_ms[kind];
     if (launches) *launches = ctx->prof.launches[kind];
     if (bytes) *bytes = ctx->prof.bytes[kind];
+  });
+}
+
+int sw_profile_read_kernels(sw_ctx* ctx, int32_t kind, int64_t* kernels) {
+  if (!ctx || !kernels || kind < 0 || kind >= swgb::KK_COUNT) return SW_ERR_ARG;
+  return guarded(ctx, [&] {
+    ctx->prof.resolve();
+    *kernels = ctx->prof.kernels[kind];
   });
 }
 

@@ -1830,7 +1830,9 @@ void zero_state(sw_elastic* es, int S, bool adjoint) {
 }
 
 template <int TZ>
-void launch_stencil_tz(const sw_elastic* es, cudaStream_t st, const Args& a, int S, bool stress) {
+// returns the number of kernels launched
+int launch_stencil_tz(const sw_elastic* es, cudaStream_t st, const Args& a, int S, bool stress) {
+  int nk = 1;
   if (es->vec) {  // four points per thread: 512 per block
     const dim3 grid((es->g.nx + 511) / 512, (es->g.nz + TZ - 1) / TZ, S);
     if (stress) {
@@ -1838,6 +1840,7 @@ void launch_stencil_tz(const sw_elastic* es, cudaStream_t st, const Args& a, int
     } else if (es->split_disp) {  // ux and uz updates as two launches
       k_el_disp4<TZ, 0><<<grid, BX, 0, st>>>(a);
       k_el_disp4<TZ, 1><<<grid, BX, 0, st>>>(a);
+      nk = 2;
     } else {
       k_el_disp4<TZ><<<grid, BX, 0, st>>>(a);
     }
@@ -1847,12 +1850,13 @@ void launch_stencil_tz(const sw_elastic* es, cudaStream_t st, const Args& a, int
     else k_el_disp<TZ><<<grid, BX, 0, st>>>(a);
   }
   check_cuda(cudaGetLastError(), stress ? "stress launch" : "displacement launch");
+  return nk;
 }
 
-void launch_stencil(const sw_elastic* es, cudaStream_t st, const Args& a, int S, bool stress) {
-  if (es->tz == 16) launch_stencil_tz<16>(es, st, a, S, stress);
-  else if (es->tz == 32) launch_stencil_tz<32>(es, st, a, S, stress);
-  else launch_stencil_tz<8>(es, st, a, S, stress);
+int launch_stencil(const sw_elastic* es, cudaStream_t st, const Args& a, int S, bool stress) {
+  if (es->tz == 16) return launch_stencil_tz<16>(es, st, a, S, stress);
+  if (es->tz == 32) return launch_stencil_tz<32>(es, st, a, S, stress);
+  return launch_stencil_tz<8>(es, st, a, S, stress);
 }
 
 // stress, [sigma sources], displacement, [force sources], [recording]
@@ -1867,8 +1871,8 @@ void full_step(Run& R, int S, int it, bool record, int kind, float* sU[2], float
   es->ctx->prof.end(R.st, kind, ev);
   if (R.any_mt) R.inject_sigma(S, it);
   es->ctx->prof.begin(R.st, kind, R.step_bytes(S, sU != nullptr), &ev);
-  launch_stencil(es, R.st, a, S, false);
-  es->ctx->prof.end(R.st, kind, ev);
+  const int nk = launch_stencil(es, R.st, a, S, false);
+  es->ctx->prof.end(R.st, kind, ev, nk);
   if (R.any_force) R.inject_force(S, it, false, nullptr, sD);
   if (record) R.record(S, it);
 }
@@ -1879,9 +1883,9 @@ void adjoint_step(Run& R, int S, int it) {
   Args a = R.args(true);
   cudaEvent_t ev = nullptr;
   es->ctx->prof.begin(R.st, KK_ADJOINT, R.step_bytes(S, false), &ev);
-  launch_stencil(es, R.st, a, S, true);
-  launch_stencil(es, R.st, a, S, false);
-  es->ctx->prof.end(R.st, KK_ADJOINT, ev);
+  int nk = launch_stencil(es, R.st, a, S, true);
+  nk += launch_stencil(es, R.st, a, S, false);
+  es->ctx->prof.end(R.st, KK_ADJOINT, ev, nk);
   R.inject_force(S, it, true, es->d_scales.as<float>() + 1, nullptr);
 }
 

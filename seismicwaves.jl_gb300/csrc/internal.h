@@ -53,17 +53,18 @@ enum KernelKind {
 struct Profiler {
   bool on = false;
   double total_ms[KK_COUNT] = {};
-  long long launches[KK_COUNT] = {};
+  long long launches[KK_COUNT] = {};  // timed brackets (one step of a kind, one kernel call)
+  long long kernels[KK_COUNT] = {};   // kernel launches inside them
   double bytes[KK_COUNT] = {};
   struct Pending {
     cudaEvent_t a, b;
-    int kind;
+    int kind, nk;
   };
   std::vector<Pending> pending;
   std::vector<cudaEvent_t> pool;
   cudaEvent_t get();
   void begin(cudaStream_t s, int kind, double bytes_, cudaEvent_t* a_out);
-  void end(cudaStream_t s, int kind, cudaEvent_t a);
+  void end(cudaStream_t s, int kind, cudaEvent_t a, int nk = 1);  // nk: kernels launched since begin
   void resolve();  // synchronises on the pending events, accumulates, recycles
   ~Profiler();
 };

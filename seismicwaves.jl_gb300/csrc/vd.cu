@@ -1413,7 +1413,7 @@ struct Run {
     a.po = po;
     a.acc = vd->acc.as<float>();
     launch_p(a, S, true);
-    vd->ctx->prof.end(st, KK_ADJOINT, ev);
+    vd->ctx->prof.end(st, KK_ADJOINT, ev, 2);
     vd->ctx->prof.begin(st, KK_SRCREC, 0.0, &ev);
     k_vd_adjinj<<<S, 128, 0, st>>>(ddesc, it, vd->g.F, ap, pc, po, vd->acc.as<float>(), a.idt);
     check_cuda(cudaGetLastError(), "adjoint injection launch");
