@@ -970,13 +970,13 @@ def run_gb300(a):
         return
     # roofline of the dominant kernel (largest total time among the stencil kinds)
     nd = w.vp.ndim
-    # 2D, 4-warp one-step stencil: the x strips run as a second launch unless variant bit 18 is set
+    # 2D, 4-warp one-step stencil: the x strips run as extra blocks unless variant bit 18 is set
     xs = nd == 2 and not (veff >= 0 and veff & (262144 | 512 | 3))
 
     def kname(m):
         if nd == 3:
             return f"k_ac3d_inner + k_ac3d_zslab + k_ac3d_yslab<{m}>"
-        return f"k_ac2d_step<{m}> + k_ac2d_xstrip<{m}>" if xs else f"k_ac2d_step<{m}>"
+        return f"k_ac2d_step<{m}, XS> (x strips as extra blocks)" if xs else f"k_ac2d_step<{m}>"
 
     if nd == 2 and veff >= 0 and (veff & 256) and nshots >= 4:
         adj, adj_what = "k_ac2d_adj_grp", "adjoint + correlation (4 shots per block, Kahan sums)"

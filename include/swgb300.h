@@ -230,8 +230,9 @@ int sw_acoustic_forward_snapshots(sw_wavesim* ws, int32_t nshots, const sw_acous
  * 3D: + 65536 runs the step as one launch instead of three (rows outside the
  * y / z strips, the z slabs, the y slabs); + 131072 runs the three launches
  * without the software pipeline.  2D, 4 warps per block: by default the
- * 4-point lane groups that meet an x strip are advanced by a launch of their
- * own after the stencil launch; + 262144 keeps them in the one launch.
+ * 4-point lane groups that meet an x strip are advanced by extra blocks at the
+ * end of the stencil launch, one group per thread (the main blocks skip
+ * them); + 262144 keeps them in the main blocks' per-point C-PML path.
  * Results do not depend on any of them beyond rounding. */
 int sw_wavesim_set_tuning(sw_wavesim* ws, int32_t tz, int32_t variant);
 
@@ -281,9 +282,9 @@ int sw_wavesim_use_graphs(sw_wavesim* ws, int32_t on);
 int sw_profile_enable(sw_ctx* ctx, int32_t on);
 int sw_profile_read(sw_ctx* ctx, int32_t kind, double* total_ms, int64_t* launches, double* bytes);
 /* Kernel launches inside the brackets that sw_profile_read counts as
- * `launches` (one bracket per step of a kind; the 2D step with its x strips,
- * the 3D step as three launches, the variable-density adjoint pair and the
- * elastic displacement pair launch several kernels). */
+ * `launches` (one bracket per step of a kind; the 3D step as three launches,
+ * the variable-density adjoint pair and the elastic displacement pair launch
+ * several kernels). */
 int sw_profile_read_kernels(sw_ctx* ctx, int32_t kind, int64_t* kernels);
 
 /* ---------------------------------------------------------------------------

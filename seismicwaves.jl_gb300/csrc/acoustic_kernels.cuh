@@ -391,8 +391,9 @@ struct Ac2dRow {
   }
 
   // XS (x strips split off): a lane whose four points meet an x strip
-  // (xstrip) stores nothing here; k_ac2d_xstrip advances those points.  Every
-  // other lane's points lie outside the x strips and inside the grid's
+  // (xstrip) stores nothing here; the x-strip blocks of the launch
+  // (xstrip_item) advance those points.  Every other lane's points lie
+  // outside the x strips and inside the grid's
   // interior, so a row outside the z strips takes the interior path in every
   // warp and a z strip row needs only the z term.
   template <bool XS = false>
@@ -492,6 +493,56 @@ struct Ac2dRow {
   }
 };
 
+// The 4-point lane groups that meet an x strip (x0 < H or x0 + 3 >= nx - H,
+// x0 = 0, 4, .. < P): nl groups x0 = 0 .. 4 (nl - 1) on the left, then the
+// groups from x0 = xr up to the padded row end; ng in all.
+__host__ __device__ __forceinline__ void xstrip_groups(int nx, int H, int P, int& nl, int& xr, int& ng) {
+  nl = (H + 3) / 4;
+  const int lo = nx - H - 3 > 0 ? nx - H - 3 : 0;
+  xr = ((lo + 3) / 4) * 4;
+  if (xr < 4 * nl) xr = 4 * nl;
+  ng = nl + (P - xr > 0 ? (P - xr) / 4 : 0);
+}
+
+// The points that the main blocks of k_ac2d_step<.., XS = true> leave: work
+// item t is one (lane group of the x strips, row, shot); it loads its rows
+// and runs the general path of Ac2dRow (both strips per point), so every
+// point is advanced by the same arithmetic as in the single-path kernel.
+// Not inlined: its registers (and spills) stay out of the main blocks' path.
+template <int MODE>
+__device__ __noinline__ void xstrip_item(const StepArgs& A, long long t) {
+  const int nx = A.n0, nz = A.n1, P = A.P, H = A.halo;
+  int nl, xr, ng;
+  xstrip_groups(nx, H, P, nl, xr, ng);
+  const int g = (int)(t % ng);
+  const long long rest = t / ng;
+  const int z = 1 + (int)(rest % (nz - 2));
+  const int shot = (int)(rest / (nz - 2));
+  if (shot >= A.nshots) return;
+  const int x0 = g < nl ? 4 * g : xr + 4 * (g - nl);
+  const float* __restrict__ pc = fptr(A.pcur, shot);
+  const float* di = fptr(A.din, shot);
+  const long long row = (long long)z * P;
+  float rm[4], r0[4], rp[4], o[4], f[4], dv[4] = {}, g4[4] = {}, c4[4] = {};
+  ld4(rm, pc + row - P + x0);
+  ld4(r0, pc + row + x0);
+  ld4(rp, pc + row + P + x0);
+  ld4rw(o, di + row + x0);
+  ld4(f, A.fact + row + x0);
+  const float left = x0 > 0 ? pc[row + x0 - 1] : 0.f;
+  const float right = x0 + 4 < P ? pc[row + x0 + 4] : 0.f;
+  Ac2dRow<MODE> R;
+  R.init(A, shot, x0);
+  R.fastx = false;
+  constexpr bool ADJ = MODE == MODE_ADJ || MODE == MODE_ADJW;
+  if (ADJ) {
+    dld4(dv, dptr(A.dcorr, shot, A.dbf16), row + x0, A.dbf16);
+    ld4rw(g4, R.gg + row + x0);
+    if (MODE == MODE_ADJ) ld4rw(c4, R.gcp + row + x0);
+  }
+  R.update(z, rm, r0, rp, o, f, dv, g4, c4, left, right);
+}
+
 // Minimum resident blocks per SM for a block of NW warps: keeps the forward
 // kernels at <= 64 registers (8 blocks of 4 warps, no spills; measured 4.1 /
 // 4.5 TB/s forward / recompute against 3.8 / 4.3 at 7 blocks); the per-shot
@@ -504,9 +555,20 @@ struct Ac2dBounds {
                                                   : (NW == 4 ? 8 : NW == 8 ? 4 : 2);
 };
 
+// XS: the lanes that meet an x strip store nothing in the main blocks (the
+// first nshots x tiles_x x tiles_z); the blocks after them take the lane
+// groups of the x strips, one per thread (xstrip_item), so that this work
+// fills the tail of the launch.
 template <int MODE, int NW, int DP = 1, bool XS = false>
 __global__ void __launch_bounds__(32 * NW, (Ac2dBounds<MODE, NW>::MINB - (DP - 1))) k_ac2d_step(const StepArgs A) {
   constexpr unsigned FULL = 0xffffffffu;
+  if constexpr (XS) {
+    const long long nb_main = (long long)A.nshots * A.tiles_x * A.tiles_y * A.tiles_z;
+    if ((long long)blockIdx.x >= nb_main) {
+      xstrip_item<MODE>(A, ((long long)blockIdx.x - nb_main) * (32 * NW) + threadIdx.x);
+      return;
+    }
+  }
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   constexpr int nwarps = NW;
   const int S = A.nshots;
@@ -639,56 +701,6 @@ __global__ void __launch_bounds__(32 * NW, (Ac2dBounds<MODE, NW>::MINB - (DP - 1
   }
 }
 
-
-// The 4-point lane groups that meet an x strip (x0 < H or x0 + 3 >= nx - H,
-// x0 = 0, 4, .. < P): nl groups x0 = 0 .. 4 (nl - 1) on the left, then the
-// groups from x0 = xr up to the padded row end; ng in all.
-__host__ __device__ __forceinline__ void xstrip_groups(int nx, int H, int P, int& nl, int& xr, int& ng) {
-  nl = (H + 3) / 4;
-  const int lo = nx - H - 3 > 0 ? nx - H - 3 : 0;
-  xr = ((lo + 3) / 4) * 4;
-  if (xr < 4 * nl) xr = 4 * nl;
-  ng = nl + (P - xr > 0 ? (P - xr) / 4 : 0);
-}
-
-// The points that k_ac2d_step<.., XS = true> leaves: one thread per (lane
-// group of the x strips, row, shot) loads its rows and runs the general path
-// of Ac2dRow (both strips per point), so every point is advanced by the same
-// arithmetic as in the single launch.
-template <int MODE>
-__global__ void __launch_bounds__(128) k_ac2d_xstrip(const StepArgs A) {
-  const int nx = A.n0, nz = A.n1, P = A.P, H = A.halo;
-  int nl, xr, ng;
-  xstrip_groups(nx, H, P, nl, xr, ng);
-  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  const int g = (int)(t % ng);
-  const long long rest = t / ng;
-  const int z = 1 + (int)(rest % (nz - 2));
-  const int shot = (int)(rest / (nz - 2));
-  if (shot >= A.nshots) return;
-  const int x0 = g < nl ? 4 * g : xr + 4 * (g - nl);
-  const float* __restrict__ pc = fptr(A.pcur, shot);
-  const float* di = fptr(A.din, shot);
-  const long long row = (long long)z * P;
-  float rm[4], r0[4], rp[4], o[4], f[4], dv[4] = {}, g4[4] = {}, c4[4] = {};
-  ld4(rm, pc + row - P + x0);
-  ld4(r0, pc + row + x0);
-  ld4(rp, pc + row + P + x0);
-  ld4rw(o, di + row + x0);
-  ld4(f, A.fact + row + x0);
-  const float left = x0 > 0 ? pc[row + x0 - 1] : 0.f;
-  const float right = x0 + 4 < P ? pc[row + x0 + 4] : 0.f;
-  Ac2dRow<MODE> R;
-  R.init(A, shot, x0);
-  R.fastx = false;
-  constexpr bool ADJ = MODE == MODE_ADJ || MODE == MODE_ADJW;
-  if (ADJ) {
-    dld4(dv, dptr(A.dcorr, shot, A.dbf16), row + x0, A.dbf16);
-    ld4rw(g4, R.gg + row + x0);
-    if (MODE == MODE_ADJ) ld4rw(c4, R.gcp + row + x0);
-  }
-  R.update(z, rm, r0, rp, o, f, dv, g4, c4, left, right);
-}
 
 // ---------------------------------------------------------------------------
 // 2D, two time steps per pass (temporal blocking) for the forward kinds and

@@ -31,8 +31,8 @@ from . import _lib
 
 _cache: dict = {}
 
-# (variant, tz) of sw_wavesim_set_tuning; 2D: 262144 = the x strips inside
-# the one stencil launch instead of a launch of their own
+# (variant, tz) of sw_wavesim_set_tuning; 2D: 262144 = the x strips in the
+# main blocks' per-point path instead of extra blocks of their own
 CANDIDATES_2D = [(0, 4), (0, 8), (0, 16), (2, 8), (512, 8), (1024, 0), (256, 8), (262144, 8)]
 # 3D: 131072 = inner rows without the software pipeline, 65536 = one launch per step
 CANDIDATES_3D = [(0, 8), (0, 16), (0, 32), (2, 8), (131072, 8), (131072, 16), (131074, 16), (65536, 16)]

@@ -1,12 +1,12 @@
-"""The 2D one-step stencil with its x strips in a launch of their own (the
-default: k_ac2d_step with XS, then k_ac2d_xstrip for the 4-point lane groups
-that meet an x strip) against the single launch (tuning variant bit 18).
-Every point is advanced by exactly one of the two launches with the same
-arithmetic, so traces, misfit and gradient must be bit-identical: grids whose
-x strips end inside a lane group (odd nx, halo not a multiple of 4), no
-strips, strips that leave a single interior group, checkpointing (K > 1),
-BF16 recompute buffers, the per-shot Kahan adjoint (muting) and sources and
-receivers inside the strips."""
+"""The 2D one-step stencil with its x strips split off (the default:
+k_ac2d_step with XS, whose main blocks leave the 4-point lane groups that
+meet an x strip to extra blocks at the end of the launch, one group per
+thread) against the single path (tuning variant bit 18).  Every point is
+advanced exactly once with the same arithmetic, so traces, misfit and
+gradient must be bit-identical: grids whose x strips end inside a lane group
+(odd nx, halo not a multiple of 4), no strips, strips that leave a single
+interior group, checkpointing (K > 1), BF16 recompute buffers, the per-shot
+Kahan adjoint (muting) and sources and receivers inside the strips."""
 import numpy as np
 import pytest
 
