@@ -1016,6 +1016,8 @@ def run_gb300(a):
             "kernels": {kinds[k][0]: {"ms": prof[k][0], "launches": prof[k][1],
                                       "GB_per_s": (prof[k][2] / (prof[k][0] / 1e3) / 1e9) if prof[k][0] else None}
                         for k in kinds}}
+    if plain:  # the plain path moves at least the batch's stencil bytes (it re-reads `fact` per shot)
+        plain["hbm_frac_lower_bound"] = kern_bytes / (plain["ms_per_step"] / 1e3) / 1e9 / peak
     # kernels per gradient (a profiled step may launch several) x timed gradients
     total_launches = kernels_per_call * a.steps
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
