@@ -31,6 +31,9 @@ def test_version_and_bad_args(sw):
     assert lib.sw_ctx_create(0, None, None) == sw._lib.SW_ERR_ARG
     assert lib.sw_wavesim_destroy(None) == sw._lib.SW_ERR_ARG
     assert lib.sw_profile_enable(None, 1) == sw._lib.SW_ERR_ARG
+    n = ctypes.c_int64(-1)
+    assert lib.sw_profile_read_kernels(None, 0, ctypes.byref(n)) == sw._lib.SW_ERR_ARG and n.value == -1
+    assert lib.sw_wavesim_set_tuning(None, 0, 262144) == sw._lib.SW_ERR_ARG
 
 
 @pytest.mark.parametrize("halo,freetop", [(20, False), (20, True), (7, False), (1, True), (0, False)])
